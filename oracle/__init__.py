@@ -1,0 +1,270 @@
+"""CPU oracle for the HydroEXA per-level advance (TEST INFRASTRUCTURE ONLY).
+
+This package is the checker the CUDA path is compared against.  Only tests/,
+``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg import it; the
+product package ``hydroexa_gb300`` never does.
+
+``build()`` compiles ``hx_oracle_capi.cpp`` (a scalar C++ restatement of the
+reference's arithmetic, see ``hx_oracle.hpp`` for the file:line map) into
+``oracle/_build/libhx_oracle.so`` with ``-O2 -ffp-contract=off -fopenmp``.
+``build_ref()`` compiles the reference's own header-only point kernels from the
+reference source tree into ``oracle/_ref/libhx_ref.so`` (only where that tree
+exists; used to pin the oracle and to regenerate ``tests/golden``).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+BUILD_DIR = HERE / "_build"
+LIB_PATH = BUILD_DIR / "libhx_oracle.so"
+REF_LIB_PATH = HERE / "_ref" / "libhx_ref.so"
+
+METHOD_CLASSIC = 0
+METHOD_HYDROSTATIC = 1
+LIMITER_FLOAT_ABS = 0
+LIMITER_INT_ABS = 1
+
+
+def build(force: bool = False) -> Path:
+    """Compile the oracle shared library (a few seconds)."""
+    src = [HERE / "hx_oracle_capi.cpp", HERE / "hx_oracle.hpp"]
+    if LIB_PATH.exists() and not force:
+        mt = LIB_PATH.stat().st_mtime
+        if all(s.stat().st_mtime <= mt for s in src):
+            return LIB_PATH
+    BUILD_DIR.mkdir(exist_ok=True)
+    tmp = LIB_PATH.with_suffix(f".{os.getpid()}.tmp")
+    cmd = [os.environ.get("CXX", "g++"), "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared",
+           "-std=c++17", str(HERE / "hx_oracle_capi.cpp"), "-o", str(tmp)]
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+def build_ref() -> Path | None:
+    """Compile the reference's point kernels if the reference tree is present."""
+    ref_root = Path(os.environ.get("HX_REFERENCE_ROOT", "/root/reference"))
+    if not (ref_root / "include" / "solvers" / "kernels").is_dir():
+        return None
+    subprocess.run(["sh", str(HERE / "build_ref.sh")], check=True, stdout=subprocess.DEVNULL)
+    return REF_LIB_PATH
+
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            build()
+        _lib = ctypes.CDLL(str(LIB_PATH))
+    return _lib
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _suffix(dtype) -> str:
+    return "f64" if np.dtype(dtype) == np.float64 else "f32"
+
+
+def _real(dtype):
+    return ctypes.c_double if np.dtype(dtype) == np.float64 else ctypes.c_float
+
+
+def set_threads(n: int) -> None:
+    lib().hxo_set_threads(ctypes.c_int(int(n)))
+
+
+def max_threads() -> int:
+    return int(lib().hxo_max_threads())
+
+
+def _bc(lo, hi):
+    return (np.ascontiguousarray(lo, dtype=np.int32), np.ascontiguousarray(hi, dtype=np.int32))
+
+
+def roe_hydrostatic_points(states: np.ndarray, normals: np.ndarray) -> np.ndarray:
+    """states (n, 6) = (hi, hui, hvi, hj, huj, hvj); normals (n, 2) -> F (n, 3)."""
+    s = np.ascontiguousarray(states)
+    nr = np.ascontiguousarray(normals, dtype=s.dtype)
+    out = np.empty((s.shape[0], 3), dtype=s.dtype)
+    getattr(lib(), "hxo_roe_hydrostatic_points_" + _suffix(s.dtype))(
+        ctypes.c_long(s.shape[0]), _ptr(s), _ptr(nr), _ptr(out))
+    return out
+
+
+def roe_classic_points(states: np.ndarray, aux: np.ndarray):
+    """states (n, 10); aux (n, 4) = (dt, dx, nx, ny) -> (F, S_minus, S_plus), each (n, 3)."""
+    s = np.ascontiguousarray(states)
+    a = np.ascontiguousarray(aux, dtype=s.dtype)
+    F = np.empty((s.shape[0], 3), dtype=s.dtype)
+    Sm = np.empty_like(F)
+    Sp = np.empty_like(F)
+    getattr(lib(), "hxo_roe_classic_points_" + _suffix(s.dtype))(
+        ctypes.c_long(s.shape[0]), _ptr(s), _ptr(a), _ptr(F), _ptr(Sm), _ptr(Sp))
+    return F, Sm, Sp
+
+
+def van_leer_slope_points(q3: np.ndarray, mode: int = LIMITER_FLOAT_ABS) -> np.ndarray:
+    q = np.ascontiguousarray(q3)
+    out = np.empty(q.shape[0], dtype=q.dtype)
+    getattr(lib(), "hxo_van_leer_slope_points_" + _suffix(q.dtype))(
+        ctypes.c_long(q.shape[0]), _ptr(q), ctypes.c_int(mode), _ptr(out))
+    return out
+
+
+class Level:
+    """Single-box level: planes (ny, nx), x fastest, with the inputs-file BC codes."""
+
+    def __init__(self, nx, ny, dx, dy, bc_lo=(0, 0), bc_hi=(0, 0)):
+        self.nx, self.ny, self.dx, self.dy = int(nx), int(ny), float(dx), float(dy)
+        self.bc_lo, self.bc_hi = _bc(bc_lo, bc_hi)
+
+
+def advance(level: Level, method: int, h, hu, hv, z, n, dt, mode=LIMITER_FLOAT_ABS, faces=False):
+    """One advance by dt; returns (h, hu, hv) [, face arrays]."""
+    dtype = np.asarray(h).dtype
+    R = _real(dtype)
+    arrs = [np.ascontiguousarray(a, dtype=dtype) for a in (h, hu, hv, z, n)]
+    out = [np.empty_like(arrs[0]) for _ in range(3)]
+    L = level
+    sfx = _suffix(dtype)
+    base = [ctypes.c_int(L.nx), ctypes.c_int(L.ny), R(L.dx), R(L.dy), _ptr(L.bc_lo), _ptr(L.bc_hi)]
+    base += [_ptr(a) for a in arrs] + [R(dt)] + [_ptr(o) for o in out]
+    nxf, nyf = (L.nx + 1) * L.ny, L.nx * (L.ny + 1)
+    if method == METHOD_HYDROSTATIC:
+        if not faces:
+            getattr(lib(), "hxo_advance_hydrostatic_" + sfx)(*base, ctypes.c_int(mode))
+            return tuple(out)
+        fx = [np.empty((3, L.ny, L.nx + 1), dtype=dtype) for _ in range(2)]
+        fy = [np.empty((3, L.ny + 1, L.nx), dtype=dtype) for _ in range(2)]
+        getattr(lib(), "hxo_advance_hydrostatic_faces_" + sfx)(
+            *base, ctypes.c_int(mode), _ptr(fx[0]), _ptr(fx[1]), _ptr(fy[0]), _ptr(fy[1]))
+        return tuple(out), {"FLx": fx[0], "FRx": fx[1], "FLy": fy[0], "FRy": fy[1]}
+    if not faces:
+        getattr(lib(), "hxo_advance_classic_" + sfx)(*base)
+        return tuple(out)
+    fx = [np.empty((3, L.ny, L.nx + 1), dtype=dtype) for _ in range(3)]
+    fy = [np.empty((3, L.ny + 1, L.nx), dtype=dtype) for _ in range(3)]
+    getattr(lib(), "hxo_advance_classic_faces_" + sfx)(*base, *[_ptr(a) for a in fx + fy])
+    del nxf, nyf
+    return tuple(out), {"Fx": fx[0], "Smx": fx[1], "Spx": fx[2], "Fy": fy[0], "Smy": fy[1], "Spy": fy[2]}
+
+
+def compute_dt(level: Level, h, hu, hv, z):
+    """(min per-cell CFL bound, max(|u|,|v|)) over the level, before the CFL factor."""
+    dtype = np.asarray(h).dtype
+    R = _real(dtype)
+    arrs = [np.ascontiguousarray(a, dtype=dtype) for a in (h, hu, hv, z)]
+    mn, mx = R(), R()
+    getattr(lib(), "hxo_compute_dt_" + _suffix(dtype))(
+        ctypes.c_int(level.nx), ctypes.c_int(level.ny), R(level.dx), R(level.dy),
+        *[_ptr(a) for a in arrs], ctypes.byref(mn), ctypes.byref(mx))
+    return float(mn.value), float(mx.value)
+
+
+def run(level: Level, method: int, h, hu, hv, z, n, nsteps, cfl, mode=LIMITER_FLOAT_ABS):
+    """nsteps of the single-level time loop in place on copies; returns (h, hu, hv, t, dt_last, status)."""
+    dtype = np.asarray(h).dtype
+    R = _real(dtype)
+    st = [np.array(a, dtype=dtype, copy=True, order="C") for a in (h, hu, hv)]
+    zz = np.ascontiguousarray(z, dtype=dtype)
+    nn = np.ascontiguousarray(n, dtype=dtype)
+    t, dtl = R(), R()
+    rc = getattr(lib(), "hxo_run_" + _suffix(dtype))(
+        ctypes.c_int(method), ctypes.c_int(level.nx), ctypes.c_int(level.ny), R(level.dx), R(level.dy),
+        _ptr(level.bc_lo), _ptr(level.bc_hi), *[_ptr(a) for a in st], _ptr(zz), _ptr(nn),
+        ctypes.c_int(nsteps), R(cfl), ctypes.c_int(mode), ctypes.byref(t), ctypes.byref(dtl))
+    return st[0], st[1], st[2], float(t.value), float(dtl.value), int(rc)
+
+
+def tag_cells(variant, U, T, tags, valid_lo, valid_hi, dx, dy, time, h_th, u_th, z_th, set_value=2):
+    """Tag the valid box.  U (3, ny, nx) and T (2, ny, nx) carry one ghost ring:
+    array index [c, j+1, i+1] holds cell (i, j); tags (ny, nx) covers the same
+    grown box and is modified in place."""
+    dtype = U.dtype
+    R = _real(dtype)
+    U = np.ascontiguousarray(U)
+    T = np.ascontiguousarray(T, dtype=dtype)
+    assert tags.dtype == np.int8 and tags.flags.c_contiguous
+    _, uy, ux = U.shape
+    _, ty, tx = T.shape
+    gy, gx = tags.shape
+    getattr(lib(), "hxo_tag_cells_" + _suffix(dtype))(
+        ctypes.c_int(variant),
+        _ptr(U), ctypes.c_longlong(ux), ctypes.c_longlong(ux * uy), ctypes.c_int(-1), ctypes.c_int(-1),
+        _ptr(T), ctypes.c_longlong(tx), ctypes.c_longlong(tx * ty), ctypes.c_int(-1), ctypes.c_int(-1),
+        _ptr(tags), ctypes.c_longlong(gx), ctypes.c_int(-1), ctypes.c_int(-1),
+        ctypes.c_int(valid_lo[0]), ctypes.c_int(valid_lo[1]), ctypes.c_int(valid_hi[0]), ctypes.c_int(valid_hi[1]),
+        R(dx), R(dy), R(time), R(h_th), R(u_th), R(z_th), ctypes.c_byte(set_value))
+    return tags
+
+
+def masked_average_down(fine: np.ndarray, rx: int, ry: int, fine_volume: float, nodata: float = -9999.0):
+    """fine (ncomp, nyf, nxf) -> crse (ncomp, nyf//ry, nxf//rx)."""
+    f = np.ascontiguousarray(fine)
+    nc, nyf, nxf = f.shape
+    nxc, nyc = nxf // rx, nyf // ry
+    c = np.empty((nc, nyc, nxc), dtype=f.dtype)
+    R = _real(f.dtype)
+    getattr(lib(), "hxo_masked_average_down_" + _suffix(f.dtype))(
+        _ptr(f), ctypes.c_longlong(nxf), ctypes.c_longlong(nxf * nyf), ctypes.c_int(0), ctypes.c_int(0),
+        _ptr(c), ctypes.c_longlong(nxc), ctypes.c_longlong(nxc * nyc), ctypes.c_int(0), ctypes.c_int(0),
+        ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(nxc - 1), ctypes.c_int(nyc - 1),
+        ctypes.c_int(nc), ctypes.c_int(rx), ctypes.c_int(ry), R(fine_volume), R(nodata))
+    return c
+
+
+# --- reference kernels compiled verbatim (only where the reference tree exists) ---
+
+_ref = None
+
+
+def ref_lib() -> ctypes.CDLL:
+    global _ref
+    if _ref is None:
+        if not REF_LIB_PATH.exists():
+            if build_ref() is None:
+                raise FileNotFoundError("reference tree not available to build oracle/_ref")
+        _ref = ctypes.CDLL(str(REF_LIB_PATH))
+    return _ref
+
+
+def ref_roe_hydrostatic_points(states, normals):
+    s = np.ascontiguousarray(states)
+    nr = np.ascontiguousarray(normals, dtype=s.dtype)
+    out = np.empty((s.shape[0], 3), dtype=s.dtype)
+    getattr(ref_lib(), "hxref_roe_hydrostatic_" + _suffix(s.dtype))(
+        ctypes.c_long(s.shape[0]), _ptr(s), _ptr(nr), _ptr(out))
+    return out
+
+
+def ref_roe_classic_points(states, aux):
+    s = np.ascontiguousarray(states)
+    a = np.ascontiguousarray(aux, dtype=s.dtype)
+    F = np.empty((s.shape[0], 3), dtype=s.dtype)
+    Sm = np.empty_like(F)
+    Sp = np.empty_like(F)
+    getattr(ref_lib(), "hxref_roe_classic_" + _suffix(s.dtype))(
+        ctypes.c_long(s.shape[0]), _ptr(s), _ptr(a), _ptr(F), _ptr(Sm), _ptr(Sp))
+    return F, Sm, Sp
+
+
+def ref_masked_average_down(fine, rx, ry, fine_volume, nodata=-9999.0):
+    f = np.ascontiguousarray(fine)
+    nc, nyf, nxf = f.shape
+    c = np.empty((nc, nyf // ry, nxf // rx), dtype=f.dtype)
+    R = _real(f.dtype)
+    getattr(ref_lib(), "hxref_masked_avgdown_" + _suffix(f.dtype))(
+        ctypes.c_int(nxf), ctypes.c_int(nyf), ctypes.c_int(nc), _ptr(f), ctypes.c_int(rx), ctypes.c_int(ry),
+        R(fine_volume), R(nodata), _ptr(c))
+    return c
