@@ -1,0 +1,349 @@
+"""Throughput benchmark of the per-level advance on GB300.
+
+One step = one advance of the whole level (all cells), with the next step's
+CFL bound fused in; K timed steps follow W untimed warm-up steps.  Workload:
+a seeded 8192 x 8192 FP64 fractal-terrain circular dam break (hydrostatic-Roe,
+MUSCL van Leer, 20% NODATA, walls).  The inputs (4.3 GB) exceed the 129 MB L2,
+so no flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Multi-GPU: one process per GPU under torchrun, each advancing its own replica
+(the level does not shard across GPUs here: replicas only, weak scaling);
+value = all cells updated by all ranks / max over ranks of the timed region.
+
+--impl reference times the reference's arithmetic on the host cores: the
+reference itself cannot be built on this machine (it needs AMReX, MPI and
+HDF5), so the oracle's OpenMP restatement of the same per-box arithmetic runs
+instead, on a bounded sample of the workload per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+BASE = json.loads((ROOT / "BASELINE.json").read_text()) if (ROOT / "BASELINE.json").exists() else {}
+METRIC = BASE.get("metric", "FP64 Mcell-updates/s")
+UNIT = "Mcell-updates/s"
+PEAKS = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+HBM_GBS = float(PEAKS.get("hbm_gbs", 6800.0))
+HBM_SRC = "measured" if "hbm_gbs" in PEAKS else "fallback"
+# FP64 issue roof: measured DFMA rate of this machine's GB300 (0.597 T inst/s,
+# 1.19 TFLOP/s; profiles/fp64_pipe_probe.md)
+FP64_DFMA_PER_S = 0.597e12
+BYTES_PER_CELL = {"f64": 64, "f32": 32}  # read h hu hv z n, write h hu hv
+NX = NY = 8192
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) == 7:
+                self.rows.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4) if r[3 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def make_case(nx, ny):
+    from hydroexa_gb300 import workloads
+    return workloads.fractal_dam_break(nx, ny, seed=3)
+
+
+def cpu_sample(case, nsteps_max=50, budget_s=12.0, method=1):
+    """Oracle restatement (OpenMP, all host threads) on a bounded window of the
+    workload: a 1024 x 1024 crop with walls, stepped until ~budget_s."""
+    import numpy as np
+    import oracle
+    oracle.build()
+    w = 1024
+    j0 = (case.geom.ny - w) // 2
+    i0 = (case.geom.nx - w) // 2
+    sl = (slice(j0, j0 + w), slice(i0, i0 + w))
+    arrs = [np.ascontiguousarray(a[sl]) for a in (case.h, case.hu, case.hv, case.z, case.n)]
+    L = oracle.Level(w, w, case.geom.dx, case.geom.dy, (0, 0), (0, 0))
+    threads = oracle.max_threads()
+    h, hu, hv = arrs[0], arrs[1], arrs[2]
+    done = 0
+    t0 = time.perf_counter()
+    while done < nsteps_max:
+        mn, _ = oracle.compute_dt(L, h, hu, hv, arrs[3])
+        h, hu, hv = oracle.advance(L, method, h, hu, hv, arrs[3], arrs[4], mn * case.cfl)
+        done += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    el = time.perf_counter() - t0
+    return {"value": w * w * done / el / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"oracle OpenMP restatement (not the reference binary), {done} steps of a {w}x{w} crop of the "
+                      f"{case.geom.nx}x{case.geom.ny} workload, {el:.1f} s"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    case = make_case(NX, NY)
+    import numpy as np  # noqa: F401
+    import oracle
+    oracle.build()
+    # warm-up: W bounded steps; timed: K bounded steps (1024x1024 crop each)
+    w_budget = 2.0
+    for _ in range(args.warmup):
+        cpu_sample(case, nsteps_max=1, budget_s=w_budget)
+    vals = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        vals.append(cpu_sample(case, nsteps_max=1, budget_s=60.0))
+    el = time.perf_counter() - t0
+    value = 1024 * 1024 * args.steps / el / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": config_dict(),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": vals[0]["cores"], "kind": "port",
+                         "sample": "one advance (hydrostatic-Roe, with its CFL reduction) of a 1024x1024 crop of the "
+                                   "8192x8192 workload per step; oracle OpenMP restatement of the reference's "
+                                   "per-box arithmetic (the reference needs AMReX/MPI/HDF5 and cannot be built here)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def config_dict():
+    return {"workload": "fractal-terrain circular dam break 8192x8192 FP64, hydrostatic-Roe MUSCL van Leer, "
+                        "20% NODATA, reflective walls (BASELINE configs[2])",
+            "nx": NX, "ny": NY, "method": "HydrostaticRoe", "precision": "FP64",
+            "l2": "no flush: 4.3 GB of inputs per step > 129 MB L2", "seed": 3}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="native", choices=["native", "reference"])
+    ap.add_argument("--arith", default="fast", choices=["fast", "exact"])
+    ap.add_argument("--size", type=int, default=NX, help="level side (default 8192)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import ctypes
+    import numpy as np
+    import torch
+
+    import hydroexa_gb300
+    from hydroexa_gb300 import capi
+    from hydroexa_gb300.level import Level
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    hydroexa_gb300.build()
+    arith = capi.HX_ARITH_FAST if args.arith == "fast" else capi.HX_ARITH_EXACT
+    global NX, NY
+    NX = NY = args.size
+    case = make_case(NX, NY)
+    cells = NX * NY
+    lev = Level.from_numpy(case.geom, case.h, case.hu, case.hv, case.z, case.n, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    method = capi.HX_METHOD_HYDROSTATIC_ROE
+
+    def barrier():
+        torch.cuda.synchronize(dev)
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+
+    # ---- warm-up
+    assert lev.run(method, args.warmup, case.cfl, arith=arith) == 0
+    # ---- timed: K steps, one advance kernel each (+ the initial CFL pass)
+    barrier()
+    n0 = capi.launch_count()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        lev.run(method, args.steps, case.cfl, arith=arith, check_status=False)
+        e1.record(stream)
+        e1.synchronize()
+    barrier()
+    launches = capi.launch_count() - n0
+    status = lev.status.read()
+    assert status == 0, f"device status {status}"
+    ms = e0.elapsed_time(e1)
+    if dist is not None:
+        t = torch.tensor([ms], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = ws * cells * args.steps / (ms * 1e-3) / 1e6
+
+    # ---- dominant kernel: per-launch duration with events on its stream
+    acc_out = torch.empty_like(lev.state)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * 5)]
+    dt = 0.5 * lev.compute_dt()[0] * case.cfl
+    for k in range(5):
+        ev[2 * k].record(stream)
+        lev.advance(method, dt, out=acc_out, arith=arith)
+        ev[2 * k + 1].record(stream)
+    torch.cuda.synchronize(dev)
+    kms = statistics.mean(ev[2 * k].elapsed_time(ev[2 * k + 1]) for k in range(5))
+    achieved_gbs = BYTES_PER_CELL["f64"] * cells / (kms * 1e-3) / 1e9
+    profile = load_profile_summary()
+
+    # ---- end to end through the host-buffer C-ABI call (pinned host memory)
+    e2e = None
+    if True:  # every rank times its own replica end to end
+        pin = [torch.from_numpy(a.copy()).pin_memory() for a in (case.h, case.hu, case.hv, case.z, case.n)]
+        P = [ctypes.c_void_p(t.data_ptr()) for t in pin]
+        lo = (ctypes.c_int32 * 2)(*case.geom.bc_lo)
+        hi = (ctypes.c_int32 * 2)(*case.geom.bc_hi)
+        tout = ctypes.c_double()
+        sh = ctypes.c_void_p(stream.cuda_stream)
+        L = capi.lib()
+
+        def e2e_step():
+            rc = L.hx_level_run_host_f64(method, NX, NY, case.geom.dx, case.geom.dy, lo, hi, P[0], P[1], P[2], P[3],
+                                         P[4], 1, case.cfl, arith, ctypes.byref(tout), sh)
+            assert rc == 0, rc
+        for _ in range(2):
+            e2e_step()
+        ke = max(3, min(args.steps, 10))
+        barrier()
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        for _ in range(ke):
+            e2e_step()
+        f1.record(stream)
+        f1.synchronize()
+        ems = f0.elapsed_time(f1)
+        if dist is not None:
+            t = torch.tensor([ems], device=dev, dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ems = float(t.item())
+        L.hx_host_cache_release()
+        e2e = {"value": ws * cells * ke / (ems * 1e-3) / 1e6, "unit": UNIT, "h2d_bytes_per_step": 40 * cells,
+               "d2h_bytes_per_step": 24 * cells + 12, "steps": ke,
+               "call": "hx_level_run_host_f64 (host buffers in/out, one step per call)"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_sample(case)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded fractal terrain; no dataset)",
+            "config": dict(config_dict(), arith=args.arith, nx=NX, ny=NY),
+            "e2e": e2e,
+            "gpu_launches": launches,
+            "roofline": {
+                "bound": "hbm", "achieved": achieved_gbs, "peak": HBM_GBS, "unit": "GB/s",
+                "frac": achieved_gbs / HBM_GBS, "traffic": profile.get("traffic_bytes_per_launch"),
+                "peak_source": HBM_SRC,
+                "kernel": "k_hydro_tile<double,%s,LevelSrc>" % ("true" if arith else "false"),
+                "kernel_ms": kms, "algorithmic_bytes_per_launch": BYTES_PER_CELL["f64"] * cells,
+                "note": "FP64-issue bound on GB300: see fp64_pipe",
+                "fp64_pipe": fp64_pipe(profile, kms),
+            },
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def load_profile_summary():
+    """Per-launch DRAM traffic and FP64 instruction counts of the dominant
+    kernel from the committed ncu summary (profiles/), when present."""
+    p = ROOT / "profiles" / "k_hydro_tile_metrics.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except ValueError:
+            return {}
+    return {}
+
+
+def fp64_pipe(profile, kms):
+    """Achieved FP64 instruction rate of the dominant kernel against the
+    measured DFMA issue rate (the binding roof of the FP64 advance)."""
+    inst = profile.get("fp64_inst_per_cell")
+    if not inst:
+        return {"peak_dfma_per_s": FP64_DFMA_PER_S, "achieved": None, "frac": None}
+    cells = NX * NY
+    rate = inst * cells / (kms * 1e-3)
+    return {"peak_dfma_per_s": FP64_DFMA_PER_S, "achieved_inst_per_s": rate, "frac": rate / FP64_DFMA_PER_S,
+            "inst_per_cell": inst, "source": "ncu smsp__inst_executed_pipe_fp64 per cell (profiles/)"}
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,528 @@
+// C-ABI layer: argument checks, view conversion and launches.  Sees only the
+// launcher declarations (hx_launch.h), never the kernel bodies, so each
+// arithmetic form is compiled exactly once with its own flags.
+#include <atomic>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "hx_launch.h"
+
+using namespace hx;
+
+namespace {
+
+thread_local std::string g_err;
+std::atomic<unsigned long long> g_launches{0};
+
+int fail(int code, const char* fmt, ...) __attribute__((format(printf, 2, 3)));
+int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+int launched(cudaError_t e, const char* what, int n = 1) {
+    if (e != cudaSuccess) return fail(HX_ERR_LAUNCH, "%s: %s", what, cudaGetErrorString(e));
+    g_launches.fetch_add((unsigned long long)n, std::memory_order_relaxed);
+    return HX_OK;
+}
+
+template <class A> struct Elem;
+template <> struct Elem<hx_array4_f64> { using T = double; };
+template <> struct Elem<hx_array4_f32> { using T = float; };
+template <> struct Elem<hx_array4_i8> { using T = signed char; };
+
+template <class A> V4<typename Elem<A>::T> to_v4(const A& a) {
+    V4<typename Elem<A>::T> v;
+    v.p = a.p;
+    v.js = a.jstride;
+    v.ns = a.nstride;
+    v.lo0 = a.lo[0];
+    v.lo1 = a.lo[1];
+    v.hi0 = a.hi[0];
+    v.hi1 = a.hi[1];
+    v.nc = a.ncomp;
+    return v;
+}
+
+// The view must hold comps [0, ncomp) over [lo0-g, hi0+g] x [lo1-g, hi1+g].
+template <class A> bool covers(const A* a, const hx_box& b, int g, int ncomp, const char* name) {
+    if (!a || !a->p) { fail(HX_ERR_ARG, "%s: null view", name); return false; }
+    if (a->ncomp < ncomp) { fail(HX_ERR_ARG, "%s: needs %d components, has %d", name, ncomp, a->ncomp); return false; }
+    if (a->lo[0] > b.lo[0] - g || a->lo[1] > b.lo[1] - g || a->hi[0] < b.hi[0] + g || a->hi[1] < b.hi[1] + g) {
+        fail(HX_ERR_ARG, "%s: view [%d,%d]x[%d,%d] does not cover [%d,%d]x[%d,%d]", name, a->lo[0], a->hi[0], a->lo[1],
+             a->hi[1], b.lo[0] - g, b.hi[0] + g, b.lo[1] - g, b.hi[1] + g);
+        return false;
+    }
+    if (a->jstride < (int64_t)(a->hi[0] - a->lo[0] + 1)) { fail(HX_ERR_ARG, "%s: jstride too small", name); return false; }
+    return true;
+}
+
+bool box_ok(const hx_box& b) {
+    if (b.hi[0] < b.lo[0] || b.hi[1] < b.lo[1]) { fail(HX_ERR_ARG, "empty box"); return false; }
+    return true;
+}
+
+IBox ibox(const hx_box& b) { return IBox{b.lo[0], b.lo[1], b.hi[0], b.hi[1]}; }
+
+template <class A> Cells3<typename Elem<A>::T> cells3(const A& a) {
+    Cells3<typename Elem<A>::T> c;
+    for (int k = 0; k < 3; ++k) c.p[k] = a.p + (int64_t)k * a.nstride;
+    c.js = a.jstride;
+    c.lo0 = a.lo[0];
+    c.lo1 = a.lo[1];
+    return c;
+}
+template <class A> Cells3W<typename Elem<A>::T> cells3w(const A& a) {
+    Cells3W<typename Elem<A>::T> c;
+    for (int k = 0; k < 3; ++k) c.p[k] = a.p + (int64_t)k * a.nstride;
+    c.js = a.jstride;
+    c.lo0 = a.lo[0];
+    c.lo1 = a.lo[1];
+    return c;
+}
+template <class A> Plane<typename Elem<A>::T> plane(const A& a, int comp) {
+    Plane<typename Elem<A>::T> p;
+    p.p = a.p + (int64_t)comp * a.nstride;
+    p.js = a.jstride;
+    p.lo0 = a.lo[0];
+    p.lo1 = a.lo[1];
+    return p;
+}
+
+template <class R> StepCtl<R> host_ctl(R dt, R dx, R dy, hx_dt_accum* next_dt, uint32_t* status) {
+    StepCtl<R> c;
+    c.dt_host = dt;
+    c.cfl = R(1);
+    c.dt_in = nullptr;
+    c.dt_out = reinterpret_cast<DtAccum*>(next_dt);
+    c.dt_reset = nullptr;
+    c.status = status;
+    c.time = nullptr;
+    c.dx = dx;
+    c.dy = dy;
+    return c;
+}
+
+// ---------------------------------------------------------------- box forms
+template <class R, class A>
+int advance_box_hydro(const A* eta, const A* Ue, const A* Te, const A* Uo, A* Un, hx_box vb, R dt, R dx, R dy,
+                      const A* FL, const A* FR, hx_dt_accum* nd, uint32_t* status, int arith, cudaStream_t st) {
+    if (!box_ok(vb)) return HX_ERR_ARG;
+    if (!covers(eta, vb, 2, 1, "eta_ext") || !covers(Ue, vb, 2, 3, "U_ext") || !covers(Te, vb, 2, 2, "T_ext") ||
+        !covers(Uo, vb, 0, 3, "U_old") || !covers(Un, vb, 0, 3, "U_new"))
+        return HX_ERR_ARG;
+    if (!(dx > R(0)) || !(dy > R(0))) return fail(HX_ERR_ARG, "dx, dy must be positive");
+    FaceOut<R> fo{};
+    fo.on = 0;
+    if (FL || FR) {
+        if (!FL || !FR) return fail(HX_ERR_ARG, "FL and FR come together");
+        hx_box bx{{vb.lo[0], vb.lo[1]}, {vb.hi[0] + 1, vb.hi[1]}};
+        hx_box by{{vb.lo[0], vb.lo[1]}, {vb.hi[0], vb.hi[1] + 1}};
+        if (!covers(&FL[0], bx, 0, 3, "FL[x]") || !covers(&FR[0], bx, 0, 3, "FR[x]") ||
+            !covers(&FL[1], by, 0, 3, "FL[y]") || !covers(&FR[1], by, 0, 3, "FR[y]"))
+            return HX_ERR_ARG;
+        for (int d = 0; d < 2; ++d) { fo.FL[d] = to_v4(FL[d]); fo.FR[d] = to_v4(FR[d]); }
+        fo.on = 1;
+    }
+    BoxSrc<R> src;
+    src.eta = to_v4(*eta);
+    src.U = to_v4(*Ue);
+    src.T = to_v4(*Te);
+    src.glo0 = vb.lo[0] - 2; src.glo1 = vb.lo[1] - 2; src.ghi0 = vb.hi[0] + 2; src.ghi1 = vb.hi[1] + 2;
+    const StepCtl<R> ctl = host_ctl<R>(dt, dx, dy, nd, status);
+    cudaError_t e = (arith == HX_ARITH_EXACT)
+                        ? launch_hydro<R, false, BoxSrc<R>>(src, cells3(*Uo), plane(*Te, 1), cells3w(*Un), fo, ibox(vb), ctl, st)
+                        : launch_hydro<R, true, BoxSrc<R>>(src, cells3(*Uo), plane(*Te, 1), cells3w(*Un), fo, ibox(vb), ctl, st);
+    return launched(e, "hx_advance_box_hydrostatic");
+}
+
+template <class R, class A>
+int advance_box_roe(const A* eta, A* Uo, const A* T, A* Un, hx_box vb, R dt, R dx, R dy, const A* F, const A* Sm,
+                    const A* Sp, hx_dt_accum* nd, uint32_t* status, int arith, cudaStream_t st) {
+    if (!box_ok(vb)) return HX_ERR_ARG;
+    if (!covers(eta, vb, 1, 1, "eta") || !covers(Uo, vb, 1, 3, "U_old") || !covers(T, vb, 1, 2, "T") ||
+        !covers(Un, vb, 0, 3, "U_new"))
+        return HX_ERR_ARG;
+    if (!(dx > R(0)) || !(dy > R(0))) return fail(HX_ERR_ARG, "dx, dy must be positive");
+    FaceOut9<R> fo{};
+    fo.on = 0;
+    if (F || Sm || Sp) {
+        if (!F || !Sm || !Sp) return fail(HX_ERR_ARG, "F, Sm and Sp come together");
+        hx_box bx{{vb.lo[0], vb.lo[1]}, {vb.hi[0] + 1, vb.hi[1]}};
+        hx_box by{{vb.lo[0], vb.lo[1]}, {vb.hi[0], vb.hi[1] + 1}};
+        for (int d = 0; d < 2; ++d) {
+            const hx_box& b = d ? by : bx;
+            if (!covers(&F[d], b, 0, 3, "F") || !covers(&Sm[d], b, 0, 3, "Sm") || !covers(&Sp[d], b, 0, 3, "Sp"))
+                return HX_ERR_ARG;
+            fo.F[d] = to_v4(F[d]); fo.Sm[d] = to_v4(Sm[d]); fo.Sp[d] = to_v4(Sp[d]);
+        }
+        fo.on = 1;
+    }
+    BoxSrc<R> src;
+    src.eta = to_v4(*eta);
+    src.U = to_v4(*Uo);
+    src.T = to_v4(*T);
+    src.glo0 = vb.lo[0] - 1; src.glo1 = vb.lo[1] - 1; src.ghi0 = vb.hi[0] + 1; src.ghi1 = vb.hi[1] + 1;
+    RebuildOut<R> hb;
+    hb.U = to_v4(*Uo);
+    hb.on = 1;
+    const StepCtl<R> ctl = host_ctl<R>(dt, dx, dy, nd, status);
+    cudaError_t e = (arith == HX_ARITH_EXACT)
+                        ? launch_classic<R, false, BoxSrc<R>>(src, cells3w(*Un), fo, hb, ibox(vb), ctl, st)
+                        : launch_classic<R, true, BoxSrc<R>>(src, cells3w(*Un), fo, hb, ibox(vb), ctl, st);
+    return launched(e, "hx_advance_box_roe");
+}
+
+template <class R, class A>
+int dt_reduce_box(const A* U, const A* T, hx_box vb, R dx, R dy, hx_dt_accum* acc, cudaStream_t st) {
+    if (!box_ok(vb)) return HX_ERR_ARG;
+    if (!covers(U, vb, 0, 3, "U") || !covers(T, vb, 0, 1, "T")) return HX_ERR_ARG;
+    if (!acc) return fail(HX_ERR_ARG, "null accumulator");
+    // exact form: the bound is a monotone function of exactly rounded terms
+    return launched(launch_dt_reduce<R, false>(cells3(*U), plane(*T, 0), ibox(vb), dx, dy,
+                                               reinterpret_cast<DtAccum*>(acc), st),
+                    "hx_dt_reduce_box");
+}
+
+template <class R, class A>
+int tag_box(int method, const A* U, const A* T, hx_array4_i8* tags, hx_box vb, R dx, R dy, R time, R hth, R uth,
+            R zth, signed char setv, cudaStream_t st) {
+    if (!box_ok(vb)) return HX_ERR_ARG;
+    if (method != HX_METHOD_ROE && method != HX_METHOD_HYDROSTATIC_ROE) return fail(HX_ERR_ARG, "unknown method");
+    if (!covers(U, vb, 1, 3, "U") || !covers(T, vb, 1, 1, "T") || !covers(tags, vb, 0, 1, "tags")) return HX_ERR_ARG;
+    return launched(launch_tag<R>(method, to_v4(*U), to_v4(*T), to_v4(*tags), ibox(vb), dx, dy, time, hth, uth, zth,
+                                  setv, st),
+                    "hx_tag_box");
+}
+
+template <class R, class A>
+int mavg_box(const A* fine, A* crse, hx_box cb, int scomp, int ccomp, int ncomp, int rx, int ry, R fv, R nodata,
+             cudaStream_t st) {
+    if (!box_ok(cb)) return HX_ERR_ARG;
+    if (rx < 1 || ry < 1 || ncomp < 1 || scomp < 0 || ccomp < 0) return fail(HX_ERR_ARG, "bad ratio or components");
+    hx_box fb{{cb.lo[0] * rx, cb.lo[1] * ry}, {cb.hi[0] * rx + rx - 1, cb.hi[1] * ry + ry - 1}};
+    if (!covers(fine, fb, 0, scomp + ncomp, "fine") || !covers(crse, cb, 0, ccomp + ncomp, "crse")) return HX_ERR_ARG;
+    return launched(launch_masked_avgdown<R>(to_v4(*fine), to_v4(*crse), ibox(cb), scomp, ccomp, ncomp, rx, ry, fv,
+                                             nodata, st),
+                    "hx_masked_average_down_box");
+}
+
+// ---------------------------------------------------------------- level forms
+template <class L> bool level_ok(const L* lv) {
+    if (!lv || !lv->h || !lv->hu || !lv->hv || !lv->z || !lv->n) { fail(HX_ERR_ARG, "level: null plane"); return false; }
+    if (lv->nx < 2 || lv->ny < 2) { fail(HX_ERR_ARG, "level: nx, ny must be >= 2"); return false; }
+    if (lv->pitch < lv->nx) { fail(HX_ERR_ARG, "level: pitch < nx"); return false; }
+    if (!(lv->dx > 0) || !(lv->dy > 0)) { fail(HX_ERR_ARG, "level: dx, dy must be positive"); return false; }
+    return true;
+}
+
+template <class R, class L> LevelSrc<R> level_src(const L* lv, int g) {
+    LevelSrc<R> s;
+    s.h = lv->h; s.hu = lv->hu; s.hv = lv->hv; s.z = lv->z; s.n = lv->n;
+    s.pitch = lv->pitch;
+    s.nx = lv->nx; s.ny = lv->ny;
+    s.bc_xlo = lv->bc_lo[0]; s.bc_ylo = lv->bc_lo[1]; s.bc_xhi = lv->bc_hi[0]; s.bc_yhi = lv->bc_hi[1];
+    s.glo0 = -g; s.glo1 = -g; s.ghi0 = lv->nx - 1 + g; s.ghi1 = lv->ny - 1 + g;
+    return s;
+}
+
+template <class R, class L>
+int level_advance(int method, const L* lv, const StepCtl<R>& ctl, R* ho, R* huo, R* hvo, int arith, cudaStream_t st) {
+    const IBox vb{0, 0, lv->nx - 1, lv->ny - 1};
+    Cells3W<R> out;
+    out.p[0] = ho; out.p[1] = huo; out.p[2] = hvo;
+    out.js = lv->pitch; out.lo0 = 0; out.lo1 = 0;
+    cudaError_t e;
+    if (method == HX_METHOD_HYDROSTATIC_ROE) {
+        Cells3<R> uo;
+        uo.p[0] = lv->h; uo.p[1] = lv->hu; uo.p[2] = lv->hv;
+        uo.js = lv->pitch; uo.lo0 = 0; uo.lo1 = 0;
+        Plane<R> np{lv->n, lv->pitch, 0, 0};
+        FaceOut<R> fo{};
+        fo.on = 0;
+        const LevelSrc<R> src = level_src<R>(lv, 2);
+        e = (arith == HX_ARITH_EXACT) ? launch_hydro<R, false, LevelSrc<R>>(src, uo, np, out, fo, vb, ctl, st)
+                                      : launch_hydro<R, true, LevelSrc<R>>(src, uo, np, out, fo, vb, ctl, st);
+    } else {
+        FaceOut9<R> fo{};
+        fo.on = 0;
+        RebuildOut<R> hb{};
+        hb.on = 0;
+        const LevelSrc<R> src = level_src<R>(lv, 1);
+        e = (arith == HX_ARITH_EXACT) ? launch_classic<R, false, LevelSrc<R>>(src, out, fo, hb, vb, ctl, st)
+                                      : launch_classic<R, true, LevelSrc<R>>(src, out, fo, hb, vb, ctl, st);
+    }
+    return launched(e, "hx_level_advance");
+}
+
+template <class R, class L> int level_dt(const L* lv, hx_dt_accum* acc, cudaStream_t st) {
+    if (!level_ok(lv)) return HX_ERR_ARG;
+    if (!acc) return fail(HX_ERR_ARG, "null accumulator");
+    Cells3<R> U;
+    U.p[0] = lv->h; U.p[1] = lv->hu; U.p[2] = lv->hv;
+    U.js = lv->pitch; U.lo0 = 0; U.lo1 = 0;
+    Plane<R> Z{lv->z, lv->pitch, 0, 0};
+    const IBox vb{0, 0, lv->nx - 1, lv->ny - 1};
+    return launched(launch_dt_reduce<R, false>(U, Z, vb, lv->dx, lv->dy, reinterpret_cast<DtAccum*>(acc), st),
+                    "hx_level_dt_reduce");
+}
+
+constexpr int64_t kRunWork = 3 * (int64_t)sizeof(DtAccum);
+
+template <class R, class L>
+int level_run(int method, L* lv, R* ha, R* hua, R* hva, int nsteps, R cfl, void* work, uint32_t* status, R* time_dev,
+              int arith, int* final_in_alt, cudaStream_t st) {
+    if (!level_ok(lv)) return HX_ERR_ARG;
+    if (!ha || !hua || !hva) return fail(HX_ERR_ARG, "null alternate planes");
+    if (!work) return fail(HX_ERR_ARG, "null work buffer");
+    if (nsteps < 0) return fail(HX_ERR_ARG, "nsteps < 0");
+    if (!(cfl > R(0))) return fail(HX_ERR_ARG, "cfl must be positive");
+    if (method != HX_METHOD_ROE && method != HX_METHOD_HYDROSTATIC_ROE) return fail(HX_ERR_ARG, "unknown method");
+    DtAccum* slot = reinterpret_cast<DtAccum*>(work);
+    cudaError_t e = cudaMemsetAsync(slot, 0, 2 * sizeof(DtAccum), st);
+    if (e != cudaSuccess) return fail(HX_ERR_CUDA, "memset: %s", cudaGetErrorString(e));
+    int rc = level_dt<R>(lv, reinterpret_cast<hx_dt_accum*>(&slot[0]), st);
+    if (rc) return rc;
+    const R* A[3] = {lv->h, lv->hu, lv->hv};
+    R* B[3] = {ha, hua, hva};
+    L cur = *lv;
+    for (int s = 0; s < nsteps; ++s) {
+        StepCtl<R> ctl;
+        ctl.dt_host = R(0);
+        ctl.cfl = cfl;
+        ctl.dt_in = &slot[s % 3];
+        ctl.dt_out = &slot[(s + 1) % 3];
+        ctl.dt_reset = &slot[(s + 2) % 3];
+        ctl.status = status;
+        ctl.time = time_dev;
+        ctl.dx = lv->dx;
+        ctl.dy = lv->dy;
+        const bool even = (s % 2) == 0;
+        cur.h = even ? A[0] : B[0];
+        cur.hu = even ? A[1] : B[1];
+        cur.hv = even ? A[2] : B[2];
+        R* o0 = even ? B[0] : const_cast<R*>(A[0]);
+        R* o1 = even ? B[1] : const_cast<R*>(A[1]);
+        R* o2 = even ? B[2] : const_cast<R*>(A[2]);
+        rc = level_advance<R>(method, &cur, ctl, o0, o1, o2, arith, st);
+        if (rc) return rc;
+    }
+    if (final_in_alt) *final_in_alt = nsteps % 2;
+    return HX_OK;
+}
+
+template <class R> int accum_read(const hx_dt_accum* acc, R* dtmin, R* maxvel, cudaStream_t st) {
+    if (!acc) return fail(HX_ERR_ARG, "null accumulator");
+    DtAccum h;
+    cudaError_t e = cudaMemcpyAsync(&h, acc, sizeof h, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return fail(HX_ERR_CUDA, "accumulator read: %s", cudaGetErrorString(e));
+    if (dtmin) *dtmin = accum_dt_min<R>(h.rate_bits, h.flags);
+    if (maxvel) *maxvel = from_bits<R>(h.maxvel_bits);
+    return (h.flags & DTF_NAN) ? HX_STATUS_NAN : HX_OK;
+}
+
+// ---------------------------------------------------------------- host form
+struct HostCache {
+    void* base = nullptr;
+    size_t bytes = 0;
+    ~HostCache() { if (base) cudaFree(base); }
+};
+thread_local HostCache g_host;
+
+}  // namespace
+
+// ============================================================================
+extern "C" {
+
+const char* hx_version(void) { return "hydroexa_gb300 0.1.0 (sm_103a)"; }
+const char* hx_last_error(void) { return g_err.c_str(); }
+uint64_t hx_launch_count(void) { return g_launches.load(); }
+
+int hx_status_clear(uint32_t* s, hx_stream_t st) {
+    if (!s) return fail(HX_ERR_ARG, "null status");
+    cudaError_t e = cudaMemsetAsync(s, 0, sizeof(uint32_t), (cudaStream_t)st);
+    return e == cudaSuccess ? HX_OK : fail(HX_ERR_CUDA, "status clear: %s", cudaGetErrorString(e));
+}
+
+int hx_status_read(const uint32_t* s, hx_stream_t st) {
+    if (!s) return fail(HX_ERR_ARG, "null status");
+    uint32_t v = 0;
+    cudaError_t e = cudaMemcpyAsync(&v, s, sizeof v, cudaMemcpyDeviceToHost, (cudaStream_t)st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)st);
+    if (e != cudaSuccess) return fail(HX_ERR_CUDA, "status read: %s", cudaGetErrorString(e));
+    return (int)(v & 0x7fffffffu);
+}
+
+int64_t hx_dt_accum_bytes(void) { return (int64_t)sizeof(DtAccum); }
+
+int hx_dt_accum_reset(hx_dt_accum* acc, hx_stream_t st) {
+    if (!acc) return fail(HX_ERR_ARG, "null accumulator");
+    cudaError_t e = cudaMemsetAsync(acc, 0, sizeof(DtAccum), (cudaStream_t)st);
+    return e == cudaSuccess ? HX_OK : fail(HX_ERR_CUDA, "accumulator reset: %s", cudaGetErrorString(e));
+}
+int hx_dt_accum_read_f64(const hx_dt_accum* a, double* m, double* v, hx_stream_t st) {
+    return accum_read<double>(a, m, v, (cudaStream_t)st);
+}
+int hx_dt_accum_read_f32(const hx_dt_accum* a, float* m, float* v, hx_stream_t st) {
+    return accum_read<float>(a, m, v, (cudaStream_t)st);
+}
+
+int hx_advance_box_hydrostatic_f64(const hx_array4_f64* eta, const hx_array4_f64* Ue, const hx_array4_f64* Te,
+                                   const hx_array4_f64* Uo, hx_array4_f64* Un, hx_box vb, double dt, double dx,
+                                   double dy, const hx_array4_f64* FL, const hx_array4_f64* FR, hx_dt_accum* nd,
+                                   uint32_t* status, int arith, hx_stream_t st) {
+    return advance_box_hydro<double>(eta, Ue, Te, Uo, Un, vb, dt, dx, dy, FL, FR, nd, status, arith, (cudaStream_t)st);
+}
+int hx_advance_box_hydrostatic_f32(const hx_array4_f32* eta, const hx_array4_f32* Ue, const hx_array4_f32* Te,
+                                   const hx_array4_f32* Uo, hx_array4_f32* Un, hx_box vb, float dt, float dx,
+                                   float dy, const hx_array4_f32* FL, const hx_array4_f32* FR, hx_dt_accum* nd,
+                                   uint32_t* status, int arith, hx_stream_t st) {
+    return advance_box_hydro<float>(eta, Ue, Te, Uo, Un, vb, dt, dx, dy, FL, FR, nd, status, arith, (cudaStream_t)st);
+}
+int hx_advance_box_roe_f64(const hx_array4_f64* eta, hx_array4_f64* Uo, const hx_array4_f64* T, hx_array4_f64* Un,
+                           hx_box vb, double dt, double dx, double dy, const hx_array4_f64* F,
+                           const hx_array4_f64* Sm, const hx_array4_f64* Sp, hx_dt_accum* nd, uint32_t* status,
+                           int arith, hx_stream_t st) {
+    return advance_box_roe<double>(eta, Uo, T, Un, vb, dt, dx, dy, F, Sm, Sp, nd, status, arith, (cudaStream_t)st);
+}
+int hx_advance_box_roe_f32(const hx_array4_f32* eta, hx_array4_f32* Uo, const hx_array4_f32* T, hx_array4_f32* Un,
+                           hx_box vb, float dt, float dx, float dy, const hx_array4_f32* F, const hx_array4_f32* Sm,
+                           const hx_array4_f32* Sp, hx_dt_accum* nd, uint32_t* status, int arith, hx_stream_t st) {
+    return advance_box_roe<float>(eta, Uo, T, Un, vb, dt, dx, dy, F, Sm, Sp, nd, status, arith, (cudaStream_t)st);
+}
+int hx_dt_reduce_box_f64(const hx_array4_f64* U, const hx_array4_f64* T, hx_box vb, double dx, double dy,
+                         hx_dt_accum* acc, hx_stream_t st) {
+    return dt_reduce_box<double>(U, T, vb, dx, dy, acc, (cudaStream_t)st);
+}
+int hx_dt_reduce_box_f32(const hx_array4_f32* U, const hx_array4_f32* T, hx_box vb, float dx, float dy,
+                         hx_dt_accum* acc, hx_stream_t st) {
+    return dt_reduce_box<float>(U, T, vb, dx, dy, acc, (cudaStream_t)st);
+}
+int hx_tag_box_f64(int method, const hx_array4_f64* U, const hx_array4_f64* T, hx_array4_i8* tags, hx_box vb,
+                   double dx, double dy, double time, double h, double u, double z, signed char sv, hx_stream_t st) {
+    return tag_box<double>(method, U, T, tags, vb, dx, dy, time, h, u, z, sv, (cudaStream_t)st);
+}
+int hx_tag_box_f32(int method, const hx_array4_f32* U, const hx_array4_f32* T, hx_array4_i8* tags, hx_box vb,
+                   float dx, float dy, float time, float h, float u, float z, signed char sv, hx_stream_t st) {
+    return tag_box<float>(method, U, T, tags, vb, dx, dy, time, h, u, z, sv, (cudaStream_t)st);
+}
+int hx_masked_average_down_box_f64(const hx_array4_f64* fine, hx_array4_f64* crse, hx_box cb, int scomp, int ccomp,
+                                   int ncomp, int rx, int ry, double fv, double nodata, hx_stream_t st) {
+    return mavg_box<double>(fine, crse, cb, scomp, ccomp, ncomp, rx, ry, fv, nodata, (cudaStream_t)st);
+}
+int hx_masked_average_down_box_f32(const hx_array4_f32* fine, hx_array4_f32* crse, hx_box cb, int scomp, int ccomp,
+                                   int ncomp, int rx, int ry, float fv, float nodata, hx_stream_t st) {
+    return mavg_box<float>(fine, crse, cb, scomp, ccomp, ncomp, rx, ry, fv, nodata, (cudaStream_t)st);
+}
+
+int hx_level_advance_f64(int method, const hx_level_f64* L, double dt, double* ho, double* huo, double* hvo,
+                         hx_dt_accum* nd, uint32_t* status, int arith, hx_stream_t st) {
+    if (!level_ok(L)) return HX_ERR_ARG;
+    if (!ho || !huo || !hvo) return fail(HX_ERR_ARG, "null output planes");
+    if (method != HX_METHOD_ROE && method != HX_METHOD_HYDROSTATIC_ROE) return fail(HX_ERR_ARG, "unknown method");
+    return level_advance<double>(method, L, host_ctl<double>(dt, L->dx, L->dy, nd, status), ho, huo, hvo, arith,
+                                 (cudaStream_t)st);
+}
+int hx_level_advance_f32(int method, const hx_level_f32* L, float dt, float* ho, float* huo, float* hvo,
+                         hx_dt_accum* nd, uint32_t* status, int arith, hx_stream_t st) {
+    if (!level_ok(L)) return HX_ERR_ARG;
+    if (!ho || !huo || !hvo) return fail(HX_ERR_ARG, "null output planes");
+    if (method != HX_METHOD_ROE && method != HX_METHOD_HYDROSTATIC_ROE) return fail(HX_ERR_ARG, "unknown method");
+    return level_advance<float>(method, L, host_ctl<float>(dt, L->dx, L->dy, nd, status), ho, huo, hvo, arith,
+                                (cudaStream_t)st);
+}
+int hx_level_dt_reduce_f64(const hx_level_f64* L, hx_dt_accum* acc, hx_stream_t st) {
+    return level_dt<double>(L, acc, (cudaStream_t)st);
+}
+int hx_level_dt_reduce_f32(const hx_level_f32* L, hx_dt_accum* acc, hx_stream_t st) {
+    return level_dt<float>(L, acc, (cudaStream_t)st);
+}
+
+int64_t hx_level_run_work_bytes(void) { return kRunWork; }
+
+int hx_level_run_f64(int method, hx_level_f64* L, double* ha, double* hua, double* hva, int nsteps, double cfl,
+                     void* work, uint32_t* status, double* time_dev, int arith, int* fin, hx_stream_t st) {
+    return level_run<double>(method, L, ha, hua, hva, nsteps, cfl, work, status, time_dev, arith, fin,
+                             (cudaStream_t)st);
+}
+int hx_level_run_f32(int method, hx_level_f32* L, float* ha, float* hua, float* hva, int nsteps, float cfl,
+                     void* work, uint32_t* status, float* time_dev, int arith, int* fin, hx_stream_t st) {
+    return level_run<float>(method, L, ha, hua, hva, nsteps, cfl, work, status, time_dev, arith, fin,
+                            (cudaStream_t)st);
+}
+
+int hx_level_run_host_f64(int method, int nx, int ny, double dx, double dy, const int32_t bc_lo[2],
+                          const int32_t bc_hi[2], double* h, double* hu, double* hv, const double* z, const double* n,
+                          int nsteps, double cfl, int arith, double* time_out, hx_stream_t stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    if (nx < 2 || ny < 2) return fail(HX_ERR_ARG, "nx, ny must be >= 2");
+    if (!h || !hu || !hv || !z || !n || !bc_lo || !bc_hi) return fail(HX_ERR_ARG, "null host buffer");
+    const size_t N = (size_t)nx * ny, pb = N * sizeof(double);
+    const size_t need = 8 * pb + 512;
+    if (g_host.bytes < need) {
+        if (g_host.base) cudaFree(g_host.base);
+        g_host.base = nullptr;
+        g_host.bytes = 0;
+        cudaError_t e = cudaMalloc(&g_host.base, need);
+        if (e != cudaSuccess) return fail(HX_ERR_CUDA, "device buffers: %s", cudaGetErrorString(e));
+        g_host.bytes = need;
+    }
+    double* d = (double*)g_host.base;
+    double* P[8];
+    for (int k = 0; k < 8; ++k) P[k] = d + k * N;
+    char* tail = (char*)(d + 8 * N);
+    uint32_t* status = (uint32_t*)tail;
+    double* tdev = (double*)(tail + 64);
+    void* work = tail + 128;
+    const double* src[5] = {h, hu, hv, z, n};
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < 5 && e == cudaSuccess; ++k) e = cudaMemcpyAsync(P[k], src[k], pb, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(tail, 0, 128, st);
+    if (e != cudaSuccess) return fail(HX_ERR_CUDA, "upload: %s", cudaGetErrorString(e));
+    hx_level_f64 L{P[0], P[1], P[2], P[3], P[4], (int64_t)nx, nx, ny, dx, dy, {bc_lo[0], bc_lo[1]}, {bc_hi[0], bc_hi[1]}};
+    int fin = 0;
+    int rc = level_run<double>(method, &L, P[5], P[6], P[7], nsteps, cfl, work, status, tdev, arith, &fin, st);
+    if (rc) return rc;
+    double* res[3] = {fin ? P[5] : P[0], fin ? P[6] : P[1], fin ? P[7] : P[2]};
+    double* dst[3] = {h, hu, hv};
+    for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = cudaMemcpyAsync(dst[k], res[k], pb, cudaMemcpyDeviceToHost, st);
+    uint32_t sv = 0;
+    double tv = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&sv, status, 4, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&tv, tdev, 8, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return fail(HX_ERR_CUDA, "download: %s", cudaGetErrorString(e));
+    if (time_out) *time_out = tv;
+    return (int)sv;
+}
+
+void hx_host_cache_release(void) {
+    if (g_host.base) cudaFree(g_host.base);
+    g_host.base = nullptr;
+    g_host.bytes = 0;
+}
+
+int hx_debug_roe_points_f64(int method, int arith, long n, const double* st, const double* aux, double* out,
+                            hx_stream_t s) {
+    if (n < 0 || (n > 0 && (!st || !aux || !out))) return fail(HX_ERR_ARG, "bad point arrays");
+    cudaError_t e = arith == HX_ARITH_EXACT ? launch_points<double, false>(method, n, st, aux, out, (cudaStream_t)s)
+                                            : launch_points<double, true>(method, n, st, aux, out, (cudaStream_t)s);
+    return launched(e, "hx_debug_roe_points");
+}
+int hx_debug_roe_points_f32(int method, int arith, long n, const float* st, const float* aux, float* out,
+                            hx_stream_t s) {
+    if (n < 0 || (n > 0 && (!st || !aux || !out))) return fail(HX_ERR_ARG, "bad point arrays");
+    cudaError_t e = arith == HX_ARITH_EXACT ? launch_points<float, false>(method, n, st, aux, out, (cudaStream_t)s)
+                                            : launch_points<float, true>(method, n, st, aux, out, (cudaStream_t)s);
+    return launched(e, "hx_debug_roe_points");
+}
+
+}  // extern "C"

@@ -1,0 +1,446 @@
+// Device building blocks of the GB300 per-level advance: constants, point
+// Riemann solvers, limiter, ghost rules and the dt accumulator.
+//
+// Two arithmetic forms of every formula:
+//   FAST == false  repeats the reference's operation order term by term; the
+//                  translation unit that instantiates it is compiled with
+//                  --fmad=false, so results equal the reference's host
+//                  arithmetic bit for bit (sqrt and division are IEEE in both;
+//                  only cbrt in the Manning factor may differ by an ulp).
+//   FAST == true   same mathematics with shared reciprocals and square roots
+//                  and contracted multiply-adds: ~1e-15 relative per step.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/hydroexa_gb300.h"
+
+namespace hx {
+
+template <class R> struct Cst;
+template <> struct Cst<double> {
+    // include/utils/Constants.H:25-78
+    static constexpr double g = 9.81;
+    static constexpr double half_g = 0.5 * 9.81;
+    static constexpr double sqrt_g = 3.1320919526731650;  // sqrt(9.81), correctly rounded
+    static constexpr double toldry = 1e-6;
+    static constexpr double tol12 = 1e-12;
+    static constexpr double tol10 = 1e-10;
+};
+template <> struct Cst<float> {
+    static constexpr float g = 9.81f;
+    static constexpr float half_g = 0.5f * 9.81f;
+    static constexpr float sqrt_g = 3.13209195f;
+    static constexpr float toldry = 1e-6f;
+    static constexpr float tol12 = 1e-12f;
+    static constexpr float tol10 = 1e-10f;
+};
+
+// std::max(0, x) of the reference: (0 < x) ? x : 0 (NaN -> 0).
+template <class R> __device__ __forceinline__ R max0(R x) { return (R(0) < x) ? x : R(0); }
+template <class R> __device__ __forceinline__ R smax(R a, R b) { return (a < b) ? b : a; }
+
+// NODATA predicate of the hydrostatic face kernel and compute_dt_Impl
+// (HydrostaticRoe.cpp:41,238): |z + 9999| < 1e-10, evaluated in double as the
+// reference's literal -9999.0 forces.
+template <class R> __device__ __forceinline__ bool is_nodata(R z) {
+    return fabs((double)z + 9999.0) < 1e-10;
+}
+
+template <class R> __device__ __forceinline__ bool bits_nonfinite(R x);
+template <> __device__ __forceinline__ bool bits_nonfinite<double>(double x) {
+    return ((unsigned long long)__double_as_longlong(x) & 0x7FF0000000000000ull) == 0x7FF0000000000000ull;
+}
+template <> __device__ __forceinline__ bool bits_nonfinite<float>(float x) {
+    return ((unsigned)__float_as_uint(x) & 0x7F800000u) == 0x7F800000u;
+}
+
+// ----------------------------------------------------------------------------
+// MUSCL van Leer slope (src/solvers/HydrostaticRoe.cpp:173-195), floating abs.
+// ----------------------------------------------------------------------------
+template <class R, bool FAST> __device__ __forceinline__ R van_leer_slope(R qm, R q, R qp) {
+    const R dm = q - qm;
+    const R dp = qp - q;
+    if (fabs(dp) <= Cst<R>::tol12) return R(0);
+    if constexpr (!FAST) {
+        const R r = dm / dp;
+        return (r + fabs(r)) / (R(1) + fabs(r)) * dp;
+    } else {
+        // phi(r) dp with r = dm/dp is 0 for r <= 0 and 2 dm dp / (dm + dp) otherwise.
+        const R p = dm * dp;
+        return (p > R(0)) ? (R(2) * p) / (dm + dp) : R(0);
+    }
+}
+
+// ----------------------------------------------------------------------------
+// Homogeneous Roe flux (include/solvers/kernels/HydrostaticRoe.H:44-159) for a
+// face of direction DIR (0: normal +x, 1: normal +y).  The normal is fixed at
+// compile time, so the rotation by (nx, ny) becomes a relabelling, which is
+// value-exact.  Exact form: inputs are the face depths and global momenta.
+// ----------------------------------------------------------------------------
+template <int DIR, class R>
+__device__ __forceinline__ void roe_hydrostatic_exact(R hi, R hui, R hvi, R hj, R huj, R hvj, R& F0, R& F1,
+                                                      R& F2) {
+    using C = Cst<R>;
+    hi = (hi >= C::toldry) ? hi : R(0);
+    hj = (hj >= C::toldry) ? hj : R(0);
+    const R si = (hi > R(0)) ? sqrt(hi) : R(0);
+    const R sj = (hj > R(0)) ? sqrt(hj) : R(0);
+    const R ui = (hi > R(0)) ? hui / hi : R(0);
+    const R vi = (hi > R(0)) ? hvi / hi : R(0);
+    const R uj = (hj > R(0)) ? huj / hj : R(0);
+    const R vj = (hj > R(0)) ? hvj / hj : R(0);
+    R uni, uti, unj, utj;
+    if (DIR == 0) { uni = ui; uti = vi; unj = uj; utj = vj; }
+    else { uni = vi; uti = -ui; unj = vj; utj = -uj; }
+    const R hsum = hi + hj;
+    const R hm = (0.5 * hsum > C::toldry) ? R(0.5) * hsum : C::toldry;
+    const R cm = sqrt(C::g * hm);
+    const R sden = si + sj + C::tol12;
+    const R um = (uni * si + unj * sj) / sden;
+    const R vm = (uti * si + utj * sj) / sden;
+    R l0 = um - cm;
+    const R l1 = um;
+    R l2 = um + cm;
+    {
+        const R ci = sqrt(C::g * hi), cj = sqrt(C::g * hj);
+        R ei = uni - ci, ej = unj - cj;
+        if (ei < R(0) && ej > R(0)) l0 = ei * (ej - l0) / (ej - ei);
+        ei = uni + ci;
+        ej = unj + cj;
+        if (ei < R(0) && ej > R(0)) l2 = ej * (l2 - ei) / (ej - ei);
+    }
+    const R den = R(2) * cm + C::tol12;
+    const R dh = hj - hi;
+    const R dhu = hj * unj - hi * uni;
+    const R dhv = hj * utj - hi * uti;
+    const R a0 = (l2 * dh - dhu) / den;
+    const R a1 = (-vm * dh + dhv) / cm;
+    const R a2 = (-l0 * dh + dhu) / den;
+    R f0 = R(0.5) * (hi * uni + hj * unj);
+    R f1 = R(0.5) * (hi * uni * uni + C::half_g * hi * hi + hj * unj * unj + C::half_g * hj * hj);
+    R f2 = R(0.5) * (hi * uni * uti + hj * unj * utj);
+    const R w0 = R(0.5) * fabs(l0) * a0;
+    f0 -= w0;
+    f1 -= w0 * l0;
+    f2 -= w0 * vm;
+    const R w1 = R(0.5) * fabs(l1) * a1;  // contact wave: eigenvector (0, 0, c)
+    f2 -= w1 * cm;
+    const R w2 = R(0.5) * fabs(l2) * a2;
+    f0 -= w2;
+    f1 -= w2 * l2;
+    f2 -= w2 * vm;
+    F0 = f0;
+    if (DIR == 0) { F1 = f1; F2 = f2; }
+    else { F1 = -f2; F2 = f1; }
+}
+
+// Fast form: inputs are the face depths and face velocities (the reference
+// rebuilds the velocity as (h u)/h, which equals u to an ulp).  One division
+// serves both Roe-average quotients and one serves the three wave strengths;
+// the wave speeds sqrt(g h) reuse sqrt(h).
+template <class R, int DIR>
+__device__ __forceinline__ void roe_hydrostatic_fast(R hi, R ui, R vi, R hj, R uj, R vj, R& F0, R& F1, R& F2) {
+    using C = Cst<R>;
+    const bool wi = hi >= C::toldry, wj = hj >= C::toldry;
+    hi = wi ? hi : R(0);
+    hj = wj ? hj : R(0);
+    ui = wi ? ui : R(0);
+    vi = wi ? vi : R(0);
+    uj = wj ? uj : R(0);
+    vj = wj ? vj : R(0);
+    const R si = sqrt(hi), sj = sqrt(hj);
+    R uni, uti, unj, utj;
+    if (DIR == 0) { uni = ui; uti = vi; unj = uj; utj = vj; }
+    else { uni = vi; uti = -ui; unj = vj; utj = -uj; }
+    const R hh = R(0.5) * (hi + hj);
+    const R hm = (hh > C::toldry) ? hh : C::toldry;
+    const R cm = sqrt(C::g * hm);
+    const R den = R(2) * cm + C::tol12;
+    const R sden = si + sj + C::tol12;
+    // one division for 1/sden, 1/den and 1/cm
+    const R q = R(1) / (sden * (cm * den));
+    const R rs = (cm * den) * q;
+    const R rden = (sden * cm) * q;
+    const R rcm = (sden * den) * q;
+    const R um = (uni * si + unj * sj) * rs;
+    const R vm = (uti * si + utj * sj) * rs;
+    R l0 = um - cm;
+    const R l1 = um;
+    R l2 = um + cm;
+    {
+        const R ci = C::sqrt_g * si, cj = C::sqrt_g * sj;
+        R ei = uni - ci, ej = unj - cj;
+        if (ei < R(0) && ej > R(0)) l0 = ei * (ej - l0) / (ej - ei);
+        ei = uni + ci;
+        ej = unj + cj;
+        if (ei < R(0) && ej > R(0)) l2 = ej * (l2 - ei) / (ej - ei);
+    }
+    const R dh = hj - hi;
+    const R qi = hi * uni, qj = hj * unj;
+    const R dhu = qj - qi;
+    const R dhv = hj * utj - hi * uti;
+    const R a0 = (l2 * dh - dhu) * rden;
+    const R a1 = (dhv - vm * dh) * rcm;
+    const R a2 = (dhu - l0 * dh) * rden;
+    const R w0 = R(0.5) * fabs(l0) * a0;
+    const R w1 = R(0.5) * fabs(l1) * a1;
+    const R w2 = R(0.5) * fabs(l2) * a2;
+    const R f0 = R(0.5) * (qi + qj) - (w0 + w2);
+    const R f1 = R(0.5) * (qi * uni + qj * unj + C::half_g * (hi * hi + hj * hj)) - (w0 * l0 + w2 * l2);
+    const R f2 = R(0.5) * (qi * uti + qj * utj) - ((w0 + w2) * vm + w1 * cm);
+    F0 = f0;
+    if (DIR == 0) { F1 = f1; F2 = f2; }
+    else { F1 = -f2; F2 = f1; }
+}
+
+// ----------------------------------------------------------------------------
+// Classic Roe flux with bed-slope thrust, Manning friction and positivity
+// guard (include/solvers/kernels/Roe.H:51-309), direction fixed at compile
+// time.  Outputs F, S-, S+ in global coordinates.
+// ----------------------------------------------------------------------------
+template <class R, bool FAST, int DIR>
+__device__ __forceinline__ void roe_classic(R hi, R hui, R hvi, R zi, R ni, R hj, R huj, R hvj, R zj, R nj, R dx,
+                                            R F[3], R Sm[3], R Sp[3]) {
+    using C = Cst<R>;
+    const R T12 = C::tol12, TD = C::toldry;
+    hi = (hi >= TD) ? hi : R(0);
+    hj = (hj >= TD) ? hj : R(0);
+    R si, sj, ui, vi, uj, vj;
+    if constexpr (!FAST) {
+        si = (hi > R(0)) ? sqrt(hi) : R(0);
+        sj = (hj > R(0)) ? sqrt(hj) : R(0);
+        ui = (hi > R(0)) ? hui / hi : R(0);
+        vi = (hi > R(0)) ? hvi / hi : R(0);
+        uj = (hj > R(0)) ? huj / hj : R(0);
+        vj = (hj > R(0)) ? hvj / hj : R(0);
+    } else {
+        si = sqrt(hi);
+        sj = sqrt(hj);
+        const R ri = (hi > R(0)) ? R(1) / hi : R(0);
+        const R rj = (hj > R(0)) ? R(1) / hj : R(0);
+        ui = hui * ri; vi = hvi * ri; uj = huj * rj; vj = hvj * rj;
+    }
+    R uni, uti, unj, utj;
+    if (DIR == 0) { uni = ui; uti = vi; unj = uj; utj = vj; }
+    else { uni = vi; uti = -ui; unj = vj; utj = -uj; }
+    const R hsum = hi + hj;
+    const R hm = (R(0.5) * hsum > TD) ? R(0.5) * hsum : TD;
+    const R cm = sqrt(C::g * hm);
+    const R sden = si + sj + T12;
+    const R um = (uni * si + unj * sj) / sden;
+    const R vm = (uti * si + utj * sj) / sden;
+    R l0 = um - cm;
+    const R l1 = um;
+    R l2 = um + cm;
+    {
+        R ci, cj;
+        if constexpr (!FAST) { ci = sqrt(C::g * hi); cj = sqrt(C::g * hj); }
+        else { ci = C::sqrt_g * si; cj = C::sqrt_g * sj; }
+        R ei = uni - ci, ej = unj - cj;
+        if (ei < R(0) && ej > R(0)) l0 = ei * (ej - l0) / (ej - ei);
+        ei = uni + ci;
+        ej = unj + cj;
+        if (ei < R(0) && ej > R(0)) l2 = ej * (l2 - ei) / (ej - ei);
+    }
+    const R den = R(2) * cm + T12;
+    const R dh = hj - hi;
+    const R dhu = hj * unj - hi * uni;
+    const R dhv = hj * utj - hi * uti;
+    const R a0 = (l2 * dh - dhu) / den;
+    const R a1 = (-vm * dh + dhv) / cm;
+    const R a2 = (-l0 * dh + dhu) / den;
+
+    const R dz = zj - zi;
+    const R di = hi + zi;
+    const R dj = hj + zj;
+    const R dd = dj - di;
+    R thrust, tau;
+    {
+        const R ta = -C::g * hm * dz;
+        R dzt;
+        if ((dz >= R(0)) && (di < zj)) dzt = hi;
+        else if ((dz < R(0)) && (dj < zi)) dzt = hj;
+        else dzt = dz;
+        const R hr = (dz >= R(0)) ? hi : hj;
+        const R tb = -C::g * (hr - R(0.5) * fabs(dzt)) * dzt;
+        thrust = ((dz * dd >= R(0)) && (um * dz > R(0))) ? smax(ta, tb) : tb;
+        const R nm = R(0.5) * (ni + nj);
+        if constexpr (!FAST) {
+            const R sf = (nm * nm * sqrt(um * um + vm * vm) * um) / smax(TD, hm * cbrt(hm));
+            tau = C::g * hm * sf * dx;
+        } else {
+            // the friction term vanishes identically when the face roughness is zero
+            if (nm != R(0)) {
+                const R sf = (nm * nm * sqrt(um * um + vm * vm) * um) / smax(TD, hm * cbrt(hm));
+                tau = C::g * hm * sf * dx;
+            } else {
+                tau = R(0);
+            }
+        }
+    }
+    R b0 = (thrust - tau) / den;
+    const R b1 = R(0);
+    R b2 = -b0;
+    {
+        const R l0s = (fabs(l0) > T12) ? l0 : (l0 >= R(0) ? T12 : -T12);
+        const R l2s = (fabs(l2) > T12) ? l2 : (l2 >= R(0) ? T12 : -T12);
+        const R hi1 = hi + a0 - (b0 / l0s);
+        const R hj3 = hj - a2 + (b2 / l2s);
+        R ml = fabs(l0);
+        ml = smax(ml, fabs(l1));
+        ml = smax(ml, fabs(l2));
+        const R ldt = dx / (ml + T12);
+        const R d1 = hi - hi1;
+        const R d1s = (fabs(d1) > T12) ? d1 : (d1 >= R(0) ? T12 : -T12);
+        const R d3 = hj - hj3;
+        const R d3s = (fabs(d3) > T12) ? d3 : (d3 >= R(0) ? T12 : -T12);
+        const bool g1 = (hi1 < -TD) && (hj3 > TD);
+        const bool g3 = (hi1 > TD) && (hj3 < -TD);
+        if (g1 || g3) {
+            const R dt1 = (dx * R(0.5) / l0s) * (hi / d1s);
+            const R dt3 = (dx * R(0.5) / l2s) * (hj / d3s);
+            if (g1 && (dt1 < ldt)) {
+                const R b1min = -(hi + a0) * fabs(l0);
+                const R b3min = -(hj - a2) * l2;
+                if (-b1min >= b3min) b0 = b1min;
+                b2 = -b0;
+            }
+            if (g3 && (dt3 < ldt)) {
+                const R b1min = -(hi + a0) * fabs(l0);
+                const R b3min = -(hj - a2) * l2;
+                if (-b3min >= b1min) b2 = b3min;
+                b0 = -b2;
+            }
+        }
+    }
+    R f0 = R(0.5) * (hi * uni + hj * unj);
+    R f1 = R(0.5) * (hi * uni * uni + C::half_g * hi * hi + hj * unj * unj + C::half_g * hj * hj);
+    R f2 = R(0.5) * (hi * uni * uti + hj * unj * utj);
+    R m0 = 0, m1 = 0, m2 = 0, p0 = 0, p1 = 0, p2 = 0;
+    {
+        const R w = R(0.5) * fabs(l0) * a0;
+        f0 -= w; f1 -= w * l0; f2 -= w * vm;
+        if (l0 > R(0)) { m0 += b0; m1 += b0 * l0; m2 += b0 * vm; }
+        else if (l0 < R(0)) { p0 += b0; p1 += b0 * l0; p2 += b0 * vm; }
+    }
+    {
+        const R w = R(0.5) * fabs(l1) * a1;
+        f2 -= w * cm;
+        if (l1 > R(0)) { m2 += b1 * cm; }
+        else if (l1 < R(0)) { p2 += b1 * cm; }
+    }
+    {
+        const R w = R(0.5) * fabs(l2) * a2;
+        f0 -= w; f1 -= w * l2; f2 -= w * vm;
+        if (l2 > R(0)) { m0 += b2; m1 += b2 * l2; m2 += b2 * vm; }
+        else if (l2 < R(0)) { p0 += b2; p1 += b2 * l2; p2 += b2 * vm; }
+    }
+    F[0] = f0; Sm[0] = m0; Sp[0] = p0;
+    if (DIR == 0) {
+        F[1] = f1; F[2] = f2; Sm[1] = m1; Sm[2] = m2; Sp[1] = p1; Sp[2] = p2;
+    } else {
+        F[1] = -f2; F[2] = f1; Sm[1] = -m2; Sm[2] = m1; Sp[1] = -p2; Sp[2] = p1;
+    }
+}
+
+// ----------------------------------------------------------------------------
+// dt accumulator (hx_dt_accum).  min over cells of fl(1/x_c) equals
+// fl(1/max x_c) because rounded division is monotone, so the device keeps the
+// largest wave-speed rate x_c = (|u|+c)/dx + (|v|+c)/dy of the wet cells and
+// flags for the constant bounds of dry (1e6) and NODATA (1e30) cells.  All
+// values are non-negative, so their IEEE bit patterns order as integers.
+// ----------------------------------------------------------------------------
+struct DtAccum {
+    unsigned long long rate_bits;    // max rate over wet cells (R's bit pattern)
+    unsigned long long maxvel_bits;  // max of max(|u|,|v|)
+    unsigned int flags;              // 1: a dry cell, 2: a NODATA cell, 4: NaN seen
+    unsigned int pad[11];
+};
+static_assert(sizeof(DtAccum) == 64, "hx_dt_accum is 64 bytes");
+
+enum { DTF_DRY = 1, DTF_NODATA = 2, DTF_NAN = 4 };
+
+template <class R> __device__ __forceinline__ unsigned long long to_bits(R x);
+template <> __device__ __forceinline__ unsigned long long to_bits<double>(double x) {
+    return (unsigned long long)__double_as_longlong(x);
+}
+template <> __device__ __forceinline__ unsigned long long to_bits<float>(float x) {
+    return (unsigned long long)__float_as_uint(x);
+}
+template <class R> __host__ __device__ __forceinline__ R from_bits(unsigned long long b);
+template <> __host__ __device__ __forceinline__ double from_bits<double>(unsigned long long b) {
+    union { unsigned long long u; double d; } c;
+    c.u = b;
+    return c.d;
+}
+template <> __host__ __device__ __forceinline__ float from_bits<float>(unsigned long long b) {
+    union { unsigned u; float f; } c;
+    c.u = (unsigned)b;
+    return c.f;
+}
+
+// min CFL bound (before the CFL factor) of an accumulator: the reference's
+// 1.0 / rate evaluated in double and stored in R.
+template <class R> __host__ __device__ __forceinline__ R accum_dt_min(unsigned long long rate_bits, unsigned flags) {
+    const R rate = from_bits<R>(rate_bits);
+    R m = R(3.4e38);
+    if (sizeof(R) == 8) m = (R)1.7976931348623157e308;
+    if (rate > R(0)) m = (R)(1.0 / (double)rate);
+    if (flags & DTF_DRY) m = (m < R(1.e6)) ? m : R(1.e6);
+    if (flags & DTF_NODATA) m = (m < R(1.e30)) ? m : R(1.e30);
+    return m;
+}
+
+// Per-cell contribution of compute_dt_Impl (HydrostaticRoe.cpp:41-61).
+template <class R, bool FAST>
+__device__ __forceinline__ void dt_cell_contrib(R h, R hu, R hv, R z, R dx, R dy, R idx, R idy, R& rate, R& mv,
+                                                unsigned& flags) {
+    rate = R(0);
+    mv = R(0);
+    if (is_nodata(z)) { flags |= DTF_NODATA; return; }
+    if (!(h > Cst<R>::tol12)) { flags |= DTF_DRY; return; }
+    R u, v;
+    if constexpr (!FAST) { u = hu / h; v = hv / h; }
+    else { const R r = R(1) / h; u = hu * r; v = hv * r; }
+    const R c = sqrt(Cst<R>::g * h);
+    const R sx = fabs(u) + c;
+    const R sy = fabs(v) + c;
+    if constexpr (!FAST) rate = sx / dx + sy / dy;
+    else rate = sx * idx + sy * idy;
+    mv = smax(fabs(u), fabs(v));
+    if (bits_nonfinite(rate)) { flags |= DTF_NAN; rate = R(0); mv = R(0); }
+}
+
+// Block-wide reduction of (rate, maxvel, flags) into acc.  All threads of the
+// block must call it.  Integer max on the non-negative bit patterns.
+template <class R, int NT>
+__device__ __forceinline__ void block_fold_dt(R rate, R mv, unsigned flags, DtAccum* acc) {
+    unsigned long long rb = to_bits(rate), vb = to_bits(mv);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long r2 = __shfl_xor_sync(0xffffffffu, rb, o);
+        const unsigned long long v2 = __shfl_xor_sync(0xffffffffu, vb, o);
+        rb = r2 > rb ? r2 : rb;
+        vb = v2 > vb ? v2 : vb;
+    }
+    flags = __reduce_or_sync(0xffffffffu, flags);
+    __shared__ unsigned long long s_r[NT / 32], s_v[NT / 32];
+    __shared__ unsigned s_f[NT / 32];
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) { s_r[w] = rb; s_v[w] = vb; s_f[w] = flags; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < NT / 32; ++k) {
+            rb = s_r[k] > rb ? s_r[k] : rb;
+            vb = s_v[k] > vb ? s_v[k] : vb;
+            flags |= s_f[k];
+        }
+        if (rb) atomicMax(&acc->rate_bits, rb);
+        if (vb) atomicMax(&acc->maxvel_bits, vb);
+        if (flags) atomicOr(&acc->flags, flags);
+    }
+}
+
+}  // namespace hx

@@ -1,0 +1,27 @@
+// Fast arithmetic form: shared reciprocals and square roots, contracted
+// multiply-adds (nvcc's default --fmad=true).
+#include "hx_kernels.cuh"
+
+namespace hx {
+#define HX_INST(R)                                                                                             \
+    template cudaError_t launch_hydro<R, true, LevelSrc<R>>(const LevelSrc<R>&, const Cells3<R>&,             \
+                                                            const Plane<R>&, const Cells3W<R>&,                \
+                                                            const FaceOut<R>&, const IBox&, const StepCtl<R>&,  \
+                                                            cudaStream_t);                                     \
+    template cudaError_t launch_hydro<R, true, BoxSrc<R>>(const BoxSrc<R>&, const Cells3<R>&, const Plane<R>&, \
+                                                          const Cells3W<R>&, const FaceOut<R>&, const IBox&,   \
+                                                          const StepCtl<R>&, cudaStream_t);                    \
+    template cudaError_t launch_classic<R, true, LevelSrc<R>>(const LevelSrc<R>&, const Cells3W<R>&,          \
+                                                              const FaceOut9<R>&, const RebuildOut<R>&,        \
+                                                              const IBox&, const StepCtl<R>&, cudaStream_t);   \
+    template cudaError_t launch_classic<R, true, BoxSrc<R>>(const BoxSrc<R>&, const Cells3W<R>&,              \
+                                                            const FaceOut9<R>&, const RebuildOut<R>&,          \
+                                                            const IBox&, const StepCtl<R>&, cudaStream_t);     \
+    template cudaError_t launch_dt_reduce<R, true>(const Cells3<R>&, const Plane<R>&, const IBox&, R, R,       \
+                                                   DtAccum*, cudaStream_t);
+HX_INST(double)
+HX_INST(float)
+#undef HX_INST
+template cudaError_t launch_points<double, true>(int, long, const double*, const double*, double*, cudaStream_t);
+template cudaError_t launch_points<float, true>(int, long, const float*, const float*, float*, cudaStream_t);
+}  // namespace hx

@@ -1,0 +1,199 @@
+// Internal view types shared by the kernels and the C-ABI layer.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace hx {
+
+struct IBox {
+    int lo0, lo1, hi0, hi1;
+};
+
+// Array4-like strided view: element (i, j, c) at p[(i-lo0) + (j-lo1)*js + c*ns].
+template <class T> struct V4 {
+    T* p;
+    long long js, ns;
+    int lo0, lo1, hi0, hi1, nc;
+    __device__ __forceinline__ T ld(int i, int j, int c) const {
+        return p[(long long)(i - lo0) + (long long)(j - lo1) * js + (long long)c * ns];
+    }
+    __device__ __forceinline__ T& ref(int i, int j, int c) const {
+        return p[(long long)(i - lo0) + (long long)(j - lo1) * js + (long long)c * ns];
+    }
+};
+
+// One plane read at valid cells: (i-lo0) + (j-lo1)*js.
+template <class R> struct Plane {
+    const R* p;
+    long long js;
+    int lo0, lo1;
+    __device__ __forceinline__ R ld(int i, int j) const {
+        return __ldg(p + (long long)(i - lo0) + (long long)(j - lo1) * js);
+    }
+};
+
+// Three planes read at valid cells (the stored state u_o).
+template <class R> struct Cells3 {
+    const R* p[3];
+    long long js;
+    int lo0, lo1;
+    __device__ __forceinline__ R ld(int c, int i, int j) const {
+        return __ldg(p[c] + (long long)(i - lo0) + (long long)(j - lo1) * js);
+    }
+};
+
+// Three planes written at valid cells (U_new).
+template <class R> struct Cells3W {
+    R* p[3];
+    long long js;
+    int lo0, lo1;
+    __device__ __forceinline__ void st(int i, int j, R a, R b, R c) const {
+        const long long o = (long long)(i - lo0) + (long long)(j - lo1) * js;
+        p[0][o] = a;
+        p[1][o] = b;
+        p[2][o] = c;
+    }
+};
+
+// Optional hydrostatic face output: FL/FR nodal arrays per direction, 3 comps.
+template <class R> struct FaceOut {
+    V4<R> FL[2], FR[2];
+    int on;
+    // x face (gi, gj): FL = (F0, Fa, Fc), FR = (F0, Fb, Fc)
+    __device__ __forceinline__ void store_x(int gi, int gj, const IBox& vb, R F0, R Fa, R Fb, R Fc, bool extra) const {
+        if (!on) return;
+        if (gi < vb.lo0 || gi > vb.hi0 + 1 || gj < vb.lo1 || gj > vb.hi1) return;
+        if (extra && gi != vb.hi0 + 1) return;
+        FL[0].ref(gi, gj, 0) = F0; FL[0].ref(gi, gj, 1) = Fa; FL[0].ref(gi, gj, 2) = Fc;
+        FR[0].ref(gi, gj, 0) = F0; FR[0].ref(gi, gj, 1) = Fb; FR[0].ref(gi, gj, 2) = Fc;
+    }
+    // y face: FL = (F0, Fa, Fb), FR = (F0, Fa, Fc)
+    __device__ __forceinline__ void store_y(int gi, int gj, const IBox& vb, R F0, R Fa, R Fb, R Fc, bool extra) const {
+        if (!on) return;
+        if (gi < vb.lo0 || gi > vb.hi0 || gj < vb.lo1 || gj > vb.hi1 + 1) return;
+        if (extra && gj != vb.hi1 + 1) return;
+        FL[1].ref(gi, gj, 0) = F0; FL[1].ref(gi, gj, 1) = Fa; FL[1].ref(gi, gj, 2) = Fb;
+        FR[1].ref(gi, gj, 0) = F0; FR[1].ref(gi, gj, 1) = Fa; FR[1].ref(gi, gj, 2) = Fc;
+    }
+};
+
+// Optional classic face output: F, S-, S+ nodal arrays per direction.
+template <class R> struct FaceOut9 {
+    V4<R> F[2], Sm[2], Sp[2];
+    int on;
+    __device__ __forceinline__ void put(int d, int gi, int gj, const R* f, const R* m, const R* p) const {
+        for (int k = 0; k < 3; ++k) {
+            F[d].ref(gi, gj, k) = f[k];
+            Sm[d].ref(gi, gj, k) = m[k];
+            Sp[d].ref(gi, gj, k) = p[k];
+        }
+    }
+    __device__ __forceinline__ void store_x(int gi, int gj, const IBox& vb, const R* f, const R* m, const R* p,
+                                            bool extra) const {
+        if (!on) return;
+        if (gi < vb.lo0 || gi > vb.hi0 + 1 || gj < vb.lo1 || gj > vb.hi1) return;
+        if (extra && gi != vb.hi0 + 1) return;
+        put(0, gi, gj, f, m, p);
+    }
+    __device__ __forceinline__ void store_y(int gi, int gj, const IBox& vb, const R* f, const R* m, const R* p,
+                                            bool extra) const {
+        if (!on) return;
+        if (gi < vb.lo0 || gi > vb.hi0 || gj < vb.lo1 || gj > vb.hi1 + 1) return;
+        if (extra && gj != vb.hi1 + 1) return;
+        put(1, gi, gj, f, m, p);
+    }
+};
+
+// Optional write-back of the rebuilt depth into U_old comp 0 on the box grown
+// by one cell (the classic solver rebuilds in place, src/solvers/Roe.cpp:339).
+// A grown-tile cell is written by the tile that owns it: its own columns/rows,
+// plus the box's ghost ring next to them.
+template <class R> struct RebuildOut {
+    V4<R> U;
+    int on;
+    __device__ __forceinline__ void store(int gi, int gj, const IBox& vb, R hp) const {
+        if (!on) return;
+        const int tx0 = vb.lo0 + (int)blockIdx.x * 32, ty0 = vb.lo1 + (int)blockIdx.y * 8;
+        int xa = tx0, xb = tx0 + 31, ya = ty0, yb = ty0 + 7;
+        if (xb > vb.hi0) xb = vb.hi0;
+        if (yb > vb.hi1) yb = vb.hi1;
+        if (xa == vb.lo0) xa = vb.lo0 - 1;
+        if (xb == vb.hi0) xb = vb.hi0 + 1;
+        if (ya == vb.lo1) ya = vb.lo1 - 1;
+        if (yb == vb.hi1) yb = vb.hi1 + 1;
+        if (gi < xa || gi > xb || gj < ya || gj > yb) return;
+        if (gi < U.lo0 || gi > U.hi0 || gj < U.lo1 || gj > U.hi1) return;
+        U.ref(gi, gj, 0) = hp;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Sources of the grown tile.
+// ---------------------------------------------------------------------------
+
+// A whole level as one box with no stored ghosts: the physical-boundary ghost
+// values of include/boundaries/BCFill.H:35-86 are generated here.  Wall (code
+// 0): eta and tangential momentum mirrored, normal momentum mirrored and
+// negated.  Open: the edge cell copied.  Terrain always copies the edge.
+template <class R> struct LevelSrc {
+    const R* h; const R* hu; const R* hv; const R* z; const R* n;
+    long long pitch;
+    int nx, ny;
+    int bc_xlo, bc_xhi, bc_ylo, bc_yhi;
+    int glo0, glo1, ghi0, ghi1;  // grown region that may be fetched
+
+    __device__ __forceinline__ bool inside(int i, int j) const {
+        return i >= glo0 && i <= ghi0 && j >= glo1 && j <= ghi1;
+    }
+    // (eta, z, hu, hv, n) of any cell in the grown region.
+    __device__ __forceinline__ void fetch(int i, int j, R& eta, R& zz, R& qx, R& qy, R& nn) const {
+        int mi = i, mj = j;
+        bool nx_neg = false, ny_neg = false;
+        if (i < 0) { if (bc_xlo == 0) { mi = -1 - i; nx_neg = true; } else mi = 0; }
+        else if (i >= nx) { if (bc_xhi == 0) { mi = 2 * nx - 1 - i; nx_neg = true; } else mi = nx - 1; }
+        if (j < 0) { if (bc_ylo == 0) { mj = -1 - j; ny_neg = true; } else mj = 0; }
+        else if (j >= ny) { if (bc_yhi == 0) { mj = 2 * ny - 1 - j; ny_neg = true; } else mj = ny - 1; }
+        const int ei = i < 0 ? 0 : (i >= nx ? nx - 1 : i);
+        const int ej = j < 0 ? 0 : (j >= ny ? ny - 1 : j);
+        const long long pm = (long long)mi + (long long)mj * pitch;
+        const long long pe = (long long)ei + (long long)ej * pitch;
+        eta = __ldg(h + pm) + __ldg(z + pm);
+        zz = __ldg(z + pe);
+        nn = __ldg(n + pe);
+        const R a = __ldg(hu + pm), b = __ldg(hv + pm);
+        qx = nx_neg ? -a : a;
+        qy = ny_neg ? -b : b;
+    }
+};
+
+// A box whose ghosts were filled by AMReX (FillPatch): read them as they are.
+template <class R> struct BoxSrc {
+    V4<R> eta, U, T;  // eta comp 0; U comps 1,2 (hu, hv); T comps 0,1 (z, n)
+    int glo0, glo1, ghi0, ghi1;
+    __device__ __forceinline__ bool inside(int i, int j) const {
+        return i >= glo0 && i <= ghi0 && j >= glo1 && j <= ghi1;
+    }
+    __device__ __forceinline__ void fetch(int i, int j, R& e, R& zz, R& qx, R& qy, R& nn) const {
+        e = eta.ld(i, j, 0);
+        zz = T.ld(i, j, 0);
+        nn = T.ld(i, j, 1);
+        qx = U.ld(i, j, 1);
+        qy = U.ld(i, j, 2);
+    }
+};
+
+// Per-step control.  dt is either a host value (dt_in == nullptr) or cfl times
+// the min CFL bound held in the accumulator dt_in (level time loop).
+template <class R> struct StepCtl {
+    R dt_host;
+    R cfl;
+    const struct DtAccum* dt_in;
+    struct DtAccum* dt_out;       // next-step bound of the updated state (may be null)
+    struct DtAccum* dt_reset;     // accumulator to clear for the step after next (may be null)
+    unsigned* status;      // may be null
+    R* time;               // simulated time, advanced by block 0 (may be null)
+    R dx, dy;
+};
+
+}  // namespace hx

@@ -1,0 +1,555 @@
+// Tile kernels of the per-level advance.  Included by hx_exact.cu (compiled
+// with --fmad=false) and hx_fast.cu; each instantiates its arithmetic form.
+//
+// One CTA advances a TX x TY tile of cells.  It stages the tile and its MUSCL
+// halo in shared memory (h rebuilt from eta and z on load, velocities and eta
+// derived once per cell), computes each cell's van Leer slopes once per
+// direction, each face flux once, then the update of its own cell, and folds
+// the next step's CFL bound of the updated cell into the dt accumulator.  The
+// reference runs these as separate passes over separate arrays
+// (src/solvers/HydrostaticRoe.cpp:490-606): here each cell is read once and
+// written once per step.
+#pragma once
+
+#include "hx_device.cuh"
+#include "hx_internal.h"
+
+namespace hx {
+
+constexpr int TX = 32;
+constexpr int TY = 8;
+constexpr int NT = TX * TY;
+
+// ---------------------------------------------------------------------------
+// Hydrostatic-Roe tile kernel.
+// ---------------------------------------------------------------------------
+template <class R> struct HydroSmem {
+    static constexpr int GX = TX + 4, GY = TY + 4;
+    R z[GY][GX], eta[GY][GX], u[GY][GX], v[GY][GX];
+    R sxe[TY][TX + 2], sxu[TY][TX + 2], sxv[TY][TX + 2];  // x-slopes of tile columns -1..TX
+    R sye[TY + 2][TX], syu[TY + 2][TX], syv[TY + 2][TX];  // y-slopes of tile rows -1..TY
+    R fx[4][TY][TX + 1];                                  // x faces: F0, FL1, FR1, F2
+    R fy[4][TY + 1][TX];                                  // y faces: F0, F1, FL2, FR2
+};
+
+// One hydrostatic face (src/solvers/HydrostaticRoe.cpp:218-396).  L and R are
+// the cells on either side; sX are the cells' slopes along the face normal.
+template <class R, bool FAST, int DIR>
+__device__ __forceinline__ void hydro_face(R zL, R zR, R eL, R eR, R seL, R seR, R uL, R uR, R suL, R suR, R vL,
+                                           R vR, R svL, R svR, R& F0, R& Fa, R& Fb, R& Fc) {
+    if (is_nodata(zL) || is_nodata(zR)) {
+        F0 = R(0); Fa = R(0); Fb = R(0); Fc = R(0);
+        return;
+    }
+    const R zf = smax(zL, zR);
+    const R etaLf = eL + R(0.5) * seL;
+    const R etaRf = eR - R(0.5) * seR;
+    const R uLf = uL + R(0.5) * suL;
+    const R uRf = uR - R(0.5) * suR;
+    const R vLf = vL + R(0.5) * svL;
+    const R vRf = vR - R(0.5) * svR;
+    const R hLu = max0(etaLf - zL);
+    const R hRu = max0(etaRf - zR);
+    const R hLs = max0(etaLf - zf);
+    const R hRs = max0(etaRf - zf);
+    R f0, f1, f2;
+    if constexpr (!FAST) {
+        const R huL = (hLs > R(0)) ? hLs * uLf : R(0);
+        const R hvL = (hLs > R(0)) ? hLs * vLf : R(0);
+        const R huR = (hRs > R(0)) ? hRs * uRf : R(0);
+        const R hvR = (hRs > R(0)) ? hRs * vRf : R(0);
+        roe_hydrostatic_exact<DIR>(hLs, huL, hvL, hRs, huR, hvR, f0, f1, f2);
+    } else {
+        roe_hydrostatic_fast<R, DIR>(hLs, uLf, vLf, hRs, uRf, vRf, f0, f1, f2);
+    }
+    // hydrostatic pressure correction, rotated with the normal
+    R pL, pR;
+    if constexpr (!FAST) {
+        pL = Cst<R>::half_g * (hLu * hLu - hLs * hLs);
+        pR = Cst<R>::half_g * (hRu * hRu - hRs * hRs);
+    } else {
+        // (a^2 - b^2) = (a - b)(a + b) is exactly zero whenever a == b (lake at rest)
+        pL = Cst<R>::half_g * ((hLu - hLs) * (hLu + hLs));
+        pR = Cst<R>::half_g * ((hRu - hRs) * (hRu + hRs));
+    }
+    F0 = f0;
+    if (DIR == 0) { Fa = f1 + pL; Fb = f1 + pR; Fc = f2; }
+    else { Fa = f1; Fb = f2 + pL; Fc = f2 + pR; }
+}
+
+template <class R> __device__ __forceinline__ bool resolve_dt(const StepCtl<R>& c, R& dt) {
+    if (c.dt_in == nullptr) { dt = c.dt_host; return true; }
+    if (c.status && (*((volatile unsigned*)c.status) & HX_STATUS_DT_COLLAPSE)) return false;
+    const R m = accum_dt_min<R>(c.dt_in->rate_bits, c.dt_in->flags);
+    if (m < R(1.e-12)) {
+        if (c.status && threadIdx.x == 0) atomicOr(c.status, (unsigned)HX_STATUS_DT_COLLAPSE);
+        return false;
+    }
+    dt = m * c.cfl;
+    return true;
+}
+
+template <class R> __device__ __forceinline__ void step_bookkeeping(const StepCtl<R>& c, R dt) {
+    if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) {
+        if (c.dt_reset) {
+            c.dt_reset->rate_bits = 0ull;
+            c.dt_reset->maxvel_bits = 0ull;
+            c.dt_reset->flags = 0u;
+        }
+        if (c.time) *c.time += dt;
+    }
+}
+
+template <class R, bool FAST, class Src>
+__global__ void __launch_bounds__(NT) k_hydro_tile(Src src, Cells3<R> uo, Plane<R> nplane, Cells3W<R> out,
+                                                   FaceOut<R> fo, IBox vb, StepCtl<R> ctl) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    HydroSmem<R>& S = *reinterpret_cast<HydroSmem<R>*>(smem_raw);
+    constexpr int GX = HydroSmem<R>::GX, GY = HydroSmem<R>::GY;
+
+    R dt;
+    if (!resolve_dt(ctl, dt)) return;
+    step_bookkeeping(ctl, dt);
+
+    const int t = threadIdx.x;
+    const int tx = t & (TX - 1), ty = t / TX;
+    const int x0 = vb.lo0 + blockIdx.x * TX;
+    const int y0 = vb.lo1 + blockIdx.y * TY;
+
+    // --- A: grown tile -> h rebuilt, eta = h + z, velocities -----------------
+    for (int idx = t; idx < GX * GY; idx += NT) {
+        const int r = idx / GX, c = idx - r * GX;
+        const int gi = x0 + c - 2, gj = y0 + r - 2;
+        R e = R(0), zz = R(0), qx = R(0), qy = R(0), nn = R(0);
+        if (src.inside(gi, gj)) src.fetch(gi, gj, e, zz, qx, qy, nn);
+        const R hp = max0(e - zz);  // HydrostaticRoe.cpp:498
+        R uu, vv;
+        if constexpr (!FAST) {
+            uu = (hp > Cst<R>::tol12) ? qx / hp : R(0);
+            vv = (hp > Cst<R>::tol12) ? qy / hp : R(0);
+        } else {
+            const R rh = (hp > Cst<R>::tol12) ? R(1) / hp : R(0);
+            uu = qx * rh;
+            vv = qy * rh;
+        }
+        S.z[r][c] = zz;
+        S.eta[r][c] = hp + zz;  // HydrostaticRoe.cpp:257-260
+        S.u[r][c] = uu;
+        S.v[r][c] = vv;
+    }
+    __syncthreads();
+
+    // --- B: van Leer slopes, once per cell and direction ---------------------
+    {
+        const int r = ty + 2, c = tx + 2;
+        S.sxe[ty][tx + 1] = van_leer_slope<R, FAST>(S.eta[r][c - 1], S.eta[r][c], S.eta[r][c + 1]);
+        S.sxu[ty][tx + 1] = van_leer_slope<R, FAST>(S.u[r][c - 1], S.u[r][c], S.u[r][c + 1]);
+        S.sxv[ty][tx + 1] = van_leer_slope<R, FAST>(S.v[r][c - 1], S.v[r][c], S.v[r][c + 1]);
+        S.sye[ty + 1][tx] = van_leer_slope<R, FAST>(S.eta[r - 1][c], S.eta[r][c], S.eta[r + 1][c]);
+        S.syu[ty + 1][tx] = van_leer_slope<R, FAST>(S.u[r - 1][c], S.u[r][c], S.u[r + 1][c]);
+        S.syv[ty + 1][tx] = van_leer_slope<R, FAST>(S.v[r - 1][c], S.v[r][c], S.v[r + 1][c]);
+    }
+    if (t < 2 * TY + 2 * TX) {
+        if (t < 2 * TY) {  // x-slopes of tile columns -1 and TX
+            const int row = t % TY, col = (t < TY) ? -1 : TX;
+            const int r = row + 2, c = col + 2;
+            S.sxe[row][col + 1] = van_leer_slope<R, FAST>(S.eta[r][c - 1], S.eta[r][c], S.eta[r][c + 1]);
+            S.sxu[row][col + 1] = van_leer_slope<R, FAST>(S.u[r][c - 1], S.u[r][c], S.u[r][c + 1]);
+            S.sxv[row][col + 1] = van_leer_slope<R, FAST>(S.v[r][c - 1], S.v[r][c], S.v[r][c + 1]);
+        } else {  // y-slopes of tile rows -1 and TY
+            const int m = t - 2 * TY;
+            const int col = m % TX, row = (m < TX) ? -1 : TY;
+            const int r = row + 2, c = col + 2;
+            S.sye[row + 1][col] = van_leer_slope<R, FAST>(S.eta[r - 1][c], S.eta[r][c], S.eta[r + 1][c]);
+            S.syu[row + 1][col] = van_leer_slope<R, FAST>(S.u[r - 1][c], S.u[r][c], S.u[r + 1][c]);
+            S.syv[row + 1][col] = van_leer_slope<R, FAST>(S.v[r - 1][c], S.v[r][c], S.v[r + 1][c]);
+        }
+    }
+    __syncthreads();
+
+    // --- C: faces.  Each thread: the x face at the left of its cell and the y
+    // face below it; extra threads: the right column and the top row. --------
+    auto xface = [&](int fi, int fj) {
+        const int r = fj + 2, cl = fi + 1, cr = fi + 2;
+        R F0, Fa, Fb, Fc;
+        hydro_face<R, FAST, 0>(S.z[r][cl], S.z[r][cr], S.eta[r][cl], S.eta[r][cr], S.sxe[fj][fi], S.sxe[fj][fi + 1],
+                               S.u[r][cl], S.u[r][cr], S.sxu[fj][fi], S.sxu[fj][fi + 1], S.v[r][cl], S.v[r][cr],
+                               S.sxv[fj][fi], S.sxv[fj][fi + 1], F0, Fa, Fb, Fc);
+        S.fx[0][fj][fi] = F0; S.fx[1][fj][fi] = Fa; S.fx[2][fj][fi] = Fb; S.fx[3][fj][fi] = Fc;
+        fo.store_x(x0 + fi, y0 + fj, vb, F0, Fa, Fb, Fc, fi == TX);
+    };
+    auto yface = [&](int fi, int fj) {
+        const int c = fi + 2, rl = fj + 1, rr = fj + 2;
+        R F0, Fa, Fb, Fc;
+        hydro_face<R, FAST, 1>(S.z[rl][c], S.z[rr][c], S.eta[rl][c], S.eta[rr][c], S.sye[fj][fi], S.sye[fj + 1][fi],
+                               S.u[rl][c], S.u[rr][c], S.syu[fj][fi], S.syu[fj + 1][fi], S.v[rl][c], S.v[rr][c],
+                               S.syv[fj][fi], S.syv[fj + 1][fi], F0, Fa, Fb, Fc);
+        S.fy[0][fj][fi] = F0; S.fy[1][fj][fi] = Fa; S.fy[2][fj][fi] = Fb; S.fy[3][fj][fi] = Fc;
+        fo.store_y(x0 + fi, y0 + fj, vb, F0, Fa, Fb, Fc, fj == TY);
+    };
+    {
+        const int gi = x0 + tx, gj = y0 + ty;
+        // a face is needed if it bounds a valid cell
+        if (gi <= vb.hi0 + 1 && gj <= vb.hi1) xface(tx, ty);
+        if (gi <= vb.hi0 && gj <= vb.hi1 + 1) yface(tx, ty);
+        if (t < TY) {
+            if (x0 + TX <= vb.hi0 + 1 && y0 + t <= vb.hi1) xface(TX, t);
+        } else if (t >= 32 && t < 32 + TX) {
+            const int m = t - 32;
+            if (x0 + m <= vb.hi0 && y0 + TY <= vb.hi1 + 1) yface(m, TY);
+        }
+    }
+    __syncthreads();
+
+    // --- D: update, Manning friction, dry clamp (HydrostaticRoe.cpp:551-604) --
+    const int gi = x0 + tx, gj = y0 + ty;
+    const bool valid = gi <= vb.hi0 && gj <= vb.hi1;
+    R rate = R(0), mv = R(0);
+    unsigned flags = 0;
+    if (valid) {
+        R cx, cy;
+        cx = dt / ctl.dx;
+        cy = dt / ctl.dy;
+        R un[3];
+        const R o0 = uo.ld(0, gi, gj), o1 = uo.ld(1, gi, gj), o2 = uo.ld(2, gi, gj);
+        const R dx0 = S.fx[0][ty][tx + 1] - S.fx[0][ty][tx];
+        const R dx1 = S.fx[1][ty][tx + 1] - S.fx[2][ty][tx];
+        const R dx2 = S.fx[3][ty][tx + 1] - S.fx[3][ty][tx];
+        const R dy0 = S.fy[0][ty + 1][tx] - S.fy[0][ty][tx];
+        const R dy1 = S.fy[1][ty + 1][tx] - S.fy[1][ty][tx];
+        const R dy2 = S.fy[2][ty + 1][tx] - S.fy[3][ty][tx];
+        if constexpr (!FAST) {
+            un[0] = o0 - cx * dx0 - cy * dy0;
+            un[1] = o1 - cx * dx1 - cy * dy1;
+            un[2] = o2 - cx * dx2 - cy * dy2;
+        } else {
+            un[0] = (o0 - cx * dx0) - cy * dy0;
+            un[1] = (o1 - cx * dx1) - cy * dy1;
+            un[2] = (o2 - cx * dx2) - cy * dy2;
+        }
+        const R hh = un[0];
+        if (hh >= Cst<R>::toldry) {
+            const R nv = nplane.ld(gi, gj);
+            const R nsq = nv * nv;
+            if (nsq > Cst<R>::tol12) {  // the friction factor needs a rough bed
+                const R qx = un[1], qy = un[2];
+                R modM, fac;
+                if constexpr (!FAST) {
+                    const R inv_h = R(1.0) / hh;
+                    const R uu = qx * inv_h, vv = qy * inv_h;
+                    modM = sqrt(uu * uu + vv * vv);
+                    if (modM > Cst<R>::tol12) {
+                        const R h43 = hh * cbrt(hh);
+                        const R tt = dt * Cst<R>::g * nsq * modM / h43;
+                        const R ff = sqrt(R(1.0) + R(4.0) * tt);
+                        fac = R(2.0) / (R(1.0) + ff);
+                        un[1] = qx * fac;
+                        un[2] = qy * fac;
+                    }
+                } else {
+                    const R inv_h = R(1) / hh;
+                    modM = sqrt(qx * qx + qy * qy) * inv_h;
+                    if (modM > Cst<R>::tol12) {
+                        const R h43 = hh * cbrt(hh);
+                        const R tt = dt * Cst<R>::g * nsq * modM / h43;
+                        const R ff = sqrt(R(1) + R(4) * tt);
+                        fac = R(2) / (R(1) + ff);
+                        un[1] = qx * fac;
+                        un[2] = qy * fac;
+                    }
+                }
+            }
+        } else {
+            un[0] = smax(hh, R(0));
+            un[1] = R(0);
+            un[2] = R(0);
+        }
+        out.st(gi, gj, un[0], un[1], un[2]);
+        if (bits_nonfinite(un[0]) || bits_nonfinite(un[1]) || bits_nonfinite(un[2])) flags |= DTF_NAN;
+        if (ctl.dt_out) {
+            const R zc = S.z[ty + 2][tx + 2];
+            dt_cell_contrib<R, FAST>(un[0], un[1], un[2], zc, ctl.dx, ctl.dy, R(1) / ctl.dx, R(1) / ctl.dy, rate,
+                                     mv, flags);
+        }
+    }
+    if (ctl.dt_out) block_fold_dt<R, NT>(rate, mv, flags, ctl.dt_out);
+    if ((flags & DTF_NAN) && ctl.status) atomicOr(ctl.status, (unsigned)HX_STATUS_NAN);
+}
+
+// ---------------------------------------------------------------------------
+// Classic Roe tile kernel (src/solvers/Roe.cpp:184-248, 327-434).
+// ---------------------------------------------------------------------------
+template <class R> struct ClassicSmem {
+    static constexpr int GX = TX + 2, GY = TY + 2;
+    R h[GY][GX], hu[GY][GX], hv[GY][GX], z[GY][GX], n[GY][GX];
+    R fx[9][TY][TX + 1];  // F0..2, S-0..2, S+0..2
+    R fy[9][TY + 1][TX];
+};
+
+template <class R, bool FAST, class Src>
+__global__ void __launch_bounds__(NT) k_classic_tile(Src src, Cells3W<R> out, FaceOut9<R> fo, RebuildOut<R> hb,
+                                                     IBox vb, StepCtl<R> ctl) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    ClassicSmem<R>& S = *reinterpret_cast<ClassicSmem<R>*>(smem_raw);
+    constexpr int GX = ClassicSmem<R>::GX, GY = ClassicSmem<R>::GY;
+
+    R dt;
+    if (!resolve_dt(ctl, dt)) return;
+    step_bookkeeping(ctl, dt);
+
+    const int t = threadIdx.x;
+    const int tx = t & (TX - 1), ty = t / TX;
+    const int x0 = vb.lo0 + blockIdx.x * TX;
+    const int y0 = vb.lo1 + blockIdx.y * TY;
+
+    for (int idx = t; idx < GX * GY; idx += NT) {
+        const int r = idx / GX, c = idx - r * GX;
+        const int gi = x0 + c - 1, gj = y0 + r - 1;
+        R e = R(0), zz = R(0), qx = R(0), qy = R(0), nn = R(0);
+        if (src.inside(gi, gj)) src.fetch(gi, gj, e, zz, qx, qy, nn);
+        const R hp = max0(e - zz);  // Roe.cpp:246, in place on the grown tile
+        S.h[r][c] = hp;
+        S.hu[r][c] = qx;
+        S.hv[r][c] = qy;
+        S.z[r][c] = zz;
+        S.n[r][c] = nn;
+        hb.store(gi, gj, vb, hp);
+    }
+    __syncthreads();
+
+    auto xface = [&](int fi, int fj) {
+        const int r = fj + 1, cl = fi, cr = fi + 1;
+        R F[3], Sm[3], Sp[3];
+        roe_classic<R, FAST, 0>(S.h[r][cl], S.hu[r][cl], S.hv[r][cl], S.z[r][cl], S.n[r][cl], S.h[r][cr],
+                                S.hu[r][cr], S.hv[r][cr], S.z[r][cr], S.n[r][cr], ctl.dx, F, Sm, Sp);
+        for (int k = 0; k < 3; ++k) { S.fx[k][fj][fi] = F[k]; S.fx[3 + k][fj][fi] = Sm[k]; S.fx[6 + k][fj][fi] = Sp[k]; }
+        fo.store_x(x0 + fi, y0 + fj, vb, F, Sm, Sp, fi == TX);
+    };
+    auto yface = [&](int fi, int fj) {
+        const int c = fi + 1, rl = fj, rr = fj + 1;
+        R F[3], Sm[3], Sp[3];
+        roe_classic<R, FAST, 1>(S.h[rl][c], S.hu[rl][c], S.hv[rl][c], S.z[rl][c], S.n[rl][c], S.h[rr][c],
+                                S.hu[rr][c], S.hv[rr][c], S.z[rr][c], S.n[rr][c], ctl.dy, F, Sm, Sp);
+        for (int k = 0; k < 3; ++k) { S.fy[k][fj][fi] = F[k]; S.fy[3 + k][fj][fi] = Sm[k]; S.fy[6 + k][fj][fi] = Sp[k]; }
+        fo.store_y(x0 + fi, y0 + fj, vb, F, Sm, Sp, fj == TY);
+    };
+    {
+        const int gi = x0 + tx, gj = y0 + ty;
+        if (gi <= vb.hi0 + 1 && gj <= vb.hi1) xface(tx, ty);
+        if (gi <= vb.hi0 && gj <= vb.hi1 + 1) yface(tx, ty);
+        if (t < TY) {
+            if (x0 + TX <= vb.hi0 + 1 && y0 + t <= vb.hi1) xface(TX, t);
+        } else if (t >= 32 && t < 32 + TX) {
+            const int m = t - 32;
+            if (x0 + m <= vb.hi0 && y0 + TY <= vb.hi1 + 1) yface(m, TY);
+        }
+    }
+    __syncthreads();
+
+    const int gi = x0 + tx, gj = y0 + ty;
+    const bool valid = gi <= vb.hi0 && gj <= vb.hi1;
+    R rate = R(0), mv = R(0);
+    unsigned flags = 0;
+    if (valid) {
+        const R cx = dt / ctl.dx, cy = dt / ctl.dy;
+        const R uo[3] = {S.h[ty + 1][tx + 1], S.hu[ty + 1][tx + 1], S.hv[ty + 1][tx + 1]};
+        R un[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            // Roe.cpp:426-430, in this order
+            un[k] = uo[k] - cx * (S.fx[k][ty][tx + 1] - S.fx[k][ty][tx]) - cy * (S.fy[k][ty + 1][tx] - S.fy[k][ty][tx]) -
+                    cx * (S.fx[6 + k][ty][tx + 1] + S.fx[3 + k][ty][tx]) -
+                    cy * (S.fy[6 + k][ty + 1][tx] + S.fy[3 + k][ty][tx]);
+        }
+        out.st(gi, gj, un[0], un[1], un[2]);
+        if (bits_nonfinite(un[0]) || bits_nonfinite(un[1]) || bits_nonfinite(un[2])) flags |= DTF_NAN;
+        if (ctl.dt_out) {
+            dt_cell_contrib<R, FAST>(un[0], un[1], un[2], S.z[ty + 1][tx + 1], ctl.dx, ctl.dy, R(1) / ctl.dx,
+                                     R(1) / ctl.dy, rate, mv, flags);
+        }
+    }
+    if (ctl.dt_out) block_fold_dt<R, NT>(rate, mv, flags, ctl.dt_out);
+    if ((flags & DTF_NAN) && ctl.status) atomicOr(ctl.status, (unsigned)HX_STATUS_NAN);
+}
+
+// ---------------------------------------------------------------------------
+// compute_dt_Impl over a box (HydrostaticRoe.cpp:19-65, Roe.cpp:20-76).
+// ---------------------------------------------------------------------------
+template <class R, bool FAST>
+__global__ void __launch_bounds__(NT) k_dt_reduce(Cells3<R> U, Plane<R> Z, IBox vb, R dx, R dy, DtAccum* acc) {
+    const int i = vb.lo0 + blockIdx.x * TX + (threadIdx.x & (TX - 1));
+    const int j = vb.lo1 + blockIdx.y * TY + threadIdx.x / TX;
+    R rate = R(0), mv = R(0);
+    unsigned flags = 0;
+    if (i <= vb.hi0 && j <= vb.hi1)
+        dt_cell_contrib<R, FAST>(U.ld(0, i, j), U.ld(1, i, j), U.ld(2, i, j), Z.ld(i, j), dx, dy, R(1) / dx,
+                                 R(1) / dy, rate, mv, flags);
+    block_fold_dt<R, NT>(rate, mv, flags, acc);
+}
+
+// ---------------------------------------------------------------------------
+// tag_cells_Impl (HydrostaticRoe.cpp:109-169 method 1; Roe.cpp:121-179 method 0).
+// ---------------------------------------------------------------------------
+template <class R>
+__global__ void __launch_bounds__(NT) k_tag(int method, V4<R> U, V4<R> T, V4<signed char> tags, IBox vb, R dx, R dy,
+                                            R time, R h_th, R u_th, R z_th, signed char set_value) {
+    const int i = vb.lo0 + blockIdx.x * TX + (threadIdx.x & (TX - 1));
+    const int j = vb.lo1 + blockIdx.y * TY + threadIdx.x / TX;
+    if (i > vb.hi0 || j > vb.hi1) return;
+    const R zE = T.ld(i + 1, j, 0), zW = T.ld(i - 1, j, 0), zN = T.ld(i, j + 1, 0), zS = T.ld(i, j - 1, 0);
+    if (method == HX_METHOD_HYDROSTATIC_ROE) {
+        if (is_nodata(zE) || is_nodata(zW) || is_nodata(zN) || is_nodata(zS)) return;
+    } else {
+        if ((double)zE == -9999.0 || (double)zW == -9999.0 || (double)zN == -9999.0 || (double)zS == -9999.0) return;
+    }
+    bool tag = false;
+    {
+        // the reference divides by the double 2.0 * dx and stores the quotient in Real
+        const R dhdx = (R)((double)(U.ld(i + 1, j, 0) - U.ld(i - 1, j, 0)) / (2.0 * (double)dx));
+        const R dhdy = (R)((double)(U.ld(i, j + 1, 0) - U.ld(i, j - 1, 0)) / (2.0 * (double)dy));
+        if (sqrt(dhdx * dhdx + dhdy * dhdy) > h_th) tag = true;
+    }
+    auto umag = [&](int ii, int jj) -> R {
+        const R hh = U.ld(ii, jj, 0);
+        if (hh < R(1.0e-6)) return R(0);
+        const R uu = U.ld(ii, jj, 1) / hh, vv = U.ld(ii, jj, 2) / hh;
+        return sqrt(uu * uu + vv * vv);
+    };
+    if (!tag && (double)time <= 1.0e-8) {
+        const R dzdx = (R)((double)(zE - zW) / (2.0 * (double)dx));
+        const R dzdy = (R)((double)(zN - zS) / (2.0 * (double)dy));
+        if (sqrt(dzdx * dzdx + dzdy * dzdy) > z_th) tag = true;
+    }
+    if (!tag) {
+        const R uE = umag(i + 1, j), uW = umag(i - 1, j), uN = umag(i, j + 1), uS = umag(i, j - 1);
+        const R dudx = (R)((double)(uE - uW) / (2.0 * (double)dx));
+        const R dudy = (R)((double)(uN - uS) / (2.0 * (double)dy));
+        if (sqrt(dudx * dudx + dudy * dudy) > u_th) tag = true;
+    }
+    if (tag) tags.ref(i, j, 0) = set_value;
+}
+
+// ---------------------------------------------------------------------------
+// masked_avgdown_with_vol over a coarse box (MaskedAverageDown.H:64-104).
+// ---------------------------------------------------------------------------
+template <class R>
+__global__ void __launch_bounds__(NT) k_masked_avgdown(V4<R> fine, V4<R> crse, IBox cb, int scomp, int ccomp,
+                                                       int ncomp, int rx, int ry, R fv, R nodata) {
+    const int i = cb.lo0 + blockIdx.x * TX + (threadIdx.x & (TX - 1));
+    const int j = cb.lo1 + blockIdx.y * TY + threadIdx.x / TX;
+    if (i > cb.hi0 || j > cb.hi1) return;
+    for (int n = 0; n < ncomp; ++n) {
+        R cd = R(0), cv = R(0);
+        int nvalid = 0;
+        for (int jr = 0; jr < ry; ++jr)
+            for (int ir = 0; ir < rx; ++ir) {
+                const R val = fine.ld(i * rx + ir, j * ry + jr, scomp + n);
+                if (!isnan(val) && (double)fabs(val - nodata) > 1e-3) {
+                    ++nvalid;
+                    cv += fv;
+                    cd += val * fv;
+                }
+            }
+        crse.ref(i, j, ccomp + n) = (nvalid * 2 >= rx * ry && cv > R(0)) ? cd / cv : nodata;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Point evaluation of the Riemann solvers (diagnostic entry, golden vectors).
+// method 1: states (n, 6) = (hi hui hvi hj huj hvj), aux (n, 2) = normal;
+// method 0: states (n, 10), aux (n, 4) = (dt dx nx ny).  out: (n, 3) F then,
+// for method 0, (n, 3) S- and (n, 3) S+.
+// ---------------------------------------------------------------------------
+template <class R, bool FAST>
+__global__ void k_points(int method, long n, const R* __restrict__ st, const R* __restrict__ aux, R* __restrict__ out) {
+    const long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    if (method == HX_METHOD_HYDROSTATIC_ROE) {
+        const R* q = st + 6 * p;
+        const bool ydir = aux[2 * p + 1] != R(0);
+        R f0, f1, f2;
+        if constexpr (!FAST) {
+            if (ydir) roe_hydrostatic_exact<1>(q[0], q[1], q[2], q[3], q[4], q[5], f0, f1, f2);
+            else roe_hydrostatic_exact<0>(q[0], q[1], q[2], q[3], q[4], q[5], f0, f1, f2);
+        } else {
+            const R ui = q[0] > R(0) ? q[1] / q[0] : R(0), vi = q[0] > R(0) ? q[2] / q[0] : R(0);
+            const R uj = q[3] > R(0) ? q[4] / q[3] : R(0), vj = q[3] > R(0) ? q[5] / q[3] : R(0);
+            if (ydir) roe_hydrostatic_fast<R, 1>(q[0], ui, vi, q[3], uj, vj, f0, f1, f2);
+            else roe_hydrostatic_fast<R, 0>(q[0], ui, vi, q[3], uj, vj, f0, f1, f2);
+        }
+        out[3 * p] = f0; out[3 * p + 1] = f1; out[3 * p + 2] = f2;
+    } else {
+        const R* q = st + 10 * p;
+        const R* a = aux + 4 * p;
+        R F[3], Sm[3], Sp[3];
+        if (a[3] != R(0)) roe_classic<R, FAST, 1>(q[0], q[1], q[2], q[3], q[4], q[5], q[6], q[7], q[8], q[9], a[1], F, Sm, Sp);
+        else roe_classic<R, FAST, 0>(q[0], q[1], q[2], q[3], q[4], q[5], q[6], q[7], q[8], q[9], a[1], F, Sm, Sp);
+        for (int k = 0; k < 3; ++k) { out[3 * p + k] = F[k]; out[3 * n + 3 * p + k] = Sm[k]; out[6 * n + 3 * p + k] = Sp[k]; }
+    }
+}
+
+}  // namespace hx
+
+// ---------------------------------------------------------------------------
+// Launchers (explicitly instantiated per arithmetic form).
+// ---------------------------------------------------------------------------
+#include "hx_launch.h"
+
+namespace hx {
+
+template <class K> inline cudaError_t ensure_smem(K kernel, size_t bytes) {
+    if (bytes <= 48 * 1024) return cudaSuccess;
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+template <class R, bool FAST, class Src>
+cudaError_t launch_hydro(const Src& src, const Cells3<R>& uo, const Plane<R>& np, const Cells3W<R>& out,
+                         const FaceOut<R>& fo, const IBox& vb, const StepCtl<R>& ctl, cudaStream_t st) {
+    const size_t sm = sizeof(HydroSmem<R>);
+    auto k = k_hydro_tile<R, FAST, Src>;
+    cudaError_t e = ensure_smem(k, sm);
+    if (e != cudaSuccess) return e;
+    k<<<tile_grid(vb, TX, TY), NT, sm, st>>>(src, uo, np, out, fo, vb, ctl);
+    return cudaGetLastError();
+}
+
+template <class R, bool FAST, class Src>
+cudaError_t launch_classic(const Src& src, const Cells3W<R>& out, const FaceOut9<R>& fo, const RebuildOut<R>& hb,
+                           const IBox& vb, const StepCtl<R>& ctl, cudaStream_t st) {
+    const size_t sm = sizeof(ClassicSmem<R>);
+    auto k = k_classic_tile<R, FAST, Src>;
+    cudaError_t e = ensure_smem(k, sm);
+    if (e != cudaSuccess) return e;
+    k<<<tile_grid(vb, TX, TY), NT, sm, st>>>(src, out, fo, hb, vb, ctl);
+    return cudaGetLastError();
+}
+
+template <class R, bool FAST>
+cudaError_t launch_dt_reduce(const Cells3<R>& U, const Plane<R>& Z, const IBox& vb, R dx, R dy, DtAccum* acc,
+                             cudaStream_t st) {
+    k_dt_reduce<R, FAST><<<tile_grid(vb, TX, TY), NT, 0, st>>>(U, Z, vb, dx, dy, acc);
+    return cudaGetLastError();
+}
+
+template <class R, bool FAST>
+cudaError_t launch_points(int method, long n, const R* st, const R* aux, R* out, cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    k_points<R, FAST><<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(method, n, st, aux, out);
+    return cudaGetLastError();
+}
+
+template <class R>
+cudaError_t launch_tag(int method, const V4<R>& U, const V4<R>& T, const V4<signed char>& tags, const IBox& vb, R dx,
+                       R dy, R time, R h_th, R u_th, R z_th, signed char set_value, cudaStream_t st) {
+    k_tag<R><<<tile_grid(vb, TX, TY), NT, 0, st>>>(method, U, T, tags, vb, dx, dy, time, h_th, u_th, z_th, set_value);
+    return cudaGetLastError();
+}
+
+template <class R>
+cudaError_t launch_masked_avgdown(const V4<R>& fine, const V4<R>& crse, const IBox& cb, int scomp, int ccomp,
+                                  int ncomp, int rx, int ry, R fv, R nodata, cudaStream_t st) {
+    k_masked_avgdown<R><<<tile_grid(cb, TX, TY), NT, 0, st>>>(fine, crse, cb, scomp, ccomp, ncomp, rx, ry, fv, nodata);
+    return cudaGetLastError();
+}
+
+}  // namespace hx

@@ -1,0 +1,38 @@
+// Launcher declarations.  Definitions live in hx_kernels.cuh and are
+// explicitly instantiated by hx_exact.cu (compiled --fmad=false, FAST=false)
+// and hx_fast.cu (FAST=true), so this header never instantiates a kernel.
+#pragma once
+
+#include "hx_device.cuh"
+#include "hx_internal.h"
+
+namespace hx {
+
+template <class R, bool FAST, class Src>
+cudaError_t launch_hydro(const Src& src, const Cells3<R>& uo, const Plane<R>& np, const Cells3W<R>& out,
+                         const FaceOut<R>& fo, const IBox& vb, const StepCtl<R>& ctl, cudaStream_t st);
+
+template <class R, bool FAST, class Src>
+cudaError_t launch_classic(const Src& src, const Cells3W<R>& out, const FaceOut9<R>& fo, const RebuildOut<R>& hb,
+                           const IBox& vb, const StepCtl<R>& ctl, cudaStream_t st);
+
+template <class R, bool FAST>
+cudaError_t launch_dt_reduce(const Cells3<R>& U, const Plane<R>& Z, const IBox& vb, R dx, R dy, DtAccum* acc,
+                             cudaStream_t st);
+
+template <class R, bool FAST>
+cudaError_t launch_points(int method, long n, const R* st, const R* aux, R* out, cudaStream_t stream);
+
+template <class R>
+cudaError_t launch_tag(int method, const V4<R>& U, const V4<R>& T, const V4<signed char>& tags, const IBox& vb, R dx,
+                       R dy, R time, R h_th, R u_th, R z_th, signed char set_value, cudaStream_t st);
+
+template <class R>
+cudaError_t launch_masked_avgdown(const V4<R>& fine, const V4<R>& crse, const IBox& cb, int scomp, int ccomp,
+                                  int ncomp, int rx, int ry, R fv, R nodata, cudaStream_t st);
+
+inline dim3 tile_grid(const IBox& b, int tx, int ty) {
+    return dim3((unsigned)((b.hi0 - b.lo0 + 1 + tx - 1) / tx), (unsigned)((b.hi1 - b.lo1 + 1 + ty - 1) / ty));
+}
+
+}  // namespace hx

@@ -1,0 +1,305 @@
+/*
+ * hydroexa_gb300.h -- C ABI of the GB300 (sm_103a) per-level advance of HydroEXA.
+ *
+ * The entry points replace the per-box bodies of the reference solver's
+ * operator surface (include/solvers/BaseSolver.H:57-191, dispatched by
+ * include/solvers/SolverVariant.H:45-192).  A C++ SolverVariant alternative
+ * keeps AMReX's FillPatch, flux registers and clustering and calls these once
+ * per MFIter box, passing the Array4 of each MultiFab as an hx_array4_* view.
+ *
+ * Conventions
+ *  - Views are borrowed device pointers.  Element (i, j, comp) of a view is
+ *    p[(i - lo[0]) + (j - lo[1]) * jstride + comp * nstride], exactly the
+ *    layout of amrex::Array4 (x fastest, ghosts included in [lo, hi]).
+ *  - Every call is stream-ordered and asynchronous on the given stream and
+ *    allocates nothing.  Calls on different streams are independent.
+ *  - Return value: HX_OK, or a negative argument/launch error detected on the
+ *    host (HX_ERR_ARG, HX_ERR_LAUNCH).  Numerical conditions found on the
+ *    device (dt collapse, NaN) are OR-ed into a device status word, read with
+ *    hx_status_read(); the adapter maps a nonzero status to amrex::Abort,
+ *    as the reference does (src/solvers/HydrostaticRoe.cpp:77-80).
+ *  - The dt reduction is a device accumulator (hx_dt_accum) so a whole time
+ *    loop can run without a host round trip; hx_dt_accum_read() is the
+ *    synchronising read that replaces ReduceOps::value().
+ *
+ * Precision: every entry has an _f64 form (the reference's DOUBLE build) and
+ * an _f32 form (SINGLE build).  Arithmetic: HX_ARITH_EXACT repeats the
+ * reference's operation order with no multiply-add contraction (bit-for-bit
+ * the reference's host arithmetic up to cbrt); HX_ARITH_FAST shares
+ * reciprocals and square roots between terms and contracts multiply-adds,
+ * agreeing with the exact form to ~1e-15 relative per step.
+ */
+#ifndef HYDROEXA_GB300_H
+#define HYDROEXA_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* hx_stream_t; /* same handle as cudaStream_t */
+
+enum {
+    HX_OK = 0,
+    HX_ERR_ARG = -1,
+    HX_ERR_LAUNCH = -2,
+    HX_ERR_CUDA = -3,
+};
+
+/* Device status bits (OR-ed). */
+enum {
+    HX_STATUS_DT_COLLAPSE = 1, /* min CFL bound < 1e-12 (HydrostaticRoe.cpp:77, Roe.cpp:88) */
+    HX_STATUS_NAN = 2,         /* a NaN or Inf appeared in an updated state */
+    HX_STATUS_BOUNDS = 4,      /* a view did not cover the stencil the call needs */
+    HX_STATUS_TIMEOUT = 8,     /* a bounded device-side wait gave up */
+};
+
+enum { HX_ARITH_EXACT = 0, HX_ARITH_FAST = 1 };
+enum { HX_METHOD_ROE = 0, HX_METHOD_HYDROSTATIC_ROE = 1 };
+/* Inputs-file boundary codes (HydroEXA.lo_bc / hi_bc): 0 wall, else open. */
+enum { HX_BC_REFLECTIVE = 0, HX_BC_TRANSMISSIVE = 1 };
+
+typedef struct hx_array4_f64 {
+    double* p;
+    int64_t jstride;
+    int64_t nstride;
+    int32_t lo[2];
+    int32_t hi[2];
+    int32_t ncomp;
+} hx_array4_f64;
+
+typedef struct hx_array4_f32 {
+    float* p;
+    int64_t jstride;
+    int64_t nstride;
+    int32_t lo[2];
+    int32_t hi[2];
+    int32_t ncomp;
+} hx_array4_f32;
+
+typedef struct hx_array4_i8 {
+    signed char* p;
+    int64_t jstride;
+    int64_t nstride;
+    int32_t lo[2];
+    int32_t hi[2];
+    int32_t ncomp;
+} hx_array4_i8;
+
+/* Inclusive cell box, like amrex::Box in 2-D. */
+typedef struct hx_box {
+    int32_t lo[2];
+    int32_t hi[2];
+} hx_box;
+
+/* Device-resident dt accumulator: min per-cell CFL bound and max(|u|,|v|),
+ * both before the CFL factor, as in compute_dt_Impl's ReduceOps<Min,Max>.
+ * Opaque; 64-byte aligned device memory of hx_dt_accum_bytes() bytes. */
+typedef struct hx_dt_accum hx_dt_accum;
+
+/* ---- library ------------------------------------------------------------ */
+
+/* Version string and the last host-side error message of this thread. */
+const char* hx_version(void);
+const char* hx_last_error(void);
+/* Number of kernels this library launched since load (all entry points). */
+uint64_t hx_launch_count(void);
+
+/* Device status word: one uint32 of device memory owned by the caller. */
+int hx_status_clear(uint32_t* status_dev, hx_stream_t stream);
+/* Synchronises the stream and returns the status bits (or a negative error). */
+int hx_status_read(const uint32_t* status_dev, hx_stream_t stream);
+
+/* dt accumulator in caller-owned device memory of hx_dt_accum_bytes() bytes. */
+int64_t hx_dt_accum_bytes(void);
+int hx_dt_accum_reset(hx_dt_accum* acc, hx_stream_t stream);
+/* Synchronising read (the ReduceOps::value() of compute_dt_Impl). */
+int hx_dt_accum_read_f64(const hx_dt_accum* acc, double* dt_min, double* max_vel, hx_stream_t stream);
+int hx_dt_accum_read_f32(const hx_dt_accum* acc, float* dt_min, float* max_vel, hx_stream_t stream);
+
+/* ---- per-box operators (AMReX keeps the ghost fill) ---------------------- */
+
+/*
+ * Hydrostatic-Roe advance of one box (replaces the per-box body of
+ * HydrostaticRoe::compute_fluxes_Impl, src/solvers/HydrostaticRoe.cpp:484-606:
+ * h rebuild, x and y dual face fluxes, update with Manning friction and dry
+ * clamp), fused into one kernel.
+ *   eta_ext  free surface, >= 2 ghosts filled (FillPatchEta)
+ *   U_ext    comps 1,2 = hu, hv with >= 2 ghosts filled (FillPatch)
+ *   T_ext    comps 0,1 = z, Manning n with >= 2 ghosts filled (FillPatchTerrain)
+ *   U_old    the stored state of the valid box (comp 0 is the stored depth)
+ *   U_new    destination, valid box
+ *   FL/FR    optional (NULL) nodal face arrays for reflux, 3 comps each,
+ *            [0] = x faces, [1] = y faces (HydrostaticRoe.cpp:442-454)
+ *   next_dt  optional: min CFL bound / max|vel| of U_new are folded in
+ *            (compute_dt_Impl of the next step, fused)
+ *   status   optional device status word
+ */
+int hx_advance_box_hydrostatic_f64(const hx_array4_f64* eta_ext, const hx_array4_f64* U_ext,
+                                   const hx_array4_f64* T_ext, const hx_array4_f64* U_old, hx_array4_f64* U_new,
+                                   hx_box valid, double dt, double dx, double dy, const hx_array4_f64* FL,
+                                   const hx_array4_f64* FR, hx_dt_accum* next_dt, uint32_t* status, int arith,
+                                   hx_stream_t stream);
+int hx_advance_box_hydrostatic_f32(const hx_array4_f32* eta_ext, const hx_array4_f32* U_ext,
+                                   const hx_array4_f32* T_ext, const hx_array4_f32* U_old, hx_array4_f32* U_new,
+                                   hx_box valid, float dt, float dx, float dy, const hx_array4_f32* FL,
+                                   const hx_array4_f32* FR, hx_dt_accum* next_dt, uint32_t* status, int arith,
+                                   hx_stream_t stream);
+
+/*
+ * Classic Roe advance of one box (replaces Roe::compute_fluxes_Impl's per-box
+ * body, src/solvers/Roe.cpp:327-434: in-place h rebuild on the grown tile,
+ * first-order F / S- / S+ faces, four-term update).
+ *   eta      free surface with >= 1 ghost (FillPatchEta)
+ *   U_old    comps 1,2 with >= 1 ghost (FillPatch); comp 0 is overwritten on
+ *            the grown box with max(0, eta - z), as the reference does
+ *   T        z, n with >= 1 ghost
+ *   F, Sm, Sp optional nodal face arrays ([0] x, [1] y) for the reflux
+ *            selection (Roe.cpp:369-388)
+ */
+int hx_advance_box_roe_f64(const hx_array4_f64* eta, hx_array4_f64* U_old, const hx_array4_f64* T,
+                           hx_array4_f64* U_new, hx_box valid, double dt, double dx, double dy,
+                           const hx_array4_f64* F, const hx_array4_f64* Sm, const hx_array4_f64* Sp,
+                           hx_dt_accum* next_dt, uint32_t* status, int arith, hx_stream_t stream);
+int hx_advance_box_roe_f32(const hx_array4_f32* eta, hx_array4_f32* U_old, const hx_array4_f32* T,
+                           hx_array4_f32* U_new, hx_box valid, float dt, float dx, float dy,
+                           const hx_array4_f32* F, const hx_array4_f32* Sm, const hx_array4_f32* Sp,
+                           hx_dt_accum* next_dt, uint32_t* status, int arith, hx_stream_t stream);
+
+/*
+ * Per-cell CFL bound of one box folded into acc (replaces the ReduceOps pass of
+ * compute_dt_Impl, src/solvers/HydrostaticRoe.cpp:19-65 and
+ * src/solvers/Roe.cpp:20-76; the two are arithmetically identical).
+ */
+int hx_dt_reduce_box_f64(const hx_array4_f64* U, const hx_array4_f64* T, hx_box valid, double dx, double dy,
+                         hx_dt_accum* acc, hx_stream_t stream);
+int hx_dt_reduce_box_f32(const hx_array4_f32* U, const hx_array4_f32* T, hx_box valid, float dx, float dy,
+                         hx_dt_accum* acc, hx_stream_t stream);
+
+/*
+ * Gradient tagging of one box (replaces tag_cells_Impl:
+ * src/solvers/HydrostaticRoe.cpp:88-171 when method is
+ * HX_METHOD_HYDROSTATIC_ROE, src/solvers/Roe.cpp:100-181 when HX_METHOD_ROE).
+ * U and T must cover one ghost around the box.  Writes set_value
+ * (amrex::TagBox::SET) to tagged cells only.
+ */
+int hx_tag_box_f64(int method, const hx_array4_f64* U, const hx_array4_f64* T, hx_array4_i8* tags, hx_box valid,
+                   double dx, double dy, double time, double h_thresh, double umag_thresh, double z_thresh,
+                   signed char set_value, hx_stream_t stream);
+int hx_tag_box_f32(int method, const hx_array4_f32* U, const hx_array4_f32* T, hx_array4_i8* tags, hx_box valid,
+                   float dx, float dy, float time, float h_thresh, float umag_thresh, float z_thresh,
+                   signed char set_value, hx_stream_t stream);
+
+/*
+ * NODATA-aware volume-weighted restriction of the coarse box crse_box
+ * (replaces the kernel of amrex::masked_average_down,
+ * src/utils/MaskedAverageDown.cpp:45-60 and include/utils/MaskedAverageDown.H:64-104).
+ * Components scomp..scomp+ncomp-1 of fine go to ccomp.. of crse.
+ */
+int hx_masked_average_down_box_f64(const hx_array4_f64* fine, hx_array4_f64* crse, hx_box crse_box, int scomp,
+                                   int ccomp, int ncomp, int rx, int ry, double fine_volume, double nodata,
+                                   hx_stream_t stream);
+int hx_masked_average_down_box_f32(const hx_array4_f32* fine, hx_array4_f32* crse, hx_box crse_box, int scomp,
+                                   int ccomp, int ncomp, int rx, int ry, float fine_volume, float nodata,
+                                   hx_stream_t stream);
+
+/* ---- single-box level with the physical boundary fused into the loader --- */
+
+/*
+ * A whole level held as one box [0,nx) x [0,ny) with no ghost cells: planes
+ * h, hu, hv (state) and z, n (terrain), each with row pitch `pitch` elements.
+ * The ghost values the reference's FillPatch + HydroPhysBC produce at the
+ * domain edge (include/boundaries/BCFill.H:35-86,159-181: wall = mirror, normal
+ * momentum negated; open = copy edge; terrain always copies the edge) are
+ * generated inside the tile loader instead of stored.
+ */
+typedef struct hx_level_f64 {
+    const double* h;
+    const double* hu;
+    const double* hv;
+    const double* z;
+    const double* n;
+    int64_t pitch;
+    int32_t nx, ny;
+    double dx, dy;
+    int32_t bc_lo[2];
+    int32_t bc_hi[2];
+} hx_level_f64;
+
+typedef struct hx_level_f32 {
+    const float* h;
+    const float* hu;
+    const float* hv;
+    const float* z;
+    const float* n;
+    int64_t pitch;
+    int32_t nx, ny;
+    float dx, dy;
+    int32_t bc_lo[2];
+    int32_t bc_hi[2];
+} hx_level_f32;
+
+/* One advance of the level by dt (host value); writes h/hu/hv_out (same pitch). */
+int hx_level_advance_f64(int method, const hx_level_f64* L, double dt, double* h_out, double* hu_out,
+                         double* hv_out, hx_dt_accum* next_dt, uint32_t* status, int arith, hx_stream_t stream);
+int hx_level_advance_f32(int method, const hx_level_f32* L, float dt, float* h_out, float* hu_out, float* hv_out,
+                         hx_dt_accum* next_dt, uint32_t* status, int arith, hx_stream_t stream);
+
+/* compute_dt_Impl over the level (no ghosts needed). */
+int hx_level_dt_reduce_f64(const hx_level_f64* L, hx_dt_accum* acc, hx_stream_t stream);
+int hx_level_dt_reduce_f32(const hx_level_f32* L, hx_dt_accum* acc, hx_stream_t stream);
+
+/*
+ * nsteps of the single-level time loop of the reference driver
+ * (src/HydroEXA.cpp:259-266 with AmrMeshState::ComputeDt and AdvanceLevel at
+ * one level): dt = cfl * min CFL bound of the current state, status
+ * HX_STATUS_DT_COLLAPSE if that minimum is below 1e-12, then advance.  The dt
+ * chain stays on the device (three rotating accumulators in `work`, the next
+ * step's bound fused into each advance), so the loop issues one kernel per
+ * step and can be captured in a CUDA graph.  The state ping-pongs between the
+ * level's planes and (h_alt, hu_alt, hv_alt); *final_in_alt reports where the
+ * last state is.  time_dev (optional, 1 value) accumulates the simulated time.
+ * work: caller-owned device memory of hx_level_run_work_bytes() bytes.
+ */
+int64_t hx_level_run_work_bytes(void);
+int hx_level_run_f64(int method, hx_level_f64* L, double* h_alt, double* hu_alt, double* hv_alt, int nsteps,
+                     double cfl, void* work, uint32_t* status, double* time_dev, int arith, int* final_in_alt,
+                     hx_stream_t stream);
+int hx_level_run_f32(int method, hx_level_f32* L, float* h_alt, float* hu_alt, float* hv_alt, int nsteps,
+                     float cfl, void* work, uint32_t* status, float* time_dev, int arith, int* final_in_alt,
+                     hx_stream_t stream);
+
+/*
+ * Host-buffer form of hx_level_run for callers whose level lives in host
+ * memory: copies h, hu, hv, z, n (host, pitch nx) to the device, runs nsteps,
+ * copies the state back.  Device buffers are allocated by the call and cached
+ * per thread for the next call of the same size (hx_host_cache_release frees
+ * them).  Returns the status bits (>= 0) or a negative error.
+ */
+int hx_level_run_host_f64(int method, int nx, int ny, double dx, double dy, const int32_t bc_lo[2],
+                          const int32_t bc_hi[2], double* h, double* hu, double* hv, const double* z,
+                          const double* n, int nsteps, double cfl, int arith, double* time_out, hx_stream_t stream);
+void hx_host_cache_release(void);
+
+/* ---- diagnostics --------------------------------------------------------- */
+
+/*
+ * Evaluate the device Riemann solvers on arrays of face states (device
+ * memory), for checking them against golden vectors.  method
+ * HX_METHOD_HYDROSTATIC_ROE: states (n, 6) = (hi hui hvi hj huj hvj), aux
+ * (n, 2) = face normal, out (n, 3) = F (include/solvers/kernels/HydrostaticRoe.H:44).
+ * method HX_METHOD_ROE: states (n, 10) = (hi hui hvi zi ni hj huj hvj zj nj),
+ * aux (n, 4) = (dt dx nx ny), out (3, n, 3) = F, S-, S+
+ * (include/solvers/kernels/Roe.H:51).  Normals must be (1,0) or (0,1).
+ */
+int hx_debug_roe_points_f64(int method, int arith, long n, const double* states, const double* aux, double* out,
+                            hx_stream_t stream);
+int hx_debug_roe_points_f32(int method, int arith, long n, const float* states, const float* aux, float* out,
+                            hx_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HYDROEXA_GB300_H */

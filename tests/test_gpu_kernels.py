@@ -1,0 +1,187 @@
+"""Device point solvers against the golden vectors, tagging and the NODATA
+restriction against the oracle (bit-exact), the per-box drop-in forms against
+the level form, and device status reporting."""
+import ctypes
+from pathlib import Path
+
+import numpy as np
+import pytest
+import torch
+
+from hydroexa_gb300 import capi, workloads
+from hydroexa_gb300.level import DtAccum, Level, Status, array4, box
+
+pytestmark = pytest.mark.gpu
+GOLD = Path(__file__).resolve().parent / "golden"
+EXACT, FAST = capi.HX_ARITH_EXACT, capi.HX_ARITH_FAST
+
+
+def dptr(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def run_points(hxlib, method, arith, states, aux, dev):
+    st = torch.from_numpy(np.ascontiguousarray(states)).to(dev)
+    ax = torch.from_numpy(np.ascontiguousarray(aux)).to(dev)
+    n = states.shape[0]
+    out = torch.empty((3 if method == 0 else 1) * n * 3, dtype=st.dtype, device=dev)
+    sfx = "f64" if st.dtype == torch.float64 else "f32"
+    hxlib.check(getattr(hxlib.lib(), f"hx_debug_roe_points_{sfx}")(method, arith, n, dptr(st), dptr(ax), dptr(out),
+                                                                    None), "points")
+    torch.cuda.synchronize()
+    return out.cpu().numpy()
+
+
+def test_hydrostatic_points_golden(cuda, hxlib):
+    g = np.load(GOLD / "roe_hydrostatic_f64.npz")
+    got = run_points(hxlib, 1, EXACT, g["states"], g["normals"], cuda).reshape(-1, 3)
+    assert np.array_equal(got, g["F"])
+    fast = run_points(hxlib, 1, FAST, g["states"], g["normals"], cuda).reshape(-1, 3)
+    scale = np.abs(g["F"]).max(axis=1, keepdims=True) + 1e-300
+    assert (np.abs(fast - g["F"]) / scale).max() <= 1e-12
+
+
+def test_classic_points_golden(cuda, hxlib):
+    g = np.load(GOLD / "roe_classic_f64.npz")
+    got = run_points(hxlib, 0, EXACT, g["states"], g["aux"], cuda).reshape(3, -1, 3)
+    assert np.array_equal(got[0], g["F"]) and np.array_equal(got[1], g["Sm"]) and np.array_equal(got[2], g["Sp"])
+
+
+def test_points_f32_golden(cuda, hxlib):
+    g = np.load(GOLD / "roe_hydrostatic_f32.npz")
+    got = run_points(hxlib, 1, FAST, g["states"], g["normals"], cuda).reshape(-1, 3)
+    scale = np.abs(g["F"]).max(axis=1, keepdims=True) + 1e-30
+    assert (np.abs(got - g["F"]) / scale).max() <= 1e-5
+
+
+def ghosted(a, g=1):
+    """(c, ny, nx) -> (c, ny+2g, nx+2g) with edge-copied ghosts."""
+    return np.pad(a, ((0, 0), (g, g), (g, g)), mode="edge")
+
+
+@pytest.mark.parametrize("method", [0, 1])
+@pytest.mark.parametrize("time", [0.0, 0.5])
+def test_tags_bit_exact(cuda, hxlib, oracle_lib, method, time):
+    case = workloads.fractal_dam_break(70, 45, seed=31, amplitude=2.0, nodata_frac=0.15)
+    g = case.geom
+    L = oracle_lib.Level(g.nx, g.ny, g.dx, g.dy, g.bc_lo, g.bc_hi)
+    h, hu, hv, *_ = oracle_lib.run(L, 1, case.h, case.hu, case.hv, case.z, case.n, 8, case.cfl)
+    U = ghosted(np.stack([h, hu, hv]))
+    T = ghosted(np.stack([case.z, case.n]))
+    rng = np.random.default_rng(1)
+    tags0 = (rng.random(U.shape[1:]) < 0.05).astype(np.int8)  # pre-existing tags stay
+    for th in ((0.5, 0.5, 2.0), (5.0, 20.0, 50.0)):
+        ref = oracle_lib.tag_cells(method, U, T, tags0.copy(), (0, 0), (g.nx - 1, g.ny - 1), g.dx, g.dy, time, *th)
+        Ut = torch.from_numpy(U).to(cuda)
+        Tt = torch.from_numpy(T).to(cuda)
+        Gt = torch.from_numpy(tags0.copy()).to(cuda)
+        rc = hxlib.lib().hx_tag_box_f64(method, ctypes.byref(array4(Ut, (-1, -1))), ctypes.byref(array4(Tt, (-1, -1))),
+                                        ctypes.byref(array4(Gt, (-1, -1))), box((0, 0), (g.nx - 1, g.ny - 1)), g.dx,
+                                        g.dy, time, *th, 2, None)
+        hxlib.check(rc, "tag")
+        got = Gt.cpu().numpy()
+        assert np.array_equal(got, ref)
+        assert (ref == 2).sum() > 10
+
+
+@pytest.mark.parametrize("r", [2, 4])
+def test_masked_average_down_bit_exact(cuda, hxlib, oracle_lib, r):
+    g = np.load(GOLD / "masked_avgdown_f64.npz")
+    fine = torch.from_numpy(g["fine"]).to(cuda)
+    nc, nyf, nxf = g["fine"].shape
+    crse = torch.full((nc, nyf // r, nxf // r), 123.0, dtype=torch.float64, device=cuda)
+    rc = hxlib.lib().hx_masked_average_down_box_f64(ctypes.byref(array4(fine)), ctypes.byref(array4(crse)),
+                                                    box((0, 0), (nxf // r - 1, nyf // r - 1)), 0, 0, nc, r, r,
+                                                    float(g["fine_volume"]), -9999.0, None)
+    hxlib.check(rc, "mavg")
+    got = crse.cpu().numpy()
+    assert np.array_equal(got, g[f"crse_r{r}"], equal_nan=True)
+
+
+def test_box_form_matches_level_form(cuda, hxlib, oracle_lib):
+    """The AMReX drop-in (ghost-filled per-box views, four boxes) equals the
+    single-box level form, including the FL/FR face arrays the reflux needs."""
+    case = workloads.fractal_dam_break(64, 48, seed=41, amplitude=1.5, nodata_frac=0.1)
+    g = case.geom
+    L = oracle_lib.Level(g.nx, g.ny, g.dx, g.dy, g.bc_lo, g.bc_hi)
+    h, hu, hv, *_ = oracle_lib.run(L, 1, case.h, case.hu, case.hv, case.z, case.n, 5, case.cfl)
+    mn, _ = oracle_lib.compute_dt(L, h, hu, hv, case.z)
+    dt = mn * case.cfl
+    (rh, rhu, rhv), F = oracle_lib.advance(L, 1, h, hu, hv, case.z, case.n, dt, faces=True)
+    # ghost-filled arrays (2 ghosts) exactly as FillPatch + HydroPhysBC leave them
+    G = 2
+    eta = h + case.z
+    ext = lambda a, mode_x, mode_y: _bc_ext(a, G, mode_x, mode_y)
+    eta_e = ext(eta, "even", "even")
+    hu_e = ext(hu, "odd", "even")
+    hv_e = ext(hv, "even", "odd")
+    z_e = ext(case.z, "edge", "edge")
+    n_e = ext(case.n, "edge", "edge")
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(cuda)
+    Eta = dev(eta_e[None])
+    Uext = dev(np.stack([np.zeros_like(hu_e), hu_e, hv_e]))
+    Text = dev(np.stack([z_e, n_e]))
+    Uold = dev(np.stack([h, hu, hv]))
+    Unew = torch.zeros_like(Uold)
+    FLx = torch.zeros((3, g.ny, g.nx + 1), dtype=torch.float64, device=cuda)
+    FRx = torch.zeros_like(FLx)
+    FLy = torch.zeros((3, g.ny + 1, g.nx), dtype=torch.float64, device=cuda)
+    FRy = torch.zeros_like(FLy)
+    acc = DtAccum(cuda)
+    for (x0, x1), (y0, y1) in [((0, 29), (0, 20)), ((30, 63), (0, 20)), ((0, 29), (21, 47)), ((30, 63), (21, 47))]:
+        FLarr = (capi.Array4F64 * 2)(array4(FLx), array4(FLy))
+        FRarr = (capi.Array4F64 * 2)(array4(FRx), array4(FRy))
+        rc = hxlib.lib().hx_advance_box_hydrostatic_f64(
+            ctypes.byref(array4(Eta, (-G, -G))), ctypes.byref(array4(Uext, (-G, -G))),
+            ctypes.byref(array4(Text, (-G, -G))), ctypes.byref(array4(Uold)), ctypes.byref(array4(Unew)),
+            box((x0, y0), (x1, y1)), dt, g.dx, g.dy, FLarr, FRarr, acc.ptr, None, EXACT, None)
+        hxlib.check(rc, "box")
+    got = Unew.cpu().numpy()
+    assert np.array_equal(got[0], rh) and np.array_equal(got[1], rhu) and np.array_equal(got[2], rhv)
+    for name, t in (("FLx", FLx), ("FRx", FRx), ("FLy", FLy), ("FRy", FRy)):
+        assert np.array_equal(t.cpu().numpy(), F[name]), name
+    mn2, mx2 = oracle_lib.compute_dt(L, rh, rhu, rhv, case.z)
+    assert acc.read() == (mn2, mx2)
+
+
+def _bc_ext(a, G, mx, my):
+    """Ghost extension of a (ny, nx) plane: 'even' mirror, 'odd' mirror with
+    sign flip, 'edge' copy -- x rule then y rule (corners unused)."""
+    ny, nx = a.shape
+    out = np.zeros((ny + 2 * G, nx + 2 * G))
+    out[G:G + ny, G:G + nx] = a
+    for k in range(1, G + 1):
+        for side in (0, 1):
+            src = (k - 1) if side == 0 else nx - k
+            dst = G - k if side == 0 else G + nx - 1 + k
+            col = a[:, 0 if side == 0 else nx - 1] if mx == "edge" else a[:, src]
+            out[G:G + ny, dst] = -col if mx == "odd" else col
+    for k in range(1, G + 1):
+        for side in (0, 1):
+            src = (k - 1) if side == 0 else ny - k
+            dst = G - k if side == 0 else G + ny - 1 + k
+            row = out[G if side == 0 else G + ny - 1, :] if my == "edge" else out[G + src, :]
+            out[dst, :] = -row if my == "odd" else row
+    return out
+
+
+def test_dt_collapse_sets_status(cuda):
+    """A velocity explosion collapses the CFL bound below 1e-12: the loop stops
+    and reports HX_STATUS_DT_COLLAPSE (the reference aborts,
+    HydrostaticRoe.cpp:77-80) -- made on the host, no GPU fault involved."""
+    case = workloads.dam_break(32, 32, nsteps=3)
+    case.hu[5, 5] = 1.0e15
+    lev = Level.from_numpy(case.geom, case.h, case.hu, case.hv, case.z, case.n, device=cuda)
+    st = lev.run(capi.HX_METHOD_HYDROSTATIC_ROE, 3, case.cfl, arith=EXACT)
+    assert st & capi.HX_STATUS_DT_COLLAPSE
+    assert lev.time.item() == 0.0  # no step advanced the clock
+
+
+def test_nan_input_sets_status(cuda):
+    case = workloads.dam_break(32, 32)
+    case.h[7, 9] = np.nan
+    lev = Level.from_numpy(case.geom, case.h, case.hu, case.hv, case.z, case.n, device=cuda)
+    out = lev.advance(capi.HX_METHOD_HYDROSTATIC_ROE, 1e-4, arith=FAST)
+    torch.cuda.synchronize()
+    assert lev.status.read() & capi.HX_STATUS_NAN
+    assert torch.isnan(out).any()

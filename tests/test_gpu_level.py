@@ -1,0 +1,160 @@
+"""CUDA level advance, dt reduction and time loop against the oracle.
+
+Tolerances (BASELINE): conserved state within 1e-12 relative per step.  The
+exact arithmetic form is held to equality with the oracle (no friction) or
+1e-14 (friction: cbrt may differ by an ulp); the fast form to 1e-12 per step.
+FP32 is compared with the oracle instantiated in float at 1e-5.
+"""
+import numpy as np
+import pytest
+import torch
+
+from hydroexa_gb300 import capi, workloads
+from hydroexa_gb300.level import Level
+
+pytestmark = pytest.mark.gpu
+
+EXACT, FAST = capi.HX_ARITH_EXACT, capi.HX_ARITH_FAST
+
+
+def rel_err(a, b):
+    """max |a - b| / max |b| per component, worst component."""
+    worst = 0.0
+    for x, y in zip(a, b):
+        x = np.asarray(x, dtype=np.float64)
+        y = np.asarray(y, dtype=np.float64)
+        scale = max(np.abs(y).max(), 1e-300)
+        worst = max(worst, np.abs(x - y).max() / scale)
+    return worst
+
+
+def cases():
+    out = []
+    out.append(("dam_break", workloads.dam_break(64, 64)))
+    out.append(("lake_nodata", workloads.lake_at_rest(64, 64, seed=3, nodata_frac=0.1)))
+    out.append(("fractal", workloads.fractal_dam_break(96, 80, seed=5)))
+    c = workloads.fractal_dam_break(96, 80, seed=6, amplitude=1.0)
+    c.n[c.z > -9000] = 0.03
+    out.append(("friction", c))
+    c = workloads.fractal_dam_break(64, 64, seed=8, amplitude=1.0, nodata_frac=0.0)
+    c.geom.bc_lo, c.geom.bc_hi = (1, 0), (0, 1)
+    out.append(("mixed_bc", c))
+    c = workloads.fractal_dam_break(37, 23, seed=9, amplitude=0.5)
+    c.geom.bc_lo, c.geom.bc_hi = (1, 1), (1, 1)
+    out.append(("ragged_open", c))
+    return out
+
+
+def evolve(oracle, case, method, steps):
+    """A non-trivial state: the case advanced `steps` steps by the oracle."""
+    g = case.geom
+    L = oracle.Level(g.nx, g.ny, g.dx, g.dy, g.bc_lo, g.bc_hi)
+    h, hu, hv, *_ = oracle.run(L, method, case.h, case.hu, case.hv, case.z, case.n, steps, case.cfl)
+    return L, h, hu, hv
+
+
+def to_level(case, h, hu, hv, device, dtype=torch.float64):
+    return Level.from_numpy(case.geom, h, hu, hv, case.z, case.n, dtype=dtype, device=device)
+
+
+@pytest.mark.parametrize("method", [capi.HX_METHOD_HYDROSTATIC_ROE, capi.HX_METHOD_ROE])
+@pytest.mark.parametrize("name,case", cases(), ids=[c[0] for c in cases()])
+def test_advance_matches_oracle(cuda, oracle_lib, method, name, case):
+    L, h, hu, hv = evolve(oracle_lib, case, method, 6)
+    mn, _ = oracle_lib.compute_dt(L, h, hu, hv, case.z)
+    dt = mn * case.cfl
+    ref = oracle_lib.advance(L, method, h, hu, hv, case.z, case.n, dt)
+    lev = to_level(case, h, hu, hv, cuda)
+    got = lev.advance(method, dt, arith=EXACT).cpu().numpy()
+    friction = (case.n[case.z > -9000] != 0).any()
+    if friction:
+        assert rel_err(got, ref) <= 1e-14
+    else:
+        for k in range(3):
+            assert np.array_equal(got[k], ref[k]), (name, k, rel_err([got[k]], [ref[k]]))
+    fast = lev.advance(method, dt, arith=FAST).cpu().numpy()
+    assert rel_err(fast, ref) <= 1e-12
+    assert lev.status.read() == 0
+
+
+@pytest.mark.parametrize("name,case", cases(), ids=[c[0] for c in cases()])
+def test_dt_reduce_matches_oracle(cuda, oracle_lib, name, case):
+    L, h, hu, hv = evolve(oracle_lib, case, 1, 4)
+    mn, mx = oracle_lib.compute_dt(L, h, hu, hv, case.z)
+    lev = to_level(case, h, hu, hv, cuda)
+    gmn, gmx = lev.compute_dt()
+    assert gmn == mn and gmx == mx
+
+
+@pytest.mark.parametrize("method", [capi.HX_METHOD_HYDROSTATIC_ROE, capi.HX_METHOD_ROE])
+def test_time_loop_matches_oracle(cuda, oracle_lib, method):
+    """hx_level_run: device-resident dt chain (fused next-step bound) over 25
+    steps equals the oracle's host time loop."""
+    case = workloads.fractal_dam_break(80, 72, seed=12, amplitude=2.0)
+    g = case.geom
+    L = oracle_lib.Level(g.nx, g.ny, g.dx, g.dy, g.bc_lo, g.bc_hi)
+    ref = oracle_lib.run(L, method, case.h, case.hu, case.hv, case.z, case.n, 25, case.cfl)
+    lev = to_level(case, case.h, case.hu, case.hv, cuda)
+    st = lev.run(method, 25, case.cfl, arith=EXACT)
+    assert st == 0
+    got = lev.state.cpu().numpy()
+    assert rel_err(got, ref[:3]) == 0.0
+    assert lev.time.item() == pytest.approx(ref[3], rel=1e-15)
+    lev2 = to_level(case, case.h, case.hu, case.hv, cuda)
+    lev2.run(method, 25, case.cfl, arith=FAST)
+    assert rel_err(lev2.state.cpu().numpy(), ref[:3]) <= 1e-10
+
+
+@pytest.mark.parametrize("arith", [EXACT, FAST])
+def test_lake_at_rest_1000_steps(cuda, arith):
+    """C-property over 1000 steps on the 512^2 Gaussian mound with roughness
+    (no NODATA block: see test_nodata_wall_drops_pressure)."""
+    case = workloads.lake_at_rest(512, 512, seed=2, nodata_frac=0.0, nsteps=1000)
+    lev = to_level(case, case.h, case.hu, case.hv, cuda)
+    assert lev.run(capi.HX_METHOD_HYDROSTATIC_ROE, 1000, case.cfl, arith=arith) == 0
+    s = lev.state
+    wet = s[0] > 1e-6
+    vel = torch.sqrt(s[1] ** 2 + s[2] ** 2)[wet] / s[0][wet]
+    assert vel.max().item() <= 1e-13
+
+
+@pytest.mark.parametrize("method", [capi.HX_METHOD_HYDROSTATIC_ROE, capi.HX_METHOD_ROE])
+def test_mass_conservation_flat_bed_gpu(cuda, method):
+    case = workloads.fractal_dam_break(256, 256, seed=1, amplitude=0.0, nodata_frac=0.0)
+    lev = to_level(case, case.h, case.hu, case.hv, cuda)
+    m0 = lev.state[0].sum().item()
+    assert lev.run(method, 300, case.cfl, arith=FAST) == 0
+    m1 = lev.state[0].sum().item()
+    assert abs(m1 - m0) / m0 < 1e-12
+
+
+def test_fp32_advance(cuda, oracle_lib):
+    case = workloads.fractal_dam_break(64, 64, seed=21, amplitude=1.0)
+    L, h, hu, hv = evolve(oracle_lib, case, 1, 5)
+    f = [a.astype(np.float32) for a in (h, hu, hv, case.z, case.n)]
+    mn, _ = oracle_lib.compute_dt(L, f[0], f[1], f[2], f[3])
+    dt = np.float32(mn * case.cfl)
+    ref = oracle_lib.advance(L, 1, f[0], f[1], f[2], f[3], f[4], float(dt))
+    lev = Level.from_numpy(case.geom, *f, dtype=torch.float32, device=cuda)
+    got = lev.advance(1, float(dt), arith=FAST).cpu().numpy()
+    assert rel_err(got, ref) <= 1e-5
+
+
+def test_host_buffer_run(cuda, oracle_lib, hxlib):
+    """hx_level_run_host_f64 (host buffers in, host buffers out) equals the
+    device-resident run."""
+    import ctypes
+    case = workloads.fractal_dam_break(64, 48, seed=4, amplitude=1.0)
+    h, hu, hv = case.h.copy(), case.hu.copy(), case.hv.copy()
+    t = ctypes.c_double()
+    lo = (ctypes.c_int32 * 2)(*case.geom.bc_lo)
+    hi = (ctypes.c_int32 * 2)(*case.geom.bc_hi)
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    rc = hxlib.lib().hx_level_run_host_f64(1, 64, 48, case.geom.dx, case.geom.dy, lo, hi, P(h), P(hu), P(hv),
+                                           P(case.z), P(case.n), 10, case.cfl, EXACT, ctypes.byref(t), None)
+    assert rc == 0
+    lev = to_level(case, case.h, case.hu, case.hv, cuda)
+    lev.run(1, 10, case.cfl, arith=EXACT)
+    got = lev.state.cpu().numpy()
+    assert np.array_equal(got[0], h) and np.array_equal(got[1], hu) and np.array_equal(got[2], hv)
+    assert t.value == lev.time.item()

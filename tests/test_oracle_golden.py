@@ -1,0 +1,88 @@
+"""The oracle pinned against the reference: golden vectors produced by the
+reference's own kernels (tests/golden/make_golden.py) and, where the reference
+tree is present, a live comparison with those kernels compiled verbatim."""
+import os
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+GOLD = Path(__file__).resolve().parent / "golden"
+
+
+def bits_equal(a, b):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    ia = a.view(np.int64 if a.dtype == np.float64 else np.int32)
+    ib = b.view(np.int64 if b.dtype == np.float64 else np.int32)
+    return np.array_equal(ia, ib)
+
+
+@pytest.mark.parametrize("sfx", ["f64", "f32"])
+def test_roe_hydrostatic_golden(oracle_lib, sfx):
+    g = np.load(GOLD / f"roe_hydrostatic_{sfx}.npz")
+    F = oracle_lib.roe_hydrostatic_points(g["states"], g["normals"])
+    assert bits_equal(F, g["F"])
+
+
+@pytest.mark.parametrize("sfx", ["f64", "f32"])
+def test_roe_classic_golden(oracle_lib, sfx):
+    g = np.load(GOLD / f"roe_classic_{sfx}.npz")
+    F, Sm, Sp = oracle_lib.roe_classic_points(g["states"], g["aux"])
+    assert bits_equal(F, g["F"]) and bits_equal(Sm, g["Sm"]) and bits_equal(Sp, g["Sp"])
+
+
+def test_golden_covers_branches(oracle_lib):
+    """The golden set drives the dry clamp, both sonic fixes and both guards."""
+    g = np.load(GOLD / "roe_hydrostatic_f64.npz")
+    s = g["states"]
+    assert (s[:, 0] < 1e-6).sum() > 100 and (s[:, 3] < 1e-6).sum() > 100
+    n = g["normals"]
+    un_i = np.where(n[:, 0] == 1, s[:, 1], s[:, 2]) / np.where(s[:, 0] > 1e-6, s[:, 0], np.inf)
+    un_j = np.where(n[:, 0] == 1, s[:, 4], s[:, 5]) / np.where(s[:, 3] > 1e-6, s[:, 3], np.inf)
+    ci, cj = np.sqrt(9.81 * s[:, 0]), np.sqrt(9.81 * s[:, 3])
+    sonic0 = ((un_i - ci) < 0) & ((un_j - cj) > 0)
+    sonic2 = ((un_i + ci) < 0) & ((un_j + cj) > 0)
+    assert sonic0.sum() > 20 and sonic2.sum() > 20
+
+
+def test_masked_avgdown_golden(oracle_lib):
+    g = np.load(GOLD / "masked_avgdown_f64.npz")
+    for r in (2, 4):
+        c = oracle_lib.masked_average_down(g["fine"], r, r, float(g["fine_volume"]))
+        assert np.array_equal(c, g[f"crse_r{r}"], equal_nan=True)
+
+
+def _ref_available():
+    ref = Path(os.environ.get("HX_REFERENCE_ROOT", "/root/reference"))
+    return (ref / "include" / "solvers" / "kernels").is_dir()
+
+
+@pytest.mark.skipif(not _ref_available(), reason="reference tree not present")
+def test_oracle_matches_reference_kernels_live(oracle_lib):
+    rng = np.random.default_rng(11)
+    n = 3000
+    s = np.abs(rng.normal(0.3, 0.4, (n, 6)))
+    s[:, [1, 2, 4, 5]] = rng.normal(0, 1.5, (n, 4))
+    s[::5, 0] = 0.0
+    s[::9, 3] = 5e-7
+    nr = np.zeros((n, 2))
+    nr[::2, 0] = 1
+    nr[1::2, 1] = 1
+    assert bits_equal(oracle_lib.roe_hydrostatic_points(s, nr), oracle_lib.ref_roe_hydrostatic_points(s, nr))
+    s10 = np.column_stack([s[:, :3], rng.normal(0, 1, n), rng.uniform(0, 0.05, n), s[:, 3:], rng.normal(0, 1, n),
+                           rng.uniform(0, 0.05, n)])
+    aux = np.column_stack([np.full(n, 1e-3), np.full(n, 0.05), nr])
+    A = oracle_lib.roe_classic_points(s10, aux)
+    B = oracle_lib.ref_roe_classic_points(s10, aux)
+    assert all(bits_equal(a, b) for a, b in zip(A, B))
+
+
+def test_limiter_abs_switch(oracle_lib):
+    """The two resolutions of the reference limiter's unqualified abs():
+    r = 0.5 gives phi = 2/3 with the floating abs and 0.5 with int abs."""
+    q = np.array([[0.0, 0.5, 1.5]])  # dm = 0.5, dp = 1.0 -> r = 0.5
+    f = oracle_lib.van_leer_slope_points(q, oracle_lib.LIMITER_FLOAT_ABS)[0]
+    i = oracle_lib.van_leer_slope_points(q, oracle_lib.LIMITER_INT_ABS)[0]
+    assert f == pytest.approx(2.0 / 3.0, rel=1e-15)
+    assert i == pytest.approx(0.5, rel=1e-15)
