@@ -174,6 +174,7 @@ def config_dict():
 
 
 def main():
+    global NX, NY
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
@@ -184,6 +185,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    NX = NY = args.size
     if args.impl == "reference":
         return run_reference(args)
 
@@ -204,8 +206,6 @@ def main():
         dist.init_process_group("nccl", device_id=dev)
     hydroexa_gb300.build()
     arith = capi.HX_ARITH_FAST if args.arith == "fast" else capi.HX_ARITH_EXACT
-    global NX, NY
-    NX = NY = args.size
     case = make_case(NX, NY)
     cells = NX * NY
     lev = Level.from_numpy(case.geom, case.h, case.hu, case.hv, case.z, case.n, device=dev)
@@ -324,7 +324,7 @@ def main():
 def load_profile_summary():
     """Per-launch DRAM traffic and FP64 instruction counts of the dominant
     kernel from the committed ncu summary (profiles/), when present."""
-    p = ROOT / "profiles" / "k_hydro_tile_metrics.json"
+    p = ROOT / "profiles" / "k_hydro_tile_metrics.txt"  # JSON figures from the ncu summary
     if p.exists():
         try:
             return json.loads(p.read_text())

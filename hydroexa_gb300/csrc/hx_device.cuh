@@ -38,13 +38,13 @@ template <> struct Cst<float> {
 };
 
 // std::max(0, x) of the reference: (0 < x) ? x : 0 (NaN -> 0).
-template <class R> __device__ __forceinline__ R max0(R x) { return (R(0) < x) ? x : R(0); }
-template <class R> __device__ __forceinline__ R smax(R a, R b) { return (a < b) ? b : a; }
+template <class R> __host__ __device__ __forceinline__ R max0(R x) { return (R(0) < x) ? x : R(0); }
+template <class R> __host__ __device__ __forceinline__ R smax(R a, R b) { return (a < b) ? b : a; }
 
 // NODATA predicate of the hydrostatic face kernel and compute_dt_Impl
 // (HydrostaticRoe.cpp:41,238): |z + 9999| < 1e-10, evaluated in double as the
 // reference's literal -9999.0 forces.
-template <class R> __device__ __forceinline__ bool is_nodata(R z) {
+template <class R> __host__ __device__ __forceinline__ bool is_nodata(R z) {
     return fabs((double)z + 9999.0) < 1e-10;
 }
 
@@ -59,7 +59,7 @@ template <> __device__ __forceinline__ bool bits_nonfinite<float>(float x) {
 // ----------------------------------------------------------------------------
 // MUSCL van Leer slope (src/solvers/HydrostaticRoe.cpp:173-195), floating abs.
 // ----------------------------------------------------------------------------
-template <class R, bool FAST> __device__ __forceinline__ R van_leer_slope(R qm, R q, R qp) {
+template <class R, bool FAST> __host__ __device__ __forceinline__ R van_leer_slope(R qm, R q, R qp) {
     const R dm = q - qm;
     const R dp = qp - q;
     if (fabs(dp) <= Cst<R>::tol12) return R(0);
@@ -80,7 +80,7 @@ template <class R, bool FAST> __device__ __forceinline__ R van_leer_slope(R qm, 
 // value-exact.  Exact form: inputs are the face depths and global momenta.
 // ----------------------------------------------------------------------------
 template <int DIR, class R>
-__device__ __forceinline__ void roe_hydrostatic_exact(R hi, R hui, R hvi, R hj, R huj, R hvj, R& F0, R& F1,
+__host__ __device__ __forceinline__ void roe_hydrostatic_exact(R hi, R hui, R hvi, R hj, R huj, R hvj, R& F0, R& F1,
                                                       R& F2) {
     using C = Cst<R>;
     hi = (hi >= C::toldry) ? hi : R(0);
@@ -141,7 +141,7 @@ __device__ __forceinline__ void roe_hydrostatic_exact(R hi, R hui, R hvi, R hj, 
 // serves both Roe-average quotients and one serves the three wave strengths;
 // the wave speeds sqrt(g h) reuse sqrt(h).
 template <class R, int DIR>
-__device__ __forceinline__ void roe_hydrostatic_fast(R hi, R ui, R vi, R hj, R uj, R vj, R& F0, R& F1, R& F2) {
+__host__ __device__ __forceinline__ void roe_hydrostatic_fast(R hi, R ui, R vi, R hj, R uj, R vj, R& F0, R& F1, R& F2) {
     using C = Cst<R>;
     const bool wi = hi >= C::toldry, wj = hj >= C::toldry;
     hi = wi ? hi : R(0);
@@ -201,7 +201,7 @@ __device__ __forceinline__ void roe_hydrostatic_fast(R hi, R ui, R vi, R hj, R u
 // time.  Outputs F, S-, S+ in global coordinates.
 // ----------------------------------------------------------------------------
 template <class R, bool FAST, int DIR>
-__device__ __forceinline__ void roe_classic(R hi, R hui, R hvi, R zi, R ni, R hj, R huj, R hvj, R zj, R nj, R dx,
+__host__ __device__ __forceinline__ void roe_classic(R hi, R hui, R hvi, R zi, R ni, R hj, R huj, R hvj, R zj, R nj, R dx,
                                             R F[3], R Sm[3], R Sp[3]) {
     using C = Cst<R>;
     const R T12 = C::tol12, TD = C::toldry;

@@ -178,6 +178,7 @@ class Level:
 
         Returns the device status bits (read with a stream synchronisation when
         ``check_status``)."""
+        self.status.clear(stream)
         d = self._desc(self.state)
         fin = ctypes.c_int(0)
         capi.check(getattr(capi.lib(), f"hx_level_run_{self.sfx}")(

@@ -32,26 +32,50 @@ def run_points(hxlib, method, arith, states, aux, dev):
     return out.cpu().numpy()
 
 
+def term_scale(states):
+    """Magnitude of the terms a face flux is made of (h u^2 + g h^2 / 2 + |h u|
+    on both sides): fluxes that cancel to ~0 are judged against it."""
+    s = np.asarray(states, dtype=np.float64)
+    thrust = 0.0
+    if s.shape[1] == 10:  # classic states also carry the bed: add the thrust g h |dz|
+        thrust = 9.81 * (s[:, 0] + s[:, 5]) * np.abs(s[:, 8] - s[:, 3])
+        s = s[:, [0, 1, 2, 5, 6, 7]]
+    hi, hj = s[:, 0], s[:, 3]
+    qi = np.abs(s[:, 1]) + np.abs(s[:, 2])
+    qj = np.abs(s[:, 4]) + np.abs(s[:, 5])
+    ui = np.where(hi > 0, qi / np.where(hi > 0, hi, 1), 0)
+    uj = np.where(hj > 0, qj / np.where(hj > 0, hj, 1), 0)
+    return (qi * ui + qj * uj + 4.905 * (hi ** 2 + hj ** 2) + qi + qj + thrust + 1e-300)[:, None]
+
+
 def test_hydrostatic_points_golden(cuda, hxlib):
     g = np.load(GOLD / "roe_hydrostatic_f64.npz")
     got = run_points(hxlib, 1, EXACT, g["states"], g["normals"], cuda).reshape(-1, 3)
     assert np.array_equal(got, g["F"])
     fast = run_points(hxlib, 1, FAST, g["states"], g["normals"], cuda).reshape(-1, 3)
-    scale = np.abs(g["F"]).max(axis=1, keepdims=True) + 1e-300
-    assert (np.abs(fast - g["F"]) / scale).max() <= 1e-12
+    assert (np.abs(fast - g["F"]) / term_scale(g["states"])).max() <= 1e-13
 
 
 def test_classic_points_golden(cuda, hxlib):
+    """Bit-equal where the face has no Manning roughness; with roughness the
+    friction term goes through cbrt, where CUDA and glibc may differ by an ulp."""
     g = np.load(GOLD / "roe_classic_f64.npz")
     got = run_points(hxlib, 0, EXACT, g["states"], g["aux"], cuda).reshape(3, -1, 3)
-    assert np.array_equal(got[0], g["F"]) and np.array_equal(got[1], g["Sm"]) and np.array_equal(got[2], g["Sp"])
+    smooth = (g["states"][:, 4] + g["states"][:, 9]) == 0
+    sc = term_scale(g["states"])
+    for k, name in enumerate(("F", "Sm", "Sp")):
+        assert np.array_equal(got[k][smooth], g[name][smooth]), name
+        assert (np.abs(got[k] - g[name]) / sc).max() <= 1e-14, name
+    fast = run_points(hxlib, 0, FAST, g["states"], g["aux"], cuda).reshape(3, -1, 3)
+    for k, name in enumerate(("F", "Sm", "Sp")):
+        assert (np.abs(fast[k] - g[name]) / sc).max() <= 1e-12, name
 
 
 def test_points_f32_golden(cuda, hxlib):
     g = np.load(GOLD / "roe_hydrostatic_f32.npz")
     got = run_points(hxlib, 1, FAST, g["states"], g["normals"], cuda).reshape(-1, 3)
-    scale = np.abs(g["F"]).max(axis=1, keepdims=True) + 1e-30
-    assert (np.abs(got - g["F"]) / scale).max() <= 1e-5
+    # the reference's SINGLE build promotes double literals; the FP32 kernel stays in float
+    assert (np.abs(got - g["F"]) / term_scale(g["states"])).max() <= 5e-5
 
 
 def ghosted(a, g=1):

@@ -60,6 +60,8 @@ def to_level(case, h, hu, hv, device, dtype=torch.float64):
 @pytest.mark.parametrize("method", [capi.HX_METHOD_HYDROSTATIC_ROE, capi.HX_METHOD_ROE])
 @pytest.mark.parametrize("name,case", cases(), ids=[c[0] for c in cases()])
 def test_advance_matches_oracle(cuda, oracle_lib, method, name, case):
+    if method == capi.HX_METHOD_ROE and (case.z == -9999.0).any():
+        pytest.skip("classic Roe has no NODATA wall: see test_classic_roe_nodata_collapses")
     L, h, hu, hv = evolve(oracle_lib, case, method, 6)
     mn, _ = oracle_lib.compute_dt(L, h, hu, hv, case.z)
     dt = mn * case.cfl
@@ -90,10 +92,12 @@ def test_dt_reduce_matches_oracle(cuda, oracle_lib, name, case):
 def test_time_loop_matches_oracle(cuda, oracle_lib, method):
     """hx_level_run: device-resident dt chain (fused next-step bound) over 25
     steps equals the oracle's host time loop."""
-    case = workloads.fractal_dam_break(80, 72, seed=12, amplitude=2.0)
+    nod = 0.2 if method == capi.HX_METHOD_HYDROSTATIC_ROE else 0.0
+    case = workloads.fractal_dam_break(80, 72, seed=12, amplitude=2.0, nodata_frac=nod)
     g = case.geom
     L = oracle_lib.Level(g.nx, g.ny, g.dx, g.dy, g.bc_lo, g.bc_hi)
     ref = oracle_lib.run(L, method, case.h, case.hu, case.hv, case.z, case.n, 25, case.cfl)
+    assert ref[5] == 0
     lev = to_level(case, case.h, case.hu, case.hv, cuda)
     st = lev.run(method, 25, case.cfl, arith=EXACT)
     assert st == 0
@@ -103,6 +107,20 @@ def test_time_loop_matches_oracle(cuda, oracle_lib, method):
     lev2 = to_level(case, case.h, case.hu, case.hv, cuda)
     lev2.run(method, 25, case.cfl, arith=FAST)
     assert rel_err(lev2.state.cpu().numpy(), ref[:3]) <= 1e-10
+
+
+def test_classic_roe_nodata_collapses(cuda, oracle_lib):
+    """Reference behaviour, reproduced: the classic solver has no NODATA wall, so
+    a wet cell next to a NODATA cell (bed -9999 m, roughness -9999) drains into
+    it, velocities explode and the CFL bound collapses; the oracle's time loop
+    stops (status 1) and the device loop reports HX_STATUS_DT_COLLAPSE."""
+    case = workloads.fractal_dam_break(80, 72, seed=12, amplitude=2.0, nodata_frac=0.2)
+    g = case.geom
+    L = oracle_lib.Level(g.nx, g.ny, g.dx, g.dy, g.bc_lo, g.bc_hi)
+    ref = oracle_lib.run(L, capi.HX_METHOD_ROE, case.h, case.hu, case.hv, case.z, case.n, 60, case.cfl)
+    lev = to_level(case, case.h, case.hu, case.hv, cuda)
+    st = lev.run(capi.HX_METHOD_ROE, 60, case.cfl, arith=EXACT)
+    assert ref[5] == 1 and (st & capi.HX_STATUS_DT_COLLAPSE)
 
 
 @pytest.mark.parametrize("arith", [EXACT, FAST])
