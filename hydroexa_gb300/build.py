@@ -1,11 +1,12 @@
 """Build the CUDA library ``hydroexa_gb300/libhydroexa_gb300.so`` for sm_103a.
 
-Three translation units compiled in parallel, then linked:
+Four translation units compiled in parallel, then linked:
 
 * ``hx_exact.cu``  -- exact arithmetic form, ``--fmad=false`` (no multiply-add
   contraction, the reference's host rounding); tags and restriction kernels.
 * ``hx_fast.cu``   -- fast arithmetic form (shared reciprocals, contraction).
 * ``hx_capi.cu``   -- the C ABI declared in ``include/hydroexa_gb300.h``.
+* ``hx_noalloc.cu`` -- the allocation-free time loop (scratch in a static device array).
 
 The build is in-tree (objects in ``_build/``), takes well under a minute, and
 needs only nvcc; the CUDA runtime is linked statically so the library loads
@@ -31,6 +32,7 @@ UNITS = {
     "hx_exact": ["--fmad=false"],
     "hx_fast": [],
     "hx_capi": [],
+    "hx_noalloc": [],
 }
 
 

@@ -106,6 +106,8 @@ def _declare(L):
                                         c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_double, c_int,
                                         POINTER(c_double), c_void_p]
     L.hx_host_cache_release.restype = None
+    L.hx_level_run_static_f64.argtypes = [c_int, POINTER(LevelF64), c_int, c_double, c_void_p, c_void_p, c_int,
+                                          c_void_p]
 
 
 def check(rc: int, what: str = "") -> int:
@@ -133,5 +135,6 @@ EXPORTED = [
     "hx_masked_average_down_box_f64", "hx_masked_average_down_box_f32", "hx_level_advance_f64",
     "hx_level_advance_f32", "hx_level_dt_reduce_f64", "hx_level_dt_reduce_f32", "hx_level_run_work_bytes",
     "hx_level_run_f64", "hx_level_run_f32", "hx_level_run_host_f64", "hx_host_cache_release",
-    "hx_debug_roe_points_f64", "hx_debug_roe_points_f32",
+    "hx_debug_roe_points_f64", "hx_debug_roe_points_f32", "hx_level_run_static_f64",
 ]
+HX_STATIC_RUN_MAX_CELLS = 262144

@@ -339,6 +339,13 @@ thread_local HostCache g_host;
 
 }  // namespace
 
+namespace hx {
+// Shared with the other C-ABI translation units: launch counting and the
+// thread's last error text.
+void note_launches(int n) { g_launches.fetch_add((unsigned long long)n, std::memory_order_relaxed); }
+int set_error(int code, const char* msg) { return fail(code, "%s", msg); }
+}  // namespace hx
+
 // ============================================================================
 extern "C" {
 

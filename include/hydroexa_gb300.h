@@ -282,6 +282,35 @@ int hx_level_run_host_f64(int method, int nx, int ny, double dx, double dy, cons
                           const double* n, int nsteps, double cfl, int arith, double* time_out, hx_stream_t stream);
 void hx_host_cache_release(void);
 
+/*
+ * Allocation-free form of hx_level_run_f64.  No counterpart in the reference:
+ * it is for callers that cannot allocate device memory of their own.  HydroEXA
+ * runs on AMReX, whose arena reserves most of the GPU's memory at start-up
+ * (three quarters by default) and serves all later requests itself, so a
+ * cudaMalloc issued by a library in the middle of the time loop can fail or
+ * compete with the arena; other host codes forbid allocation once their loop
+ * has started.  This call allocates nothing: the scratch the loop needs (the
+ * alternate state planes it ping-pongs into and the three rotating CFL
+ * accumulators) is one fixed array inside this library,
+ * 256 bytes + 3 x HX_STATIC_RUN_MAX_CELLS doubles (6 MiB), which every GPU that
+ * loads the library holds until the process exits.
+ *   - The level must satisfy ny * pitch <= HX_STATIC_RUN_MAX_CELLS (512 x 512);
+ *     a larger one is rejected with HX_ERR_ARG and an explanatory
+ *     hx_last_error().  Use hx_level_run_f64 with your own scratch for it.
+ *   - The state is advanced in place: level->h, hu, hv hold the result.
+ *     status and time_dev are optional caller-owned device words as in
+ *     hx_level_run_f64.
+ *   - The first call on a device looks up the array's device address
+ *     (cudaGetSymbolAddress) with that device current and caches it; make that
+ *     first call before any stream capture.
+ *   - Every call uses the same array and each call clears the accumulators it
+ *     needs when it starts.  Calls that overlap on the GPU -- on two streams, or
+ *     from two host threads -- race on the array and corrupt each other.
+ */
+#define HX_STATIC_RUN_MAX_CELLS 262144
+int hx_level_run_static_f64(int method, hx_level_f64* level, int nsteps, double cfl, uint32_t* status,
+                            double* time_dev, int arith, hx_stream_t stream);
+
 /* ---- diagnostics --------------------------------------------------------- */
 
 /*
