@@ -183,6 +183,9 @@ def main():
     ap.add_argument("--arith", default="fast", choices=["fast", "exact"])
     ap.add_argument("--size", type=int, default=NX, help="level side (default 8192)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--precision", default="f64", choices=["f64", "f32"])
+    ap.add_argument("--no-ensemble", action="store_true")
+    ap.add_argument("--method", default="hydrostatic", choices=["hydrostatic", "roe"])
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     NX = NY = args.size
@@ -208,9 +211,14 @@ def main():
     arith = capi.HX_ARITH_FAST if args.arith == "fast" else capi.HX_ARITH_EXACT
     case = make_case(NX, NY)
     cells = NX * NY
-    lev = Level.from_numpy(case.geom, case.h, case.hu, case.hv, case.z, case.n, device=dev)
+    dtype = torch.float64 if args.precision == "f64" else torch.float32
+    if args.method == "roe":
+        # the classic solver has no NODATA wall: time it on the same terrain without the NODATA mask
+        from hydroexa_gb300 import workloads
+        case = workloads.fractal_dam_break(NX, NY, seed=3, nodata_frac=0.0)
+    lev = Level.from_numpy(case.geom, case.h, case.hu, case.hv, case.z, case.n, dtype=dtype, device=dev)
     stream = torch.cuda.current_stream(dev)
-    method = capi.HX_METHOD_HYDROSTATIC_ROE
+    method = capi.HX_METHOD_HYDROSTATIC_ROE if args.method == "hydrostatic" else capi.HX_METHOD_ROE
 
     def barrier():
         torch.cuda.synchronize(dev)
@@ -251,12 +259,12 @@ def main():
         ev[2 * k + 1].record(stream)
     torch.cuda.synchronize(dev)
     kms = statistics.mean(ev[2 * k].elapsed_time(ev[2 * k + 1]) for k in range(5))
-    achieved_gbs = BYTES_PER_CELL["f64"] * cells / (kms * 1e-3) / 1e9
+    achieved_gbs = BYTES_PER_CELL[args.precision] * cells / (kms * 1e-3) / 1e9
     profile = load_profile_summary()
 
     # ---- end to end through the host-buffer C-ABI call (pinned host memory)
     e2e = None
-    if True:  # every rank times its own replica end to end
+    if args.precision == "f64":  # every rank times its own replica end to end (the host-buffer call is FP64)
         pin = [torch.from_numpy(a.copy()).pin_memory() for a in (case.h, case.hu, case.hv, case.z, case.n)]
         P = [ctypes.c_void_p(t.data_ptr()) for t in pin]
         lo = (ctypes.c_int32 * 2)(*case.geom.bc_lo)
@@ -290,27 +298,37 @@ def main():
                "d2h_bytes_per_step": 24 * cells + 12, "steps": ke,
                "call": "hx_level_run_host_f64 (host buffers in/out, one step per call)"}
 
+    ens = None
+    if args.precision == "f64" and args.method == "hydrostatic" and not args.no_ensemble:
+        del lev
+        torch.cuda.empty_cache()
+        ens = ensemble_measure(dev)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_sample(case)
+        cpu = cpu_sample(case, method=method)
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64", "data": "synthetic (seeded fractal terrain; no dataset)",
-            "config": dict(config_dict(), arith=args.arith, nx=NX, ny=NY),
+            "dtype": args.precision, "data": "synthetic (seeded fractal terrain; no dataset)",
+            "config": dict(config_dict(), arith=args.arith, nx=NX, ny=NY, precision=args.precision.upper(),
+                           method={"hydrostatic": "HydrostaticRoe", "roe": "Roe (no NODATA)"}[args.method]),
             "e2e": e2e,
             "gpu_launches": launches,
             "roofline": {
                 "bound": "hbm", "achieved": achieved_gbs, "peak": HBM_GBS, "unit": "GB/s",
                 "frac": achieved_gbs / HBM_GBS, "traffic": profile.get("traffic_bytes_per_launch"),
                 "peak_source": HBM_SRC,
-                "kernel": "k_hydro_tile<double,%s,LevelSrc>" % ("true" if arith else "false"),
-                "kernel_ms": kms, "algorithmic_bytes_per_launch": BYTES_PER_CELL["f64"] * cells,
+                "kernel": "%s<%s,%s,LevelSrc>" % ("k_hydro_tile" if args.method == "hydrostatic" else "k_classic_tile",
+                                                  "double" if args.precision == "f64" else "float",
+                                                  "true" if arith else "false"),
+                "kernel_ms": kms, "algorithmic_bytes_per_launch": BYTES_PER_CELL[args.precision] * cells,
                 "note": "FP64-issue bound on GB300: see fp64_pipe",
-                "fp64_pipe": fp64_pipe(profile, kms),
+                "fp64_pipe": fp64_pipe(profile, kms) if (args.precision, args.method) == ("f64", "hydrostatic") else None,
             },
+            "ensemble": ens,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
         }
@@ -319,6 +337,59 @@ def main():
         dist.barrier()
         dist.destroy_process_group()
     return 0
+
+
+def ensemble_measure(dev, steps=24, warmup=6, plain_steps=6):
+    """BASELINE configs[3]: 256 independent dam breaks, sides log-uniform in
+    [64, 1024].  Batched (one persistent launch per step, CUDA graph, tile shape
+    per size class from the autotuner) against the members advanced one after
+    another, (a) with the per-level device time loop and (b) with the
+    reference's per-step host read of the CFL bound.  A bounded sample of the
+    500-step runs: `steps` (multiple of 6) timed steps after `warmup`."""
+    import torch
+
+    from hydroexa_gb300 import capi, workloads
+    from hydroexa_gb300.ensemble import SHAPE_NAMES, Ensemble, autotune
+
+    cases = workloads.ensemble(count=256, seed=4)
+    cells = sum(c.cells for c in cases)
+    cfl = cases[0].cfl
+    per_class, report = autotune(cases, device=dev, steps=6)
+    stream = torch.cuda.current_stream(dev)
+
+    def timed(fn):
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) * 1e-3
+
+    ens = Ensemble(cases, device=dev)
+    ens.set_shapes_by_class(per_class)
+    assert all(x == 0 for x in ens.run(warmup, cfl))
+    n0 = capi.launch_count()
+    t_b = timed(lambda: ens.run(steps, cfl, check_status=False))
+    launches = capi.launch_count() - n0
+    assert all(x == 0 for x in ens.status.cpu().tolist())
+    del ens
+    ref = Ensemble(cases, device=dev)
+    ref.member_loop(1, cfl)
+    t_m = timed(lambda: ref.member_loop(steps, cfl))
+    ref.plain_loop(1, cfl)
+    t_p = timed(lambda: ref.plain_loop(plain_steps, cfl))
+    del ref
+    v_b = cells * steps / t_b / 1e6
+    v_m = cells * steps / t_m / 1e6
+    v_p = cells * plain_steps / t_p / 1e6
+    return {"workload": "256 independent FP64 dam breaks (hydrostatic-Roe), sides log-uniform in [64,1024] (seed 4), "
+                        "%d cells, %d timed steps per member (sample of the 500-step runs)" % (cells, steps),
+            "batched": v_b, "member_loop": v_m, "plain_loop_host_dt": v_p, "unit": UNIT,
+            "speedup_vs_member_loop": v_b / v_m, "speedup_vs_plain_loop": v_b / v_p,
+            "batched_launches": launches,
+            "tile_shape_per_class": [SHAPE_NAMES[x] for x in per_class],
+            "class_edges": [128, 384]}
 
 
 def load_profile_summary():

@@ -1,12 +1,13 @@
 """Build the CUDA library ``hydroexa_gb300/libhydroexa_gb300.so`` for sm_103a.
 
-Four translation units compiled in parallel, then linked:
+Five translation units compiled in parallel, then linked:
 
 * ``hx_exact.cu``  -- exact arithmetic form, ``--fmad=false`` (no multiply-add
   contraction, the reference's host rounding); tags and restriction kernels.
 * ``hx_fast.cu``   -- fast arithmetic form (shared reciprocals, contraction).
 * ``hx_capi.cu``   -- the C ABI declared in ``include/hydroexa_gb300.h``.
 * ``hx_noalloc.cu`` -- the allocation-free time loop (scratch in a static device array).
+* ``hx_ensemble.cu`` -- the batched-ensemble plan, dt initialisation and CUDA-graph replay.
 
 The build is in-tree (objects in ``_build/``), takes well under a minute, and
 needs only nvcc; the CUDA runtime is linked statically so the library loads
@@ -33,6 +34,7 @@ UNITS = {
     "hx_fast": [],
     "hx_capi": [],
     "hx_noalloc": [],
+    "hx_ensemble": [],
 }
 
 

@@ -59,6 +59,16 @@ def _level(real):
 LevelF64 = _level(c_double)
 LevelF32 = _level(c_float)
 
+
+class EnsembleMemberF64(Structure):
+    _fields_ = [("level", LevelF64), ("h_alt", c_void_p), ("hu_alt", c_void_p), ("hv_alt", c_void_p),
+                ("tile_shape", c_int32)]
+
+
+HX_TILE_32x8 = 0
+HX_TILE_16x16 = 1
+HX_TILE_64x4 = 2
+
 _lib = None
 
 
@@ -106,6 +116,11 @@ def _declare(L):
                                         c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_double, c_int,
                                         POINTER(c_double), c_void_p]
     L.hx_host_cache_release.restype = None
+    L.hx_ensemble_work_bytes.restype = c_int64
+    L.hx_ensemble_work_bytes.argtypes = [c_int]
+    L.hx_ensemble_tiles.argtypes = [c_int, POINTER(EnsembleMemberF64), POINTER(c_int64)]
+    L.hx_ensemble_run_f64.argtypes = [c_int, POINTER(EnsembleMemberF64), c_int, c_double, c_void_p, c_void_p,
+                                      c_void_p, c_int, c_int, POINTER(c_int), c_void_p]
     L.hx_level_run_static_f64.argtypes = [c_int, POINTER(LevelF64), c_int, c_double, c_void_p, c_void_p, c_int,
                                           c_void_p]
 
@@ -136,5 +151,6 @@ EXPORTED = [
     "hx_level_advance_f32", "hx_level_dt_reduce_f64", "hx_level_dt_reduce_f32", "hx_level_run_work_bytes",
     "hx_level_run_f64", "hx_level_run_f32", "hx_level_run_host_f64", "hx_host_cache_release",
     "hx_debug_roe_points_f64", "hx_debug_roe_points_f32", "hx_level_run_static_f64",
+    "hx_ensemble_work_bytes", "hx_ensemble_tiles", "hx_ensemble_run_f64",
 ]
 HX_STATIC_RUN_MAX_CELLS = 262144

@@ -262,7 +262,8 @@ int level_advance(int method, const L* lv, const StepCtl<R>& ctl, R* ho, R* huo,
     return launched(e, "hx_level_advance");
 }
 
-template <class R, class L> int level_dt(const L* lv, hx_dt_accum* acc, cudaStream_t st) {
+template <class R, class L>
+int level_dt(const L* lv, hx_dt_accum* acc, cudaStream_t st, int arith = HX_ARITH_EXACT) {
     if (!level_ok(lv)) return HX_ERR_ARG;
     if (!acc) return fail(HX_ERR_ARG, "null accumulator");
     Cells3<R> U;
@@ -270,7 +271,9 @@ template <class R, class L> int level_dt(const L* lv, hx_dt_accum* acc, cudaStre
     U.js = lv->pitch; U.lo0 = 0; U.lo1 = 0;
     Plane<R> Z{lv->z, lv->pitch, 0, 0};
     const IBox vb{0, 0, lv->nx - 1, lv->ny - 1};
-    return launched(launch_dt_reduce<R, false>(U, Z, vb, lv->dx, lv->dy, reinterpret_cast<DtAccum*>(acc), st),
+    DtAccum* a = reinterpret_cast<DtAccum*>(acc);
+    return launched(arith == HX_ARITH_EXACT ? launch_dt_reduce<R, false>(U, Z, vb, lv->dx, lv->dy, a, st)
+                                            : launch_dt_reduce<R, true>(U, Z, vb, lv->dx, lv->dy, a, st),
                     "hx_level_dt_reduce");
 }
 
@@ -288,7 +291,7 @@ int level_run(int method, L* lv, R* ha, R* hua, R* hva, int nsteps, R cfl, void*
     DtAccum* slot = reinterpret_cast<DtAccum*>(work);
     cudaError_t e = cudaMemsetAsync(slot, 0, 2 * sizeof(DtAccum), st);
     if (e != cudaSuccess) return fail(HX_ERR_CUDA, "memset: %s", cudaGetErrorString(e));
-    int rc = level_dt<R>(lv, reinterpret_cast<hx_dt_accum*>(&slot[0]), st);
+    int rc = level_dt<R>(lv, reinterpret_cast<hx_dt_accum*>(&slot[0]), st, arith);
     if (rc) return rc;
     const R* A[3] = {lv->h, lv->hu, lv->hv};
     R* B[3] = {ha, hua, hva};

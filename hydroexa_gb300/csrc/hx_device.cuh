@@ -12,9 +12,11 @@
 #pragma once
 
 #include <cstdint>
+#include <cstring>
 #include <cuda_runtime.h>
 
 #include "../../include/hydroexa_gb300.h"
+#include "hx_dual.cuh"
 
 namespace hx {
 
@@ -27,6 +29,9 @@ template <> struct Cst<double> {
     static constexpr double toldry = 1e-6;
     static constexpr double tol12 = 1e-12;
     static constexpr double tol10 = 1e-10;
+    // IEEE bit patterns of the positive tolerances (for integer comparisons)
+    static constexpr long long toldry_bits = 0x3eb0c6f7a0b5ed8dll;
+    static constexpr long long tol12_bits = 0x3d719799812dea11ll;
 };
 template <> struct Cst<float> {
     static constexpr float g = 9.81f;
@@ -35,6 +40,17 @@ template <> struct Cst<float> {
     static constexpr float toldry = 1e-6f;
     static constexpr float tol12 = 1e-12f;
     static constexpr float tol10 = 1e-10f;
+    static constexpr int toldry_bits = 0x358637bd;
+    static constexpr int tol12_bits = 0x2b8cbccc;
+};
+
+template <> struct Cst<Dual> {
+    static constexpr Dual g = Dual(9.81);
+    static constexpr Dual half_g = Dual(0.5 * 9.81);
+    static constexpr Dual sqrt_g = Dual(3.1320919526731650);
+    static constexpr Dual toldry = Dual(1e-6);
+    static constexpr Dual tol12 = Dual(1e-12);
+    static constexpr Dual tol10 = Dual(1e-10);
 };
 
 // std::max(0, x) of the reference: (0 < x) ? x : 0 (NaN -> 0).
@@ -55,6 +71,90 @@ template <> __device__ __forceinline__ bool bits_nonfinite<double>(double x) {
 template <> __device__ __forceinline__ bool bits_nonfinite<float>(float x) {
     return ((unsigned)__float_as_uint(x) & 0x7F800000u) == 0x7F800000u;
 }
+template <> __device__ __forceinline__ bool bits_nonfinite<Dual>(Dual x) {
+    return bits_nonfinite<double>(x.v) || bits_nonfinite<double>(x.d);
+}
+
+// ----------------------------------------------------------------------------
+// Comparisons on IEEE bit patterns.  On GB300 a double-precision compare,
+// min or max issues on the scarce FP64 pipe; the same decision taken on the
+// integer pipe is free by comparison.  For non-NaN x:
+//   x > c  (c > 0)   <=>  bits(x) > bits(c) as signed integers
+//   x > 0            <=>  bits(x) > 0           (+0 and -0 are not > 0)
+//   x < 0            <=>  bits(x) > sign bit as unsigned (-0 is not < 0)
+// and okey() maps doubles to integers with the same order (for max of signed
+// values).  Used by the fast form only; NaN inputs are flagged separately.
+// ----------------------------------------------------------------------------
+__host__ __device__ __forceinline__ long long sbits(double x) {
+#ifdef __CUDA_ARCH__
+    return __double_as_longlong(x);
+#else
+    long long b;
+    memcpy(&b, &x, sizeof b);
+    return b;
+#endif
+}
+__host__ __device__ __forceinline__ int sbits(float x) {
+#ifdef __CUDA_ARCH__
+    return __float_as_int(x);
+#else
+    int b;
+    memcpy(&b, &x, sizeof b);
+    return b;
+#endif
+}
+template <class R> __host__ __device__ __forceinline__ bool gt_bits(R x, decltype(sbits(R(0))) cb) {
+    return sbits(x) > cb;
+}
+template <class R> __host__ __device__ __forceinline__ bool ge_bits(R x, decltype(sbits(R(0))) cb) {
+    return sbits(x) >= cb;
+}
+template <class R> __host__ __device__ __forceinline__ bool pos_i(R x) { return sbits(x) > 0; }
+__host__ __device__ __forceinline__ bool neg_i(double x) {
+    return (unsigned long long)sbits(x) > 0x8000000000000000ull;
+}
+__host__ __device__ __forceinline__ bool neg_i(float x) { return (unsigned)sbits(x) > 0x80000000u; }
+template <class R> __host__ __device__ __forceinline__ R max0_i(R x) { return pos_i(x) ? x : R(0); }
+__host__ __device__ __forceinline__ bool abs_le_bits(double x, long long cb) {
+    return (sbits(x) & 0x7FFFFFFFFFFFFFFFll) <= cb;
+}
+__host__ __device__ __forceinline__ bool abs_le_bits(float x, int cb) { return (sbits(x) & 0x7FFFFFFF) <= cb; }
+__host__ __device__ __forceinline__ long long okey(double x) {
+    const long long b = sbits(x);
+    return b >= 0 ? b : (b ^ 0x7FFFFFFFFFFFFFFFll);
+}
+__host__ __device__ __forceinline__ int okey(float x) {
+    const int b = sbits(x);
+    return b >= 0 ? b : (b ^ 0x7FFFFFFF);
+}
+// std::max(a, b) = (a < b) ? b : a
+template <class R> __host__ __device__ __forceinline__ R smax_i(R a, R b) { return okey(a) < okey(b) ? b : a; }
+// max of two non-negative values
+template <class R> __host__ __device__ __forceinline__ R nnmax_i(R a, R b) { return sbits(a) < sbits(b) ? b : a; }
+
+// Reciprocal of a positive normal x by Newton-Raphson, y <- y + y (1 - x y)
+// (Markstein, IBM J. Res. Dev. 34, 1990), twice, from the hardware estimate
+// rcp.approx.ftz.f64: four FMAs instead of a full IEEE division.  Callers only
+// pass finite, positive, normal arguments.
+__host__ __device__ __forceinline__ double rcp_nr(double x) {
+#ifdef __CUDA_ARCH__
+    double y;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    double e = fma(-x, y, 1.0);
+    y = fma(y, e, y);
+    e = fma(-x, y, 1.0);
+    return fma(y, e, y);
+#else
+    return 1.0 / x;
+#endif
+}
+__host__ __device__ __forceinline__ float rcp_nr(float x) {
+#ifdef __CUDA_ARCH__
+    return __frcp_rn(x);
+#else
+    return 1.0f / x;
+#endif
+}
 
 // ----------------------------------------------------------------------------
 // MUSCL van Leer slope (src/solvers/HydrostaticRoe.cpp:173-195), floating abs.
@@ -62,14 +162,18 @@ template <> __device__ __forceinline__ bool bits_nonfinite<float>(float x) {
 template <class R, bool FAST> __host__ __device__ __forceinline__ R van_leer_slope(R qm, R q, R qp) {
     const R dm = q - qm;
     const R dp = qp - q;
-    if (fabs(dp) <= Cst<R>::tol12) return R(0);
+    if constexpr (FAST) {
+        if (abs_le_bits(dp, Cst<R>::tol12_bits)) return R(0);
+    } else {
+        if (fabs(dp) <= Cst<R>::tol12) return R(0);
+    }
     if constexpr (!FAST) {
         const R r = dm / dp;
         return (r + fabs(r)) / (R(1) + fabs(r)) * dp;
     } else {
         // phi(r) dp with r = dm/dp is 0 for r <= 0 and 2 dm dp / (dm + dp) otherwise.
         const R p = dm * dp;
-        return (p > R(0)) ? (R(2) * p) / (dm + dp) : R(0);
+        return pos_i(p) ? (p + p) * rcp_nr(dm + dp) : R(0);
     }
 }
 
@@ -141,9 +245,11 @@ __host__ __device__ __forceinline__ void roe_hydrostatic_exact(R hi, R hui, R hv
 // serves both Roe-average quotients and one serves the three wave strengths;
 // the wave speeds sqrt(g h) reuse sqrt(h).
 template <class R, int DIR>
-__host__ __device__ __forceinline__ void roe_hydrostatic_fast(R hi, R ui, R vi, R hj, R uj, R vj, R& F0, R& F1, R& F2) {
+__host__ __device__ __forceinline__ void roe_hydrostatic_fast(R hi, R ui, R vi, R hj, R uj, R vj, R& F0, R& F1,
+                                                             R& F2) {
     using C = Cst<R>;
-    const bool wi = hi >= C::toldry, wj = hj >= C::toldry;
+    // depths arrive non-negative (capped with max(0, .)), so bit comparisons apply
+    const bool wi = ge_bits(hi, C::toldry_bits), wj = ge_bits(hj, C::toldry_bits);
     hi = wi ? hi : R(0);
     hj = wj ? hj : R(0);
     ui = wi ? ui : R(0);
@@ -155,13 +261,14 @@ __host__ __device__ __forceinline__ void roe_hydrostatic_fast(R hi, R ui, R vi, 
     if (DIR == 0) { uni = ui; uti = vi; unj = uj; utj = vj; }
     else { uni = vi; uti = -ui; unj = vj; utj = -uj; }
     const R hh = R(0.5) * (hi + hj);
-    const R hm = (hh > C::toldry) ? hh : C::toldry;
+    const R hm = gt_bits(hh, C::toldry_bits) ? hh : C::toldry;
     const R cm = sqrt(C::g * hm);
     const R den = R(2) * cm + C::tol12;
     const R sden = si + sj + C::tol12;
-    // one division for 1/sden, 1/den and 1/cm
-    const R q = R(1) / (sden * (cm * den));
-    const R rs = (cm * den) * q;
+    // one reciprocal for 1/sden, 1/den and 1/cm
+    const R cd = cm * den;
+    const R q = rcp_nr(sden * cd);
+    const R rs = cd * q;
     const R rden = (sden * cm) * q;
     const R rcm = (sden * den) * q;
     const R um = (uni * si + unj * sj) * rs;
@@ -172,21 +279,22 @@ __host__ __device__ __forceinline__ void roe_hydrostatic_fast(R hi, R ui, R vi, 
     {
         const R ci = C::sqrt_g * si, cj = C::sqrt_g * sj;
         R ei = uni - ci, ej = unj - cj;
-        if (ei < R(0) && ej > R(0)) l0 = ei * (ej - l0) / (ej - ei);
+        if (neg_i(ei) && pos_i(ej)) l0 = ei * (ej - l0) / (ej - ei);
         ei = uni + ci;
         ej = unj + cj;
-        if (ei < R(0) && ej > R(0)) l2 = ej * (l2 - ei) / (ej - ei);
+        if (neg_i(ei) && pos_i(ej)) l2 = ej * (l2 - ei) / (ej - ei);
     }
     const R dh = hj - hi;
     const R qi = hi * uni, qj = hj * unj;
     const R dhu = qj - qi;
     const R dhv = hj * utj - hi * uti;
-    const R a0 = (l2 * dh - dhu) * rden;
-    const R a1 = (dhv - vm * dh) * rcm;
-    const R a2 = (dhu - l0 * dh) * rden;
-    const R w0 = R(0.5) * fabs(l0) * a0;
-    const R w1 = R(0.5) * fabs(l1) * a1;
-    const R w2 = R(0.5) * fabs(l2) * a2;
+    const R hrden = R(0.5) * rden;
+    const R a0h = (l2 * dh - dhu) * hrden;  // alpha0 / 2
+    const R a1h = (dhv - vm * dh) * (R(0.5) * rcm);
+    const R a2h = (dhu - l0 * dh) * hrden;
+    const R w0 = fabs(l0) * a0h;
+    const R w1 = fabs(l1) * a1h;
+    const R w2 = fabs(l2) * a2h;
     const R f0 = R(0.5) * (qi + qj) - (w0 + w2);
     const R f1 = R(0.5) * (qi * uni + qj * unj + C::half_g * (hi * hi + hj * hj)) - (w0 * l0 + w2 * l2);
     const R f2 = R(0.5) * (qi * uti + qj * utj) - ((w0 + w2) * vm + w1 * cm);
@@ -360,7 +468,7 @@ struct DtAccum {
 };
 static_assert(sizeof(DtAccum) == 64, "hx_dt_accum is 64 bytes");
 
-enum { DTF_DRY = 1, DTF_NODATA = 2, DTF_NAN = 4 };
+enum { DTF_DRY = 1, DTF_NODATA = 2, DTF_NAN = 4, DTF_COLLAPSED = 8 };
 
 template <class R> __device__ __forceinline__ unsigned long long to_bits(R x);
 template <> __device__ __forceinline__ unsigned long long to_bits<double>(double x) {
@@ -369,6 +477,7 @@ template <> __device__ __forceinline__ unsigned long long to_bits<double>(double
 template <> __device__ __forceinline__ unsigned long long to_bits<float>(float x) {
     return (unsigned long long)__float_as_uint(x);
 }
+template <> __device__ __forceinline__ unsigned long long to_bits<Dual>(Dual x) { return to_bits<double>(x.v); }
 template <class R> __host__ __device__ __forceinline__ R from_bits(unsigned long long b);
 template <> __host__ __device__ __forceinline__ double from_bits<double>(unsigned long long b) {
     union { unsigned long long u; double d; } c;
@@ -393,23 +502,30 @@ template <class R> __host__ __device__ __forceinline__ R accum_dt_min(unsigned l
     return m;
 }
 
-// Per-cell contribution of compute_dt_Impl (HydrostaticRoe.cpp:41-61).
+// Per-cell contribution of compute_dt_Impl (HydrostaticRoe.cpp:41-61).  nod is
+// the cell's NODATA predicate |z + 9999| < 1e-10.
 template <class R, bool FAST>
-__device__ __forceinline__ void dt_cell_contrib(R h, R hu, R hv, R z, R dx, R dy, R idx, R idy, R& rate, R& mv,
+__device__ __forceinline__ void dt_cell_contrib(R h, R hu, R hv, bool nod, R dx, R dy, R idx, R idy, R& rate, R& mv,
                                                 unsigned& flags) {
     rate = R(0);
     mv = R(0);
-    if (is_nodata(z)) { flags |= DTF_NODATA; return; }
-    if (!(h > Cst<R>::tol12)) { flags |= DTF_DRY; return; }
-    R u, v;
-    if constexpr (!FAST) { u = hu / h; v = hv / h; }
-    else { const R r = R(1) / h; u = hu * r; v = hv * r; }
-    const R c = sqrt(Cst<R>::g * h);
-    const R sx = fabs(u) + c;
-    const R sy = fabs(v) + c;
-    if constexpr (!FAST) rate = sx / dx + sy / dy;
-    else rate = sx * idx + sy * idy;
-    mv = smax(fabs(u), fabs(v));
+    if (nod) { flags |= DTF_NODATA; return; }
+    if constexpr (!FAST) {
+        if (!(h > Cst<R>::tol12)) { flags |= DTF_DRY; return; }
+        const R u = hu / h, v = hv / h;
+        const R c = sqrt(Cst<R>::g * h);
+        const R sx = fabs(u) + c;
+        const R sy = fabs(v) + c;
+        rate = sx / dx + sy / dy;
+        mv = smax(fabs(u), fabs(v));
+    } else {
+        if (!gt_bits(h, Cst<R>::tol12_bits)) { flags |= DTF_DRY; return; }
+        const R r = rcp_nr(h);
+        const R u = hu * r, v = hv * r;
+        const R c = sqrt(Cst<R>::g * h);
+        rate = (fabs(u) + c) * idx + (fabs(v) + c) * idy;
+        mv = nnmax_i(fabs(u), fabs(v));
+    }
     if (bits_nonfinite(rate)) { flags |= DTF_NAN; rate = R(0); mv = R(0); }
 }
 

@@ -27,6 +27,32 @@ namespace hx {
 HX_INST(double)
 HX_INST(float)
 #undef HX_INST
+template cudaError_t launch_ensemble<double, false>(const EnsInstance<double>*, int, long long, int, double, unsigned long long*, int, cudaStream_t);
+template int ensemble_blocks_per_sm<double, false>();
 template cudaError_t launch_points<double, false>(int, long, const double*, const double*, double*, cudaStream_t);
 template cudaError_t launch_points<float, false>(int, long, const float*, const float*, float*, cudaStream_t);
+}  // namespace hx
+
+// ---------------------------------------------------------------------------
+// Tangent-linear step: the exact tile body carried on dual numbers.
+// ---------------------------------------------------------------------------
+namespace hx {
+__global__ void __launch_bounds__(NT) k_hydro_tangent(LevelSrc<Dual> src, Cells3<Dual> uo, Plane<Dual> np,
+                                                      Cells3W<Dual> out, IBox vb, Dual dt, double dx, double dy) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    HydroSmem<Dual>& S = *reinterpret_cast<HydroSmem<Dual>*>(smem_raw);
+    FaceOut<Dual> fo{};
+    fo.on = 0;
+    hydro_tile_body<Dual, false, TX, TY, NT>(S, src, uo, np, out, fo, vb, vb.lo0 + (int)blockIdx.x * TX,
+                                             vb.lo1 + (int)blockIdx.y * TY, dt, Dual(dx), Dual(dy), nullptr, nullptr);
+}
+
+cudaError_t launch_tangent(const LevelSrc<Dual>& src, const Cells3<Dual>& uo, const Plane<Dual>& np,
+                           const Cells3W<Dual>& out, const IBox& vb, Dual dt, double dx, double dy, cudaStream_t st) {
+    const size_t sm = sizeof(HydroSmem<Dual>);
+    cudaError_t e = ensure_smem(k_hydro_tangent, sm);
+    if (e != cudaSuccess) return e;
+    k_hydro_tangent<<<tile_grid(vb, TX, TY), NT, sm, st>>>(src, uo, np, out, vb, dt, dx, dy);
+    return cudaGetLastError();
+}
 }  // namespace hx

@@ -22,6 +22,8 @@ namespace hx {
 HX_INST(double)
 HX_INST(float)
 #undef HX_INST
+template cudaError_t launch_ensemble<double, true>(const EnsInstance<double>*, int, long long, int, double, unsigned long long*, int, cudaStream_t);
+template int ensemble_blocks_per_sm<double, true>();
 template cudaError_t launch_points<double, true>(int, long, const double*, const double*, double*, cudaStream_t);
 template cudaError_t launch_points<float, true>(int, long, const float*, const float*, float*, cudaStream_t);
 }  // namespace hx

@@ -6,6 +6,12 @@
 
 namespace hx {
 
+// Read-only load: through the read-only data cache for plain reals, a plain
+// load for other element types (the dual numbers of the tangent model).
+template <class T> __device__ __forceinline__ T ld_ro(const T* p) { return *p; }
+template <> __device__ __forceinline__ double ld_ro<double>(const double* p) { return __ldg(p); }
+template <> __device__ __forceinline__ float ld_ro<float>(const float* p) { return __ldg(p); }
+
 struct IBox {
     int lo0, lo1, hi0, hi1;
 };
@@ -29,7 +35,7 @@ template <class R> struct Plane {
     long long js;
     int lo0, lo1;
     __device__ __forceinline__ R ld(int i, int j) const {
-        return __ldg(p + (long long)(i - lo0) + (long long)(j - lo1) * js);
+        return ld_ro(p + (long long)(i - lo0) + (long long)(j - lo1) * js);
     }
 };
 
@@ -39,7 +45,7 @@ template <class R> struct Cells3 {
     long long js;
     int lo0, lo1;
     __device__ __forceinline__ R ld(int c, int i, int j) const {
-        return __ldg(p[c] + (long long)(i - lo0) + (long long)(j - lo1) * js);
+        return ld_ro(p[c] + (long long)(i - lo0) + (long long)(j - lo1) * js);
     }
 };
 
@@ -158,10 +164,10 @@ template <class R> struct LevelSrc {
         const int ej = j < 0 ? 0 : (j >= ny ? ny - 1 : j);
         const long long pm = (long long)mi + (long long)mj * pitch;
         const long long pe = (long long)ei + (long long)ej * pitch;
-        eta = __ldg(h + pm) + __ldg(z + pm);
-        zz = __ldg(z + pe);
-        nn = __ldg(n + pe);
-        const R a = __ldg(hu + pm), b = __ldg(hv + pm);
+        eta = ld_ro(h + pm) + ld_ro(z + pm);
+        zz = ld_ro(z + pe);
+        nn = ld_ro(n + pe);
+        const R a = ld_ro(hu + pm), b = ld_ro(hv + pm);
         qx = nx_neg ? -a : a;
         qy = ny_neg ? -b : b;
     }
@@ -194,6 +200,23 @@ template <class R> struct StepCtl {
     unsigned* status;      // may be null
     R* time;               // simulated time, advanced by block 0 (may be null)
     R dx, dy;
+};
+
+// One member of a batched ensemble (device memory, one per instance).
+template <class R> struct EnsInstance {
+    R* st[2][3];          // state planes (h, hu, hv) for the two parities
+    const R* z;
+    const R* n;
+    long long pitch;
+    long long tile_base;  // queue index of the instance's first tile
+    int nx, ny;
+    R dx, dy;
+    int bc[4];            // x-lo, x-hi, y-lo, y-hi codes
+    int shape;            // tile shape id (HX_TILE_*)
+    int tiles_x;
+    struct DtAccum* slots;  // three accumulators
+    unsigned* status;
+    R* time;
 };
 
 }  // namespace hx

@@ -23,35 +23,47 @@ constexpr int NT = TX * TY;
 // ---------------------------------------------------------------------------
 // Hydrostatic-Roe tile kernel.
 // ---------------------------------------------------------------------------
-template <class R> struct HydroSmem {
-    static constexpr int GX = TX + 4, GY = TY + 4;
+template <class R, int TXv = TX, int TYv = TY> struct HydroSmem {
+    static constexpr int GX = TXv + 4, GY = TYv + 4;
     R z[GY][GX], eta[GY][GX], u[GY][GX], v[GY][GX];
-    R sxe[TY][TX + 2], sxu[TY][TX + 2], sxv[TY][TX + 2];  // x-slopes of tile columns -1..TX
-    R sye[TY + 2][TX], syu[TY + 2][TX], syv[TY + 2][TX];  // y-slopes of tile rows -1..TY
-    R fx[4][TY][TX + 1];                                  // x faces: F0, FL1, FR1, F2
-    R fy[4][TY + 1][TX];                                  // y faces: F0, F1, FL2, FR2
+    R sxe[TYv][TXv + 2], sxu[TYv][TXv + 2], sxv[TYv][TXv + 2];  // x-slopes of tile columns -1..TX
+    R sye[TYv + 2][TXv], syu[TYv + 2][TXv], syv[TYv + 2][TXv];  // y-slopes of tile rows -1..TY
+    R fx[4][TYv][TXv + 1];                                      // x faces: F0, FL1, FR1, F2
+    R fy[4][TYv + 1][TXv];                                      // y faces: F0, F1, FL2, FR2
+    unsigned char nod[GY][GX];                                  // NODATA predicate of each grown-tile cell
 };
 
 // One hydrostatic face (src/solvers/HydrostaticRoe.cpp:218-396).  L and R are
 // the cells on either side; sX are the cells' slopes along the face normal.
 template <class R, bool FAST, int DIR>
-__device__ __forceinline__ void hydro_face(R zL, R zR, R eL, R eR, R seL, R seR, R uL, R uR, R suL, R suR, R vL,
-                                           R vR, R svL, R svR, R& F0, R& Fa, R& Fb, R& Fc) {
-    if (is_nodata(zL) || is_nodata(zR)) {
+__device__ __forceinline__ void hydro_face(bool wall, R zL, R zR, R eL, R eR, R seL, R seR, R uL, R uR, R suL, R suR,
+                                           R vL, R vR, R svL, R svR, R& F0, R& Fa, R& Fb, R& Fc) {
+    // wall: either side is NODATA (HydrostaticRoe.cpp:237-245)
+    if (wall) {
         F0 = R(0); Fa = R(0); Fb = R(0); Fc = R(0);
         return;
     }
-    const R zf = smax(zL, zR);
+    R zf;
+    if constexpr (FAST) zf = smax_i(zL, zR);
+    else zf = smax(zL, zR);
     const R etaLf = eL + R(0.5) * seL;
     const R etaRf = eR - R(0.5) * seR;
     const R uLf = uL + R(0.5) * suL;
     const R uRf = uR - R(0.5) * suR;
     const R vLf = vL + R(0.5) * svL;
     const R vRf = vR - R(0.5) * svR;
-    const R hLu = max0(etaLf - zL);
-    const R hRu = max0(etaRf - zR);
-    const R hLs = max0(etaLf - zf);
-    const R hRs = max0(etaRf - zf);
+    R hLu, hRu, hLs, hRs;
+    if constexpr (FAST) {
+        hLu = max0_i(etaLf - zL);
+        hRu = max0_i(etaRf - zR);
+        hLs = max0_i(etaLf - zf);
+        hRs = max0_i(etaRf - zf);
+    } else {
+        hLu = max0(etaLf - zL);
+        hRu = max0(etaRf - zR);
+        hLs = max0(etaLf - zf);
+        hRs = max0(etaRf - zf);
+    }
     R f0, f1, f2;
     if constexpr (!FAST) {
         const R huL = (hLs > R(0)) ? hLs * uLf : R(0);
@@ -77,12 +89,19 @@ __device__ __forceinline__ void hydro_face(R zL, R zR, R eL, R eR, R seL, R seR,
     else { Fa = f1; Fb = f2 + pL; Fc = f2 + pR; }
 }
 
+// dt of a step of the device time loop.  A collapse (min CFL bound < 1e-12,
+// HydrostaticRoe.cpp:77-80) is carried forward as a flag in the next
+// accumulator, so every later step sees it in launch-constant data and every
+// thread of every block takes the same early exit.
 template <class R> __device__ __forceinline__ bool resolve_dt(const StepCtl<R>& c, R& dt) {
     if (c.dt_in == nullptr) { dt = c.dt_host; return true; }
-    if (c.status && (*((volatile unsigned*)c.status) & HX_STATUS_DT_COLLAPSE)) return false;
-    const R m = accum_dt_min<R>(c.dt_in->rate_bits, c.dt_in->flags);
-    if (m < R(1.e-12)) {
-        if (c.status && threadIdx.x == 0) atomicOr(c.status, (unsigned)HX_STATUS_DT_COLLAPSE);
+    const unsigned fl = c.dt_in->flags;
+    const R m = accum_dt_min<R>(c.dt_in->rate_bits, fl);
+    if ((fl & DTF_COLLAPSED) || m < R(1.e-12)) {
+        if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) {
+            if (c.status) atomicOr(c.status, (unsigned)HX_STATUS_DT_COLLAPSE);
+            if (c.dt_out) atomicOr(&c.dt_out->flags, (unsigned)DTF_COLLAPSED);
+        }
         return false;
     }
     dt = m * c.cfl;
@@ -100,38 +119,41 @@ template <class R> __device__ __forceinline__ void step_bookkeeping(const StepCt
     }
 }
 
-template <class R, bool FAST, class Src>
-__global__ void __launch_bounds__(NT) k_hydro_tile(Src src, Cells3<R> uo, Plane<R> nplane, Cells3W<R> out,
-                                                   FaceOut<R> fo, IBox vb, StepCtl<R> ctl) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    HydroSmem<R>& S = *reinterpret_cast<HydroSmem<R>*>(smem_raw);
-    constexpr int GX = HydroSmem<R>::GX, GY = HydroSmem<R>::GY;
-
-    R dt;
-    if (!resolve_dt(ctl, dt)) return;
-    step_bookkeeping(ctl, dt);
-
+// The advance of one TXv x TYv tile with origin (x0, y0) by NTv threads (any
+// NTv; each thread takes cells t, t+NTv, ...).  Shared by the plain per-level
+// kernel and the ensemble kernel.  The caller has resolved dt.  Every thread
+// of the block must call it (it synchronises).
+// LINEAR: store the state after the flux update but before friction and the
+// dry clamp (used by the adjoint).  post_flags (optional): OR-ed with 1 when a
+// cell of the tile took the friction branch and 2 when one took the dry clamp.
+template <class R, bool FAST, int TXv, int TYv, int NTv, class Src, bool LINEAR = false>
+__device__ __forceinline__ void hydro_tile_body(HydroSmem<R, TXv, TYv>& S, const Src& src, const Cells3<R>& uo,
+                                                const Plane<R>& nplane, const Cells3W<R>& out, const FaceOut<R>& fo,
+                                                const IBox& vb, int x0, int y0, R dt, R dx, R dy, DtAccum* dt_out,
+                                                unsigned* status, unsigned* post_flags = nullptr) {
+    constexpr int GX = HydroSmem<R, TXv, TYv>::GX, GY = HydroSmem<R, TXv, TYv>::GY;
+    constexpr int CELLS = TXv * TYv;
     const int t = threadIdx.x;
-    const int tx = t & (TX - 1), ty = t / TX;
-    const int x0 = vb.lo0 + blockIdx.x * TX;
-    const int y0 = vb.lo1 + blockIdx.y * TY;
+    __syncthreads();  // the previous tile of this block is done with S
 
     // --- A: grown tile -> h rebuilt, eta = h + z, velocities -----------------
-    for (int idx = t; idx < GX * GY; idx += NT) {
+    for (int idx = t; idx < GX * GY; idx += NTv) {
         const int r = idx / GX, c = idx - r * GX;
         const int gi = x0 + c - 2, gj = y0 + r - 2;
         R e = R(0), zz = R(0), qx = R(0), qy = R(0), nn = R(0);
         if (src.inside(gi, gj)) src.fetch(gi, gj, e, zz, qx, qy, nn);
-        const R hp = max0(e - zz);  // HydrostaticRoe.cpp:498
-        R uu, vv;
+        R hp, uu, vv;
         if constexpr (!FAST) {
+            hp = max0(e - zz);  // HydrostaticRoe.cpp:498
             uu = (hp > Cst<R>::tol12) ? qx / hp : R(0);
             vv = (hp > Cst<R>::tol12) ? qy / hp : R(0);
         } else {
-            const R rh = (hp > Cst<R>::tol12) ? R(1) / hp : R(0);
+            hp = max0_i(e - zz);
+            const R rh = gt_bits(hp, Cst<R>::tol12_bits) ? rcp_nr(hp) : R(0);
             uu = qx * rh;
             vv = qy * rh;
         }
+        S.nod[r][c] = is_nodata(zz) ? 1 : 0;
         S.z[r][c] = zz;
         S.eta[r][c] = hp + zz;  // HydrostaticRoe.cpp:257-260
         S.u[r][c] = uu;
@@ -140,76 +162,78 @@ __global__ void __launch_bounds__(NT) k_hydro_tile(Src src, Cells3<R> uo, Plane<
     __syncthreads();
 
     // --- B: van Leer slopes, once per cell and direction ---------------------
-    {
-        const int r = ty + 2, c = tx + 2;
-        S.sxe[ty][tx + 1] = van_leer_slope<R, FAST>(S.eta[r][c - 1], S.eta[r][c], S.eta[r][c + 1]);
-        S.sxu[ty][tx + 1] = van_leer_slope<R, FAST>(S.u[r][c - 1], S.u[r][c], S.u[r][c + 1]);
-        S.sxv[ty][tx + 1] = van_leer_slope<R, FAST>(S.v[r][c - 1], S.v[r][c], S.v[r][c + 1]);
-        S.sye[ty + 1][tx] = van_leer_slope<R, FAST>(S.eta[r - 1][c], S.eta[r][c], S.eta[r + 1][c]);
-        S.syu[ty + 1][tx] = van_leer_slope<R, FAST>(S.u[r - 1][c], S.u[r][c], S.u[r + 1][c]);
-        S.syv[ty + 1][tx] = van_leer_slope<R, FAST>(S.v[r - 1][c], S.v[r][c], S.v[r + 1][c]);
+    auto xslopes = [&](int row, int col) {  // tile cell (col, row), col in -1..TXv
+        const int r = row + 2, c = col + 2;
+        S.sxe[row][col + 1] = van_leer_slope<R, FAST>(S.eta[r][c - 1], S.eta[r][c], S.eta[r][c + 1]);
+        S.sxu[row][col + 1] = van_leer_slope<R, FAST>(S.u[r][c - 1], S.u[r][c], S.u[r][c + 1]);
+        S.sxv[row][col + 1] = van_leer_slope<R, FAST>(S.v[r][c - 1], S.v[r][c], S.v[r][c + 1]);
+    };
+    auto yslopes = [&](int row, int col) {  // row in -1..TYv
+        const int r = row + 2, c = col + 2;
+        S.sye[row + 1][col] = van_leer_slope<R, FAST>(S.eta[r - 1][c], S.eta[r][c], S.eta[r + 1][c]);
+        S.syu[row + 1][col] = van_leer_slope<R, FAST>(S.u[r - 1][c], S.u[r][c], S.u[r + 1][c]);
+        S.syv[row + 1][col] = van_leer_slope<R, FAST>(S.v[r - 1][c], S.v[r][c], S.v[r + 1][c]);
+    };
+    for (int k = t; k < CELLS; k += NTv) {
+        xslopes(k / TXv, k % TXv);
+        yslopes(k / TXv, k % TXv);
     }
-    if (t < 2 * TY + 2 * TX) {
-        if (t < 2 * TY) {  // x-slopes of tile columns -1 and TX
-            const int row = t % TY, col = (t < TY) ? -1 : TX;
-            const int r = row + 2, c = col + 2;
-            S.sxe[row][col + 1] = van_leer_slope<R, FAST>(S.eta[r][c - 1], S.eta[r][c], S.eta[r][c + 1]);
-            S.sxu[row][col + 1] = van_leer_slope<R, FAST>(S.u[r][c - 1], S.u[r][c], S.u[r][c + 1]);
-            S.sxv[row][col + 1] = van_leer_slope<R, FAST>(S.v[r][c - 1], S.v[r][c], S.v[r][c + 1]);
-        } else {  // y-slopes of tile rows -1 and TY
-            const int m = t - 2 * TY;
-            const int col = m % TX, row = (m < TX) ? -1 : TY;
-            const int r = row + 2, c = col + 2;
-            S.sye[row + 1][col] = van_leer_slope<R, FAST>(S.eta[r - 1][c], S.eta[r][c], S.eta[r + 1][c]);
-            S.syu[row + 1][col] = van_leer_slope<R, FAST>(S.u[r - 1][c], S.u[r][c], S.u[r + 1][c]);
-            S.syv[row + 1][col] = van_leer_slope<R, FAST>(S.v[r - 1][c], S.v[r][c], S.v[r + 1][c]);
+    for (int k = t; k < 2 * TYv + 2 * TXv; k += NTv) {
+        if (k < 2 * TYv) xslopes(k % TYv, (k < TYv) ? -1 : TXv);  // columns -1 and TX
+        else {
+            const int m = k - 2 * TYv;
+            yslopes((m < TXv) ? -1 : TYv, m % TXv);                // rows -1 and TY
         }
     }
     __syncthreads();
 
-    // --- C: faces.  Each thread: the x face at the left of its cell and the y
-    // face below it; extra threads: the right column and the top row. --------
+    // --- C: faces.  The x face at the left of each cell and the y face below
+    // it, then the right column and the top row. ------------------------------
     auto xface = [&](int fi, int fj) {
         const int r = fj + 2, cl = fi + 1, cr = fi + 2;
         R F0, Fa, Fb, Fc;
-        hydro_face<R, FAST, 0>(S.z[r][cl], S.z[r][cr], S.eta[r][cl], S.eta[r][cr], S.sxe[fj][fi], S.sxe[fj][fi + 1],
-                               S.u[r][cl], S.u[r][cr], S.sxu[fj][fi], S.sxu[fj][fi + 1], S.v[r][cl], S.v[r][cr],
-                               S.sxv[fj][fi], S.sxv[fj][fi + 1], F0, Fa, Fb, Fc);
+        hydro_face<R, FAST, 0>(S.nod[r][cl] | S.nod[r][cr], S.z[r][cl], S.z[r][cr], S.eta[r][cl], S.eta[r][cr],
+                               S.sxe[fj][fi], S.sxe[fj][fi + 1], S.u[r][cl], S.u[r][cr], S.sxu[fj][fi],
+                               S.sxu[fj][fi + 1], S.v[r][cl], S.v[r][cr], S.sxv[fj][fi], S.sxv[fj][fi + 1], F0, Fa,
+                               Fb, Fc);
         S.fx[0][fj][fi] = F0; S.fx[1][fj][fi] = Fa; S.fx[2][fj][fi] = Fb; S.fx[3][fj][fi] = Fc;
-        fo.store_x(x0 + fi, y0 + fj, vb, F0, Fa, Fb, Fc, fi == TX);
+        fo.store_x(x0 + fi, y0 + fj, vb, F0, Fa, Fb, Fc, fi == TXv);
     };
     auto yface = [&](int fi, int fj) {
         const int c = fi + 2, rl = fj + 1, rr = fj + 2;
         R F0, Fa, Fb, Fc;
-        hydro_face<R, FAST, 1>(S.z[rl][c], S.z[rr][c], S.eta[rl][c], S.eta[rr][c], S.sye[fj][fi], S.sye[fj + 1][fi],
-                               S.u[rl][c], S.u[rr][c], S.syu[fj][fi], S.syu[fj + 1][fi], S.v[rl][c], S.v[rr][c],
-                               S.syv[fj][fi], S.syv[fj + 1][fi], F0, Fa, Fb, Fc);
+        hydro_face<R, FAST, 1>(S.nod[rl][c] | S.nod[rr][c], S.z[rl][c], S.z[rr][c], S.eta[rl][c], S.eta[rr][c],
+                               S.sye[fj][fi], S.sye[fj + 1][fi], S.u[rl][c], S.u[rr][c], S.syu[fj][fi],
+                               S.syu[fj + 1][fi], S.v[rl][c], S.v[rr][c], S.syv[fj][fi], S.syv[fj + 1][fi], F0, Fa,
+                               Fb, Fc);
         S.fy[0][fj][fi] = F0; S.fy[1][fj][fi] = Fa; S.fy[2][fj][fi] = Fb; S.fy[3][fj][fi] = Fc;
-        fo.store_y(x0 + fi, y0 + fj, vb, F0, Fa, Fb, Fc, fj == TY);
+        fo.store_y(x0 + fi, y0 + fj, vb, F0, Fa, Fb, Fc, fj == TYv);
     };
-    {
+    for (int k = t; k < CELLS; k += NTv) {
+        const int tx = k % TXv, ty = k / TXv;
         const int gi = x0 + tx, gj = y0 + ty;
         // a face is needed if it bounds a valid cell
         if (gi <= vb.hi0 + 1 && gj <= vb.hi1) xface(tx, ty);
         if (gi <= vb.hi0 && gj <= vb.hi1 + 1) yface(tx, ty);
-        if (t < TY) {
-            if (x0 + TX <= vb.hi0 + 1 && y0 + t <= vb.hi1) xface(TX, t);
-        } else if (t >= 32 && t < 32 + TX) {
-            const int m = t - 32;
-            if (x0 + m <= vb.hi0 && y0 + TY <= vb.hi1 + 1) yface(m, TY);
+    }
+    for (int k = t; k < TYv + TXv; k += NTv) {
+        if (k < TYv) {
+            if (x0 + TXv <= vb.hi0 + 1 && y0 + k <= vb.hi1) xface(TXv, k);
+        } else {
+            const int m = k - TYv;
+            if (x0 + m <= vb.hi0 && y0 + TYv <= vb.hi1 + 1) yface(m, TYv);
         }
     }
     __syncthreads();
 
     // --- D: update, Manning friction, dry clamp (HydrostaticRoe.cpp:551-604) --
-    const int gi = x0 + tx, gj = y0 + ty;
-    const bool valid = gi <= vb.hi0 && gj <= vb.hi1;
     R rate = R(0), mv = R(0);
-    unsigned flags = 0;
-    if (valid) {
-        R cx, cy;
-        cx = dt / ctl.dx;
-        cy = dt / ctl.dy;
+    unsigned flags = 0, pflags = 0;
+    const R cx = dt / dx, cy = dt / dy;
+    for (int k = t; k < CELLS; k += NTv) {
+        const int tx = k % TXv, ty = k / TXv;
+        const int gi = x0 + tx, gj = y0 + ty;
+        if (gi > vb.hi0 || gj > vb.hi1) continue;
         R un[3];
         const R o0 = uo.ld(0, gi, gj), o1 = uo.ld(1, gi, gj), o2 = uo.ld(2, gi, gj);
         const R dx0 = S.fx[0][ty][tx + 1] - S.fx[0][ty][tx];
@@ -218,62 +242,169 @@ __global__ void __launch_bounds__(NT) k_hydro_tile(Src src, Cells3<R> uo, Plane<
         const R dy0 = S.fy[0][ty + 1][tx] - S.fy[0][ty][tx];
         const R dy1 = S.fy[1][ty + 1][tx] - S.fy[1][ty][tx];
         const R dy2 = S.fy[2][ty + 1][tx] - S.fy[3][ty][tx];
-        if constexpr (!FAST) {
-            un[0] = o0 - cx * dx0 - cy * dy0;
-            un[1] = o1 - cx * dx1 - cy * dy1;
-            un[2] = o2 - cx * dx2 - cy * dy2;
-        } else {
-            un[0] = (o0 - cx * dx0) - cy * dy0;
-            un[1] = (o1 - cx * dx1) - cy * dy1;
-            un[2] = (o2 - cx * dx2) - cy * dy2;
+        un[0] = (o0 - cx * dx0) - cy * dy0;
+        un[1] = (o1 - cx * dx1) - cy * dy1;
+        un[2] = (o2 - cx * dx2) - cy * dy2;
+        if constexpr (LINEAR) {
+            out.st(gi, gj, un[0], un[1], un[2]);
+            continue;
         }
         const R hh = un[0];
-        if (hh >= Cst<R>::toldry) {
+        bool wet, rough;
+        if constexpr (FAST) wet = ge_bits(hh, Cst<R>::toldry_bits);
+        else wet = hh >= Cst<R>::toldry;
+        if (wet) {
             const R nv = nplane.ld(gi, gj);
             const R nsq = nv * nv;
-            if (nsq > Cst<R>::tol12) {  // the friction factor needs a rough bed
+            if constexpr (FAST) rough = gt_bits(nsq, Cst<R>::tol12_bits);
+            else rough = nsq > Cst<R>::tol12;
+            if (rough) {  // the friction factor needs a rough bed
                 const R qx = un[1], qy = un[2];
-                R modM, fac;
+                R modM;
                 if constexpr (!FAST) {
                     const R inv_h = R(1.0) / hh;
                     const R uu = qx * inv_h, vv = qy * inv_h;
                     modM = sqrt(uu * uu + vv * vv);
-                    if (modM > Cst<R>::tol12) {
-                        const R h43 = hh * cbrt(hh);
-                        const R tt = dt * Cst<R>::g * nsq * modM / h43;
-                        const R ff = sqrt(R(1.0) + R(4.0) * tt);
-                        fac = R(2.0) / (R(1.0) + ff);
-                        un[1] = qx * fac;
-                        un[2] = qy * fac;
-                    }
                 } else {
-                    const R inv_h = R(1) / hh;
-                    modM = sqrt(qx * qx + qy * qy) * inv_h;
-                    if (modM > Cst<R>::tol12) {
-                        const R h43 = hh * cbrt(hh);
-                        const R tt = dt * Cst<R>::g * nsq * modM / h43;
-                        const R ff = sqrt(R(1) + R(4) * tt);
-                        fac = R(2) / (R(1) + ff);
-                        un[1] = qx * fac;
-                        un[2] = qy * fac;
-                    }
+                    modM = sqrt(qx * qx + qy * qy) * rcp_nr(hh);
+                }
+                if (modM > Cst<R>::tol12) {
+                    pflags |= 1u;
+                    const R h43 = hh * cbrt(hh);
+                    const R tt = dt * Cst<R>::g * nsq * modM / h43;
+                    const R ff = sqrt(R(1.0) + R(4.0) * tt);
+                    const R fac = R(2.0) / (R(1.0) + ff);
+                    un[1] = qx * fac;
+                    un[2] = qy * fac;
                 }
             }
         } else {
-            un[0] = smax(hh, R(0));
+            pflags |= 2u;
+            if constexpr (FAST) un[0] = neg_i(hh) ? R(0) : hh;
+            else un[0] = smax(hh, R(0));
             un[1] = R(0);
             un[2] = R(0);
         }
         out.st(gi, gj, un[0], un[1], un[2]);
         if (bits_nonfinite(un[0]) || bits_nonfinite(un[1]) || bits_nonfinite(un[2])) flags |= DTF_NAN;
-        if (ctl.dt_out) {
-            const R zc = S.z[ty + 2][tx + 2];
-            dt_cell_contrib<R, FAST>(un[0], un[1], un[2], zc, ctl.dx, ctl.dy, R(1) / ctl.dx, R(1) / ctl.dy, rate,
-                                     mv, flags);
+        if (dt_out) {
+            R rc, mc;
+            dt_cell_contrib<R, FAST>(un[0], un[1], un[2], S.nod[ty + 2][tx + 2] != 0, dx, dy, R(1) / dx, R(1) / dy,
+                                     rc, mc, flags);
+            if constexpr (FAST) {
+                rate = nnmax_i(rate, rc);
+                mv = nnmax_i(mv, mc);
+            } else {
+                rate = smax(rate, rc);
+                mv = smax(mv, mc);
+            }
         }
     }
-    if (ctl.dt_out) block_fold_dt<R, NT>(rate, mv, flags, ctl.dt_out);
-    if ((flags & DTF_NAN) && ctl.status) atomicOr(ctl.status, (unsigned)HX_STATUS_NAN);
+    if (dt_out) block_fold_dt<R, NTv>(rate, mv, flags, dt_out);
+    if ((flags & DTF_NAN) && status) atomicOr(status, (unsigned)HX_STATUS_NAN);
+    if (post_flags) {
+        pflags = __reduce_or_sync(0xffffffffu, pflags);
+        if (pflags && (threadIdx.x & 31) == 0) atomicOr(post_flags, pflags);
+    }
+}
+
+template <class R, bool FAST, class Src>
+__global__ void __launch_bounds__(NT) k_hydro_tile(Src src, Cells3<R> uo, Plane<R> nplane, Cells3W<R> out,
+                                                   FaceOut<R> fo, IBox vb, StepCtl<R> ctl) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    HydroSmem<R>& S = *reinterpret_cast<HydroSmem<R>*>(smem_raw);
+    R dt;
+    if (!resolve_dt(ctl, dt)) return;
+    step_bookkeeping(ctl, dt);
+    hydro_tile_body<R, FAST, TX, TY, NT>(S, src, uo, nplane, out, fo, vb, vb.lo0 + (int)blockIdx.x * TX,
+                                         vb.lo1 + (int)blockIdx.y * TY, dt, ctl.dx, ctl.dy, ctl.dt_out, ctl.status);
+}
+
+// ---------------------------------------------------------------------------
+// Batched ensemble: many independent single-box levels advanced by one
+// persistent launch per step.  The launch drains a queue of tiles that spans
+// every instance; each instance keeps its own dt chain (three rotating
+// accumulators), status word and clock, so instances of any size run side by
+// side and small ones no longer leave the GPU idle.
+// ---------------------------------------------------------------------------
+template <class R> constexpr size_t ens_smem_bytes() {
+    size_t a = sizeof(HydroSmem<R, 32, 8>), b = sizeof(HydroSmem<R, 16, 16>), c = sizeof(HydroSmem<R, 64, 4>);
+    return a > b ? (a > c ? a : c) : (b > c ? b : c);
+}
+
+template <class R, bool FAST>
+__global__ void __launch_bounds__(NT) k_ensemble_hydro(const EnsInstance<R>* __restrict__ inst, int ninst,
+                                                       long long total_tiles, int step, R cfl,
+                                                       unsigned long long* queue) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ long long s_tile;
+    // the other queue counter was drained by the previous launch: clear it for the next one
+    if (blockIdx.x == 0 && threadIdx.x == 0) queue[(step + 1) & 1] = 0ull;
+    const int par = step & 1;
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = (long long)atomicAdd(&queue[par], 1ull);
+        __syncthreads();
+        const long long tile = s_tile;
+        __syncthreads();
+        if (tile >= total_tiles) break;
+        int lo = 0, hi = ninst - 1;  // the instance owning this tile
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (inst[mid].tile_base <= tile) lo = mid;
+            else hi = mid - 1;
+        }
+        const EnsInstance<R>& I = inst[lo];
+        const DtAccum* din = &I.slots[step % 3];
+        const unsigned fl = din->flags;
+        const R m = accum_dt_min<R>(din->rate_bits, fl);
+        const long long local = tile - I.tile_base;
+        if ((fl & DTF_COLLAPSED) || m < R(1.e-12)) {  // launch-constant: the whole block agrees
+            if (local == 0 && threadIdx.x == 0) {
+                atomicOr(I.status, (unsigned)HX_STATUS_DT_COLLAPSE);
+                atomicOr(&I.slots[(step + 1) % 3].flags, (unsigned)DTF_COLLAPSED);
+            }
+            continue;
+        }
+        const R dt = m * cfl;
+        if (local == 0 && threadIdx.x == 0) {
+            DtAccum* r = &I.slots[(step + 2) % 3];
+            r->rate_bits = 0ull;
+            r->maxvel_bits = 0ull;
+            r->flags = 0u;
+            *I.time += dt;
+        }
+        const int bx = (int)(local % I.tiles_x), by = (int)(local / I.tiles_x);
+        LevelSrc<R> src;
+        src.h = I.st[par][0]; src.hu = I.st[par][1]; src.hv = I.st[par][2]; src.z = I.z; src.n = I.n;
+        src.pitch = I.pitch;
+        src.nx = I.nx; src.ny = I.ny;
+        src.bc_xlo = I.bc[0]; src.bc_xhi = I.bc[1]; src.bc_ylo = I.bc[2]; src.bc_yhi = I.bc[3];
+        src.glo0 = -2; src.glo1 = -2; src.ghi0 = I.nx + 1; src.ghi1 = I.ny + 1;
+        Cells3<R> uo;
+        uo.p[0] = I.st[par][0]; uo.p[1] = I.st[par][1]; uo.p[2] = I.st[par][2];
+        uo.js = I.pitch; uo.lo0 = 0; uo.lo1 = 0;
+        Cells3W<R> out;
+        out.p[0] = I.st[par ^ 1][0]; out.p[1] = I.st[par ^ 1][1]; out.p[2] = I.st[par ^ 1][2];
+        out.js = I.pitch; out.lo0 = 0; out.lo1 = 0;
+        const Plane<R> np{I.n, I.pitch, 0, 0};
+        FaceOut<R> fo{};
+        fo.on = 0;
+        const IBox vb{0, 0, I.nx - 1, I.ny - 1};
+        DtAccum* dout = &I.slots[(step + 1) % 3];
+        switch (I.shape) {
+            case HX_TILE_16x16:
+                hydro_tile_body<R, FAST, 16, 16, NT>(*reinterpret_cast<HydroSmem<R, 16, 16>*>(smem_raw), src, uo, np,
+                                                     out, fo, vb, bx * 16, by * 16, dt, I.dx, I.dy, dout, I.status);
+                break;
+            case HX_TILE_64x4:
+                hydro_tile_body<R, FAST, 64, 4, NT>(*reinterpret_cast<HydroSmem<R, 64, 4>*>(smem_raw), src, uo, np,
+                                                    out, fo, vb, bx * 64, by * 4, dt, I.dx, I.dy, dout, I.status);
+                break;
+            default:
+                hydro_tile_body<R, FAST, 32, 8, NT>(*reinterpret_cast<HydroSmem<R, 32, 8>*>(smem_raw), src, uo, np,
+                                                    out, fo, vb, bx * 32, by * 8, dt, I.dx, I.dy, dout, I.status);
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -364,8 +495,8 @@ __global__ void __launch_bounds__(NT) k_classic_tile(Src src, Cells3W<R> out, Fa
         out.st(gi, gj, un[0], un[1], un[2]);
         if (bits_nonfinite(un[0]) || bits_nonfinite(un[1]) || bits_nonfinite(un[2])) flags |= DTF_NAN;
         if (ctl.dt_out) {
-            dt_cell_contrib<R, FAST>(un[0], un[1], un[2], S.z[ty + 1][tx + 1], ctl.dx, ctl.dy, R(1) / ctl.dx,
-                                     R(1) / ctl.dy, rate, mv, flags);
+            dt_cell_contrib<R, FAST>(un[0], un[1], un[2], is_nodata(S.z[ty + 1][tx + 1]), ctl.dx, ctl.dy,
+                                     R(1) / ctl.dx, R(1) / ctl.dy, rate, mv, flags);
         }
     }
     if (ctl.dt_out) block_fold_dt<R, NT>(rate, mv, flags, ctl.dt_out);
@@ -382,8 +513,8 @@ __global__ void __launch_bounds__(NT) k_dt_reduce(Cells3<R> U, Plane<R> Z, IBox 
     R rate = R(0), mv = R(0);
     unsigned flags = 0;
     if (i <= vb.hi0 && j <= vb.hi1)
-        dt_cell_contrib<R, FAST>(U.ld(0, i, j), U.ld(1, i, j), U.ld(2, i, j), Z.ld(i, j), dx, dy, R(1) / dx,
-                                 R(1) / dy, rate, mv, flags);
+        dt_cell_contrib<R, FAST>(U.ld(0, i, j), U.ld(1, i, j), U.ld(2, i, j), is_nodata(Z.ld(i, j)), dx, dy,
+                                 R(1) / dx, R(1) / dy, rate, mv, flags);
     block_fold_dt<R, NT>(rate, mv, flags, acc);
 }
 
@@ -522,6 +653,27 @@ cudaError_t launch_classic(const Src& src, const Cells3W<R>& out, const FaceOut9
     if (e != cudaSuccess) return e;
     k<<<tile_grid(vb, TX, TY), NT, sm, st>>>(src, out, fo, hb, vb, ctl);
     return cudaGetLastError();
+}
+
+template <class R, bool FAST>
+cudaError_t launch_ensemble(const EnsInstance<R>* inst, int ninst, long long total_tiles, int step, R cfl,
+                           unsigned long long* queue, int grid, cudaStream_t st) {
+    const size_t sm = ens_smem_bytes<R>();
+    auto k = k_ensemble_hydro<R, FAST>;
+    cudaError_t e = ensure_smem(k, sm);
+    if (e != cudaSuccess) return e;
+    k<<<grid, NT, sm, st>>>(inst, ninst, total_tiles, step, cfl, queue);
+    return cudaGetLastError();
+}
+
+template <class R, bool FAST>
+int ensemble_blocks_per_sm() {
+    int n = 0;
+    if (ensure_smem(k_ensemble_hydro<R, FAST>, ens_smem_bytes<R>()) != cudaSuccess) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_ensemble_hydro<R, FAST>, NT, ens_smem_bytes<R>()) !=
+        cudaSuccess)
+        return 0;
+    return n;
 }
 
 template <class R, bool FAST>

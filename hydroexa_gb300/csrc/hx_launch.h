@@ -31,6 +31,15 @@ template <class R>
 cudaError_t launch_masked_avgdown(const V4<R>& fine, const V4<R>& crse, const IBox& cb, int scomp, int ccomp,
                                   int ncomp, int rx, int ry, R fv, R nodata, cudaStream_t st);
 
+template <class R, bool FAST>
+cudaError_t launch_ensemble(const EnsInstance<R>* inst, int ninst, long long total_tiles, int step, R cfl,
+                           unsigned long long* queue, int grid, cudaStream_t st);
+
+template <class R, bool FAST> int ensemble_blocks_per_sm();
+
+cudaError_t launch_tangent(const LevelSrc<Dual>& src, const Cells3<Dual>& uo, const Plane<Dual>& np,
+                           const Cells3W<Dual>& out, const IBox& vb, Dual dt, double dx, double dy, cudaStream_t st);
+
 inline dim3 tile_grid(const IBox& b, int tx, int ty) {
     return dim3((unsigned)((b.hi0 - b.lo0 + 1 + tx - 1) / tx), (unsigned)((b.hi1 - b.lo1 + 1 + ty - 1) / ty));
 }

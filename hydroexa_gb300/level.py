@@ -166,7 +166,10 @@ class Level:
 
     def compute_dt(self, stream=None):
         """(min per-cell CFL bound, max |vel|) of the current state, before the CFL factor."""
-        acc = DtAccum(self.state.device)
+        acc = getattr(self, "_acc", None)
+        if acc is None:
+            acc = self._acc = DtAccum(self.state.device)
+        acc.reset(stream)
         d = self._desc(self.state)
         capi.check(getattr(capi.lib(), f"hx_level_dt_reduce_{self.sfx}")(ctypes.byref(d), acc.ptr,
                                                                           _stream_handle(stream)), "hx_level_dt_reduce")

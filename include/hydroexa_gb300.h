@@ -282,6 +282,39 @@ int hx_level_run_host_f64(int method, int nx, int ny, double dx, double dy, cons
                           const double* n, int nsteps, double cfl, int arith, double* time_out, hx_stream_t stream);
 void hx_host_cache_release(void);
 
+/* ---- batched ensemble ---------------------------------------------------- */
+
+/*
+ * Many independent single-box levels (scenarios of any sizes) advanced
+ * together: one persistent kernel per step drains a tile queue spanning every
+ * member, each member keeps its own CFL dt chain, status word and clock, and
+ * the steps are replayed from a CUDA graph.  No counterpart in the reference
+ * (which advances one hierarchy per process); per member the arithmetic is
+ * exactly that of hx_level_run_f64.
+ */
+enum { HX_TILE_32x8 = 0, HX_TILE_16x16 = 1, HX_TILE_64x4 = 2 };
+
+typedef struct hx_ensemble_member_f64 {
+    hx_level_f64 level; /* state (advanced in place, see final_in_alt), terrain, geometry, BC codes */
+    double* h_alt;      /* ping-pong planes with the level's pitch */
+    double* hu_alt;
+    double* hv_alt;
+    int32_t tile_shape; /* HX_TILE_*: chosen per size class by the autotuner */
+} hx_ensemble_member_f64;
+
+/* Device scratch for n members (descriptor table, dt accumulators, queue). */
+int64_t hx_ensemble_work_bytes(int n);
+/* Total queue length (tiles) of a member list. */
+int hx_ensemble_tiles(int n, const hx_ensemble_member_f64* members, int64_t* tiles);
+/*
+ * nsteps for every member.  status: n device words (cleared by the caller),
+ * time_dev: n device doubles.  use_graph != 0 replays the launches from a CUDA
+ * graph.  *final_in_alt = 1 when the results are in the alternate planes.
+ */
+int hx_ensemble_run_f64(int n, const hx_ensemble_member_f64* members, int nsteps, double cfl, void* work,
+                        uint32_t* status, double* time_dev, int arith, int use_graph, int* final_in_alt,
+                        hx_stream_t stream);
+
 /*
  * Allocation-free form of hx_level_run_f64.  No counterpart in the reference:
  * it is for callers that cannot allocate device memory of their own.  HydroEXA

@@ -67,6 +67,8 @@ def test_classic_points_golden(cuda, hxlib):
         assert np.array_equal(got[k][smooth], g[name][smooth]), name
         assert (np.abs(got[k] - g[name]) / sc).max() <= 1e-14, name
     fast = run_points(hxlib, 0, FAST, g["states"], g["aux"], cuda).reshape(3, -1, 3)
+    # friction on a nearly dry face makes the sources large next to the flux terms
+    sc = sc + np.abs(np.stack([g["F"], g["Sm"], g["Sp"]])).max(axis=(0, 2))[:, None]
     for k, name in enumerate(("F", "Sm", "Sp")):
         assert (np.abs(fast[k] - g[name]) / sc).max() <= 1e-12, name
 
