@@ -168,7 +168,7 @@ def run_reference(args):
 
 def config_dict():
     return {"workload": "fractal-terrain circular dam break 8192x8192 FP64, hydrostatic-Roe MUSCL van Leer, "
-                        "20% NODATA, reflective walls (BASELINE configs[2])",
+                        "20% NODATA, reflective walls",
             "nx": NX, "ny": NY, "method": "HydrostaticRoe", "precision": "FP64",
             "l2": "no flush: 4.3 GB of inputs per step > 129 MB L2", "seed": 3}
 
@@ -185,6 +185,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--precision", default="f64", choices=["f64", "f32"])
     ap.add_argument("--no-ensemble", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--method", default="hydrostatic", choices=["hydrostatic", "roe"])
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -304,6 +305,11 @@ def main():
         torch.cuda.empty_cache()
         ens = ensemble_measure(dev)
 
+    adj = None
+    if args.precision == "f64" and args.method == "hydrostatic" and not args.no_adjoint:
+        torch.cuda.empty_cache()
+        adj = adjoint_measure(dev)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_sample(case, method=method)
@@ -329,6 +335,7 @@ def main():
                 "fp64_pipe": fp64_pipe(profile, kms) if (args.precision, args.method) == ("f64", "hydrostatic") else None,
             },
             "ensemble": ens,
+            "adjoint": adj,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
         }
@@ -340,7 +347,7 @@ def main():
 
 
 def ensemble_measure(dev, steps=24, warmup=6, plain_steps=6):
-    """BASELINE configs[3]: 256 independent dam breaks, sides log-uniform in
+    """256 independent dam breaks, sides log-uniform in
     [64, 1024].  Batched (one persistent launch per step, CUDA graph, tile shape
     per size class from the autotuner) against the members advanced one after
     another, (a) with the per-level device time loop and (b) with the
@@ -390,6 +397,118 @@ def ensemble_measure(dev, steps=24, warmup=6, plain_steps=6):
             "batched_launches": launches,
             "tile_shape_per_class": [SHAPE_NAMES[x] for x in per_class],
             "class_edges": [128, 384]}
+
+
+def adjoint_measure(dev, nsteps=2000, every=45, fd_eps=1e-6):
+    """Gauge-misfit gradient of a 512x512 FP64 hydrostatic-Roe run of 2000
+    steps (smooth bed of 32 Gaussians, 0.2 m hump, 64 gauges, reference series
+    from a run on a perturbed bed), checkpoints every 45 steps.  Reports the
+    forward+reverse cost against the plain forward time loop of the same steps,
+    the working set with and without checkpoints, the gradient against the
+    N-step tangent-linear model (exact arithmetic, same trajectory), and
+    central-difference directional checks (steps 1e-6 and 1e-7) of this run
+    and of a smooth, non-quiescent variant over growing horizons."""
+    import numpy as np
+    import torch
+
+    from hydroexa_gb300 import capi, workloads
+    from hydroexa_gb300.adjoint import GaugeProblem, tangent_misfit
+    from hydroexa_gb300.level import Level
+
+    case, gauges = workloads.adjoint_case(nsteps=nsteps)
+    g = case.geom
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    z, h0, zero = T(case.z), T(case.h), torch.zeros((g.ny, g.nx), dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def timed(fn):
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        out = fn()
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) * 1e-3, out
+
+    lev = Level.from_numpy(g, case.h, case.hu, case.hv, case.z, case.n, device=dev)
+    lev.run(capi.HX_METHOD_HYDROSTATIC_ROE, 20, case.cfl, arith=capi.HX_ARITH_FAST)
+    lev = Level.from_numpy(g, case.h, case.hu, case.hv, case.z, case.n, device=dev)
+    t_plain, _ = timed(lambda: lev.run(capi.HX_METHOD_HYDROSTATIC_ROE, nsteps, case.cfl, arith=capi.HX_ARITH_FAST,
+                                       check_status=False))
+    assert lev.status.read() == 0
+    del lev
+    prob = GaugeProblem(g, zero.clone(), gauges, nsteps, case.cfl, checkpoint_every=every)
+    dz = T(workloads.smooth_field(g.nx, g.ny, seed=6, amplitude=0.02))
+    href = prob.forward(z + dz, h0, zero, zero).clone()
+    prob.forward(z, h0, zero, zero)  # warm-up
+    prob.reverse(href)
+    t_fwd, series = timed(lambda: prob.forward(z, h0, zero, zero))
+    n0 = capi.launch_count()
+    t_rev, grads = timed(lambda: prob.reverse(href))
+    rev_launches = capi.launch_count() - n0
+    prob_bytes = prob.work_bytes
+    J0 = float(((series - href) ** 2).sum())
+
+    def fd_check(prob, base, href, grads, seeds, nx, ny):
+        out = {}
+        for name, k, seed in seeds:
+            d = T(workloads.smooth_field(nx, ny, seed=seed, amplitude=1.0))
+            ad = float((grads[k] * d).sum())
+            rec = {"adjoint": ad}
+            for eps in (fd_eps, fd_eps / 10):
+                plus, minus = list(base), list(base)
+                plus[k] = base[k] + eps * d
+                minus[k] = base[k] - eps * d
+                jp = float(((prob.forward(*plus) - href) ** 2).sum())
+                jm = float(((prob.forward(*minus) - href) ** 2).sum())
+                fdv = (jp - jm) / (2 * eps)
+                rec["step_%g" % eps] = {"central_difference": fdv, "rel_err": abs(ad - fdv) / max(abs(fdv), 1e-300)}
+            out[name] = rec
+        return out
+
+    fd = fd_check(prob, [z, h0, zero, zero], href, grads, (("z", 0, 7), ("h0", 1, 8)), g.nx, g.ny)
+    store_all = capi.lib().hx_adjoint_work_bytes_f64(g.nx, g.ny, g.nx, nsteps, 0)
+    del prob
+    # the exact arithmetic form: the reverse sweep against the N-step tangent-linear model of the same trajectory
+    pe = GaugeProblem(g, zero.clone(), gauges, nsteps, case.cfl, checkpoint_every=every, arith=capi.HX_ARITH_EXACT)
+    pe.forward(z, h0, zero, zero)
+    t_rev_exact, ge = timed(lambda: pe.reverse(href))
+    dirs = [T(workloads.smooth_field(g.nx, g.ny, seed=sd, amplitude=1.0)) for sd in (7, 8)] + [zero, zero]
+    t0 = time.perf_counter()
+    tan = tangent_misfit(pe, [z, h0, zero, zero], dirs, href)
+    t_tan = time.perf_counter() - t0
+    ad_e = sum(float((gk * dk).sum()) for gk, dk in zip(ge, dirs))
+    tangent = {"arith": "exact", "direction": "smooth fields (seeds 7, 8) in z and h0", "adjoint": ad_e,
+               "tangent_linear": tan, "rel_err": abs(ad_e - tan) / max(abs(tan), 1e-300),
+               "reverse_exact_s": t_rev_exact, "tangent_s": t_tan}
+    del pe
+    # the same bed and gauges from a state with no quiescent region, over growing horizons
+    scan = []
+    for hsteps in (30, 100, 300):
+        sc, sg = workloads.adjoint_smooth_case(nsteps=hsteps)
+        base = [T(sc.z), T(sc.h), T(sc.hu), T(sc.hv)]
+        sp = GaugeProblem(g, zero.clone(), sg, hsteps, sc.cfl, checkpoint_every=every)
+        sref = sp.forward(base[0] + dz, *base[1:]).clone()
+        sp.forward(*base)
+        sgr = sp.reverse(sref)
+        scan.append({"steps": hsteps, "fd": fd_check(sp, base, sref, sgr, (("z", 0, 7), ("h0", 1, 8), ("hu0", 2, 9)),
+                                                     g.nx, g.ny)})
+        del sp
+    return {"workload": "512x512 FP64 hydrostatic-Roe, %d steps, smooth bed (32 Gaussians, 0.3 m), 0.2 m hump, "
+                        "64 gauges, reference series from a perturbed bed (seed 6, 0.02 m)" % nsteps,
+            "loss": J0, "checkpoint_every": every,
+            "plain_forward_s": t_plain, "adjoint_forward_s": t_fwd, "reverse_s": t_rev,
+            "cost_vs_forward": (t_fwd + t_rev) / t_plain, "reverse_vs_forward": t_rev / t_plain,
+            "reverse_launches": rev_launches,
+            "work_bytes_checkpointed": prob_bytes, "work_bytes_store_all": int(store_all),
+            "tangent_check": tangent,
+            "fd_check": fd,
+            "fd_check_note": "the initial state is a lake at rest outside the hump: limiters there sit on their "
+                             "flat-data branch (|dp| <= 1e-12), a kink that a 1e-6 step leaves, and the exact "
+                             "linearisation of single-stage MUSCL + forward Euler grows by up to 1.064 per step",
+            "fd_horizon_scan": {"workload": "same bed and gauges, free surface 1.0 + 0.05 m undulation + 0.2 m hump, "
+                                            "smooth currents up to 0.2 m/s (no quiescent region)",
+                                "runs": scan}}
 
 
 def load_profile_summary():

@@ -1,6 +1,6 @@
 """Build the CUDA library ``hydroexa_gb300/libhydroexa_gb300.so`` for sm_103a.
 
-Five translation units compiled in parallel, then linked:
+Six translation units compiled in parallel, then linked:
 
 * ``hx_exact.cu``  -- exact arithmetic form, ``--fmad=false`` (no multiply-add
   contraction, the reference's host rounding); tags and restriction kernels.
@@ -8,6 +8,7 @@ Five translation units compiled in parallel, then linked:
 * ``hx_capi.cu``   -- the C ABI declared in ``include/hydroexa_gb300.h``.
 * ``hx_noalloc.cu`` -- the allocation-free time loop (scratch in a static device array).
 * ``hx_ensemble.cu`` -- the batched-ensemble plan, dt initialisation and CUDA-graph replay.
+* ``hx_adjoint.cu`` -- the hand-written adjoint of the hydrostatic-Roe time loop and its drivers.
 
 The build is in-tree (objects in ``_build/``), takes well under a minute, and
 needs only nvcc; the CUDA runtime is linked statically so the library loads
@@ -35,6 +36,7 @@ UNITS = {
     "hx_capi": [],
     "hx_noalloc": [],
     "hx_ensemble": [],
+    "hx_adjoint": [],
 }
 
 

@@ -121,6 +121,16 @@ def _declare(L):
     L.hx_ensemble_tiles.argtypes = [c_int, POINTER(EnsembleMemberF64), POINTER(c_int64)]
     L.hx_ensemble_run_f64.argtypes = [c_int, POINTER(EnsembleMemberF64), c_int, c_double, c_void_p, c_void_p,
                                       c_void_p, c_int, c_int, POINTER(c_int), c_void_p]
+    L.hx_adjoint_work_bytes_f64.restype = c_int64
+    L.hx_adjoint_work_bytes_f64.argtypes = [c_int, c_int, c_int64, c_int, c_int]
+    L.hx_adjoint_forward_f64.argtypes = [POINTER(LevelF64), c_int, c_double, c_int, c_void_p, c_void_p, c_int,
+                                         c_int, c_void_p, c_void_p, c_void_p]
+    L.hx_adjoint_reverse_f64.argtypes = [POINTER(LevelF64), c_int, c_double, c_int, c_void_p, c_void_p, c_double,
+                                         c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]
+    L.hx_adjoint_step_f64.argtypes = [POINTER(LevelF64), c_double, c_void_p, c_void_p, c_void_p, c_void_p,
+                                      c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_void_p]
+    L.hx_level_tangent_f64.argtypes = [POINTER(LevelF64), c_double, c_double, c_void_p, c_void_p, c_void_p,
+                                       c_void_p]
     L.hx_level_run_static_f64.argtypes = [c_int, POINTER(LevelF64), c_int, c_double, c_void_p, c_void_p, c_int,
                                           c_void_p]
 
@@ -152,5 +162,7 @@ EXPORTED = [
     "hx_level_run_f64", "hx_level_run_f32", "hx_level_run_host_f64", "hx_host_cache_release",
     "hx_debug_roe_points_f64", "hx_debug_roe_points_f32", "hx_level_run_static_f64",
     "hx_ensemble_work_bytes", "hx_ensemble_tiles", "hx_ensemble_run_f64",
+    "hx_adjoint_work_bytes_f64", "hx_adjoint_forward_f64", "hx_adjoint_reverse_f64", "hx_adjoint_step_f64",
+    "hx_level_tangent_f64",
 ]
 HX_STATIC_RUN_MAX_CELLS = 262144

@@ -1,0 +1,1116 @@
+// Hand-written adjoint (reverse mode) of the hydrostatic-Roe time loop.
+//
+// The loss is J = sum over steps n = 1..N and gauge cells g of
+// (h^n_g - href^n_g)^2.  Its gradient with respect to the initial state
+// (h, hu, hv) and the bed z is obtained by one forward sweep (states kept in
+// HBM, all of them or every L-th with the segments recomputed) and one reverse
+// sweep of three kernels per step:
+//
+//   A  post-map reverse: lambda_lin = J_post^T lambda^{n+1}, where post is the
+//      Manning factor and the dry clamp (src/solvers/HydrostaticRoe.cpp:566-603),
+//      skipped for steps where no cell took either branch;
+//   B  face reverse: per 32x8 tile, the forward values with a 3-cell halo are
+//      recomputed, every face flux (HydrostaticRoe.cpp:218-396 with the
+//      homogeneous Roe flux of include/solvers/kernels/HydrostaticRoe.H:44-159)
+//      is differentiated in reverse taking the forward's branches (dry clamps,
+//      entropy fixes, hydrostatic caps, NODATA walls), the van Leer slopes are
+//      reversed, per-cell adjoints are gathered in a fixed order (no atomics,
+//      reproducible), boundary-ghost adjoints are folded into the cells their
+//      values came from, and the h rebuild is reversed;
+//   C  one block: the dt of step n is cfl / max rate(U^n), so its adjoint
+//      flows into the cell that set the CFL bound; then the gauge misfit of
+//      state n is injected.
+#include <cstdio>
+#include <vector>
+
+#include "hx_kernels.cuh"
+
+namespace hx {
+void note_launches(int n);
+int set_error(int code, const char* msg);
+// Instantiated in hx_exact.cu (--fmad=false) and hx_fast.cu: never here, so the
+// exact form's forward sweep stays bit-identical to the exact level advance.
+extern template cudaError_t launch_adj_forward<false>(const LevelSrc<double>&, const Cells3<double>&,
+                                                      const Plane<double>&, const Cells3W<double>&, const IBox&,
+                                                      const StepCtl<double>&, const double*, unsigned*, cudaStream_t);
+extern template cudaError_t launch_adj_forward<true>(const LevelSrc<double>&, const Cells3<double>&,
+                                                     const Plane<double>&, const Cells3W<double>&, const IBox&,
+                                                     const StepCtl<double>&, const double*, unsigned*, cudaStream_t);
+extern template cudaError_t launch_adj_forward_linear<false>(const LevelSrc<double>&, const Cells3<double>&,
+                                                             const Plane<double>&, const Cells3W<double>&,
+                                                             const IBox&, double, double, const double*, cudaStream_t);
+extern template cudaError_t launch_adj_forward_linear<true>(const LevelSrc<double>&, const Cells3<double>&,
+                                                            const Plane<double>&, const Cells3W<double>&, const IBox&,
+                                                            double, double, const double*, cudaStream_t);
+extern template cudaError_t launch_dt_reduce<double, false>(const Cells3<double>&, const Plane<double>&, const IBox&,
+                                                            double, double, DtAccum*, cudaStream_t);
+extern template cudaError_t launch_dt_reduce<double, true>(const Cells3<double>&, const Plane<double>&, const IBox&,
+                                                           double, double, DtAccum*, cudaStream_t);
+}  // namespace hx
+
+using namespace hx;
+
+namespace {
+
+constexpr double G = 9.81, HG = 0.5 * 9.81, TD = 1e-6, T12 = 1e-12;
+constexpr int ATX = 32, ATY = 8, ANT = 256;
+constexpr int H3 = 3;  // forward halo of the reverse tile
+
+__device__ __forceinline__ double sgn(double x) { return x > 0.0 ? 1.0 : (x < 0.0 ? -1.0 : 0.0); }
+
+// ---------------------------------------------------------------------------
+// Reverse of the homogeneous Roe flux in the face-normal frame.  (hi, ui, vi)
+// and (hj, uj, vj) are the face depths and the normal / tangential face
+// velocities; b0..b2 the adjoints of the normal-frame flux.  Adjoints of the
+// inputs are added to g*.
+// ---------------------------------------------------------------------------
+__device__ void roe_rev(double hi, double ui, double vi, double hj, double uj, double vj, double b0, double b1,
+                        double b2, double& ghi, double& gui, double& gvi, double& ghj, double& guj, double& gvj) {
+    const bool wi = hi >= TD, wj = hj >= TD;
+    const double Hi = wi ? hi : 0.0, Hj = wj ? hj : 0.0;
+    const double Ui = wi ? ui : 0.0, Vi = wi ? vi : 0.0, Uj = wj ? uj : 0.0, Vj = wj ? vj : 0.0;
+    const double si = sqrt(Hi), sj = sqrt(Hj);
+    const double hh = 0.5 * (Hi + Hj);
+    const bool hmb = hh > TD;
+    const double hm = hmb ? hh : TD;
+    const double cm = sqrt(G * hm);
+    const double sden = si + sj + T12;
+    const double um = (Ui * si + Uj * sj) / sden;
+    const double vm = (Vi * si + Vj * sj) / sden;
+    const double l0a = um - cm, l2a = um + cm;
+    const double ci = sqrt(G * Hi), cj = sqrt(G * Hj);
+    const double e0i = Ui - ci, e0j = Uj - cj;
+    const bool fix0 = e0i < 0.0 && e0j > 0.0;
+    const double l0 = fix0 ? e0i * (e0j - l0a) / (e0j - e0i) : l0a;
+    const double e2i = Ui + ci, e2j = Uj + cj;
+    const bool fix2 = e2i < 0.0 && e2j > 0.0;
+    const double l2 = fix2 ? e2j * (l2a - e2i) / (e2j - e2i) : l2a;
+    const double l1 = um;
+    const double den = 2.0 * cm + T12;
+    const double dh = Hj - Hi;
+    const double dhu = Hj * Uj - Hi * Ui;
+    const double dhv = Hj * Vj - Hi * Vi;
+    const double a0 = (l2 * dh - dhu) / den, a1 = (dhv - vm * dh) / cm, a2 = (dhu - l0 * dh) / den;
+    const double w0 = 0.5 * fabs(l0) * a0, w1 = 0.5 * fabs(l1) * a1, w2 = 0.5 * fabs(l2) * a2;
+
+    double gHi = 0, gHj = 0, gUi = 0, gUj = 0, gVi = 0, gVj = 0;
+    // F0 = (Hi Ui + Hj Uj)/2 - w0 - w2
+    gHi += 0.5 * b0 * Ui; gUi += 0.5 * b0 * Hi; gHj += 0.5 * b0 * Uj; gUj += 0.5 * b0 * Hj;
+    // F1 = (Hi Ui^2 + HG Hi^2 + Hj Uj^2 + HG Hj^2)/2 - w0 l0 - w2 l2
+    gHi += 0.5 * b1 * (Ui * Ui + 2.0 * HG * Hi); gUi += b1 * Hi * Ui;
+    gHj += 0.5 * b1 * (Uj * Uj + 2.0 * HG * Hj); gUj += b1 * Hj * Uj;
+    // F2 = (Hi Ui Vi + Hj Uj Vj)/2 - w0 vm - w1 cm - w2 vm
+    gHi += 0.5 * b2 * Ui * Vi; gUi += 0.5 * b2 * Hi * Vi; gVi += 0.5 * b2 * Hi * Ui;
+    gHj += 0.5 * b2 * Uj * Vj; gUj += 0.5 * b2 * Hj * Vj; gVj += 0.5 * b2 * Hj * Uj;
+    const double gw0 = -b0 - b1 * l0 - b2 * vm;
+    const double gw1 = -b2 * cm;
+    const double gw2 = -b0 - b1 * l2 - b2 * vm;
+    double gl0 = -b1 * w0, gl2 = -b1 * w2, gvm = -b2 * (w0 + w2), gcm = -b2 * w1;
+    const double ga0 = gw0 * 0.5 * fabs(l0);
+    gl0 += gw0 * 0.5 * sgn(l0) * a0;
+    const double ga1 = gw1 * 0.5 * fabs(l1);
+    const double gl1 = gw1 * 0.5 * sgn(l1) * a1;
+    const double ga2 = gw2 * 0.5 * fabs(l2);
+    gl2 += gw2 * 0.5 * sgn(l2) * a2;
+    // wave strengths
+    gl2 += ga0 * dh / den;
+    double gdh = ga0 * l2 / den, gdhu = -ga0 / den, gden = -ga0 * a0 / den;
+    const double gdhv = ga1 / cm;
+    gvm += -ga1 * dh / cm;
+    gdh += -ga1 * vm / cm;
+    gcm += -ga1 * a1 / cm;
+    gdhu += ga2 / den;
+    gl0 += -ga2 * dh / den;
+    gdh += -ga2 * l0 / den;
+    gden += -ga2 * a2 / den;
+    gcm += 2.0 * gden;
+    gHj += gdh; gHi -= gdh;
+    gHj += gdhu * Uj; gUj += gdhu * Hj; gHi -= gdhu * Ui; gUi -= gdhu * Hi;
+    gHj += gdhv * Vj; gVj += gdhv * Hj; gHi -= gdhv * Vi; gVi -= gdhv * Hi;
+    // eigenvalues and the sonic fixes (the forward's branches)
+    double gum = gl1, gci = 0.0, gcj = 0.0;
+    if (fix2) {
+        const double D = e2j - e2i;
+        const double gl2a = gl2 * e2j / D;
+        const double ge2i = gl2 * e2j * (l2a - e2j) / (D * D);
+        const double ge2j = -gl2 * (l2a - e2i) * e2i / (D * D);
+        gUi += ge2i; gci += ge2i; gUj += ge2j; gcj += ge2j;
+        gum += gl2a; gcm += gl2a;
+    } else {
+        gum += gl2; gcm += gl2;
+    }
+    if (fix0) {
+        const double D = e0j - e0i;
+        const double gl0a = -gl0 * e0i / D;
+        const double ge0i = gl0 * (e0j - l0a) * e0j / (D * D);
+        const double ge0j = gl0 * e0i * (l0a - e0i) / (D * D);
+        gUi += ge0i; gci -= ge0i; gUj += ge0j; gcj -= ge0j;
+        gum += gl0a; gcm -= gl0a;
+    } else {
+        gum += gl0; gcm -= gl0;
+    }
+    if (ci > 0.0) gHi += gci * G / (2.0 * ci);
+    if (cj > 0.0) gHj += gcj * G / (2.0 * cj);
+    // Roe averages
+    const double gnu = gum / sden, gnv = gvm / sden, gsden = -(gum * um + gvm * vm) / sden;
+    gUi += gnu * si; gUj += gnu * sj; gVi += gnv * si; gVj += gnv * sj;
+    const double gsi = gnu * Ui + gnv * Vi + gsden, gsj = gnu * Uj + gnv * Vj + gsden;
+    const double ghm = gcm * G / (2.0 * cm);
+    if (hmb) { gHi += 0.5 * ghm; gHj += 0.5 * ghm; }
+    if (si > 0.0) gHi += gsi / (2.0 * si);
+    if (sj > 0.0) gHj += gsj / (2.0 * sj);
+    if (wi) { ghi += gHi; gui += gUi; gvi += gVi; }
+    if (wj) { ghj += gHj; guj += gUj; gvj += gVj; }
+}
+
+// Inputs and adjoints of one hydrostatic face: eta, z, u, v of the two cells
+// and the cells' slopes along the normal.
+struct FaceVals {
+    double eL, eR, zL, zR, uL, uR, vL, vR, seL, seR, suL, suR, svL, svR;
+};
+
+// Reverse of the hydrostatic face (HydrostaticRoe.cpp:247-396) for direction
+// DIR, given the adjoints of FL and FR (global frame).  Adds to g.
+template <int DIR>
+__device__ void face_rev(const FaceVals& f, const double gFL[3], const double gFR[3], FaceVals& g) {
+    const bool zLmax = !(f.zL < f.zR);  // std::max(zL, zR) keeps zL on ties
+    const double zf = zLmax ? f.zL : f.zR;
+    const double etaLf = f.eL + 0.5 * f.seL, etaRf = f.eR - 0.5 * f.seR;
+    const double uLf = f.uL + 0.5 * f.suL, uRf = f.uR - 0.5 * f.suR;
+    const double vLf = f.vL + 0.5 * f.svL, vRf = f.vR - 0.5 * f.svR;
+    const double dLu = etaLf - f.zL, dRu = etaRf - f.zR, dLs = etaLf - zf, dRs = etaRf - zf;
+    const double hLu = dLu > 0.0 ? dLu : 0.0, hRu = dRu > 0.0 ? dRu : 0.0;
+    const double hLs = dLs > 0.0 ? dLs : 0.0, hRs = dRs > 0.0 ? dRs : 0.0;
+    // normal frame
+    const double unL = DIR == 0 ? uLf : vLf, utL = DIR == 0 ? vLf : -uLf;
+    const double unR = DIR == 0 ? uRf : vRf, utR = DIR == 0 ? vRf : -uRf;
+    double gf0 = gFL[0] + gFR[0], gf1 = gFL[1] + gFR[1], gf2 = gFL[2] + gFR[2];
+    double gpL, gpR, b1, b2;
+    if (DIR == 0) { gpL = gFL[1]; gpR = gFR[1]; b1 = gf1; b2 = gf2; }
+    else { gpL = gFL[2]; gpR = gFR[2]; b1 = gf2; b2 = -gf1; }
+    double ghLs = 0, gunL = 0, gutL = 0, ghRs = 0, gunR = 0, gutR = 0;
+    roe_rev(hLs, unL, utL, hRs, unR, utR, gf0, b1, b2, ghLs, gunL, gutL, ghRs, gunR, gutR);
+    // pressure correction p = HG (hu^2 - hs^2)
+    const double ghLu = gpL * 2.0 * HG * hLu, ghRu = gpR * 2.0 * HG * hRu;
+    ghLs += -gpL * 2.0 * HG * hLs;
+    ghRs += -gpR * 2.0 * HG * hRs;
+    double getaL = 0, getaR = 0, gzL = 0, gzR = 0, gzf = 0;
+    if (dLu > 0.0) { getaL += ghLu; gzL -= ghLu; }
+    if (dRu > 0.0) { getaR += ghRu; gzR -= ghRu; }
+    if (dLs > 0.0) { getaL += ghLs; gzf -= ghLs; }
+    if (dRs > 0.0) { getaR += ghRs; gzf -= ghRs; }
+    if (zLmax) gzL += gzf; else gzR += gzf;
+    double guL, gvL, guR, gvR;
+    if (DIR == 0) { guL = gunL; gvL = gutL; guR = gunR; gvR = gutR; }
+    else { gvL = gunL; guL = -gutL; gvR = gunR; guR = -gutR; }
+    g.eL += getaL; g.seL += 0.5 * getaL;
+    g.eR += getaR; g.seR -= 0.5 * getaR;
+    g.uL += guL; g.suL += 0.5 * guL;
+    g.uR += guR; g.suR -= 0.5 * guR;
+    g.vL += gvL; g.svL += 0.5 * gvL;
+    g.vR += gvR; g.svR -= 0.5 * gvR;
+    g.zL += gzL;
+    g.zR += gzR;
+}
+
+// Reverse of van_leer_slope(qm, q, qp) (HydrostaticRoe.cpp:179-195).
+__device__ __forceinline__ void slope_rev(double qm, double q, double qp, double gs, double& gqm, double& gq,
+                                          double& gqp) {
+    gqm = gq = gqp = 0.0;
+    const double dm = q - qm, dp = qp - q;
+    if (fabs(dp) <= T12 || gs == 0.0) return;
+    if (dm == 0.0) {  // r = 0: the mean of the one-sided derivatives (0 and 2), d s / d dm = 1
+        gq = gs;
+        gqm = -gs;
+        return;
+    }
+    if (!(dm * dp > 0.0)) return;  // phi = 0 for r < 0
+    const double S = dm + dp;
+    const double gdm = gs * 2.0 * dp * dp / (S * S), gdp = gs * 2.0 * dm * dm / (S * S);
+    gq = gdm - gdp;
+    gqm = -gdm;
+    gqp = gdp;
+}
+
+// ---------------------------------------------------------------------------
+// Kernel B: face reverse of one tile.
+// ---------------------------------------------------------------------------
+struct AdjSmem {
+    static constexpr int GX = ATX + 2 * H3, GY = ATY + 2 * H3;
+    double hp[GY][GX], eta[GY][GX], u[GY][GX], v[GY][GX], z[GY][GX], lam[3][GY][GX];
+    unsigned char nod[GY][GX];
+    union {
+        struct {  // x pass
+            double s[3][ATY][ATX + 4];      // slopes of columns x0-2 .. x0+TX+1
+            double fa[14][ATY][ATX + 3];    // face adjoints, faces x0-1 .. x0+TX+1
+            double sp[9][ATY][ATX + 2];     // slope-reverse partials, columns x0-1 .. x0+TX
+        } x;
+        struct {  // y pass
+            double s[3][ATY + 4][ATX];
+            double fa[14][ATY + 3][ATX];
+            double sp[9][ATY + 2][ATX];
+        } y;
+    } p;
+    double fold[4][ATY][ATX];  // ghost adjoints folded into own cells (h, hu, hv, z)
+};
+
+struct AdjArgs {
+    LevelSrc<double> src;  // U^n, z, n with the level's BCs
+    const double* lam[3];  // lambda_lin
+    double* out[3];        // lambda^n
+    double* zbar;          // accumulated gradient w.r.t. z
+    long long pitch;
+    int nx, ny;
+    double cx, cy;  // dt/dx, dt/dy
+};
+
+__device__ __forceinline__ double fget(const FaceVals& f, int k) { return (&f.eL)[k]; }
+
+template <bool FAST>
+__global__ void __launch_bounds__(ANT) k_adj_faces(AdjArgs A) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    AdjSmem& S = *reinterpret_cast<AdjSmem*>(smem_raw);
+    constexpr int GX = AdjSmem::GX, GY = AdjSmem::GY;
+    const int t = threadIdx.x;
+    const int x0 = blockIdx.x * ATX, y0 = blockIdx.y * ATY;
+    const int nx = A.nx, ny = A.ny;
+
+    // forward values on the grown tile (halo 3) and lambda_lin (0 outside the domain)
+    for (int idx = t; idx < GX * GY; idx += ANT) {
+        const int r = idx / GX, c = idx - r * GX;
+        const int gi = x0 + c - H3, gj = y0 + r - H3;
+        double e = 0, zz = 0, qx = 0, qy = 0, nn = 0;
+        const bool in_grown = gi >= -2 && gi <= nx + 1 && gj >= -2 && gj <= ny + 1;
+        if (in_grown) A.src.fetch(gi, gj, e, zz, qx, qy, nn);
+        const double hp = e - zz > 0.0 ? e - zz : 0.0;
+        S.hp[r][c] = hp;
+        S.eta[r][c] = hp + zz;
+        if constexpr (FAST) {  // the forward's own velocity arithmetic, so the limiters take its branches
+            const double rh = hp > T12 ? rcp_nr(hp) : 0.0;
+            S.u[r][c] = qx * rh;
+            S.v[r][c] = qy * rh;
+        } else {
+            S.u[r][c] = hp > T12 ? qx / hp : 0.0;
+            S.v[r][c] = hp > T12 ? qy / hp : 0.0;
+        }
+        S.z[r][c] = zz;
+        S.nod[r][c] = (in_grown && is_nodata(zz)) ? 1 : 0;
+        const bool inside = gi >= 0 && gi < nx && gj >= 0 && gj < ny;
+        const long long o = (long long)gi + (long long)gj * A.pitch;
+        for (int k = 0; k < 3; ++k) S.lam[k][r][c] = inside ? A.lam[k][o] : 0.0;
+    }
+    for (int idx = t; idx < 4 * ATX * ATY; idx += ANT) (&S.fold[0][0][0])[idx] = 0.0;
+    __syncthreads();
+
+    const int tx = t % ATX, ty = t / ATX;
+    double ae = 0, au = 0, av = 0, az = 0;  // gathered adjoints of this thread's cell
+
+    // ===================== x pass =====================
+    {
+        auto& P = S.p.x;
+        for (int k = t; k < ATY * (ATX + 4); k += ANT) {  // slopes, columns x0-2 .. x0+TX+1
+            const int row = k / (ATX + 4), col = k % (ATX + 4) - 2;
+            const int r = row + H3, c = col + H3;
+            P.s[0][row][col + 2] = van_leer_slope<double, FAST>(S.eta[r][c - 1], S.eta[r][c], S.eta[r][c + 1]);
+            P.s[1][row][col + 2] = van_leer_slope<double, FAST>(S.u[r][c - 1], S.u[r][c], S.u[r][c + 1]);
+            P.s[2][row][col + 2] = van_leer_slope<double, FAST>(S.v[r][c - 1], S.v[r][c], S.v[r][c + 1]);
+        }
+        __syncthreads();
+        for (int k = t; k < ATY * (ATX + 3); k += ANT) {  // faces x0-1 .. x0+TX+1
+            const int row = k / (ATX + 3), fcol = k % (ATX + 3) - 1;  // face at the left of column fcol
+            const int f = x0 + fcol, gj = y0 + row;
+            const int r = row + H3, cl = fcol - 1 + H3, cr = fcol + H3;
+            FaceVals g{};
+            if (f >= 0 && f <= nx && gj < ny && !(S.nod[r][cl] | S.nod[r][cr])) {
+                FaceVals fv;
+                fv.eL = S.eta[r][cl]; fv.eR = S.eta[r][cr]; fv.zL = S.z[r][cl]; fv.zR = S.z[r][cr];
+                fv.uL = S.u[r][cl]; fv.uR = S.u[r][cr]; fv.vL = S.v[r][cl]; fv.vR = S.v[r][cr];
+                fv.seL = P.s[0][row][fcol - 1 + 2]; fv.seR = P.s[0][row][fcol + 2];
+                fv.suL = P.s[1][row][fcol - 1 + 2]; fv.suR = P.s[1][row][fcol + 2];
+                fv.svL = P.s[2][row][fcol - 1 + 2]; fv.svR = P.s[2][row][fcol + 2];
+                // FL(f) enters cell f-1 with -cx, FR(f) enters cell f with +cx
+                double gFL[3], gFR[3];
+                for (int c = 0; c < 3; ++c) {
+                    gFL[c] = -A.cx * S.lam[c][r][cl];
+                    gFR[c] = A.cx * S.lam[c][r][cr];
+                }
+                face_rev<0>(fv, gFL, gFR, g);
+            }
+            for (int q = 0; q < 14; ++q) P.fa[q][row][fcol + 1] = fget(g, q);
+        }
+        __syncthreads();
+        for (int k = t; k < ATY * (ATX + 2); k += ANT) {  // slope reverse, columns x0-1 .. x0+TX
+            const int row = k / (ATX + 2), col = k % (ATX + 2) - 1;
+            const int r = row + H3, c = col + H3;
+            // slope of this column: read as the R slope by face col (index col+1) and as the L slope by face col+1
+            for (int qi = 0; qi < 3; ++qi) {
+                const double gs = P.fa[9 + 2 * qi][row][col + 1] + P.fa[8 + 2 * qi][row][col + 2];
+                const double(*Q)[GX] = qi == 0 ? S.eta : (qi == 1 ? S.u : S.v);
+                double gm, g0, gp;
+                slope_rev(Q[r][c - 1], Q[r][c], Q[r][c + 1], gs, gm, g0, gp);
+                P.sp[3 * qi + 0][row][col + 1] = gm;  // to column col-1
+                P.sp[3 * qi + 1][row][col + 1] = g0;  // to column col
+                P.sp[3 * qi + 2][row][col + 1] = gp;  // to column col+1
+            }
+        }
+        __syncthreads();
+        // gather for column c: faces c (R side) and c+1 (L side), slopes c-1 (to right), c (self), c+1 (to left)
+        auto gather_x = [&](int row, int col, double& ge, double& gu, double& gv, double& gz) {
+            auto F = [&](int q, int fcol) { return (fcol >= -1 && fcol <= ATX + 1) ? P.fa[q][row][fcol + 1] : 0.0; };
+            auto SP = [&](int q, int scol) { return (scol >= -1 && scol <= ATX) ? P.sp[q][row][scol + 1] : 0.0; };
+            ge = F(1, col) + F(0, col + 1) + SP(2, col - 1) + SP(1, col) + SP(0, col + 1);
+            gu = F(5, col) + F(4, col + 1) + SP(5, col - 1) + SP(4, col) + SP(3, col + 1);
+            gv = F(7, col) + F(6, col + 1) + SP(8, col - 1) + SP(7, col) + SP(6, col + 1);
+            gz = F(3, col) + F(2, col + 1);
+        };
+        {
+            double ge, gu, gv, gz;
+            gather_x(ty, tx, ge, gu, gv, gz);
+            ae += ge; au += gu; av += gv; az += gz;
+        }
+        // x-boundary ghosts: one thread per row folds both sides
+        if (t < ATY && y0 + t < ny) {
+            const int row = t, gj = y0 + row, r = row + H3;
+            for (int side = 0; side < 2; ++side) {
+                const bool lo = side == 0;
+                if (lo ? (x0 != 0) : (x0 + ATX - 1 < nx - 1)) continue;
+                const int code = lo ? A.src.bc_xlo : A.src.bc_xhi;
+                for (int k = 1; k <= 2; ++k) {
+                    const int gi = lo ? -k : nx - 1 + k;  // ghost column
+                    const int col = gi - x0, c = col + H3;
+                    double ge, gu, gv, gz;
+                    gather_x(row, col, ge, gu, gv, gz);
+                    const double hp = S.hp[r][c];
+                    double gzt = gz + ge, ghp = ge, ghu = 0, ghv = 0;
+                    if (hp > T12) {
+                        ghu = gu / hp;
+                        ghv = gv / hp;
+                        ghp -= (gu * S.u[r][c] + gv * S.v[r][c]) / hp;
+                    }
+                    double geta = 0;
+                    if (hp > 0.0) { geta = ghp; gzt -= ghp; }
+                    const int edge = lo ? 0 : nx - 1;
+                    const int src = code == 0 ? (lo ? -1 - gi : 2 * nx - 1 - gi) : edge;
+                    const double sx = code == 0 ? -1.0 : 1.0;
+                    const int sc = src - x0, ec = edge - x0;
+                    if (sc >= 0 && sc < ATX) {
+                        S.fold[0][row][sc] += geta;
+                        S.fold[3][row][sc] += geta;
+                        S.fold[1][row][sc] += sx * ghu;
+                        S.fold[2][row][sc] += ghv;
+                    }
+                    if (ec >= 0 && ec < ATX) S.fold[3][row][ec] += gzt;
+                    (void)gj;
+                }
+            }
+        }
+        __syncthreads();
+    }
+
+    // ===================== y pass =====================
+    {
+        auto& P = S.p.y;
+        for (int k = t; k < (ATY + 4) * ATX; k += ANT) {  // slopes, rows y0-2 .. y0+TY+1
+            const int row = k / ATX - 2, col = k % ATX;
+            const int r = row + H3, c = col + H3;
+            P.s[0][row + 2][col] = van_leer_slope<double, FAST>(S.eta[r - 1][c], S.eta[r][c], S.eta[r + 1][c]);
+            P.s[1][row + 2][col] = van_leer_slope<double, FAST>(S.u[r - 1][c], S.u[r][c], S.u[r + 1][c]);
+            P.s[2][row + 2][col] = van_leer_slope<double, FAST>(S.v[r - 1][c], S.v[r][c], S.v[r + 1][c]);
+        }
+        __syncthreads();
+        for (int k = t; k < (ATY + 3) * ATX; k += ANT) {  // faces y0-1 .. y0+TY+1
+            const int frow = k / ATX - 1, col = k % ATX;
+            const int f = y0 + frow, gi = x0 + col;
+            const int c = col + H3, rl = frow - 1 + H3, rr = frow + H3;
+            FaceVals g{};
+            if (f >= 0 && f <= ny && gi < nx && !(S.nod[rl][c] | S.nod[rr][c])) {
+                FaceVals fv;
+                fv.eL = S.eta[rl][c]; fv.eR = S.eta[rr][c]; fv.zL = S.z[rl][c]; fv.zR = S.z[rr][c];
+                fv.uL = S.u[rl][c]; fv.uR = S.u[rr][c]; fv.vL = S.v[rl][c]; fv.vR = S.v[rr][c];
+                fv.seL = P.s[0][frow - 1 + 2][col]; fv.seR = P.s[0][frow + 2][col];
+                fv.suL = P.s[1][frow - 1 + 2][col]; fv.suR = P.s[1][frow + 2][col];
+                fv.svL = P.s[2][frow - 1 + 2][col]; fv.svR = P.s[2][frow + 2][col];
+                double gFL[3], gFR[3];
+                for (int q = 0; q < 3; ++q) {
+                    gFL[q] = -A.cy * S.lam[q][rl][c];
+                    gFR[q] = A.cy * S.lam[q][rr][c];
+                }
+                face_rev<1>(fv, gFL, gFR, g);
+            }
+            for (int q = 0; q < 14; ++q) P.fa[q][frow + 1][col] = fget(g, q);
+        }
+        __syncthreads();
+        for (int k = t; k < (ATY + 2) * ATX; k += ANT) {  // slope reverse, rows y0-1 .. y0+TY
+            const int row = k / ATX - 1, col = k % ATX;
+            const int r = row + H3, c = col + H3;
+            for (int qi = 0; qi < 3; ++qi) {
+                const double gs = P.fa[9 + 2 * qi][row + 1][col] + P.fa[8 + 2 * qi][row + 2][col];
+                const double(*Q)[GX] = qi == 0 ? S.eta : (qi == 1 ? S.u : S.v);
+                double gm, g0, gp;
+                slope_rev(Q[r - 1][c], Q[r][c], Q[r + 1][c], gs, gm, g0, gp);
+                P.sp[3 * qi + 0][row + 1][col] = gm;
+                P.sp[3 * qi + 1][row + 1][col] = g0;
+                P.sp[3 * qi + 2][row + 1][col] = gp;
+            }
+        }
+        __syncthreads();
+        auto gather_y = [&](int row, int col, double& ge, double& gu, double& gv, double& gz) {
+            auto F = [&](int q, int frow) { return (frow >= -1 && frow <= ATY + 1) ? P.fa[q][frow + 1][col] : 0.0; };
+            auto SP = [&](int q, int srow) { return (srow >= -1 && srow <= ATY) ? P.sp[q][srow + 1][col] : 0.0; };
+            ge = F(1, row) + F(0, row + 1) + SP(2, row - 1) + SP(1, row) + SP(0, row + 1);
+            gu = F(5, row) + F(4, row + 1) + SP(5, row - 1) + SP(4, row) + SP(3, row + 1);
+            gv = F(7, row) + F(6, row + 1) + SP(8, row - 1) + SP(7, row) + SP(6, row + 1);
+            gz = F(3, row) + F(2, row + 1);
+        };
+        {
+            double ge, gu, gv, gz;
+            gather_y(ty, tx, ge, gu, gv, gz);
+            ae += ge; au += gu; av += gv; az += gz;
+        }
+        if (t < ATX && x0 + t < nx) {
+            const int col = t, c = col + H3;
+            for (int side = 0; side < 2; ++side) {
+                const bool lo = side == 0;
+                if (lo ? (y0 != 0) : (y0 + ATY - 1 < ny - 1)) continue;
+                const int code = lo ? A.src.bc_ylo : A.src.bc_yhi;
+                for (int k = 1; k <= 2; ++k) {
+                    const int gj = lo ? -k : ny - 1 + k;
+                    const int row = gj - y0, r = row + H3;
+                    double ge, gu, gv, gz;
+                    gather_y(row, col, ge, gu, gv, gz);
+                    const double hp = S.hp[r][c];
+                    double gzt = gz + ge, ghp = ge, ghu = 0, ghv = 0;
+                    if (hp > T12) {
+                        ghu = gu / hp;
+                        ghv = gv / hp;
+                        ghp -= (gu * S.u[r][c] + gv * S.v[r][c]) / hp;
+                    }
+                    double geta = 0;
+                    if (hp > 0.0) { geta = ghp; gzt -= ghp; }
+                    const int edge = lo ? 0 : ny - 1;
+                    const int src = code == 0 ? (lo ? -1 - gj : 2 * ny - 1 - gj) : edge;
+                    const double sy = code == 0 ? -1.0 : 1.0;
+                    const int sr = src - y0, er = edge - y0;
+                    if (sr >= 0 && sr < ATY) {
+                        S.fold[0][sr][col] += geta;
+                        S.fold[3][sr][col] += geta;
+                        S.fold[1][sr][col] += ghu;
+                        S.fold[2][sr][col] += sy * ghv;
+                    }
+                    if (er >= 0 && er < ATY) S.fold[3][er][col] += gzt;
+                }
+            }
+        }
+        __syncthreads();
+    }
+
+    // ===================== own cell: rebuild reverse and outputs =====================
+    const int gi = x0 + tx, gj = y0 + ty;
+    if (gi >= nx || gj >= ny) return;
+    const int r = ty + H3, c = tx + H3;
+    const double hp = S.hp[r][c];
+    double gz = az + ae, ghp = ae, ghu = 0, ghv = 0;
+    if (hp > T12) {
+        ghu = au / hp;
+        ghv = av / hp;
+        ghp -= (au * S.u[r][c] + av * S.v[r][c]) / hp;
+    }
+    double gh = 0;
+    if (hp > 0.0) gh = ghp;  // h' = max(0, (h + z) - z): dh'/dh = 1, dh'/dz = 0
+    const long long o = (long long)gi + (long long)gj * A.pitch;
+    // lambda^n = lambda_lin (the stored state passes through the update) + the flux part + ghost folds
+    A.out[0][o] = S.lam[0][r][c] + gh + S.fold[0][ty][tx];
+    A.out[1][o] = S.lam[1][r][c] + ghu + S.fold[1][ty][tx];
+    A.out[2][o] = S.lam[2][r][c] + ghv + S.fold[2][ty][tx];
+    A.zbar[o] += gz + S.fold[3][ty][tx];
+}
+
+// ---------------------------------------------------------------------------
+// Kernel A (general steps): lambda_lin = J_post^T lambda^{n+1} from the linear
+// (pre-clamp) state, and the dt adjoint partials of the update.
+// ---------------------------------------------------------------------------
+struct PostArgs {
+    const double* lin[3];   // state after the flux update, before friction / clamp
+    const double* un[3];    // U^n
+    const double* lam[3];   // lambda^{n+1}
+    const double* nman;     // Manning n
+    double* out[3];         // lambda_lin
+    double* dtbar;          // one partial per block
+    long long pitch;
+    int nx, ny;
+    double dt;
+};
+
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5;
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) sh[w] = v;
+    __syncthreads();
+    double s = 0;
+    if (threadIdx.x == 0)
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += sh[k];
+    return s;
+}
+
+__global__ void __launch_bounds__(ANT) k_adj_post(PostArgs P) {
+    __shared__ double sh[ANT / 32];
+    const int i = blockIdx.x * ATX + (threadIdx.x % ATX), j = blockIdx.y * ATY + threadIdx.x / ATX;
+    double dtb = 0;
+    if (i < P.nx && j < P.ny) {
+        const long long o = (long long)i + (long long)j * P.pitch;
+        const double h = P.lin[0][o], qx = P.lin[1][o], qy = P.lin[2][o];
+        const double lh = P.lam[0][o], lqx = P.lam[1][o], lqy = P.lam[2][o];
+        double gh = 0, gqx = 0, gqy = 0, gdt = 0;
+        if (h >= TD) {
+            gh = lh;
+            gqx = lqx;
+            gqy = lqy;
+            const double nv = P.nman[o], nsq = nv * nv;
+            if (nsq > T12) {
+                const double u = qx / h, vv = qy / h;
+                const double modM = sqrt(u * u + vv * vv);
+                if (modM > T12) {
+                    const double h43 = h * cbrt(h);
+                    const double tt = P.dt * G * nsq * modM / h43;
+                    const double ff = sqrt(1.0 + 4.0 * tt);
+                    const double fac = 2.0 / (1.0 + ff);
+                    gqx = lqx * fac;
+                    gqy = lqy * fac;
+                    const double gfac = lqx * qx + lqy * qy;
+                    const double gff = -gfac * fac * fac / 2.0;
+                    const double gtt = gff * 2.0 / ff;
+                    gdt += gtt * tt / P.dt;
+                    const double gmod = gtt * tt / modM;
+                    const double gh43 = -gtt * tt / h43;
+                    gh += gh43 * (4.0 / 3.0) * h43 / h;
+                    const double gu = gmod * u / modM, gv = gmod * vv / modM;
+                    gqx += gu / h;
+                    gqy += gv / h;
+                    gh += -(gu * u + gv * vv) / h;
+                }
+            }
+        } else {
+            gh = h < 0.0 ? 0.0 : lh;  // max(h, 0) keeps h at h == 0 (a dry cell stays at its value); momenta are zeroed
+        }
+        P.out[0][o] = gh;
+        P.out[1][o] = gqx;
+        P.out[2][o] = gqy;
+        // the flux update is linear in dt: d(lin)/d dt = (lin - U^n) / dt
+        dtb = gdt + (gh * (h - P.un[0][o]) + gqx * (qx - P.un[1][o]) + gqy * (qy - P.un[2][o])) / P.dt;
+    }
+    const double s = block_sum(dtb, sh);
+    if (threadIdx.x == 0) P.dtbar[blockIdx.x + (long long)blockIdx.y * gridDim.x] = s;
+}
+
+// Kernel A (steps without friction or clamp): lambda_lin = lambda^{n+1}; only
+// the dt adjoint partials sum_c lambda . (U^{n+1} - U^n) / dt are needed.
+__global__ void __launch_bounds__(ANT) k_adj_dtbar_identity(const double* l0, const double* l1, const double* l2,
+                                                             const double* a0, const double* a1, const double* a2,
+                                                             const double* b0, const double* b1, const double* b2,
+                                                             long long pitch, int nx, int ny, double dt,
+                                                             double* dtbar) {
+    __shared__ double sh[ANT / 32];
+    const int i = blockIdx.x * ATX + (threadIdx.x % ATX), j = blockIdx.y * ATY + threadIdx.x / ATX;
+    double dtb = 0;
+    if (i < nx && j < ny) {
+        const long long o = (long long)i + (long long)j * pitch;
+        dtb = (l0[o] * (a0[o] - b0[o]) + l1[o] * (a1[o] - b1[o]) + l2[o] * (a2[o] - b2[o])) / dt;
+    }
+    const double s = block_sum(dtb, sh);
+    if (threadIdx.x == 0) dtbar[blockIdx.x + (long long)blockIdx.y * gridDim.x] = s;
+}
+
+// Per-block largest CFL rate of U^n (exact formula of compute_dt_Impl) and its cell.
+template <bool FAST>
+__global__ void __launch_bounds__(ANT) k_adj_rate_argmax(const double* h, const double* hu, const double* hv,
+                                                          const double* z, long long pitch, int nx, int ny, double dx,
+                                                          double dy, double* prate, long long* pidx, unsigned* pflags) {
+    __shared__ double sr[ANT / 32];
+    __shared__ long long si[ANT / 32];
+    __shared__ unsigned sf[ANT / 32];
+    const int i = blockIdx.x * ATX + (threadIdx.x % ATX), j = blockIdx.y * ATY + threadIdx.x / ATX;
+    double rate = 0;
+    long long idx = 0x7fffffffffffffffll;
+    unsigned fl = 0;
+    if (i < nx && j < ny) {
+        const long long o = (long long)i + (long long)j * pitch;
+        double mv;
+        dt_cell_contrib<double, FAST>(h[o], hu[o], hv[o], is_nodata(z[o]), dx, dy, 1.0 / dx, 1.0 / dy, rate, mv, fl);
+        if (rate > 0) idx = o;
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        const double r2 = __shfl_xor_sync(0xffffffffu, rate, off);
+        const long long i2 = __shfl_xor_sync(0xffffffffu, idx, off);
+        if (r2 > rate || (r2 == rate && i2 < idx)) { rate = r2; idx = i2; }
+    }
+    fl = __reduce_or_sync(0xffffffffu, fl);
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) { sr[w] = rate; si[w] = idx; sf[w] = fl; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < ANT / 32; ++k) {
+            if (sr[k] > rate || (sr[k] == rate && si[k] < idx)) { rate = sr[k]; idx = si[k]; }
+            fl |= sf[k];
+        }
+        const long long b = blockIdx.x + (long long)blockIdx.y * gridDim.x;
+        prate[b] = rate;
+        pidx[b] = idx;
+        pflags[b] = fl;
+    }
+}
+
+// Kernel C: dt adjoint into the cell that set the CFL bound, then the gauge
+// misfit of state n (seed * 2 (h - href)).  One block.
+__global__ void __launch_bounds__(ANT) k_adj_finish(int nblocks, const double* dtbar_p, const double* prate,
+                                                     const long long* pidx, const unsigned* pflags, double cfl,
+                                                     double dx, double dy, const double* h, const double* hu,
+                                                     const double* hv, double* lam_h, double* lam_hu, double* lam_hv,
+                                                     int with_dt, int ngauges, const long long* gauges,
+                                                     const double* href, double seed) {
+    __shared__ double sh[ANT / 32];
+    __shared__ double s_rate[ANT];
+    __shared__ long long s_idx[ANT];
+    __shared__ unsigned s_fl[ANT];
+    double d = 0, rate = 0;
+    long long idx = 0x7fffffffffffffffll;
+    unsigned fl = 0;
+    if (with_dt) {
+        for (int k = threadIdx.x; k < nblocks; k += ANT) {
+            d += dtbar_p[k];
+            if (prate[k] > rate || (prate[k] == rate && pidx[k] < idx)) { rate = prate[k]; idx = pidx[k]; }
+            fl |= pflags[k];
+        }
+    }
+    const double dtbar = block_sum(d, sh);
+    s_rate[threadIdx.x] = rate;
+    s_idx[threadIdx.x] = idx;
+    s_fl[threadIdx.x] = fl;
+    __syncthreads();
+    if (threadIdx.x == 0 && with_dt) {
+        for (int k = 1; k < ANT; ++k) {
+            if (s_rate[k] > rate || (s_rate[k] == rate && s_idx[k] < idx)) { rate = s_rate[k]; idx = s_idx[k]; }
+            fl |= s_fl[k];
+        }
+        // dt = cfl * min(1/rate, 1e6 if a dry cell, 1e30 if NODATA): differentiable through the rate only
+        const double m = accum_dt_min<double>(to_bits<double>(rate), fl);
+        if (rate > 0 && m == 1.0 / rate) {
+            const double hh = h[idx], u = hu[idx] / hh, v = hv[idx] / hh, c = sqrt(G * hh);
+            const double gr = dtbar * (-cfl / (rate * rate));  // d dt / d rate
+            const double su = sgn(u), sv = sgn(v), dc = G / (2.0 * c);
+            lam_h[idx] += gr * ((su * (-u / hh) + dc) / dx + (sv * (-v / hh) + dc) / dy);
+            lam_hu[idx] += gr * su / (hh * dx);
+            lam_hv[idx] += gr * sv / (hh * dy);
+        }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < ngauges; k += ANT) {
+        const long long gcell = gauges[k];
+        lam_h[gcell] += seed * 2.0 * (h[gcell] - href[k]);
+    }
+}
+
+// Records the dt the step used (cfl * min bound of the chain) and the gauges.
+__global__ void k_adj_record(const DtAccum* slot, double cfl, double* dt_out, const double* h, int ngauges,
+                             const long long* gauges, double* series) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) *dt_out = accum_dt_min<double>(slot->rate_bits, slot->flags) * cfl;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < ngauges; k += gridDim.x * blockDim.x)
+        series[k] = h[gauges[k]];
+}
+
+}  // namespace
+
+// ===========================================================================
+// Drivers
+// ===========================================================================
+namespace {
+
+struct AdjLayout {
+    size_t plane;                 // doubles per plane (ny * pitch)
+    int nslots, seg;              // stored states, segment length (0: every state stored)
+    size_t states, segbuf, lam, lamlin, lin, tmp, dthist, pflags, slots, status, part, total;
+    int nblocks;
+};
+
+size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+AdjLayout adj_layout(int nx, int ny, long long pitch, int nsteps, int every) {
+    AdjLayout L{};
+    L.plane = (size_t)ny * (size_t)pitch;
+    const size_t st = 3 * L.plane * sizeof(double);
+    L.seg = (every > 0 && every < nsteps) ? every : 0;
+    L.nslots = L.seg ? (nsteps / L.seg + 1) : (nsteps + 1);
+    size_t o = 0;
+    L.states = o; o += al256((size_t)L.nslots * st);
+    L.segbuf = o; o += L.seg ? al256((size_t)(L.seg + 1) * st) : 0;
+    L.tmp = o; o += L.seg ? al256(2 * st) : 0;
+    L.lam = o; o += al256(2 * st);
+    L.lamlin = o; o += al256(st);
+    L.lin = o; o += al256(st);
+    L.dthist = o; o += al256((size_t)nsteps * sizeof(double));
+    L.pflags = o; o += al256((size_t)nsteps * sizeof(unsigned));
+    L.slots = o; o += 256;
+    L.status = o; o += 256;
+    L.nblocks = ((nx + ATX - 1) / ATX) * ((ny + ATY - 1) / ATY);
+    L.part = o; o += al256((size_t)L.nblocks * (2 * sizeof(double) + sizeof(long long) + sizeof(unsigned)));
+    L.total = o;
+    return L;
+}
+
+struct Views {
+    double* base;
+    size_t plane;
+    double* state(size_t off, int k) const { return base + off / sizeof(double) + (size_t)k * 3 * plane; }
+};
+
+int adj_check(const hx_level_f64* L, int nsteps, int ngauges, const int64_t* gauges) {
+    if (!L || !L->h || !L->hu || !L->hv || !L->z || !L->n) return set_error(HX_ERR_ARG, "adjoint: null level plane");
+    if (L->nx < 2 || L->ny < 2 || L->pitch < L->nx || !(L->dx > 0) || !(L->dy > 0))
+        return set_error(HX_ERR_ARG, "adjoint: bad level geometry");
+    if (L->nx % ATX == 1 || L->ny % ATY == 1)
+        return set_error(HX_ERR_ARG, "adjoint: nx % 32 == 1 or ny % 8 == 1 is not supported (a one-cell edge tile)");
+    if (nsteps < 1) return set_error(HX_ERR_ARG, "adjoint: nsteps < 1");
+    if (ngauges < 0 || (ngauges > 0 && !gauges)) return set_error(HX_ERR_ARG, "adjoint: bad gauges");
+    if (ngauges > 0) {  // gauge offsets i + j * pitch must name cells of the level
+        std::vector<int64_t> g((size_t)ngauges);
+        if (cudaMemcpy(g.data(), gauges, g.size() * sizeof(int64_t), cudaMemcpyDeviceToHost) != cudaSuccess)
+            return set_error(HX_ERR_CUDA, "adjoint: gauges are not readable device memory");
+        for (int64_t o : g)
+            if (o < 0 || o % L->pitch >= L->nx || o / L->pitch >= L->ny)
+                return set_error(HX_ERR_ARG, "adjoint: gauge offset outside the level");
+    }
+    return HX_OK;
+}
+
+LevelSrc<double> make_src(const hx_level_f64* L, const double* const* st, int g) {
+    LevelSrc<double> s;
+    s.h = st[0]; s.hu = st[1]; s.hv = st[2]; s.z = L->z; s.n = L->n;
+    s.pitch = L->pitch;
+    s.nx = L->nx; s.ny = L->ny;
+    s.bc_xlo = L->bc_lo[0]; s.bc_ylo = L->bc_lo[1]; s.bc_xhi = L->bc_hi[0]; s.bc_yhi = L->bc_hi[1];
+    s.glo0 = -g; s.glo1 = -g; s.ghi0 = L->nx - 1 + g; s.ghi1 = L->ny - 1 + g;
+    return s;
+}
+
+template <bool FAST>
+cudaError_t forward_step(const hx_level_f64* L, double* const* in, double* const* out, StepCtl<double> ctl,
+                         const double* dt_fixed, unsigned* pflags, cudaStream_t st) {
+    const IBox vb{0, 0, L->nx - 1, L->ny - 1};
+    const double* cin[3] = {in[0], in[1], in[2]};
+    LevelSrc<double> src = make_src(L, cin, 2);
+    Cells3<double> uo;
+    for (int k = 0; k < 3; ++k) uo.p[k] = in[k];
+    uo.js = L->pitch; uo.lo0 = 0; uo.lo1 = 0;
+    Cells3W<double> o;
+    for (int k = 0; k < 3; ++k) o.p[k] = out[k];
+    o.js = L->pitch; o.lo0 = 0; o.lo1 = 0;
+    Plane<double> np{L->n, L->pitch, 0, 0};
+    return launch_adj_forward<FAST>(src, uo, np, o, vb, ctl, dt_fixed, pflags, st);
+}
+
+// The flux update of U^n alone (before friction and clamp) into lin.
+template <bool FAST>
+cudaError_t linear_step(const hx_level_f64* L, const double* Un, size_t plane, double* lin, const double* dt_dev,
+                        cudaStream_t st) {
+    const double* cin[3] = {Un, Un + plane, Un + 2 * plane};
+    LevelSrc<double> src = make_src(L, cin, 2);
+    Cells3<double> uo;
+    for (int k = 0; k < 3; ++k) uo.p[k] = cin[k];
+    uo.js = L->pitch; uo.lo0 = 0; uo.lo1 = 0;
+    Cells3W<double> o;
+    for (int k = 0; k < 3; ++k) o.p[k] = lin + k * plane;
+    o.js = L->pitch; o.lo0 = 0; o.lo1 = 0;
+    Plane<double> np{L->n, L->pitch, 0, 0};
+    return launch_adj_forward_linear<FAST>(src, uo, np, o, IBox{0, 0, L->nx - 1, L->ny - 1}, L->dx, L->dy, dt_dev, st);
+}
+
+template <bool FAST>
+int adjoint_forward(const hx_level_f64* L, int nsteps, double cfl, int ngauges, const int64_t* gauges, double* series,
+                    int checkpoint_every, void* work, uint32_t* status, cudaStream_t st) {
+    const AdjLayout A = adj_layout(L->nx, L->ny, L->pitch, nsteps, checkpoint_every);
+    Views V{static_cast<double*>(work), A.plane};
+    char* base = static_cast<char*>(work);
+    DtAccum* slot = reinterpret_cast<DtAccum*>(base + A.slots);
+    unsigned* pfl = reinterpret_cast<unsigned*>(base + A.pflags);
+    double* dth = reinterpret_cast<double*>(base + A.dthist);
+    unsigned* stw = status ? status : reinterpret_cast<unsigned*>(base + A.status);
+    const size_t pb = A.plane * sizeof(double);
+    cudaError_t e = cudaMemsetAsync(base + A.slots, 0, 512, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(pfl, 0, (size_t)nsteps * sizeof(unsigned), st);
+    // state 0 into its slot
+    double* s0 = V.state(A.states, 0);
+    const double* src0[3] = {L->h, L->hu, L->hv};
+    for (int k = 0; k < 3 && e == cudaSuccess; ++k)
+        e = cudaMemcpy2DAsync(s0 + k * A.plane, L->pitch * sizeof(double), src0[k], L->pitch * sizeof(double),
+                              L->nx * sizeof(double), L->ny, cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) return set_error(HX_ERR_CUDA, cudaGetErrorString(e));
+    {
+        Cells3<double> U;
+        U.p[0] = s0; U.p[1] = s0 + A.plane; U.p[2] = s0 + 2 * A.plane;
+        U.js = L->pitch; U.lo0 = 0; U.lo1 = 0;
+        Plane<double> Z{L->z, L->pitch, 0, 0};
+        e = launch_dt_reduce<double, FAST>(U, Z, IBox{0, 0, L->nx - 1, L->ny - 1}, L->dx, L->dy, &slot[0], st);
+        if (e != cudaSuccess) return set_error(HX_ERR_LAUNCH, cudaGetErrorString(e));
+    }
+    int launches = 1;
+    for (int n = 0; n < nsteps; ++n) {
+        double *in[3], *out[3];
+        double* a;
+        double* b;
+        if (!A.seg) {
+            a = V.state(A.states, n);
+            b = V.state(A.states, n + 1);
+        } else {
+            a = n == 0 ? s0 : V.state(A.tmp, n % 2);
+            b = V.state(A.tmp, (n + 1) % 2);
+        }
+        for (int k = 0; k < 3; ++k) { in[k] = a + k * A.plane; out[k] = b + k * A.plane; }
+        StepCtl<double> ctl;
+        ctl.dt_host = 0.0; ctl.cfl = cfl;
+        ctl.dt_in = &slot[n % 3]; ctl.dt_out = &slot[(n + 1) % 3]; ctl.dt_reset = &slot[(n + 2) % 3];
+        ctl.status = stw; ctl.time = nullptr; ctl.dx = L->dx; ctl.dy = L->dy;
+        e = forward_step<FAST>(L, in, out, ctl, nullptr, &pfl[n], st);
+        if (e == cudaSuccess) {
+            k_adj_record<<<1, 64, 0, st>>>(&slot[n % 3], cfl, &dth[n], out[0], ngauges, (const long long*)gauges,
+                                           series ? series + (size_t)n * ngauges : nullptr);
+            e = cudaGetLastError();
+        }
+        launches += 2;
+        if (e == cudaSuccess && A.seg && (n + 1) % A.seg == 0) {
+            double* ck = V.state(A.states, (n + 1) / A.seg);
+            e = cudaMemcpyAsync(ck, b, 3 * pb, cudaMemcpyDeviceToDevice, st);
+        }
+        if (e != cudaSuccess) return set_error(HX_ERR_LAUNCH, cudaGetErrorString(e));
+    }
+    note_launches(launches);
+    return HX_OK;
+}
+
+template <bool FAST>
+int adjoint_reverse(const hx_level_f64* L, int nsteps, double cfl, int ngauges, const int64_t* gauges,
+                    const double* href, double seed, int checkpoint_every, void* work, double* grad_h, double* grad_hu,
+                    double* grad_hv, double* grad_z, cudaStream_t st) {
+    const AdjLayout A = adj_layout(L->nx, L->ny, L->pitch, nsteps, checkpoint_every);
+    Views V{static_cast<double*>(work), A.plane};
+    char* base = static_cast<char*>(work);
+    const size_t pb = A.plane * sizeof(double);
+    double* dth = reinterpret_cast<double*>(base + A.dthist);
+    unsigned* pfl = reinterpret_cast<unsigned*>(base + A.pflags);
+    double* p_dt = reinterpret_cast<double*>(base + A.part);
+    double* p_rate = p_dt + A.nblocks;
+    long long* p_idx = reinterpret_cast<long long*>(p_rate + A.nblocks);
+    unsigned* p_fl = reinterpret_cast<unsigned*>(p_idx + A.nblocks);
+    const long long* gcells = reinterpret_cast<const long long*>(gauges);
+
+    std::vector<double> dt_host((size_t)nsteps);
+    std::vector<unsigned> pf_host((size_t)nsteps);
+    cudaError_t e = cudaMemcpyAsync(dt_host.data(), dth, nsteps * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(pf_host.data(), pfl, nsteps * sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(grad_z, 0, pb, st);
+    double* lamb[2] = {V.state(A.lam, 0), V.state(A.lam, 1)};
+    if (e == cudaSuccess) e = cudaMemsetAsync(lamb[0], 0, 3 * pb, st);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_adj_faces<FAST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(AdjSmem));
+    if (e != cudaSuccess) return set_error(HX_ERR_CUDA, cudaGetErrorString(e));
+    int cur = 0;  // lamb[cur] holds lambda^{n+1}
+    const IBox vb{0, 0, L->nx - 1, L->ny - 1};
+    const dim3 grid = tile_grid(vb, ATX, ATY);
+    int launches = 0;
+
+    auto finish = [&](int n, const double* Un, double* lam, int with_dt) {
+        const double* series_ref = n >= 1 ? href + (size_t)(n - 1) * ngauges : nullptr;
+        k_adj_finish<<<1, ANT, 0, st>>>(A.nblocks, p_dt, p_rate, p_idx, p_fl, cfl, L->dx, L->dy, Un, Un + A.plane,
+                                        Un + 2 * A.plane, lam, lam + A.plane, lam + 2 * A.plane, with_dt,
+                                        n >= 1 ? ngauges : 0, gcells, series_ref, seed);
+        ++launches;
+        return cudaGetLastError();
+    };
+    auto state_at = [&](int n, int seg0) -> double* {
+        if (!A.seg) return V.state(A.states, n);
+        return V.state(A.segbuf, n - seg0);
+    };
+    // reverse over segments (one segment of all steps when every state is stored)
+    const int L_seg = A.seg ? A.seg : nsteps;
+    const int nseg = (nsteps + L_seg - 1) / L_seg;
+    bool first = true;
+    for (int sg = nseg - 1; sg >= 0 && e == cudaSuccess; --sg) {
+        const int n0 = sg * L_seg, n1 = (n0 + L_seg < nsteps) ? n0 + L_seg : nsteps;
+        if (A.seg) {  // recompute the segment's states from its checkpoint with the recorded dt
+            e = cudaMemcpyAsync(V.state(A.segbuf, 0), V.state(A.states, sg), 3 * pb, cudaMemcpyDeviceToDevice, st);
+            for (int n = n0; n < n1 && e == cudaSuccess; ++n) {
+                double* a = V.state(A.segbuf, n - n0);
+                double* b = V.state(A.segbuf, n - n0 + 1);
+                double *in[3], *out[3];
+                for (int k = 0; k < 3; ++k) { in[k] = a + k * A.plane; out[k] = b + k * A.plane; }
+                StepCtl<double> ctl{};
+                ctl.dx = L->dx; ctl.dy = L->dy;
+                e = forward_step<FAST>(L, in, out, ctl, &dth[n], nullptr, st);
+                ++launches;
+            }
+        }
+        if (first && e == cudaSuccess) {  // lambda^N: the misfit of the final state
+            e = finish(nsteps, state_at(nsteps, n0), lamb[cur], 0);
+            first = false;
+        }
+        for (int n = n1 - 1; n >= n0 && e == cudaSuccess; --n) {
+            double* Un = state_at(n, n0);
+            double* Un1 = state_at(n + 1, n0);
+            const double dt = dt_host[(size_t)n];
+            double* lam1 = lamb[cur];
+            double* lam0 = lamb[cur ^ 1];
+            const double* lam_for_faces = lam1;
+            if (pf_host[(size_t)n]) {  // friction or dry clamp in this step: reverse the post map
+                double* lin = V.state(A.lin, 0);
+                double* ll = V.state(A.lamlin, 0);
+                e = linear_step<FAST>(L, Un, A.plane, lin, &dth[n], st);
+                PostArgs P;
+                for (int k = 0; k < 3; ++k) {
+                    P.lin[k] = lin + k * A.plane; P.un[k] = Un + k * A.plane; P.lam[k] = lam1 + k * A.plane;
+                    P.out[k] = ll + k * A.plane;
+                }
+                P.nman = L->n; P.dtbar = p_dt; P.pitch = L->pitch; P.nx = L->nx; P.ny = L->ny; P.dt = dt;
+                k_adj_post<<<grid, ANT, 0, st>>>(P);
+                launches += 2;
+                lam_for_faces = ll;
+            } else {
+                k_adj_dtbar_identity<<<grid, ANT, 0, st>>>(lam1, lam1 + A.plane, lam1 + 2 * A.plane, Un1,
+                                                           Un1 + A.plane, Un1 + 2 * A.plane, Un, Un + A.plane,
+                                                           Un + 2 * A.plane, L->pitch, L->nx, L->ny, dt, p_dt);
+                ++launches;
+            }
+            {
+                const double* cin[3] = {Un, Un + A.plane, Un + 2 * A.plane};
+                AdjArgs B;
+                B.src = make_src(L, cin, 2);
+                for (int k = 0; k < 3; ++k) {
+                    B.lam[k] = lam_for_faces + k * A.plane;
+                    B.out[k] = lam0 + k * A.plane;
+                }
+                B.zbar = grad_z; B.pitch = L->pitch; B.nx = L->nx; B.ny = L->ny;
+                B.cx = dt / L->dx; B.cy = dt / L->dy;
+                k_adj_faces<FAST><<<grid, ANT, sizeof(AdjSmem), st>>>(B);
+                k_adj_rate_argmax<FAST><<<grid, ANT, 0, st>>>(Un, Un + A.plane, Un + 2 * A.plane, L->z, L->pitch,
+                                                              L->nx, L->ny, L->dx, L->dy, p_rate, p_idx, p_fl);
+                launches += 2;
+            }
+            if (e == cudaSuccess) e = cudaGetLastError();
+            if (e == cudaSuccess) e = finish(n, Un, lam0, 1);
+            cur ^= 1;
+        }
+    }
+    if (e == cudaSuccess) {
+        double* g[3] = {grad_h, grad_hu, grad_hv};
+        for (int k = 0; k < 3 && e == cudaSuccess; ++k)
+            e = cudaMemcpyAsync(g[k], lamb[cur] + k * A.plane, pb, cudaMemcpyDeviceToDevice, st);
+    }
+    note_launches(launches);
+    if (e != cudaSuccess) return set_error(HX_ERR_LAUNCH, cudaGetErrorString(e));
+    return HX_OK;
+}
+
+template <bool FAST>
+int adjoint_step(const hx_level_f64* L, double dt, const double* const* lam, double* const* outs, double* zbar,
+                 double* dtbar, void* work, cudaStream_t st) {
+    const AdjLayout A = adj_layout(L->nx, L->ny, L->pitch, 1, 0);
+    char* base = static_cast<char*>(work);
+    Views V{static_cast<double*>(work), A.plane};
+    double* p_dt = reinterpret_cast<double*>(base + A.part);
+    double* dth = reinterpret_cast<double*>(base + A.dthist);
+    double* lin = V.state(A.lin, 0);
+    double* ll = V.state(A.lamlin, 0);
+    double* un = V.state(A.states, 0);  // U^n copied to the work layout (pitch of the level)
+    const IBox vb{0, 0, L->nx - 1, L->ny - 1};
+    const dim3 grid = tile_grid(vb, ATX, ATY);
+    const double* src0[3] = {L->h, L->hu, L->hv};
+    cudaError_t e = cudaMemcpyAsync(dth, &dt, sizeof(double), cudaMemcpyHostToDevice, st);
+    for (int k = 0; k < 3 && e == cudaSuccess; ++k)
+        e = cudaMemcpy2DAsync(un + k * A.plane, L->pitch * sizeof(double), src0[k], L->pitch * sizeof(double),
+                              L->nx * sizeof(double), L->ny, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_adj_faces<FAST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(AdjSmem));
+    if (e != cudaSuccess) return set_error(HX_ERR_CUDA, cudaGetErrorString(e));
+    e = linear_step<FAST>(L, un, A.plane, lin, dth, st);
+    if (e != cudaSuccess) return set_error(HX_ERR_LAUNCH, cudaGetErrorString(e));
+    PostArgs P;
+    for (int k = 0; k < 3; ++k) {
+        P.lin[k] = lin + k * A.plane; P.un[k] = un + k * A.plane; P.lam[k] = lam[k]; P.out[k] = ll + k * A.plane;
+    }
+    P.nman = L->n; P.dtbar = p_dt; P.pitch = L->pitch; P.nx = L->nx; P.ny = L->ny; P.dt = dt;
+    k_adj_post<<<grid, ANT, 0, st>>>(P);
+    AdjArgs B;
+    const double* cin[3] = {un, un + A.plane, un + 2 * A.plane};
+    B.src = make_src(L, cin, 2);
+    for (int k = 0; k < 3; ++k) { B.lam[k] = ll + k * A.plane; B.out[k] = outs[k]; }
+    B.zbar = zbar; B.pitch = L->pitch; B.nx = L->nx; B.ny = L->ny;
+    B.cx = dt / L->dx; B.cy = dt / L->dy;
+    k_adj_faces<FAST><<<grid, ANT, sizeof(AdjSmem), st>>>(B);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) {  // dtbar = sum of the per-block partials
+        std::vector<double> parts((size_t)A.nblocks);
+        e = cudaMemcpyAsync(parts.data(), p_dt, parts.size() * sizeof(double), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        double sum = 0;
+        for (double x : parts) sum += x;
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dtbar, &sum, sizeof(double), cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    }
+    note_launches(3);
+    if (e != cudaSuccess) return set_error(HX_ERR_LAUNCH, cudaGetErrorString(e));
+    return HX_OK;
+}
+
+bool arith_ok(int arith) { return arith == HX_ARITH_EXACT || arith == HX_ARITH_FAST; }
+
+}  // namespace
+
+extern "C" int64_t hx_adjoint_work_bytes_f64(int nx, int ny, int64_t pitch, int nsteps, int checkpoint_every) {
+    if (nx < 2 || ny < 2 || pitch < nx || nsteps < 1) return 0;
+    return (int64_t)adj_layout(nx, ny, pitch, nsteps, checkpoint_every).total;
+}
+
+extern "C" int hx_adjoint_forward_f64(const hx_level_f64* L, int nsteps, double cfl, int ngauges,
+                                      const int64_t* gauges, double* series, int checkpoint_every, int arith,
+                                      void* work, uint32_t* status, hx_stream_t stream) {
+    int rc = adj_check(L, nsteps, ngauges, gauges);
+    if (rc) return rc;
+    if (!work || !(cfl > 0) || (ngauges > 0 && !series) || !arith_ok(arith))
+        return set_error(HX_ERR_ARG, "adjoint forward: bad arguments");
+    return arith == HX_ARITH_FAST
+               ? adjoint_forward<true>(L, nsteps, cfl, ngauges, gauges, series, checkpoint_every, work, status,
+                                       (cudaStream_t)stream)
+               : adjoint_forward<false>(L, nsteps, cfl, ngauges, gauges, series, checkpoint_every, work, status,
+                                        (cudaStream_t)stream);
+}
+
+extern "C" int hx_adjoint_reverse_f64(const hx_level_f64* L, int nsteps, double cfl, int ngauges,
+                                      const int64_t* gauges, const double* href, double seed, int checkpoint_every,
+                                      int arith, void* work, double* grad_h, double* grad_hu, double* grad_hv,
+                                      double* grad_z, hx_stream_t stream) {
+    int rc = adj_check(L, nsteps, ngauges, gauges);
+    if (rc) return rc;
+    if (!work || !grad_h || !grad_hu || !grad_hv || !grad_z || (ngauges > 0 && !href) || !arith_ok(arith))
+        return set_error(HX_ERR_ARG, "adjoint reverse: bad arguments");
+    return arith == HX_ARITH_FAST
+               ? adjoint_reverse<true>(L, nsteps, cfl, ngauges, gauges, href, seed, checkpoint_every, work, grad_h,
+                                       grad_hu, grad_hv, grad_z, (cudaStream_t)stream)
+               : adjoint_reverse<false>(L, nsteps, cfl, ngauges, gauges, href, seed, checkpoint_every, work, grad_h,
+                                        grad_hu, grad_hv, grad_z, (cudaStream_t)stream);
+}
+
+// One reverse step with a given dt (no CFL dependence, no gauges): the
+// transpose of the step map (U^n, z) -> U^{n+1} at fixed dt, plus d/d dt.
+extern "C" int hx_adjoint_step_f64(const hx_level_f64* L, double dt, const double* lam_h, const double* lam_hu,
+                                   const double* lam_hv, double* out_h, double* out_hu, double* out_hv,
+                                   double* zbar, double* dtbar, int arith, void* work, hx_stream_t stream) {
+    int rc = adj_check(L, 1, 0, nullptr);
+    if (rc) return rc;
+    if (!lam_h || !lam_hu || !lam_hv || !out_h || !out_hu || !out_hv || !zbar || !dtbar || !work || !(dt > 0) ||
+        !arith_ok(arith))
+        return set_error(HX_ERR_ARG, "hx_adjoint_step_f64: bad arguments");
+    const double* lam[3] = {lam_h, lam_hu, lam_hv};
+    double* outs[3] = {out_h, out_hu, out_hv};
+    return arith == HX_ARITH_FAST ? adjoint_step<true>(L, dt, lam, outs, zbar, dtbar, work, (cudaStream_t)stream)
+                                  : adjoint_step<false>(L, dt, lam, outs, zbar, dtbar, work, (cudaStream_t)stream);
+}

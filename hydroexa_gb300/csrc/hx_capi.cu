@@ -520,6 +520,34 @@ void hx_host_cache_release(void) {
     g_host.bytes = 0;
 }
 
+int hx_level_tangent_f64(const hx_level_f64* L, double dt, double ddt, double* oh, double* ohu, double* ohv,
+                         hx_stream_t s) {
+    if (!level_ok(L)) return HX_ERR_ARG;
+    if (!oh || !ohu || !ohv) return fail(HX_ERR_ARG, "hx_level_tangent_f64: null output planes");
+    LevelSrc<Dual> src;
+    src.h = reinterpret_cast<const Dual*>(L->h);
+    src.hu = reinterpret_cast<const Dual*>(L->hu);
+    src.hv = reinterpret_cast<const Dual*>(L->hv);
+    src.z = reinterpret_cast<const Dual*>(L->z);
+    src.n = reinterpret_cast<const Dual*>(L->n);
+    src.pitch = L->pitch;
+    src.nx = L->nx; src.ny = L->ny;
+    src.bc_xlo = L->bc_lo[0]; src.bc_ylo = L->bc_lo[1]; src.bc_xhi = L->bc_hi[0]; src.bc_yhi = L->bc_hi[1];
+    src.glo0 = -2; src.glo1 = -2; src.ghi0 = L->nx + 1; src.ghi1 = L->ny + 1;
+    Cells3<Dual> uo;
+    uo.p[0] = src.h; uo.p[1] = src.hu; uo.p[2] = src.hv;
+    uo.js = L->pitch; uo.lo0 = 0; uo.lo1 = 0;
+    Plane<Dual> np{src.n, L->pitch, 0, 0};
+    Cells3W<Dual> out;
+    out.p[0] = reinterpret_cast<Dual*>(oh);
+    out.p[1] = reinterpret_cast<Dual*>(ohu);
+    out.p[2] = reinterpret_cast<Dual*>(ohv);
+    out.js = L->pitch; out.lo0 = 0; out.lo1 = 0;
+    const IBox vb{0, 0, L->nx - 1, L->ny - 1};
+    return launched(launch_tangent(src, uo, np, out, vb, Dual(dt, ddt), L->dx, L->dy, (cudaStream_t)s),
+                    "hx_level_tangent_f64");
+}
+
 int hx_debug_roe_points_f64(int method, int arith, long n, const double* st, const double* aux, double* out,
                             hx_stream_t s) {
     if (n < 0 || (n > 0 && (!st || !aux || !out))) return fail(HX_ERR_ARG, "bad point arrays");

@@ -24,6 +24,12 @@ HX_INST(float)
 #undef HX_INST
 template cudaError_t launch_ensemble<double, true>(const EnsInstance<double>*, int, long long, int, double, unsigned long long*, int, cudaStream_t);
 template int ensemble_blocks_per_sm<double, true>();
+template cudaError_t launch_adj_forward<true>(const LevelSrc<double>&, const Cells3<double>&, const Plane<double>&,
+                                              const Cells3W<double>&, const IBox&, const StepCtl<double>&,
+                                              const double*, unsigned*, cudaStream_t);
+template cudaError_t launch_adj_forward_linear<true>(const LevelSrc<double>&, const Cells3<double>&,
+                                                     const Plane<double>&, const Cells3W<double>&, const IBox&, double,
+                                                     double, const double*, cudaStream_t);
 template cudaError_t launch_points<double, true>(int, long, const double*, const double*, double*, cudaStream_t);
 template cudaError_t launch_points<float, true>(int, long, const float*, const float*, float*, cudaStream_t);
 }  // namespace hx

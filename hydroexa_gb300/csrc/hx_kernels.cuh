@@ -622,6 +622,44 @@ __global__ void k_points(int method, long n, const R* __restrict__ st, const R* 
 }  // namespace hx
 
 // ---------------------------------------------------------------------------
+// Forward steps of the adjoint's sweeps (see launch_adj_forward).
+// ---------------------------------------------------------------------------
+namespace hx {
+template <bool FAST>
+__global__ void __launch_bounds__(NT) k_adj_forward(LevelSrc<double> src, Cells3<double> uo, Plane<double> np,
+                                                     Cells3W<double> out, IBox vb, StepCtl<double> ctl,
+                                                     const double* dt_fixed, unsigned* post_flags) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    HydroSmem<double>& S = *reinterpret_cast<HydroSmem<double>*>(smem_raw);
+    double dt;
+    if (dt_fixed) {
+        dt = *dt_fixed;
+    } else {
+        if (!resolve_dt(ctl, dt)) return;
+        step_bookkeeping(ctl, dt);
+    }
+    FaceOut<double> fo{};
+    fo.on = 0;
+    hydro_tile_body<double, FAST, TX, TY, NT>(S, src, uo, np, out, fo, vb, vb.lo0 + (int)blockIdx.x * TX,
+                                              vb.lo1 + (int)blockIdx.y * TY, dt, ctl.dx, ctl.dy,
+                                              dt_fixed ? nullptr : ctl.dt_out, ctl.status, post_flags);
+}
+
+template <bool FAST>
+__global__ void __launch_bounds__(NT) k_adj_forward_linear(LevelSrc<double> src, Cells3<double> uo, Plane<double> np,
+                                                            Cells3W<double> out, IBox vb, double dx, double dy,
+                                                            const double* dt_fixed) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    HydroSmem<double>& S = *reinterpret_cast<HydroSmem<double>*>(smem_raw);
+    FaceOut<double> fo{};
+    fo.on = 0;
+    hydro_tile_body<double, FAST, TX, TY, NT, LevelSrc<double>, true>(
+        S, src, uo, np, out, fo, vb, vb.lo0 + (int)blockIdx.x * TX, vb.lo1 + (int)blockIdx.y * TY, *dt_fixed, dx, dy,
+        nullptr, nullptr);
+}
+}  // namespace hx
+
+// ---------------------------------------------------------------------------
 // Launchers (explicitly instantiated per arithmetic form).
 // ---------------------------------------------------------------------------
 #include "hx_launch.h"
@@ -680,6 +718,28 @@ template <class R, bool FAST>
 cudaError_t launch_dt_reduce(const Cells3<R>& U, const Plane<R>& Z, const IBox& vb, R dx, R dy, DtAccum* acc,
                              cudaStream_t st) {
     k_dt_reduce<R, FAST><<<tile_grid(vb, TX, TY), NT, 0, st>>>(U, Z, vb, dx, dy, acc);
+    return cudaGetLastError();
+}
+
+template <bool FAST>
+cudaError_t launch_adj_forward(const LevelSrc<double>& src, const Cells3<double>& uo, const Plane<double>& np,
+                               const Cells3W<double>& out, const IBox& vb, const StepCtl<double>& ctl,
+                               const double* dt_fixed, unsigned* post_flags, cudaStream_t st) {
+    const size_t sm = sizeof(HydroSmem<double>);
+    cudaError_t e = ensure_smem(k_adj_forward<FAST>, sm);
+    if (e != cudaSuccess) return e;
+    k_adj_forward<FAST><<<tile_grid(vb, TX, TY), NT, sm, st>>>(src, uo, np, out, vb, ctl, dt_fixed, post_flags);
+    return cudaGetLastError();
+}
+
+template <bool FAST>
+cudaError_t launch_adj_forward_linear(const LevelSrc<double>& src, const Cells3<double>& uo, const Plane<double>& np,
+                                      const Cells3W<double>& out, const IBox& vb, double dx, double dy,
+                                      const double* dt_fixed, cudaStream_t st) {
+    const size_t sm = sizeof(HydroSmem<double>);
+    cudaError_t e = ensure_smem(k_adj_forward_linear<FAST>, sm);
+    if (e != cudaSuccess) return e;
+    k_adj_forward_linear<FAST><<<tile_grid(vb, TX, TY), NT, sm, st>>>(src, uo, np, out, vb, dx, dy, dt_fixed);
     return cudaGetLastError();
 }
 

@@ -37,6 +37,20 @@ cudaError_t launch_ensemble(const EnsInstance<R>* inst, int ninst, long long tot
 
 template <class R, bool FAST> int ensemble_blocks_per_sm();
 
+// Forward step of the adjoint's sweeps: the tile body with dt from the device
+// chain (dt_fixed == nullptr; the step's dt is resolved from ctl) or from
+// *dt_fixed (segment recompute), recording in *post_flags whether any cell took
+// the Manning factor (1) or the dry clamp (2).
+template <bool FAST>
+cudaError_t launch_adj_forward(const LevelSrc<double>& src, const Cells3<double>& uo, const Plane<double>& np,
+                               const Cells3W<double>& out, const IBox& vb, const StepCtl<double>& ctl,
+                               const double* dt_fixed, unsigned* post_flags, cudaStream_t st);
+// The flux update alone at *dt_fixed (the state before friction and clamp).
+template <bool FAST>
+cudaError_t launch_adj_forward_linear(const LevelSrc<double>& src, const Cells3<double>& uo, const Plane<double>& np,
+                                      const Cells3W<double>& out, const IBox& vb, double dx, double dy,
+                                      const double* dt_fixed, cudaStream_t st);
+
 cudaError_t launch_tangent(const LevelSrc<Dual>& src, const Cells3<Dual>& uo, const Plane<Dual>& np,
                            const Cells3W<Dual>& out, const IBox& vb, Dual dt, double dx, double dy, cudaStream_t st);
 

@@ -147,6 +147,18 @@ def ensemble(count=256, seed=4, smin=64, smax=1024, nsteps=500, cfl=0.45, method
     return cases
 
 
+def smooth_field(nx, ny, seed, amplitude, ngauss=8):
+    """Sum of seeded Gaussians scaled to a maximum magnitude of ``amplitude``."""
+    rng = np.random.default_rng(seed)
+    X, Y = _centres(nx, ny)
+    f = np.zeros((ny, nx))
+    for _ in range(ngauss):
+        cx, cy = rng.uniform(0.0, 1.0, 2)
+        s = rng.uniform(0.05, 0.2)
+        f += rng.uniform(-1.0, 1.0) * np.exp(-((X - cx) ** 2 + (Y - cy) ** 2) / (2 * s * s))
+    return amplitude * f / max(np.abs(f).max(), 1e-300)
+
+
 def adjoint_case(nx=512, ny=512, seed=5, ngauss=32, amplitude=0.3, hump=0.2, ngauges=64, nsteps=2000, cfl=0.45):
     """Smooth bed (sum of 32 seeded Gaussians scaled to 0.3 m), free surface
     1.0 plus a 0.2 m Gaussian hump, and 64 seeded gauge cells."""
@@ -165,4 +177,20 @@ def adjoint_case(nx=512, ny=512, seed=5, ngauss=32, amplitude=0.3, hump=0.2, nga
     geom = Geometry(nx, ny, 1.0 / nx, 1.0 / ny, (0, 0), (0, 0))
     case = Case("adjoint_%dx%d" % (nx, ny), geom, h, np.zeros_like(h), np.zeros_like(h), z, np.zeros_like(h), cfl,
                 nsteps, 1)
+    return case, gauges
+
+
+def adjoint_smooth_case(nx=512, ny=512, seed=5, ngauges=64, nsteps=100, cfl=0.45):
+    """The adjoint bed and gauges with a state that has no quiescent region:
+    free surface 1.0 + 0.05 m undulation + 0.2 m hump (centre off the cell
+    boundaries) and smooth currents of up to 0.2 m/s, so the limiters stay off
+    their flat-data branch and the misfit is differentiable."""
+    case, gauges = adjoint_case(nx, ny, seed=seed, ngauges=ngauges, nsteps=nsteps, cfl=cfl)
+    X, Y = _centres(nx, ny)
+    eta = (1.0 + 0.05 * smooth_field(nx, ny, seed + 100, 1.0)
+           + 0.2 * np.exp(-((X - 0.4637) ** 2 + (Y - 0.5311) ** 2) / (2 * 0.05 ** 2)))
+    case.h = np.maximum(0.0, eta - case.z)
+    case.hu = case.h * 0.2 * smooth_field(nx, ny, seed + 101, 1.0)
+    case.hv = case.h * 0.2 * smooth_field(nx, ny, seed + 102, 1.0)
+    case.name = "adjoint_smooth_%dx%d" % (nx, ny)
     return case, gauges

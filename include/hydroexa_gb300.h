@@ -344,7 +344,61 @@ int hx_ensemble_run_f64(int n, const hx_ensemble_member_f64* members, int nsteps
 int hx_level_run_static_f64(int method, hx_level_f64* level, int nsteps, double cfl, uint32_t* status,
                             double* time_dev, int arith, hx_stream_t stream);
 
+/* ---- adjoint of the hydrostatic-Roe time loop ---------------------------- */
+
+/*
+ * Gradient of the gauge misfit J = sum_{n=1..N} sum_g (h^n_g - href^n_g)^2 of
+ * an N-step hydrostatic-Roe run (device CFL chain) with
+ * respect to the initial state (h, hu, hv) and the bed z.  No counterpart in the
+ * reference, which runs forward only.  The adjoint is hand-written: a reverse
+ * kernel of the whole step (van Leer limiter and MUSCL reconstruction, the Roe
+ * flux taking the forward's entropy-fix and dry branches, the hydrostatic cap
+ * and pressure correction, the update, Manning factor and dry clamp) plus the
+ * dependence of each step's dt on the cell that set the CFL bound.
+ *   checkpoint_every = 0: every state is kept (N + 1 states in work);
+ *   k > 0: every k-th state is kept and each k-step segment is recomputed once
+ *   in the reverse sweep (N/k + k + 1 states in work).
+ * hx_adjoint_forward_f64 runs the forward sweep: the level's planes are the
+ * initial state (not modified); series (device, N x ngauges) receives h at the
+ * gauge cells (cell index i + j * pitch) after every step.
+ * hx_adjoint_reverse_f64 then returns seed * dJ/d(h0, hu0, hv0, z) (device
+ * planes with the level's pitch), with the same work buffer and arguments.
+ * arith (HX_ARITH_FAST / HX_ARITH_EXACT) selects the forward's arithmetic
+ * form; the reverse recomputes the forward's values in the same form so that
+ * it takes the same branches.  HX_ARITH_EXACT runs the trajectory of
+ * hx_level_run_f64 with HX_ARITH_EXACT bit for bit (and of the tangent-linear
+ * step's value part).
+ * Restriction: nx % 32 != 1 and ny % 8 != 1.
+ */
+int64_t hx_adjoint_work_bytes_f64(int nx, int ny, int64_t pitch, int nsteps, int checkpoint_every);
+int hx_adjoint_forward_f64(const hx_level_f64* level, int nsteps, double cfl, int ngauges, const int64_t* gauge_cells,
+                           double* series, int checkpoint_every, int arith, void* work, uint32_t* status,
+                           hx_stream_t stream);
+int hx_adjoint_reverse_f64(const hx_level_f64* level, int nsteps, double cfl, int ngauges,
+                           const int64_t* gauge_cells, const double* href, double seed, int checkpoint_every,
+                           int arith, void* work, double* grad_h, double* grad_hu, double* grad_hv, double* grad_z,
+                           hx_stream_t stream);
+/*
+ * One reverse step at a fixed dt: (lam_h, lam_hu, lam_hv) = lambda^{n+1}
+ * (device planes) -> out = lambda^n, zbar += dJ/dz, *dtbar (device) = dJ/d dt.
+ * work: hx_adjoint_work_bytes_f64(nx, ny, pitch, 1, 0) bytes.
+ */
+int hx_adjoint_step_f64(const hx_level_f64* level, double dt, const double* lam_h, const double* lam_hu,
+                        const double* lam_hv, double* out_h, double* out_hu, double* out_hv, double* zbar,
+                        double* dtbar, int arith, void* work, hx_stream_t stream);
+
 /* ---- diagnostics --------------------------------------------------------- */
+
+/*
+ * Tangent-linear step at fixed dt, computed by carrying (value, derivative)
+ * pairs through the exact arithmetic form: every plane of the level (h, hu, hv,
+ * z, n) and of the outputs holds interleaved pairs, pitch counted in pairs;
+ * ddt is the derivative of dt.  The independent check of the adjoint.
+ */
+int hx_level_tangent_f64(const hx_level_f64* level_pairs, double dt, double ddt, double* out_h, double* out_hu,
+                         double* out_hv, hx_stream_t stream);
+
+/* ---- diagnostics (points) ------------------------------------------------ */
 
 /*
  * Evaluate the device Riemann solvers on arrays of face states (device
