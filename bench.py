@@ -32,8 +32,7 @@ from pathlib import Path
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-BASE = json.loads((ROOT / "BASELINE.json").read_text()) if (ROOT / "BASELINE.json").exists() else {}
-METRIC = BASE.get("metric", "FP64 Mcell-updates/s")
+METRIC = "FP64 Mcell-updates/s (plain vs batched, 1 GB300, %HBM roofline); adjoint/fwd cost"
 UNIT = "Mcell-updates/s"
 PEAKS = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
 HBM_GBS = float(PEAKS.get("hbm_gbs", 6800.0))

@@ -9,7 +9,7 @@
 //   A  post-map reverse: lambda_lin = J_post^T lambda^{n+1}, where post is the
 //      Manning factor and the dry clamp (src/solvers/HydrostaticRoe.cpp:566-603),
 //      skipped for steps where no cell took either branch;
-//   B  face reverse: per 32x8 tile, the forward values with a 3-cell halo are
+//   B  face reverse: per 32x16 tile, the forward values with a 3-cell halo are
 //      recomputed, every face flux (HydrostaticRoe.cpp:218-396 with the
 //      homogeneous Roe flux of include/solvers/kernels/HydrostaticRoe.H:44-159)
 //      is differentiated in reverse taking the forward's branches (dry clamps,
@@ -32,10 +32,12 @@ int set_error(int code, const char* msg);
 // exact form's forward sweep stays bit-identical to the exact level advance.
 extern template cudaError_t launch_adj_forward<false>(const LevelSrc<double>&, const Cells3<double>&,
                                                       const Plane<double>&, const Cells3W<double>&, const IBox&,
-                                                      const StepCtl<double>&, const double*, unsigned*, cudaStream_t);
+                                                      const StepCtl<double>&, const double*, unsigned*,
+                                                      const AdjRecord&, cudaStream_t);
 extern template cudaError_t launch_adj_forward<true>(const LevelSrc<double>&, const Cells3<double>&,
                                                      const Plane<double>&, const Cells3W<double>&, const IBox&,
-                                                     const StepCtl<double>&, const double*, unsigned*, cudaStream_t);
+                                                     const StepCtl<double>&, const double*, unsigned*,
+                                                     const AdjRecord&, cudaStream_t);
 extern template cudaError_t launch_adj_forward_linear<false>(const LevelSrc<double>&, const Cells3<double>&,
                                                              const Plane<double>&, const Cells3W<double>&,
                                                              const IBox&, double, double, const double*, cudaStream_t);
@@ -53,10 +55,11 @@ using namespace hx;
 namespace {
 
 constexpr double G = 9.81, HG = 0.5 * 9.81, TD = 1e-6, T12 = 1e-12;
-constexpr int ATX = 32, ATY = 8, ANT = 256;
+constexpr int ATX = 32, ATY = 16, ANT = 512;
 constexpr int H3 = 3;  // forward halo of the reverse tile
 
-__device__ __forceinline__ double sgn(double x) { return x > 0.0 ? 1.0 : (x < 0.0 ? -1.0 : 0.0); }
+// sign with sgn(+-0) = 0, decided on the integer pipe
+__device__ __forceinline__ double sgn(double x) { return pos_i(x) ? 1.0 : (neg_i(x) ? -1.0 : 0.0); }
 
 // ---------------------------------------------------------------------------
 // Reverse of the homogeneous Roe flux in the face-normal frame.  (hi, ui, vi)
@@ -163,6 +166,118 @@ __device__ void roe_rev(double hi, double ui, double vi, double hj, double uj, d
     if (wj) { ghj += gHj; guj += gUj; gvj += gVj; }
 }
 
+// Fast form of roe_rev: the forward quantities that decide branches (wet
+// tests, sonic fixes) are recomputed as roe_hydrostatic_fast computes them,
+// and every division of the reverse becomes a product with one of five
+// reciprocals (1/sden, 1/den, 1/cm, 1/si, 1/sj) obtained from a single
+// rcp_nr of their product.
+__device__ void roe_rev_fast(double hi, double ui, double vi, double hj, double uj, double vj, double b0, double b1,
+                             double b2, double& ghi, double& gui, double& gvi, double& ghj, double& guj, double& gvj) {
+    using C = Cst<double>;
+    const bool wi = ge_bits(hi, C::toldry_bits), wj = ge_bits(hj, C::toldry_bits);
+    const double Hi = wi ? hi : 0.0, Hj = wj ? hj : 0.0;
+    const double Ui = wi ? ui : 0.0, Vi = wi ? vi : 0.0, Uj = wj ? uj : 0.0, Vj = wj ? vj : 0.0;
+    const double si = sqrt(Hi), sj = sqrt(Hj);
+    const double hh = 0.5 * (Hi + Hj);
+    const bool hmb = gt_bits(hh, C::toldry_bits);
+    const double hm = hmb ? hh : TD;
+    const double cm = sqrt(G * hm);
+    const double den = 2.0 * cm + T12;
+    const double sden = si + sj + T12;
+    const double cd = cm * den, S3 = sden * cd;
+    double q3, rsi = 0.0, rsj = 0.0;
+    if (wi && wj) {
+        const double pij = si * sj;
+        const double q = rcp_nr(S3 * pij);
+        q3 = pij * q;
+        rsi = (sj * S3) * q;
+        rsj = (si * S3) * q;
+    } else {
+        q3 = rcp_nr(S3);
+        if (wi) rsi = rcp_nr(si);
+        if (wj) rsj = rcp_nr(sj);
+    }
+    const double rs = cd * q3, rden = (sden * cm) * q3, rcm = (sden * den) * q3;
+    const double um = (Ui * si + Uj * sj) * rs;
+    const double vm = (Vi * si + Vj * sj) * rs;
+    const double l0a = um - cm, l2a = um + cm;
+    const double ci = C::sqrt_g * si, cj = C::sqrt_g * sj;
+    const double e0i = Ui - ci, e0j = Uj - cj;
+    const bool fix0 = neg_i(e0i) && pos_i(e0j);
+    const double e2i = Ui + ci, e2j = Uj + cj;
+    const bool fix2 = neg_i(e2i) && pos_i(e2j);
+    double l0 = l0a, l2 = l2a, rD0 = 0.0, rD2 = 0.0;
+    if (fix0) { rD0 = rcp_nr(e0j - e0i); l0 = e0i * (e0j - l0a) * rD0; }
+    if (fix2) { rD2 = rcp_nr(e2j - e2i); l2 = e2j * (l2a - e2i) * rD2; }
+    const double l1 = um;
+    const double dh = Hj - Hi;
+    const double dhu = Hj * Uj - Hi * Ui;
+    const double dhv = Hj * Vj - Hi * Vi;
+    const double a0 = (l2 * dh - dhu) * rden, a1 = (dhv - vm * dh) * rcm, a2 = (dhu - l0 * dh) * rden;
+    const double w0 = 0.5 * fabs(l0) * a0, w1 = 0.5 * fabs(l1) * a1, w2 = 0.5 * fabs(l2) * a2;
+
+    double gHi = 0.5 * (b0 * Ui + b1 * (Ui * Ui + 2.0 * HG * Hi) + b2 * Ui * Vi);
+    double gHj = 0.5 * (b0 * Uj + b1 * (Uj * Uj + 2.0 * HG * Hj) + b2 * Uj * Vj);
+    double gUi = 0.5 * b0 * Hi + b1 * Hi * Ui + 0.5 * b2 * Hi * Vi;
+    double gUj = 0.5 * b0 * Hj + b1 * Hj * Uj + 0.5 * b2 * Hj * Vj;
+    double gVi = 0.5 * b2 * Hi * Ui, gVj = 0.5 * b2 * Hj * Uj;
+    const double gw0 = -b0 - b1 * l0 - b2 * vm;
+    const double gw1 = -b2 * cm;
+    const double gw2 = -b0 - b1 * l2 - b2 * vm;
+    double gl0 = -b1 * w0 + gw0 * 0.5 * sgn(l0) * a0;
+    double gl2 = -b1 * w2 + gw2 * 0.5 * sgn(l2) * a2;
+    double gvm = -b2 * (w0 + w2), gcm = -b2 * w1;
+    const double gl1 = gw1 * 0.5 * sgn(l1) * a1;
+    const double ga0 = gw0 * 0.5 * fabs(l0) * rden;  // already divided by den
+    const double ga1 = gw1 * 0.5 * fabs(l1) * rcm;   // already divided by cm
+    const double ga2 = gw2 * 0.5 * fabs(l2) * rden;
+    gl2 += ga0 * dh;
+    double gdh = ga0 * l2 - ga1 * vm - ga2 * l0;
+    double gdhu = ga2 - ga0;
+    const double gdhv = ga1;
+    gvm -= ga1 * dh;
+    gcm -= ga1 * a1 + 2.0 * (ga0 * a0 + ga2 * a2);
+    gl0 -= ga2 * dh;
+    gHj += gdh + gdhu * Uj + gdhv * Vj;
+    gHi -= gdh + gdhu * Ui + gdhv * Vi;
+    gUj += gdhu * Hj; gUi -= gdhu * Hi;
+    gVj += gdhv * Hj; gVi -= gdhv * Hi;
+    double gum = gl1, gci = 0.0, gcj = 0.0;
+    if (fix2) {
+        const double t = gl2 * rD2;
+        const double gl2a = t * e2j;
+        const double ge2i = t * e2j * (l2a - e2j) * rD2;
+        const double ge2j = -t * (l2a - e2i) * e2i * rD2;
+        gUi += ge2i; gci += ge2i; gUj += ge2j; gcj += ge2j;
+        gum += gl2a; gcm += gl2a;
+    } else {
+        gum += gl2; gcm += gl2;
+    }
+    if (fix0) {
+        const double t = gl0 * rD0;
+        const double gl0a = -t * e0i;
+        const double ge0i = t * (e0j - l0a) * e0j * rD0;
+        const double ge0j = t * e0i * (l0a - e0i) * rD0;
+        gUi += ge0i; gci -= ge0i; gUj += ge0j; gcj -= ge0j;
+        gum += gl0a; gcm -= gl0a;
+    } else {
+        gum += gl0; gcm -= gl0;
+    }
+    const double gnu = gum * rs, gnv = gvm * rs, gsden = -(gnu * um + gnv * vm);
+    gUi += gnu * si; gUj += gnu * sj; gVi += gnv * si; gVj += gnv * sj;
+    // s = sqrt(H) and c = sqrt(g) s: d/dH = (gs + sqrt(g) gc) / (2 s)
+    const double gsi = gnu * Ui + gnv * Vi + gsden + C::sqrt_g * gci;
+    const double gsj = gnu * Uj + gnv * Vj + gsden + C::sqrt_g * gcj;
+    if (hmb) {
+        const double ghm = 0.5 * gcm * G * rcm;
+        gHi += 0.5 * ghm; gHj += 0.5 * ghm;
+    }
+    gHi += 0.5 * gsi * rsi;
+    gHj += 0.5 * gsj * rsj;
+    if (wi) { ghi += gHi; gui += gUi; gvi += gVi; }
+    if (wj) { ghj += gHj; guj += gUj; gvj += gVj; }
+}
+
 // Inputs and adjoints of one hydrostatic face: eta, z, u, v of the two cells
 // and the cells' slopes along the normal.
 struct FaceVals {
@@ -171,16 +286,16 @@ struct FaceVals {
 
 // Reverse of the hydrostatic face (HydrostaticRoe.cpp:247-396) for direction
 // DIR, given the adjoints of FL and FR (global frame).  Adds to g.
-template <int DIR>
+template <int DIR, bool FAST>
 __device__ void face_rev(const FaceVals& f, const double gFL[3], const double gFR[3], FaceVals& g) {
-    const bool zLmax = !(f.zL < f.zR);  // std::max(zL, zR) keeps zL on ties
+    const bool zLmax = okey(f.zL) >= okey(f.zR);  // std::max(zL, zR) keeps zL on ties
     const double zf = zLmax ? f.zL : f.zR;
     const double etaLf = f.eL + 0.5 * f.seL, etaRf = f.eR - 0.5 * f.seR;
     const double uLf = f.uL + 0.5 * f.suL, uRf = f.uR - 0.5 * f.suR;
     const double vLf = f.vL + 0.5 * f.svL, vRf = f.vR - 0.5 * f.svR;
     const double dLu = etaLf - f.zL, dRu = etaRf - f.zR, dLs = etaLf - zf, dRs = etaRf - zf;
-    const double hLu = dLu > 0.0 ? dLu : 0.0, hRu = dRu > 0.0 ? dRu : 0.0;
-    const double hLs = dLs > 0.0 ? dLs : 0.0, hRs = dRs > 0.0 ? dRs : 0.0;
+    const double hLu = max0_i(dLu), hRu = max0_i(dRu);
+    const double hLs = max0_i(dLs), hRs = max0_i(dRs);
     // normal frame
     const double unL = DIR == 0 ? uLf : vLf, utL = DIR == 0 ? vLf : -uLf;
     const double unR = DIR == 0 ? uRf : vRf, utR = DIR == 0 ? vRf : -uRf;
@@ -189,16 +304,17 @@ __device__ void face_rev(const FaceVals& f, const double gFL[3], const double gF
     if (DIR == 0) { gpL = gFL[1]; gpR = gFR[1]; b1 = gf1; b2 = gf2; }
     else { gpL = gFL[2]; gpR = gFR[2]; b1 = gf2; b2 = -gf1; }
     double ghLs = 0, gunL = 0, gutL = 0, ghRs = 0, gunR = 0, gutR = 0;
-    roe_rev(hLs, unL, utL, hRs, unR, utR, gf0, b1, b2, ghLs, gunL, gutL, ghRs, gunR, gutR);
+    if constexpr (FAST) roe_rev_fast(hLs, unL, utL, hRs, unR, utR, gf0, b1, b2, ghLs, gunL, gutL, ghRs, gunR, gutR);
+    else roe_rev(hLs, unL, utL, hRs, unR, utR, gf0, b1, b2, ghLs, gunL, gutL, ghRs, gunR, gutR);
     // pressure correction p = HG (hu^2 - hs^2)
     const double ghLu = gpL * 2.0 * HG * hLu, ghRu = gpR * 2.0 * HG * hRu;
     ghLs += -gpL * 2.0 * HG * hLs;
     ghRs += -gpR * 2.0 * HG * hRs;
     double getaL = 0, getaR = 0, gzL = 0, gzR = 0, gzf = 0;
-    if (dLu > 0.0) { getaL += ghLu; gzL -= ghLu; }
-    if (dRu > 0.0) { getaR += ghRu; gzR -= ghRu; }
-    if (dLs > 0.0) { getaL += ghLs; gzf -= ghLs; }
-    if (dRs > 0.0) { getaR += ghRs; gzf -= ghRs; }
+    if (pos_i(dLu)) { getaL += ghLu; gzL -= ghLu; }
+    if (pos_i(dRu)) { getaR += ghRu; gzR -= ghRu; }
+    if (pos_i(dLs)) { getaL += ghLs; gzf -= ghLs; }
+    if (pos_i(dRs)) { getaR += ghRs; gzf -= ghRs; }
     if (zLmax) gzL += gzf; else gzR += gzf;
     double guL, gvL, guR, gvR;
     if (DIR == 0) { guL = gunL; gvL = gutL; guR = gunR; gvR = gutR; }
@@ -218,15 +334,48 @@ __device__ __forceinline__ void slope_rev(double qm, double q, double qp, double
                                           double& gqp) {
     gqm = gq = gqp = 0.0;
     const double dm = q - qm, dp = qp - q;
-    if (fabs(dp) <= T12 || gs == 0.0) return;
-    if (dm == 0.0) {  // r = 0: the mean of the one-sided derivatives (0 and 2), d s / d dm = 1
+    if (abs_le_bits(dp, Cst<double>::tol12_bits) || (sbits(gs) << 1) == 0) return;
+    if ((sbits(dm) << 1) == 0) {  // r = 0: the mean of the one-sided derivatives (0 and 2), d s / d dm = 1
         gq = gs;
         gqm = -gs;
         return;
     }
-    if (!(dm * dp > 0.0)) return;  // phi = 0 for r < 0
-    const double S = dm + dp;
-    const double gdm = gs * 2.0 * dp * dp / (S * S), gdp = gs * 2.0 * dm * dm / (S * S);
+    if (!pos_i(dm * dp)) return;  // phi = 0 for r < 0
+    const double rS = rcp_nr(dm + dp);
+    const double t = 2.0 * gs * rS * rS;
+    const double gdm = t * dp * dp, gdp = t * dm * dm;
+    gq = gdm - gdp;
+    gqm = -gdm;
+    gqp = gdp;
+}
+
+// The fast van Leer slope (van_leer_slope<double, true>, same operations) that
+// also hands back the reciprocal 1 / (dm + dp) its reverse needs.
+__device__ __forceinline__ double vl_slope_rs(double qm, double q, double qp, double& rS) {
+    const double dm = q - qm, dp = qp - q;
+    rS = 0.0;
+    if (abs_le_bits(dp, Cst<double>::tol12_bits)) return 0.0;
+    const double p = dm * dp;
+    if (!pos_i(p)) return 0.0;
+    rS = rcp_nr(dm + dp);
+    return (p + p) * rS;
+}
+
+// slope_rev with the reciprocal from vl_slope_rs (rS == 0: the slope was 0 by a branch).
+__device__ __forceinline__ void slope_rev_rs(double qm, double q, double qp, double rS, double gs, double& gqm,
+                                             double& gq, double& gqp) {
+    gqm = gq = gqp = 0.0;
+    if ((sbits(gs) << 1) == 0) return;
+    const double dm = q - qm, dp = qp - q;
+    if ((sbits(rS) << 1) == 0) {
+        if (!abs_le_bits(dp, Cst<double>::tol12_bits) && (sbits(dm) << 1) == 0) {  // r = 0: d s / d dm = 1
+            gq = gs;
+            gqm = -gs;
+        }
+        return;
+    }
+    const double t = 2.0 * gs * rS * rS;
+    const double gdm = t * dp * dp, gdp = t * dm * dm;
     gq = gdm - gdp;
     gqm = -gdm;
     gqp = gdp;
@@ -242,11 +391,13 @@ struct AdjSmem {
     union {
         struct {  // x pass
             double s[3][ATY][ATX + 4];      // slopes of columns x0-2 .. x0+TX+1
+            double rs[3][ATY][ATX + 4];     // their 1 / (dm + dp) (fast form; 0 where the slope is 0 by a branch)
             double fa[14][ATY][ATX + 3];    // face adjoints, faces x0-1 .. x0+TX+1
             double sp[9][ATY][ATX + 2];     // slope-reverse partials, columns x0-1 .. x0+TX
         } x;
         struct {  // y pass
             double s[3][ATY + 4][ATX];
+            double rs[3][ATY + 4][ATX];
             double fa[14][ATY + 3][ATX];
             double sp[9][ATY + 2][ATX];
         } y;
@@ -261,7 +412,15 @@ struct AdjArgs {
     double* zbar;          // accumulated gradient w.r.t. z
     long long pitch;
     int nx, ny;
-    double cx, cy;  // dt/dx, dt/dy
+    double cx, cy;         // dt/dx, dt/dy
+    double dx, dy, idx, idy, idt;
+    // per block: CFL rate arg max of U^n (rate, cell, flags) and, when un1 is set
+    // (a step without friction or clamp, lambda_lin = lambda^{n+1}), the dt partial
+    // sum_c lambda^{n+1} . (U^{n+1} - U^n) / dt
+    const double* un1[3];
+    double *p_dt, *p_rate;
+    long long* p_idx;
+    unsigned* p_fl;
 };
 
 __device__ __forceinline__ double fget(const FaceVals& f, int k) { return (&f.eL)[k]; }
@@ -282,16 +441,16 @@ __global__ void __launch_bounds__(ANT) k_adj_faces(AdjArgs A) {
         double e = 0, zz = 0, qx = 0, qy = 0, nn = 0;
         const bool in_grown = gi >= -2 && gi <= nx + 1 && gj >= -2 && gj <= ny + 1;
         if (in_grown) A.src.fetch(gi, gj, e, zz, qx, qy, nn);
-        const double hp = e - zz > 0.0 ? e - zz : 0.0;
+        const double hp = max0_i(e - zz);
         S.hp[r][c] = hp;
         S.eta[r][c] = hp + zz;
         if constexpr (FAST) {  // the forward's own velocity arithmetic, so the limiters take its branches
-            const double rh = hp > T12 ? rcp_nr(hp) : 0.0;
+            const double rh = gt_bits(hp, Cst<double>::tol12_bits) ? rcp_nr(hp) : 0.0;
             S.u[r][c] = qx * rh;
             S.v[r][c] = qy * rh;
         } else {
-            S.u[r][c] = hp > T12 ? qx / hp : 0.0;
-            S.v[r][c] = hp > T12 ? qy / hp : 0.0;
+            S.u[r][c] = gt_bits(hp, Cst<double>::tol12_bits) ? qx / hp : 0.0;
+            S.v[r][c] = gt_bits(hp, Cst<double>::tol12_bits) ? qy / hp : 0.0;
         }
         S.z[r][c] = zz;
         S.nod[r][c] = (in_grown && is_nodata(zz)) ? 1 : 0;
@@ -311,9 +470,15 @@ __global__ void __launch_bounds__(ANT) k_adj_faces(AdjArgs A) {
         for (int k = t; k < ATY * (ATX + 4); k += ANT) {  // slopes, columns x0-2 .. x0+TX+1
             const int row = k / (ATX + 4), col = k % (ATX + 4) - 2;
             const int r = row + H3, c = col + H3;
-            P.s[0][row][col + 2] = van_leer_slope<double, FAST>(S.eta[r][c - 1], S.eta[r][c], S.eta[r][c + 1]);
-            P.s[1][row][col + 2] = van_leer_slope<double, FAST>(S.u[r][c - 1], S.u[r][c], S.u[r][c + 1]);
-            P.s[2][row][col + 2] = van_leer_slope<double, FAST>(S.v[r][c - 1], S.v[r][c], S.v[r][c + 1]);
+            if constexpr (FAST) {
+                P.s[0][row][col + 2] = vl_slope_rs(S.eta[r][c - 1], S.eta[r][c], S.eta[r][c + 1], P.rs[0][row][col + 2]);
+                P.s[1][row][col + 2] = vl_slope_rs(S.u[r][c - 1], S.u[r][c], S.u[r][c + 1], P.rs[1][row][col + 2]);
+                P.s[2][row][col + 2] = vl_slope_rs(S.v[r][c - 1], S.v[r][c], S.v[r][c + 1], P.rs[2][row][col + 2]);
+            } else {
+                P.s[0][row][col + 2] = van_leer_slope<double, false>(S.eta[r][c - 1], S.eta[r][c], S.eta[r][c + 1]);
+                P.s[1][row][col + 2] = van_leer_slope<double, false>(S.u[r][c - 1], S.u[r][c], S.u[r][c + 1]);
+                P.s[2][row][col + 2] = van_leer_slope<double, false>(S.v[r][c - 1], S.v[r][c], S.v[r][c + 1]);
+            }
         }
         __syncthreads();
         for (int k = t; k < ATY * (ATX + 3); k += ANT) {  // faces x0-1 .. x0+TX+1
@@ -334,7 +499,7 @@ __global__ void __launch_bounds__(ANT) k_adj_faces(AdjArgs A) {
                     gFL[c] = -A.cx * S.lam[c][r][cl];
                     gFR[c] = A.cx * S.lam[c][r][cr];
                 }
-                face_rev<0>(fv, gFL, gFR, g);
+                face_rev<0, FAST>(fv, gFL, gFR, g);
             }
             for (int q = 0; q < 14; ++q) P.fa[q][row][fcol + 1] = fget(g, q);
         }
@@ -347,7 +512,8 @@ __global__ void __launch_bounds__(ANT) k_adj_faces(AdjArgs A) {
                 const double gs = P.fa[9 + 2 * qi][row][col + 1] + P.fa[8 + 2 * qi][row][col + 2];
                 const double(*Q)[GX] = qi == 0 ? S.eta : (qi == 1 ? S.u : S.v);
                 double gm, g0, gp;
-                slope_rev(Q[r][c - 1], Q[r][c], Q[r][c + 1], gs, gm, g0, gp);
+                if constexpr (FAST) slope_rev_rs(Q[r][c - 1], Q[r][c], Q[r][c + 1], P.rs[qi][row][col + 2], gs, gm, g0, gp);
+                else slope_rev(Q[r][c - 1], Q[r][c], Q[r][c + 1], gs, gm, g0, gp);
                 P.sp[3 * qi + 0][row][col + 1] = gm;  // to column col-1
                 P.sp[3 * qi + 1][row][col + 1] = g0;  // to column col
                 P.sp[3 * qi + 2][row][col + 1] = gp;  // to column col+1
@@ -382,13 +548,13 @@ __global__ void __launch_bounds__(ANT) k_adj_faces(AdjArgs A) {
                     gather_x(row, col, ge, gu, gv, gz);
                     const double hp = S.hp[r][c];
                     double gzt = gz + ge, ghp = ge, ghu = 0, ghv = 0;
-                    if (hp > T12) {
+                    if (gt_bits(hp, Cst<double>::tol12_bits)) {
                         ghu = gu / hp;
                         ghv = gv / hp;
                         ghp -= (gu * S.u[r][c] + gv * S.v[r][c]) / hp;
                     }
                     double geta = 0;
-                    if (hp > 0.0) { geta = ghp; gzt -= ghp; }
+                    if (pos_i(hp)) { geta = ghp; gzt -= ghp; }
                     const int edge = lo ? 0 : nx - 1;
                     const int src = code == 0 ? (lo ? -1 - gi : 2 * nx - 1 - gi) : edge;
                     const double sx = code == 0 ? -1.0 : 1.0;
@@ -413,9 +579,15 @@ __global__ void __launch_bounds__(ANT) k_adj_faces(AdjArgs A) {
         for (int k = t; k < (ATY + 4) * ATX; k += ANT) {  // slopes, rows y0-2 .. y0+TY+1
             const int row = k / ATX - 2, col = k % ATX;
             const int r = row + H3, c = col + H3;
-            P.s[0][row + 2][col] = van_leer_slope<double, FAST>(S.eta[r - 1][c], S.eta[r][c], S.eta[r + 1][c]);
-            P.s[1][row + 2][col] = van_leer_slope<double, FAST>(S.u[r - 1][c], S.u[r][c], S.u[r + 1][c]);
-            P.s[2][row + 2][col] = van_leer_slope<double, FAST>(S.v[r - 1][c], S.v[r][c], S.v[r + 1][c]);
+            if constexpr (FAST) {
+                P.s[0][row + 2][col] = vl_slope_rs(S.eta[r - 1][c], S.eta[r][c], S.eta[r + 1][c], P.rs[0][row + 2][col]);
+                P.s[1][row + 2][col] = vl_slope_rs(S.u[r - 1][c], S.u[r][c], S.u[r + 1][c], P.rs[1][row + 2][col]);
+                P.s[2][row + 2][col] = vl_slope_rs(S.v[r - 1][c], S.v[r][c], S.v[r + 1][c], P.rs[2][row + 2][col]);
+            } else {
+                P.s[0][row + 2][col] = van_leer_slope<double, false>(S.eta[r - 1][c], S.eta[r][c], S.eta[r + 1][c]);
+                P.s[1][row + 2][col] = van_leer_slope<double, false>(S.u[r - 1][c], S.u[r][c], S.u[r + 1][c]);
+                P.s[2][row + 2][col] = van_leer_slope<double, false>(S.v[r - 1][c], S.v[r][c], S.v[r + 1][c]);
+            }
         }
         __syncthreads();
         for (int k = t; k < (ATY + 3) * ATX; k += ANT) {  // faces y0-1 .. y0+TY+1
@@ -435,7 +607,7 @@ __global__ void __launch_bounds__(ANT) k_adj_faces(AdjArgs A) {
                     gFL[q] = -A.cy * S.lam[q][rl][c];
                     gFR[q] = A.cy * S.lam[q][rr][c];
                 }
-                face_rev<1>(fv, gFL, gFR, g);
+                face_rev<1, FAST>(fv, gFL, gFR, g);
             }
             for (int q = 0; q < 14; ++q) P.fa[q][frow + 1][col] = fget(g, q);
         }
@@ -447,7 +619,8 @@ __global__ void __launch_bounds__(ANT) k_adj_faces(AdjArgs A) {
                 const double gs = P.fa[9 + 2 * qi][row + 1][col] + P.fa[8 + 2 * qi][row + 2][col];
                 const double(*Q)[GX] = qi == 0 ? S.eta : (qi == 1 ? S.u : S.v);
                 double gm, g0, gp;
-                slope_rev(Q[r - 1][c], Q[r][c], Q[r + 1][c], gs, gm, g0, gp);
+                if constexpr (FAST) slope_rev_rs(Q[r - 1][c], Q[r][c], Q[r + 1][c], P.rs[qi][row + 2][col], gs, gm, g0, gp);
+                else slope_rev(Q[r - 1][c], Q[r][c], Q[r + 1][c], gs, gm, g0, gp);
                 P.sp[3 * qi + 0][row + 1][col] = gm;
                 P.sp[3 * qi + 1][row + 1][col] = g0;
                 P.sp[3 * qi + 2][row + 1][col] = gp;
@@ -480,13 +653,13 @@ __global__ void __launch_bounds__(ANT) k_adj_faces(AdjArgs A) {
                     gather_y(row, col, ge, gu, gv, gz);
                     const double hp = S.hp[r][c];
                     double gzt = gz + ge, ghp = ge, ghu = 0, ghv = 0;
-                    if (hp > T12) {
+                    if (gt_bits(hp, Cst<double>::tol12_bits)) {
                         ghu = gu / hp;
                         ghv = gv / hp;
                         ghp -= (gu * S.u[r][c] + gv * S.v[r][c]) / hp;
                     }
                     double geta = 0;
-                    if (hp > 0.0) { geta = ghp; gzt -= ghp; }
+                    if (pos_i(hp)) { geta = ghp; gzt -= ghp; }
                     const int edge = lo ? 0 : ny - 1;
                     const int src = code == 0 ? (lo ? -1 - gj : 2 * ny - 1 - gj) : edge;
                     const double sy = code == 0 ? -1.0 : 1.0;
@@ -504,25 +677,65 @@ __global__ void __launch_bounds__(ANT) k_adj_faces(AdjArgs A) {
         __syncthreads();
     }
 
-    // ===================== own cell: rebuild reverse and outputs =====================
+    // ===================== own cell: rebuild reverse, outputs, CFL rate, dt partial =====================
     const int gi = x0 + tx, gj = y0 + ty;
-    if (gi >= nx || gj >= ny) return;
-    const int r = ty + H3, c = tx + H3;
-    const double hp = S.hp[r][c];
-    double gz = az + ae, ghp = ae, ghu = 0, ghv = 0;
-    if (hp > T12) {
-        ghu = au / hp;
-        ghv = av / hp;
-        ghp -= (au * S.u[r][c] + av * S.v[r][c]) / hp;
+    const bool own = gi < nx && gj < ny;
+    double rate = 0.0, dtb = 0.0;
+    long long ridx = 0x7fffffffffffffffll;
+    unsigned rfl = 0;
+    if (own) {
+        const int r = ty + H3, c = tx + H3;
+        const double hp = S.hp[r][c];
+        double gz = az + ae, ghp = ae, ghu = 0, ghv = 0;
+        if (gt_bits(hp, Cst<double>::tol12_bits)) {
+            const double rh = FAST ? rcp_nr(hp) : 1.0 / hp;
+            ghu = au * rh;
+            ghv = av * rh;
+            ghp -= (au * S.u[r][c] + av * S.v[r][c]) * rh;
+        }
+        double gh = 0;
+        if (pos_i(hp)) gh = ghp;  // h' = max(0, (h + z) - z): dh'/dh = 1, dh'/dz = 0
+        const long long o = (long long)gi + (long long)gj * A.pitch;
+        // lambda^n = lambda_lin (the stored state passes through the update) + the flux part + ghost folds
+        A.out[0][o] = S.lam[0][r][c] + gh + S.fold[0][ty][tx];
+        A.out[1][o] = S.lam[1][r][c] + ghu + S.fold[1][ty][tx];
+        A.out[2][o] = S.lam[2][r][c] + ghv + S.fold[2][ty][tx];
+        A.zbar[o] += gz + S.fold[3][ty][tx];
+        const double h = A.src.h[o], hu = A.src.hu[o], hv = A.src.hv[o];
+        double mv;
+        dt_cell_contrib<double, FAST>(h, hu, hv, S.nod[r][c] != 0, A.dx, A.dy, A.idx, A.idy, rate, mv, rfl);
+        if (pos_i(rate)) ridx = o;
+        if (A.un1[0])
+            dtb = (S.lam[0][r][c] * (A.un1[0][o] - h) + S.lam[1][r][c] * (A.un1[1][o] - hu) +
+                   S.lam[2][r][c] * (A.un1[2][o] - hv)) * A.idt;
     }
-    double gh = 0;
-    if (hp > 0.0) gh = ghp;  // h' = max(0, (h + z) - z): dh'/dh = 1, dh'/dz = 0
-    const long long o = (long long)gi + (long long)gj * A.pitch;
-    // lambda^n = lambda_lin (the stored state passes through the update) + the flux part + ghost folds
-    A.out[0][o] = S.lam[0][r][c] + gh + S.fold[0][ty][tx];
-    A.out[1][o] = S.lam[1][r][c] + ghu + S.fold[1][ty][tx];
-    A.out[2][o] = S.lam[2][r][c] + ghv + S.fold[2][ty][tx];
-    A.zbar[o] += gz + S.fold[3][ty][tx];
+    // block reductions (every thread takes part)
+    __shared__ double s_sum[ANT / 32], s_rate[ANT / 32];
+    __shared__ long long s_idx[ANT / 32];
+    __shared__ unsigned s_fl[ANT / 32];
+    for (int off = 16; off > 0; off >>= 1) {
+        dtb += __shfl_xor_sync(0xffffffffu, dtb, off);
+        const double r2 = __shfl_xor_sync(0xffffffffu, rate, off);
+        const long long i2 = __shfl_xor_sync(0xffffffffu, ridx, off);
+        if (r2 > rate || (r2 == rate && i2 < ridx)) { rate = r2; ridx = i2; }
+    }
+    rfl = __reduce_or_sync(0xffffffffu, rfl);
+    const int w = t >> 5;
+    if ((t & 31) == 0) { s_sum[w] = dtb; s_rate[w] = rate; s_idx[w] = ridx; s_fl[w] = rfl; }
+    __syncthreads();
+    if (t == 0) {
+        double sum = s_sum[0];
+        for (int k = 1; k < ANT / 32; ++k) {
+            sum += s_sum[k];
+            if (s_rate[k] > rate || (s_rate[k] == rate && s_idx[k] < ridx)) { rate = s_rate[k]; ridx = s_idx[k]; }
+            rfl |= s_fl[k];
+        }
+        const long long b = blockIdx.x + (long long)blockIdx.y * gridDim.x;
+        A.p_rate[b] = rate;
+        A.p_idx[b] = ridx;
+        A.p_fl[b] = rfl;
+        if (A.un1[0]) A.p_dt[b] = sum;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -603,63 +816,6 @@ __global__ void __launch_bounds__(ANT) k_adj_post(PostArgs P) {
     if (threadIdx.x == 0) P.dtbar[blockIdx.x + (long long)blockIdx.y * gridDim.x] = s;
 }
 
-// Kernel A (steps without friction or clamp): lambda_lin = lambda^{n+1}; only
-// the dt adjoint partials sum_c lambda . (U^{n+1} - U^n) / dt are needed.
-__global__ void __launch_bounds__(ANT) k_adj_dtbar_identity(const double* l0, const double* l1, const double* l2,
-                                                             const double* a0, const double* a1, const double* a2,
-                                                             const double* b0, const double* b1, const double* b2,
-                                                             long long pitch, int nx, int ny, double dt,
-                                                             double* dtbar) {
-    __shared__ double sh[ANT / 32];
-    const int i = blockIdx.x * ATX + (threadIdx.x % ATX), j = blockIdx.y * ATY + threadIdx.x / ATX;
-    double dtb = 0;
-    if (i < nx && j < ny) {
-        const long long o = (long long)i + (long long)j * pitch;
-        dtb = (l0[o] * (a0[o] - b0[o]) + l1[o] * (a1[o] - b1[o]) + l2[o] * (a2[o] - b2[o])) / dt;
-    }
-    const double s = block_sum(dtb, sh);
-    if (threadIdx.x == 0) dtbar[blockIdx.x + (long long)blockIdx.y * gridDim.x] = s;
-}
-
-// Per-block largest CFL rate of U^n (exact formula of compute_dt_Impl) and its cell.
-template <bool FAST>
-__global__ void __launch_bounds__(ANT) k_adj_rate_argmax(const double* h, const double* hu, const double* hv,
-                                                          const double* z, long long pitch, int nx, int ny, double dx,
-                                                          double dy, double* prate, long long* pidx, unsigned* pflags) {
-    __shared__ double sr[ANT / 32];
-    __shared__ long long si[ANT / 32];
-    __shared__ unsigned sf[ANT / 32];
-    const int i = blockIdx.x * ATX + (threadIdx.x % ATX), j = blockIdx.y * ATY + threadIdx.x / ATX;
-    double rate = 0;
-    long long idx = 0x7fffffffffffffffll;
-    unsigned fl = 0;
-    if (i < nx && j < ny) {
-        const long long o = (long long)i + (long long)j * pitch;
-        double mv;
-        dt_cell_contrib<double, FAST>(h[o], hu[o], hv[o], is_nodata(z[o]), dx, dy, 1.0 / dx, 1.0 / dy, rate, mv, fl);
-        if (rate > 0) idx = o;
-    }
-    for (int off = 16; off > 0; off >>= 1) {
-        const double r2 = __shfl_xor_sync(0xffffffffu, rate, off);
-        const long long i2 = __shfl_xor_sync(0xffffffffu, idx, off);
-        if (r2 > rate || (r2 == rate && i2 < idx)) { rate = r2; idx = i2; }
-    }
-    fl = __reduce_or_sync(0xffffffffu, fl);
-    const int w = threadIdx.x >> 5;
-    if ((threadIdx.x & 31) == 0) { sr[w] = rate; si[w] = idx; sf[w] = fl; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int k = 1; k < ANT / 32; ++k) {
-            if (sr[k] > rate || (sr[k] == rate && si[k] < idx)) { rate = sr[k]; idx = si[k]; }
-            fl |= sf[k];
-        }
-        const long long b = blockIdx.x + (long long)blockIdx.y * gridDim.x;
-        prate[b] = rate;
-        pidx[b] = idx;
-        pflags[b] = fl;
-    }
-}
-
 // Kernel C: dt adjoint into the cell that set the CFL bound, then the gauge
 // misfit of state n (seed * 2 (h - href)).  One block.
 __global__ void __launch_bounds__(ANT) k_adj_finish(int nblocks, const double* dtbar_p, const double* prate,
@@ -669,9 +825,9 @@ __global__ void __launch_bounds__(ANT) k_adj_finish(int nblocks, const double* d
                                                      int with_dt, int ngauges, const long long* gauges,
                                                      const double* href, double seed) {
     __shared__ double sh[ANT / 32];
-    __shared__ double s_rate[ANT];
-    __shared__ long long s_idx[ANT];
-    __shared__ unsigned s_fl[ANT];
+    __shared__ double s_rate[ANT / 32];
+    __shared__ long long s_idx[ANT / 32];
+    __shared__ unsigned s_fl[ANT / 32];
     double d = 0, rate = 0;
     long long idx = 0x7fffffffffffffffll;
     unsigned fl = 0;
@@ -683,12 +839,20 @@ __global__ void __launch_bounds__(ANT) k_adj_finish(int nblocks, const double* d
         }
     }
     const double dtbar = block_sum(d, sh);
-    s_rate[threadIdx.x] = rate;
-    s_idx[threadIdx.x] = idx;
-    s_fl[threadIdx.x] = fl;
+    for (int o = 16; o > 0; o >>= 1) {  // arg max: the larger rate, then the lower cell offset
+        const double r2 = __shfl_xor_sync(0xffffffffu, rate, o);
+        const long long i2 = __shfl_xor_sync(0xffffffffu, idx, o);
+        if (r2 > rate || (r2 == rate && i2 < idx)) { rate = r2; idx = i2; }
+    }
+    fl = __reduce_or_sync(0xffffffffu, fl);
+    if ((threadIdx.x & 31) == 0) {
+        s_rate[threadIdx.x >> 5] = rate;
+        s_idx[threadIdx.x >> 5] = idx;
+        s_fl[threadIdx.x >> 5] = fl;
+    }
     __syncthreads();
     if (threadIdx.x == 0 && with_dt) {
-        for (int k = 1; k < ANT; ++k) {
+        for (int k = 1; k < ANT / 32; ++k) {
             if (s_rate[k] > rate || (s_rate[k] == rate && s_idx[k] < idx)) { rate = s_rate[k]; idx = s_idx[k]; }
             fl |= s_fl[k];
         }
@@ -704,16 +868,14 @@ __global__ void __launch_bounds__(ANT) k_adj_finish(int nblocks, const double* d
         }
     }
     __syncthreads();
-    for (int k = threadIdx.x; k < ngauges; k += ANT) {
+    for (int k = threadIdx.x; k < ngauges; k += ANT) {  // atomic: a cell may be listed twice
         const long long gcell = gauges[k];
-        lam_h[gcell] += seed * 2.0 * (h[gcell] - href[k]);
+        atomicAdd(&lam_h[gcell], seed * 2.0 * (h[gcell] - href[k]));
     }
 }
 
-// Records the dt the step used (cfl * min bound of the chain) and the gauges.
-__global__ void k_adj_record(const DtAccum* slot, double cfl, double* dt_out, const double* h, int ngauges,
-                             const long long* gauges, double* series) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) *dt_out = accum_dt_min<double>(slot->rate_bits, slot->flags) * cfl;
+// h of the final state at the gauge cells.
+__global__ void k_adj_series(const double* h, int ngauges, const long long* gauges, double* series) {
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < ngauges; k += gridDim.x * blockDim.x)
         series[k] = h[gauges[k]];
 }
@@ -728,7 +890,7 @@ namespace {
 struct AdjLayout {
     size_t plane;                 // doubles per plane (ny * pitch)
     int nslots, seg;              // stored states, segment length (0: every state stored)
-    size_t states, segbuf, lam, lamlin, lin, tmp, dthist, pflags, slots, status, part, total;
+    size_t states, segbuf, segbuf_stride, lam, lamlin, lin, tmp, dthist, pflags, slots, status, part, total;
     int nblocks;
 };
 
@@ -742,7 +904,8 @@ AdjLayout adj_layout(int nx, int ny, long long pitch, int nsteps, int every) {
     L.nslots = L.seg ? (nsteps / L.seg + 1) : (nsteps + 1);
     size_t o = 0;
     L.states = o; o += al256((size_t)L.nslots * st);
-    L.segbuf = o; o += L.seg ? al256((size_t)(L.seg + 1) * st) : 0;
+    L.segbuf_stride = L.seg ? al256((size_t)(L.seg + 1) * st) : 0;
+    L.segbuf = o; o += L.seg ? 2 * al256((size_t)(L.seg + 1) * st) : 0;  // two segments in flight
     L.tmp = o; o += L.seg ? al256(2 * st) : 0;
     L.lam = o; o += al256(2 * st);
     L.lamlin = o; o += al256(st);
@@ -768,7 +931,7 @@ int adj_check(const hx_level_f64* L, int nsteps, int ngauges, const int64_t* gau
     if (L->nx < 2 || L->ny < 2 || L->pitch < L->nx || !(L->dx > 0) || !(L->dy > 0))
         return set_error(HX_ERR_ARG, "adjoint: bad level geometry");
     if (L->nx % ATX == 1 || L->ny % ATY == 1)
-        return set_error(HX_ERR_ARG, "adjoint: nx % 32 == 1 or ny % 8 == 1 is not supported (a one-cell edge tile)");
+        return set_error(HX_ERR_ARG, "adjoint: nx % 32 == 1 or ny % 16 == 1 is not supported (a one-cell edge tile)");
     if (nsteps < 1) return set_error(HX_ERR_ARG, "adjoint: nsteps < 1");
     if (ngauges < 0 || (ngauges > 0 && !gauges)) return set_error(HX_ERR_ARG, "adjoint: bad gauges");
     if (ngauges > 0) {  // gauge offsets i + j * pitch must name cells of the level
@@ -794,7 +957,7 @@ LevelSrc<double> make_src(const hx_level_f64* L, const double* const* st, int g)
 
 template <bool FAST>
 cudaError_t forward_step(const hx_level_f64* L, double* const* in, double* const* out, StepCtl<double> ctl,
-                         const double* dt_fixed, unsigned* pflags, cudaStream_t st) {
+                         const double* dt_fixed, unsigned* pflags, const AdjRecord& rec, cudaStream_t st) {
     const IBox vb{0, 0, L->nx - 1, L->ny - 1};
     const double* cin[3] = {in[0], in[1], in[2]};
     LevelSrc<double> src = make_src(L, cin, 2);
@@ -805,7 +968,7 @@ cudaError_t forward_step(const hx_level_f64* L, double* const* in, double* const
     for (int k = 0; k < 3; ++k) o.p[k] = out[k];
     o.js = L->pitch; o.lo0 = 0; o.lo1 = 0;
     Plane<double> np{L->n, L->pitch, 0, 0};
-    return launch_adj_forward<FAST>(src, uo, np, o, vb, ctl, dt_fixed, pflags, st);
+    return launch_adj_forward<FAST>(src, uo, np, o, vb, ctl, dt_fixed, pflags, rec, st);
 }
 
 // The flux update of U^n alone (before friction and clamp) into lin.
@@ -869,13 +1032,16 @@ int adjoint_forward(const hx_level_f64* L, int nsteps, double cfl, int ngauges, 
         ctl.dt_host = 0.0; ctl.cfl = cfl;
         ctl.dt_in = &slot[n % 3]; ctl.dt_out = &slot[(n + 1) % 3]; ctl.dt_reset = &slot[(n + 2) % 3];
         ctl.status = stw; ctl.time = nullptr; ctl.dx = L->dx; ctl.dy = L->dy;
-        e = forward_step<FAST>(L, in, out, ctl, nullptr, &pfl[n], st);
-        if (e == cudaSuccess) {
-            k_adj_record<<<1, 64, 0, st>>>(&slot[n % 3], cfl, &dth[n], out[0], ngauges, (const long long*)gauges,
-                                           series ? series + (size_t)n * ngauges : nullptr);
+        AdjRecord rec{&dth[n], (series && n >= 1) ? series + (size_t)(n - 1) * ngauges : nullptr,
+                      (const long long*)gauges, ngauges};
+        e = forward_step<FAST>(L, in, out, ctl, nullptr, &pfl[n], rec, st);
+        if (e == cudaSuccess && n == nsteps - 1 && series && ngauges > 0) {  // gauges of the final state
+            k_adj_series<<<1, 64, 0, st>>>(out[0], ngauges, (const long long*)gauges,
+                                           series + (size_t)n * ngauges);
             e = cudaGetLastError();
+            ++launches;
         }
-        launches += 2;
+        ++launches;
         if (e == cudaSuccess && A.seg && (n + 1) % A.seg == 0) {
             double* ck = V.state(A.states, (n + 1) / A.seg);
             e = cudaMemcpyAsync(ck, b, 3 * pb, cudaMemcpyDeviceToDevice, st);
@@ -885,6 +1051,51 @@ int adjoint_forward(const hx_level_f64* L, int nsteps, double cfl, int ngauges, 
     note_launches(launches);
     return HX_OK;
 }
+
+// Faces-kernel arguments for the reverse of step n (U^n at Un; un1 = U^{n+1}
+// when lambda_lin = lambda^{n+1}, else null).
+AdjArgs faces_args(const hx_level_f64* L, const AdjLayout& A, char* base, const double* Un, const double* un1,
+                   const double* lam, double* out, double* zbar, double dt) {
+    AdjArgs B;
+    const double* cin[3] = {Un, Un + A.plane, Un + 2 * A.plane};
+    B.src = make_src(L, cin, 2);
+    for (int k = 0; k < 3; ++k) {
+        B.lam[k] = lam + k * A.plane;
+        B.out[k] = out + k * A.plane;
+        B.un1[k] = un1 ? un1 + k * A.plane : nullptr;
+    }
+    B.zbar = zbar; B.pitch = L->pitch; B.nx = L->nx; B.ny = L->ny;
+    B.cx = dt / L->dx; B.cy = dt / L->dy;
+    B.dx = L->dx; B.dy = L->dy; B.idx = 1.0 / L->dx; B.idy = 1.0 / L->dy; B.idt = 1.0 / dt;
+    B.p_dt = reinterpret_cast<double*>(base + A.part);
+    B.p_rate = B.p_dt + A.nblocks;
+    B.p_idx = reinterpret_cast<long long*>(B.p_rate + A.nblocks);
+    B.p_fl = reinterpret_cast<unsigned*>(B.p_idx + A.nblocks);
+    return B;
+}
+
+// A second stream and its events, released when the reverse sweep returns
+// (destruction is deferred by the runtime until queued work completes).
+struct SideStream {
+    cudaStream_t s = nullptr;
+    cudaEvent_t rec[2] = {nullptr, nullptr}, freed[2] = {nullptr, nullptr}, start = nullptr;
+    cudaError_t init() {
+        cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+        for (int k = 0; k < 2 && e == cudaSuccess; ++k) e = cudaEventCreateWithFlags(&rec[k], cudaEventDisableTiming);
+        for (int k = 0; k < 2 && e == cudaSuccess; ++k)
+            e = cudaEventCreateWithFlags(&freed[k], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&start, cudaEventDisableTiming);
+        return e;
+    }
+    ~SideStream() {
+        for (int k = 0; k < 2; ++k) {
+            if (rec[k]) cudaEventDestroy(rec[k]);
+            if (freed[k]) cudaEventDestroy(freed[k]);
+        }
+        if (start) cudaEventDestroy(start);
+        if (s) cudaStreamDestroy(s);
+    }
+};
 
 template <bool FAST>
 int adjoint_reverse(const hx_level_f64* L, int nsteps, double cfl, int ngauges, const int64_t* gauges,
@@ -896,10 +1107,7 @@ int adjoint_reverse(const hx_level_f64* L, int nsteps, double cfl, int ngauges, 
     const size_t pb = A.plane * sizeof(double);
     double* dth = reinterpret_cast<double*>(base + A.dthist);
     unsigned* pfl = reinterpret_cast<unsigned*>(base + A.pflags);
-    double* p_dt = reinterpret_cast<double*>(base + A.part);
-    double* p_rate = p_dt + A.nblocks;
-    long long* p_idx = reinterpret_cast<long long*>(p_rate + A.nblocks);
-    unsigned* p_fl = reinterpret_cast<unsigned*>(p_idx + A.nblocks);
+    const AdjArgs P0 = faces_args(L, A, base, V.state(A.states, 0), nullptr, grad_h, grad_h, grad_z, 1.0);
     const long long* gcells = reinterpret_cast<const long long*>(gauges);
 
     std::vector<double> dt_host((size_t)nsteps);
@@ -912,6 +1120,10 @@ int adjoint_reverse(const hx_level_f64* L, int nsteps, double cfl, int ngauges, 
     if (e == cudaSuccess) e = cudaMemsetAsync(lamb[0], 0, 3 * pb, st);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_adj_faces<FAST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(AdjSmem));
+    SideStream side;
+    if (e == cudaSuccess && A.seg) e = side.init();
+    if (e == cudaSuccess && A.seg) e = cudaEventRecord(side.start, st);
+    if (e == cudaSuccess && A.seg) e = cudaStreamWaitEvent(side.s, side.start, 0);
     if (e != cudaSuccess) return set_error(HX_ERR_CUDA, cudaGetErrorString(e));
     int cur = 0;  // lamb[cur] holds lambda^{n+1}
     const IBox vb{0, 0, L->nx - 1, L->ny - 1};
@@ -920,46 +1132,62 @@ int adjoint_reverse(const hx_level_f64* L, int nsteps, double cfl, int ngauges, 
 
     auto finish = [&](int n, const double* Un, double* lam, int with_dt) {
         const double* series_ref = n >= 1 ? href + (size_t)(n - 1) * ngauges : nullptr;
-        k_adj_finish<<<1, ANT, 0, st>>>(A.nblocks, p_dt, p_rate, p_idx, p_fl, cfl, L->dx, L->dy, Un, Un + A.plane,
-                                        Un + 2 * A.plane, lam, lam + A.plane, lam + 2 * A.plane, with_dt,
+        k_adj_finish<<<1, ANT, 0, st>>>(A.nblocks, P0.p_dt, P0.p_rate, P0.p_idx, P0.p_fl, cfl, L->dx, L->dy, Un,
+                                        Un + A.plane, Un + 2 * A.plane, lam, lam + A.plane, lam + 2 * A.plane, with_dt,
                                         n >= 1 ? ngauges : 0, gcells, series_ref, seed);
         ++launches;
         return cudaGetLastError();
     };
-    auto state_at = [&](int n, int seg0) -> double* {
-        if (!A.seg) return V.state(A.states, n);
-        return V.state(A.segbuf, n - seg0);
-    };
-    // reverse over segments (one segment of all steps when every state is stored)
     const int L_seg = A.seg ? A.seg : nsteps;
     const int nseg = (nsteps + L_seg - 1) / L_seg;
+    auto segstate = [&](int sg, int k) { return V.state(A.segbuf + (size_t)(sg & 1) * A.segbuf_stride, k); };
+    auto state_at = [&](int sg, int n) -> double* {
+        if (!A.seg) return V.state(A.states, n);
+        return segstate(sg, n - sg * L_seg);
+    };
+    // Recompute segment sg's states from its checkpoint with the recorded dt, on the side stream, into the
+    // segment buffer of its parity; the reverse of segment sg + 1 runs meanwhile on st.
+    auto recompute = [&](int sg) -> cudaError_t {
+        const int n0 = sg * L_seg, n1 = (n0 + L_seg < nsteps) ? n0 + L_seg : nsteps;
+        cudaError_t r = cudaMemcpyAsync(segstate(sg, 0), V.state(A.states, sg), 3 * pb, cudaMemcpyDeviceToDevice,
+                                        side.s);
+        for (int n = n0; n < n1 && r == cudaSuccess; ++n) {
+            double* a = segstate(sg, n - n0);
+            double* b = segstate(sg, n - n0 + 1);
+            double *in[3], *out[3];
+            for (int k = 0; k < 3; ++k) { in[k] = a + k * A.plane; out[k] = b + k * A.plane; }
+            StepCtl<double> ctl{};
+            ctl.dx = L->dx; ctl.dy = L->dy;
+            r = forward_step<FAST>(L, in, out, ctl, &dth[n], nullptr, AdjRecord{}, side.s);
+            ++launches;
+        }
+        if (r == cudaSuccess) r = cudaEventRecord(side.rec[sg & 1], side.s);
+        return r;
+    };
+    if (A.seg) e = recompute(nseg - 1);
     bool first = true;
     for (int sg = nseg - 1; sg >= 0 && e == cudaSuccess; --sg) {
         const int n0 = sg * L_seg, n1 = (n0 + L_seg < nsteps) ? n0 + L_seg : nsteps;
-        if (A.seg) {  // recompute the segment's states from its checkpoint with the recorded dt
-            e = cudaMemcpyAsync(V.state(A.segbuf, 0), V.state(A.states, sg), 3 * pb, cudaMemcpyDeviceToDevice, st);
-            for (int n = n0; n < n1 && e == cudaSuccess; ++n) {
-                double* a = V.state(A.segbuf, n - n0);
-                double* b = V.state(A.segbuf, n - n0 + 1);
-                double *in[3], *out[3];
-                for (int k = 0; k < 3; ++k) { in[k] = a + k * A.plane; out[k] = b + k * A.plane; }
-                StepCtl<double> ctl{};
-                ctl.dx = L->dx; ctl.dy = L->dy;
-                e = forward_step<FAST>(L, in, out, ctl, &dth[n], nullptr, st);
-                ++launches;
+        if (A.seg) {
+            e = cudaStreamWaitEvent(st, side.rec[sg & 1], 0);
+            if (e == cudaSuccess && sg >= 1) {  // the buffer of segment sg - 1 was last read by segment sg + 1
+                if (sg + 1 < nseg) e = cudaStreamWaitEvent(side.s, side.freed[(sg + 1) & 1], 0);
+                if (e == cudaSuccess) e = recompute(sg - 1);
             }
+            if (e != cudaSuccess) break;
         }
-        if (first && e == cudaSuccess) {  // lambda^N: the misfit of the final state
-            e = finish(nsteps, state_at(nsteps, n0), lamb[cur], 0);
+        if (first) {  // lambda^N: the misfit of the final state
+            e = finish(nsteps, state_at(sg, nsteps), lamb[cur], 0);
             first = false;
         }
         for (int n = n1 - 1; n >= n0 && e == cudaSuccess; --n) {
-            double* Un = state_at(n, n0);
-            double* Un1 = state_at(n + 1, n0);
+            double* Un = state_at(sg, n);
+            double* Un1 = state_at(sg, n + 1);
             const double dt = dt_host[(size_t)n];
             double* lam1 = lamb[cur];
             double* lam0 = lamb[cur ^ 1];
             const double* lam_for_faces = lam1;
+            const double* un1 = Un1;
             if (pf_host[(size_t)n]) {  // friction or dry clamp in this step: reverse the post map
                 double* lin = V.state(A.lin, 0);
                 double* ll = V.state(A.lamlin, 0);
@@ -969,40 +1197,29 @@ int adjoint_reverse(const hx_level_f64* L, int nsteps, double cfl, int ngauges, 
                     P.lin[k] = lin + k * A.plane; P.un[k] = Un + k * A.plane; P.lam[k] = lam1 + k * A.plane;
                     P.out[k] = ll + k * A.plane;
                 }
-                P.nman = L->n; P.dtbar = p_dt; P.pitch = L->pitch; P.nx = L->nx; P.ny = L->ny; P.dt = dt;
+                P.nman = L->n; P.dtbar = P0.p_dt; P.pitch = L->pitch; P.nx = L->nx; P.ny = L->ny; P.dt = dt;
                 k_adj_post<<<grid, ANT, 0, st>>>(P);
                 launches += 2;
                 lam_for_faces = ll;
-            } else {
-                k_adj_dtbar_identity<<<grid, ANT, 0, st>>>(lam1, lam1 + A.plane, lam1 + 2 * A.plane, Un1,
-                                                           Un1 + A.plane, Un1 + 2 * A.plane, Un, Un + A.plane,
-                                                           Un + 2 * A.plane, L->pitch, L->nx, L->ny, dt, p_dt);
-                ++launches;
+                un1 = nullptr;  // the post kernel wrote the dt partials
             }
-            {
-                const double* cin[3] = {Un, Un + A.plane, Un + 2 * A.plane};
-                AdjArgs B;
-                B.src = make_src(L, cin, 2);
-                for (int k = 0; k < 3; ++k) {
-                    B.lam[k] = lam_for_faces + k * A.plane;
-                    B.out[k] = lam0 + k * A.plane;
-                }
-                B.zbar = grad_z; B.pitch = L->pitch; B.nx = L->nx; B.ny = L->ny;
-                B.cx = dt / L->dx; B.cy = dt / L->dy;
-                k_adj_faces<FAST><<<grid, ANT, sizeof(AdjSmem), st>>>(B);
-                k_adj_rate_argmax<FAST><<<grid, ANT, 0, st>>>(Un, Un + A.plane, Un + 2 * A.plane, L->z, L->pitch,
-                                                              L->nx, L->ny, L->dx, L->dy, p_rate, p_idx, p_fl);
-                launches += 2;
-            }
+            const AdjArgs B = faces_args(L, A, base, Un, un1, lam_for_faces, lam0, grad_z, dt);
+            k_adj_faces<FAST><<<grid, ANT, sizeof(AdjSmem), st>>>(B);
+            ++launches;
             if (e == cudaSuccess) e = cudaGetLastError();
             if (e == cudaSuccess) e = finish(n, Un, lam0, 1);
             cur ^= 1;
         }
+        if (A.seg && e == cudaSuccess) e = cudaEventRecord(side.freed[sg & 1], st);
     }
     if (e == cudaSuccess) {
         double* g[3] = {grad_h, grad_hu, grad_hv};
         for (int k = 0; k < 3 && e == cudaSuccess; ++k)
             e = cudaMemcpyAsync(g[k], lamb[cur] + k * A.plane, pb, cudaMemcpyDeviceToDevice, st);
+    }
+    if (e != cudaSuccess && A.seg) {  // nothing may still run on the side stream when the buffers go back
+        cudaStreamSynchronize(side.s);
+        cudaStreamSynchronize(st);
     }
     note_launches(launches);
     if (e != cudaSuccess) return set_error(HX_ERR_LAUNCH, cudaGetErrorString(e));
@@ -1039,12 +1256,8 @@ int adjoint_step(const hx_level_f64* L, double dt, const double* const* lam, dou
     }
     P.nman = L->n; P.dtbar = p_dt; P.pitch = L->pitch; P.nx = L->nx; P.ny = L->ny; P.dt = dt;
     k_adj_post<<<grid, ANT, 0, st>>>(P);
-    AdjArgs B;
-    const double* cin[3] = {un, un + A.plane, un + 2 * A.plane};
-    B.src = make_src(L, cin, 2);
-    for (int k = 0; k < 3; ++k) { B.lam[k] = ll + k * A.plane; B.out[k] = outs[k]; }
-    B.zbar = zbar; B.pitch = L->pitch; B.nx = L->nx; B.ny = L->ny;
-    B.cx = dt / L->dx; B.cy = dt / L->dy;
+    AdjArgs B = faces_args(L, A, base, un, nullptr, ll, ll, zbar, dt);  // outputs replaced below
+    for (int k = 0; k < 3; ++k) B.out[k] = outs[k];
     k_adj_faces<FAST><<<grid, ANT, sizeof(AdjSmem), st>>>(B);
     e = cudaGetLastError();
     if (e == cudaSuccess) {  // dtbar = sum of the per-block partials

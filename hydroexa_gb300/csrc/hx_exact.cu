@@ -31,7 +31,7 @@ template cudaError_t launch_ensemble<double, false>(const EnsInstance<double>*, 
 template int ensemble_blocks_per_sm<double, false>();
 template cudaError_t launch_adj_forward<false>(const LevelSrc<double>&, const Cells3<double>&, const Plane<double>&,
                                               const Cells3W<double>&, const IBox&, const StepCtl<double>&,
-                                              const double*, unsigned*, cudaStream_t);
+                                              const double*, unsigned*, const AdjRecord&, cudaStream_t);
 template cudaError_t launch_adj_forward_linear<false>(const LevelSrc<double>&, const Cells3<double>&,
                                                      const Plane<double>&, const Cells3W<double>&, const IBox&, double,
                                                      double, const double*, cudaStream_t);

@@ -26,7 +26,7 @@ template cudaError_t launch_ensemble<double, true>(const EnsInstance<double>*, i
 template int ensemble_blocks_per_sm<double, true>();
 template cudaError_t launch_adj_forward<true>(const LevelSrc<double>&, const Cells3<double>&, const Plane<double>&,
                                               const Cells3W<double>&, const IBox&, const StepCtl<double>&,
-                                              const double*, unsigned*, cudaStream_t);
+                                              const double*, unsigned*, const AdjRecord&, cudaStream_t);
 template cudaError_t launch_adj_forward_linear<true>(const LevelSrc<double>&, const Cells3<double>&,
                                                      const Plane<double>&, const Cells3W<double>&, const IBox&, double,
                                                      double, const double*, cudaStream_t);

@@ -202,6 +202,15 @@ template <class R> struct StepCtl {
     R dx, dy;
 };
 
+// What a forward step of the adjoint's sweep records: the dt it used and h of
+// its input state at the gauge cells (null pointers: nothing).
+struct AdjRecord {
+    double* dt;
+    double* series;
+    const long long* gauges;
+    int ngauges;
+};
+
 // One member of a batched ensemble (device memory, one per instance).
 template <class R> struct EnsInstance {
     R* st[2][3];          // state planes (h, hu, hv) for the two parities

@@ -628,7 +628,7 @@ namespace hx {
 template <bool FAST>
 __global__ void __launch_bounds__(NT) k_adj_forward(LevelSrc<double> src, Cells3<double> uo, Plane<double> np,
                                                      Cells3W<double> out, IBox vb, StepCtl<double> ctl,
-                                                     const double* dt_fixed, unsigned* post_flags) {
+                                                     const double* dt_fixed, unsigned* post_flags, AdjRecord rec) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     HydroSmem<double>& S = *reinterpret_cast<HydroSmem<double>*>(smem_raw);
     double dt;
@@ -637,6 +637,11 @@ __global__ void __launch_bounds__(NT) k_adj_forward(LevelSrc<double> src, Cells3
     } else {
         if (!resolve_dt(ctl, dt)) return;
         step_bookkeeping(ctl, dt);
+    }
+    if (blockIdx.x == 0 && blockIdx.y == 0) {  // the step's dt and the gauges of its input state
+        if (rec.dt && threadIdx.x == 0) *rec.dt = dt;
+        if (rec.series)
+            for (int k = threadIdx.x; k < rec.ngauges; k += blockDim.x) rec.series[k] = uo.p[0][rec.gauges[k]];
     }
     FaceOut<double> fo{};
     fo.on = 0;
@@ -724,11 +729,11 @@ cudaError_t launch_dt_reduce(const Cells3<R>& U, const Plane<R>& Z, const IBox& 
 template <bool FAST>
 cudaError_t launch_adj_forward(const LevelSrc<double>& src, const Cells3<double>& uo, const Plane<double>& np,
                                const Cells3W<double>& out, const IBox& vb, const StepCtl<double>& ctl,
-                               const double* dt_fixed, unsigned* post_flags, cudaStream_t st) {
+                               const double* dt_fixed, unsigned* post_flags, const AdjRecord& rec, cudaStream_t st) {
     const size_t sm = sizeof(HydroSmem<double>);
     cudaError_t e = ensure_smem(k_adj_forward<FAST>, sm);
     if (e != cudaSuccess) return e;
-    k_adj_forward<FAST><<<tile_grid(vb, TX, TY), NT, sm, st>>>(src, uo, np, out, vb, ctl, dt_fixed, post_flags);
+    k_adj_forward<FAST><<<tile_grid(vb, TX, TY), NT, sm, st>>>(src, uo, np, out, vb, ctl, dt_fixed, post_flags, rec);
     return cudaGetLastError();
 }
 

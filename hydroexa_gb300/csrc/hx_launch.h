@@ -44,7 +44,7 @@ template <class R, bool FAST> int ensemble_blocks_per_sm();
 template <bool FAST>
 cudaError_t launch_adj_forward(const LevelSrc<double>& src, const Cells3<double>& uo, const Plane<double>& np,
                                const Cells3W<double>& out, const IBox& vb, const StepCtl<double>& ctl,
-                               const double* dt_fixed, unsigned* post_flags, cudaStream_t st);
+                               const double* dt_fixed, unsigned* post_flags, const AdjRecord& rec, cudaStream_t st);
 // The flux update alone at *dt_fixed (the state before friction and clamp).
 template <bool FAST>
 cudaError_t launch_adj_forward_linear(const LevelSrc<double>& src, const Cells3<double>& uo, const Plane<double>& np,

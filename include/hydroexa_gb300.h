@@ -368,7 +368,7 @@ int hx_level_run_static_f64(int method, hx_level_f64* level, int nsteps, double 
  * it takes the same branches.  HX_ARITH_EXACT runs the trajectory of
  * hx_level_run_f64 with HX_ARITH_EXACT bit for bit (and of the tangent-linear
  * step's value part).
- * Restriction: nx % 32 != 1 and ny % 8 != 1.
+ * Restriction: nx % 32 != 1 and ny % 16 != 1.
  */
 int64_t hx_adjoint_work_bytes_f64(int nx, int ny, int64_t pitch, int nsteps, int checkpoint_every);
 int hx_adjoint_forward_f64(const hx_level_f64* level, int nsteps, double cfl, int ngauges, const int64_t* gauge_cells,

@@ -1,6 +1,6 @@
 """CUDA level advance, dt reduction and time loop against the oracle.
 
-Tolerances (BASELINE): conserved state within 1e-12 relative per step.  The
+Tolerances: conserved state within 1e-12 relative per step.  The
 exact arithmetic form is held to equality with the oracle (no friction) or
 1e-14 (friction: cbrt may differ by an ulp); the fast form to 1e-12 per step.
 FP32 is compared with the oracle instantiated in float at 1e-5.
