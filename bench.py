@@ -37,9 +37,10 @@ UNIT = "Mcell-updates/s"
 PEAKS = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
 HBM_GBS = float(PEAKS.get("hbm_gbs", 6800.0))
 HBM_SRC = "measured" if "hbm_gbs" in PEAKS else "fallback"
-# FP64 issue roof: measured DFMA rate of this machine's GB300 (0.597 T inst/s,
-# 1.19 TFLOP/s; profiles/fp64_pipe_probe.md)
+# FP64 issue roof: the DFMA rate is measured on the GPU at the start of the run
+# (hx_measure_fp64_rate); this GB300 figure (0.597 T inst/s) is the fallback.
 FP64_DFMA_PER_S = 0.597e12
+FP64_SRC = "GB300 figure measured earlier (fallback)"
 BYTES_PER_CELL = {"f64": 64, "f32": 32}  # read h hu hv z n, write h hu hv
 NX = NY = 8192
 
@@ -185,6 +186,8 @@ def main():
     ap.add_argument("--precision", default="f64", choices=["f64", "f32"])
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--ensemble-count", type=int, default=256, help="ensemble members (default 256)")
+    ap.add_argument("--adjoint-steps", type=int, default=2000, help="adjoint run length (default 2000)")
     ap.add_argument("--method", default="hydrostatic", choices=["hydrostatic", "roe"])
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -198,7 +201,7 @@ def main():
 
     import hydroexa_gb300
     from hydroexa_gb300 import capi
-    from hydroexa_gb300.level import Level
+    from hydroexa_gb300.level import DtAccum, Level
 
     ws, rank, local = dist_env()
     torch.cuda.set_device(local)
@@ -208,6 +211,9 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=dev)
     hydroexa_gb300.build()
+    global FP64_DFMA_PER_S, FP64_SRC
+    FP64_DFMA_PER_S = capi.fp64_rates()[0]
+    FP64_SRC = "measured in this run (hx_measure_fp64_rate)"
     arith = capi.HX_ARITH_FAST if args.arith == "fast" else capi.HX_ARITH_EXACT
     case = make_case(NX, NY)
     cells = NX * NY
@@ -253,9 +259,10 @@ def main():
     acc_out = torch.empty_like(lev.state)
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * 5)]
     dt = 0.5 * lev.compute_dt()[0] * case.cfl
+    nxt = DtAccum(dev)  # the loop's kernel: the next step's CFL bound folded in
     for k in range(5):
         ev[2 * k].record(stream)
-        lev.advance(method, dt, out=acc_out, arith=arith)
+        lev.advance(method, dt, out=acc_out, next_dt=nxt, arith=arith)
         ev[2 * k + 1].record(stream)
     torch.cuda.synchronize(dev)
     kms = statistics.mean(ev[2 * k].elapsed_time(ev[2 * k + 1]) for k in range(5))
@@ -302,12 +309,12 @@ def main():
     if args.precision == "f64" and args.method == "hydrostatic" and not args.no_ensemble:
         del lev
         torch.cuda.empty_cache()
-        ens = ensemble_measure(dev)
+        ens = ensemble_measure(dev, count=args.ensemble_count)
 
     adj = None
     if args.precision == "f64" and args.method == "hydrostatic" and not args.no_adjoint:
         torch.cuda.empty_cache()
-        adj = adjoint_measure(dev)
+        adj = adjoint_measure(dev, nsteps=args.adjoint_steps)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -345,7 +352,7 @@ def main():
     return 0
 
 
-def ensemble_measure(dev, steps=24, warmup=6, plain_steps=6):
+def ensemble_measure(dev, steps=24, warmup=6, plain_steps=6, count=256):
     """256 independent dam breaks, sides log-uniform in
     [64, 1024].  Batched (one persistent launch per step, CUDA graph, tile shape
     per size class from the autotuner) against the members advanced one after
@@ -357,7 +364,7 @@ def ensemble_measure(dev, steps=24, warmup=6, plain_steps=6):
     from hydroexa_gb300 import capi, workloads
     from hydroexa_gb300.ensemble import SHAPE_NAMES, Ensemble, autotune
 
-    cases = workloads.ensemble(count=256, seed=4)
+    cases = workloads.ensemble(count=count, seed=4)
     cells = sum(c.cells for c in cases)
     cfl = cases[0].cfl
     per_class, report = autotune(cases, device=dev, steps=6)
@@ -389,8 +396,8 @@ def ensemble_measure(dev, steps=24, warmup=6, plain_steps=6):
     v_b = cells * steps / t_b / 1e6
     v_m = cells * steps / t_m / 1e6
     v_p = cells * plain_steps / t_p / 1e6
-    return {"workload": "256 independent FP64 dam breaks (hydrostatic-Roe), sides log-uniform in [64,1024] (seed 4), "
-                        "%d cells, %d timed steps per member (sample of the 500-step runs)" % (cells, steps),
+    return {"workload": "%d independent FP64 dam breaks (hydrostatic-Roe), sides log-uniform in [64,1024] (seed 4), "
+                        "%d cells, %d timed steps per member (sample of the 500-step runs)" % (count, cells, steps),
             "batched": v_b, "member_loop": v_m, "plain_loop_host_dt": v_p, "unit": UNIT,
             "speedup_vs_member_loop": v_b / v_m, "speedup_vs_plain_loop": v_b / v_p,
             "batched_launches": launches,
@@ -468,6 +475,16 @@ def adjoint_measure(dev, nsteps=2000, every=45, fd_eps=1e-6):
     fd = fd_check(prob, [z, h0, zero, zero], href, grads, (("z", 0, 7), ("h0", 1, 8)), g.nx, g.ny)
     store_all = capi.lib().hx_adjoint_work_bytes_f64(g.nx, g.ny, g.nx, nsteps, 0)
     del prob
+    # binomial checkpointing with 20 snapshot slots: the same gradient in a fifth of the memory
+    slots = 20
+    pb = GaugeProblem(g, zero.clone(), gauges, nsteps, case.cfl, checkpoint_every=-slots)
+    pb.forward(z, h0, zero, zero)
+    t_rev_b, gb = timed(lambda: pb.reverse(href))
+    binomial = {"slots": slots, "work_bytes": pb.work_bytes, "reverse_s": t_rev_b,
+                "cost_vs_forward": (t_fwd + t_rev_b) / t_plain,
+                "recompute_steps": int(capi.lib().hx_adjoint_recompute_steps(nsteps, -slots)),
+                "equal_to_checkpointed": all(bool(torch.equal(a, b)) for a, b in zip(gb, grads))}
+    del pb
     # the exact arithmetic form: the reverse sweep against the N-step tangent-linear model of the same trajectory
     pe = GaugeProblem(g, zero.clone(), gauges, nsteps, case.cfl, checkpoint_every=every, arith=capi.HX_ARITH_EXACT)
     pe.forward(z, h0, zero, zero)
@@ -483,7 +500,7 @@ def adjoint_measure(dev, nsteps=2000, every=45, fd_eps=1e-6):
     del pe
     # the same bed and gauges from a state with no quiescent region, over growing horizons
     scan = []
-    for hsteps in (30, 100, 300):
+    for hsteps in [h for h in (30, 100, 300) if h <= nsteps]:
         sc, sg = workloads.adjoint_smooth_case(nsteps=hsteps)
         base = [T(sc.z), T(sc.h), T(sc.hu), T(sc.hv)]
         sp = GaugeProblem(g, zero.clone(), sg, hsteps, sc.cfl, checkpoint_every=every)
@@ -500,6 +517,7 @@ def adjoint_measure(dev, nsteps=2000, every=45, fd_eps=1e-6):
             "cost_vs_forward": (t_fwd + t_rev) / t_plain, "reverse_vs_forward": t_rev / t_plain,
             "reverse_launches": rev_launches,
             "work_bytes_checkpointed": prob_bytes, "work_bytes_store_all": int(store_all),
+            "binomial": binomial,
             "tangent_check": tangent,
             "fd_check": fd,
             "fd_check_note": "the initial state is a lake at rest outside the hump: limiters there sit on their "
@@ -527,11 +545,12 @@ def fp64_pipe(profile, kms):
     measured DFMA issue rate (the binding roof of the FP64 advance)."""
     inst = profile.get("fp64_inst_per_cell")
     if not inst:
-        return {"peak_dfma_per_s": FP64_DFMA_PER_S, "achieved": None, "frac": None}
+        return {"peak_dfma_per_s": FP64_DFMA_PER_S, "peak_source": FP64_SRC, "achieved": None, "frac": None}
     cells = NX * NY
     rate = inst * cells / (kms * 1e-3)
-    return {"peak_dfma_per_s": FP64_DFMA_PER_S, "achieved_inst_per_s": rate, "frac": rate / FP64_DFMA_PER_S,
-            "inst_per_cell": inst, "source": "ncu smsp__inst_executed_pipe_fp64 per cell (profiles/)"}
+    return {"peak_dfma_per_s": FP64_DFMA_PER_S, "peak_source": FP64_SRC, "achieved_inst_per_s": rate,
+            "frac": rate / FP64_DFMA_PER_S, "inst_per_cell": inst,
+            "source": "FP64 instructions per cell from the ncu capture in profiles/"}
 
 
 if __name__ == "__main__":

@@ -1,6 +1,6 @@
 """Build the CUDA library ``hydroexa_gb300/libhydroexa_gb300.so`` for sm_103a.
 
-Six translation units compiled in parallel, then linked:
+Seven translation units compiled in parallel, then linked:
 
 * ``hx_exact.cu``  -- exact arithmetic form, ``--fmad=false`` (no multiply-add
   contraction, the reference's host rounding); tags and restriction kernels.
@@ -9,6 +9,7 @@ Six translation units compiled in parallel, then linked:
 * ``hx_noalloc.cu`` -- the allocation-free time loop (scratch in a static device array).
 * ``hx_ensemble.cu`` -- the batched-ensemble plan, dt initialisation and CUDA-graph replay.
 * ``hx_adjoint.cu`` -- the hand-written adjoint of the hydrostatic-Roe time loop and its drivers.
+* ``hx_roofs.cu`` -- the FP64 issue-rate probe (the roof the FP64-bound kernels are reported against).
 
 The build is in-tree (objects in ``_build/``), takes well under a minute, and
 needs only nvcc; the CUDA runtime is linked statically so the library loads
@@ -37,6 +38,7 @@ UNITS = {
     "hx_noalloc": [],
     "hx_ensemble": [],
     "hx_adjoint": [],
+    "hx_roofs": [],
 }
 
 

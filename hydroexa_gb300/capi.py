@@ -42,6 +42,7 @@ def _array4(real):
 Array4F64 = _array4(c_double)
 Array4F32 = _array4(c_float)
 Array4I8 = _array4(ctypes.c_byte)
+Array4I32 = _array4(c_int32)
 
 
 class Box(Structure):
@@ -96,6 +97,11 @@ def _declare(L):
                                                                    c_void_p, c_void_p, c_int, c_void_p]
         getattr(L, f"hx_advance_box_roe_{sfx}").argtypes = [P4, P4, P4, P4, Box, real, real, real, P4, P4, P4,
                                                            c_void_p, c_void_p, c_int, c_void_p]
+        getattr(L, f"hx_advance_box_hydrostatic_reflux_{sfx}").argtypes = [P4, P4, P4, P4, P4, Box, real, real, real,
+                                                                          P4, c_void_p, c_void_p, c_int, c_void_p]
+        getattr(L, f"hx_advance_box_roe_reflux_{sfx}").argtypes = [P4, P4, P4, P4, Box, real, real, real,
+                                                                  POINTER(Array4I32), Box, P4, P4, c_void_p, c_void_p,
+                                                                  c_int, c_void_p]
         getattr(L, f"hx_dt_reduce_box_{sfx}").argtypes = [P4, P4, Box, real, real, c_void_p, c_void_p]
         getattr(L, f"hx_tag_box_{sfx}").argtypes = [c_int, P4, P4, POINTER(Array4I8), Box, real, real, real, real,
                                                    real, real, ctypes.c_byte, c_void_p]
@@ -121,8 +127,20 @@ def _declare(L):
     L.hx_ensemble_tiles.argtypes = [c_int, POINTER(EnsembleMemberF64), POINTER(c_int64)]
     L.hx_ensemble_run_f64.argtypes = [c_int, POINTER(EnsembleMemberF64), c_int, c_double, c_void_p, c_void_p,
                                       c_void_p, c_int, c_int, POINTER(c_int), c_void_p]
+    L.hx_derive_eta_box_f64.argtypes = [POINTER(Array4F64), POINTER(Array4F64), POINTER(Array4F64), Box, c_void_p]
+    L.hx_derive_eta_box_f32.argtypes = [POINTER(Array4F32), POINTER(Array4F32), POINTER(Array4F32), Box, c_void_p]
+    L.hx_diagnostics_work_bytes.restype = c_int64
+    L.hx_diagnostics_work_bytes.argtypes = [Box]
+    L.hx_diagnostics_box_f64.argtypes = [POINTER(Array4F64), POINTER(Array4F64), Box, c_double, c_double, c_void_p,
+                                         c_void_p, c_void_p]
+    L.hx_diagnostics_box_f32.argtypes = [POINTER(Array4F32), POINTER(Array4F32), Box, c_float, c_float, c_void_p,
+                                         c_void_p, c_void_p]
+    L.hx_level_diagnostics_f64.argtypes = [POINTER(LevelF64), c_void_p, c_void_p, c_void_p]
+    L.hx_measure_fp64_rate.argtypes = [POINTER(c_double), POINTER(c_double), c_void_p]
     L.hx_adjoint_work_bytes_f64.restype = c_int64
     L.hx_adjoint_work_bytes_f64.argtypes = [c_int, c_int, c_int64, c_int, c_int]
+    L.hx_adjoint_recompute_steps.restype = c_int64
+    L.hx_adjoint_recompute_steps.argtypes = [c_int, c_int]
     L.hx_adjoint_forward_f64.argtypes = [POINTER(LevelF64), c_int, c_double, c_int, c_void_p, c_void_p, c_int,
                                          c_int, c_void_p, c_void_p, c_void_p]
     L.hx_adjoint_reverse_f64.argtypes = [POINTER(LevelF64), c_int, c_double, c_int, c_void_p, c_void_p, c_double,
@@ -143,6 +161,13 @@ def check(rc: int, what: str = "") -> int:
     return rc
 
 
+def fp64_rates() -> tuple:
+    """(DFMA, FFMA) thread instructions per second measured on the current GPU."""
+    d, f = c_double(), c_double()
+    check(lib().hx_measure_fp64_rate(ctypes.byref(d), ctypes.byref(f), None), "hx_measure_fp64_rate")
+    return d.value, f.value
+
+
 def version() -> str:
     return lib().hx_version().decode()
 
@@ -156,13 +181,16 @@ EXPORTED = [
     "hx_version", "hx_last_error", "hx_launch_count", "hx_status_clear", "hx_status_read", "hx_dt_accum_bytes",
     "hx_dt_accum_reset", "hx_dt_accum_read_f64", "hx_dt_accum_read_f32",
     "hx_advance_box_hydrostatic_f64", "hx_advance_box_hydrostatic_f32", "hx_advance_box_roe_f64",
-    "hx_advance_box_roe_f32", "hx_dt_reduce_box_f64", "hx_dt_reduce_box_f32", "hx_tag_box_f64", "hx_tag_box_f32",
-    "hx_masked_average_down_box_f64", "hx_masked_average_down_box_f32", "hx_level_advance_f64",
+    "hx_advance_box_roe_f32", "hx_advance_box_hydrostatic_reflux_f64", "hx_advance_box_hydrostatic_reflux_f32",
+    "hx_advance_box_roe_reflux_f64", "hx_advance_box_roe_reflux_f32", "hx_dt_reduce_box_f64", "hx_dt_reduce_box_f32", "hx_tag_box_f64", "hx_tag_box_f32",
+    "hx_masked_average_down_box_f64", "hx_masked_average_down_box_f32", "hx_derive_eta_box_f64",
+    "hx_derive_eta_box_f32", "hx_diagnostics_work_bytes", "hx_diagnostics_box_f64", "hx_diagnostics_box_f32",
+    "hx_level_diagnostics_f64", "hx_measure_fp64_rate", "hx_level_advance_f64",
     "hx_level_advance_f32", "hx_level_dt_reduce_f64", "hx_level_dt_reduce_f32", "hx_level_run_work_bytes",
     "hx_level_run_f64", "hx_level_run_f32", "hx_level_run_host_f64", "hx_host_cache_release",
     "hx_debug_roe_points_f64", "hx_debug_roe_points_f32", "hx_level_run_static_f64",
     "hx_ensemble_work_bytes", "hx_ensemble_tiles", "hx_ensemble_run_f64",
-    "hx_adjoint_work_bytes_f64", "hx_adjoint_forward_f64", "hx_adjoint_reverse_f64", "hx_adjoint_step_f64",
+    "hx_adjoint_work_bytes_f64", "hx_adjoint_recompute_steps", "hx_adjoint_forward_f64", "hx_adjoint_reverse_f64", "hx_adjoint_step_f64",
     "hx_level_tangent_f64",
 ]
 HX_STATIC_RUN_MAX_CELLS = 262144

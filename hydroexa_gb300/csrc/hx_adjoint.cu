@@ -21,6 +21,7 @@
 //      flows into the cell that set the CFL bound; then the gauge misfit of
 //      state n is injected.
 #include <cstdio>
+#include <functional>
 #include <vector>
 
 #include "hx_kernels.cuh"
@@ -889,24 +890,97 @@ namespace {
 
 struct AdjLayout {
     size_t plane;                 // doubles per plane (ny * pitch)
-    int nslots, seg;              // stored states, segment length (0: every state stored)
-    size_t states, segbuf, segbuf_stride, lam, lamlin, lin, tmp, dthist, pflags, slots, status, part, total;
+    int nslots, seg, binom;       // stored states; segment length (uniform); snapshot slots (binomial)
+    size_t states, segbuf, segbuf_stride, lam, lamlin, lin, tmp, nxt, dthist, pflags, slots, status, part, total;
     int nblocks;
 };
 
 size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
 
+// ---------------------------------------------------------------------------
+// Binomial checkpointing (Griewank's revolve schedule).  With c snapshot slots
+// (one of them holding the state the reversal starts from) and r repetitions,
+// beta(c, r) = C(c + r, c) steps can be reversed; the least number of forward
+// steps to reverse n steps, the first sweep included, is
+// t(n, c) = r n - beta(c + 1, r - 1) with r the least repetition number such
+// that beta(c, r) >= n (Griewank and Walther, ACM TOMS 26(1), 2000).  Each
+// split is chosen among the break points of the piecewise-linear cost
+// k + t(n - k, c - 1) + t(k, c), which attains that optimum.
+// ---------------------------------------------------------------------------
+long long binom_beta(int c, int r) {
+    if (c < 0 || r < 0) return 0;
+    unsigned long long v = 1;  // C(c + r, r) built as prod (c + i) / i, integral at every step
+    for (int i = 1; i <= r; ++i) {
+        const unsigned long long f = (unsigned long long)(c + i);
+        if (v > (1ull << 62) / f) return 1ll << 62;
+        v = v * f / (unsigned long long)i;
+    }
+    return (long long)v;
+}
+
+int binom_reps(long long n, int c) {
+    int r = 0;
+    while (binom_beta(c, r) < n) ++r;
+    return r;
+}
+
+long long binom_cost(long long n, int c) {
+    if (n <= 1) return 0;
+    if (c <= 1) return n * (n - 1) / 2;
+    const int r = binom_reps(n, c);
+    return (long long)r * n - binom_beta(c + 1, r - 1);
+}
+
+// Steps to advance before the next snapshot, reversing n >= 2 steps with c >= 2 slots.
+long long binom_split(long long n, int c) {
+    const int r = binom_reps(n, c);
+    long long lo = n - binom_beta(c - 1, r), hi = binom_beta(c, r - 1);
+    if (lo < 1) lo = 1;
+    if (hi > n - 1) hi = n - 1;
+    long long best_k = lo, best = -1;
+    auto consider = [&](long long k) {
+        if (k < lo || k > hi) return;
+        const long long v = k + binom_cost(n - k, c - 1) + binom_cost(k, c);
+        if (best < 0 || v < best || (v == best && k < best_k)) { best = v; best_k = k; }
+    };
+    consider(lo);
+    consider(hi);
+    for (int j = 0; j <= r + 1; ++j) {
+        const long long b1 = binom_beta(c, j), b2 = binom_beta(c - 1, j);
+        consider(b1); consider(b1 + 1); consider(n - b2); consider(n - b2 - 1);
+    }
+    return best_k;
+}
+
+// Snapshot positions the forward sweep stores (the schedule's first descent),
+// in the order the slots 1, 2, ... are taken.
+std::vector<long long> binom_chain(long long n, int c) {
+    std::vector<long long> pos;
+    long long a = 0;
+    while (n > 1 && c > 1) {
+        const long long k = binom_split(n, c);
+        a += k;
+        pos.push_back(a);
+        n -= k;
+        --c;
+    }
+    return pos;
+}
+
 AdjLayout adj_layout(int nx, int ny, long long pitch, int nsteps, int every) {
     AdjLayout L{};
     L.plane = (size_t)ny * (size_t)pitch;
     const size_t st = 3 * L.plane * sizeof(double);
+    L.binom = every < 0 ? (-every < nsteps + 1 ? -every : nsteps + 1) : 0;
+    if (L.binom == 1) L.binom = 2;  // the state the reversal starts from plus at least one snapshot
     L.seg = (every > 0 && every < nsteps) ? every : 0;
-    L.nslots = L.seg ? (nsteps / L.seg + 1) : (nsteps + 1);
+    L.nslots = L.binom ? L.binom : (L.seg ? (nsteps / L.seg + 1) : (nsteps + 1));
     size_t o = 0;
     L.states = o; o += al256((size_t)L.nslots * st);
     L.segbuf_stride = L.seg ? al256((size_t)(L.seg + 1) * st) : 0;
     L.segbuf = o; o += L.seg ? 2 * al256((size_t)(L.seg + 1) * st) : 0;  // two segments in flight
-    L.tmp = o; o += L.seg ? al256(2 * st) : 0;
+    L.tmp = o; o += L.seg ? al256(2 * st) : (L.binom ? al256(3 * st) : 0);
+    L.nxt = o; o += L.binom ? al256(st) : 0;
     L.lam = o; o += al256(2 * st);
     L.lamlin = o; o += al256(st);
     L.lin = o; o += al256(st);
@@ -1016,11 +1090,14 @@ int adjoint_forward(const hx_level_f64* L, int nsteps, double cfl, int ngauges, 
         if (e != cudaSuccess) return set_error(HX_ERR_LAUNCH, cudaGetErrorString(e));
     }
     int launches = 1;
+    // binomial: the schedule's first snapshots, taken as the sweep passes them (slot k + 1 for chain[k])
+    const std::vector<long long> chain = A.binom ? binom_chain(nsteps, A.binom) : std::vector<long long>();
+    size_t next_snap = 0;
     for (int n = 0; n < nsteps; ++n) {
         double *in[3], *out[3];
         double* a;
         double* b;
-        if (!A.seg) {
+        if (!A.seg && !A.binom) {
             a = V.state(A.states, n);
             b = V.state(A.states, n + 1);
         } else {
@@ -1045,6 +1122,14 @@ int adjoint_forward(const hx_level_f64* L, int nsteps, double cfl, int ngauges, 
         if (e == cudaSuccess && A.seg && (n + 1) % A.seg == 0) {
             double* ck = V.state(A.states, (n + 1) / A.seg);
             e = cudaMemcpyAsync(ck, b, 3 * pb, cudaMemcpyDeviceToDevice, st);
+        }
+        if (e == cudaSuccess && A.binom) {
+            if (next_snap < chain.size() && chain[next_snap] == n + 1) {
+                e = cudaMemcpyAsync(V.state(A.states, (int)next_snap + 1), b, 3 * pb, cudaMemcpyDeviceToDevice, st);
+                ++next_snap;
+            }
+            if (e == cudaSuccess && n == nsteps - 1)  // U^N: the reverse sweep starts from it
+                e = cudaMemcpyAsync(V.state(A.nxt, 0), b, 3 * pb, cudaMemcpyDeviceToDevice, st);
         }
         if (e != cudaSuccess) return set_error(HX_ERR_LAUNCH, cudaGetErrorString(e));
     }
@@ -1097,11 +1182,146 @@ struct SideStream {
     }
 };
 
+// Reverse sweep under the binomial schedule.  Snapshot slots hold states;
+// U^{n+1} of the step being reversed is kept in the nxt buffer (it was the
+// state of the step reversed just before), so every reverse step uses the
+// same kernels as with all states stored.
+template <bool FAST>
+int adjoint_reverse_binomial(const hx_level_f64* L, int nsteps, double cfl, int ngauges, const int64_t* gauges,
+                             const double* href, double seed, void* work, const AdjLayout& A, double* const* grad,
+                             double* grad_z, cudaStream_t st) {
+    Views V{static_cast<double*>(work), A.plane};
+    char* base = static_cast<char*>(work);
+    const size_t pb = A.plane * sizeof(double);
+    double* dth = reinterpret_cast<double*>(base + A.dthist);
+    unsigned* pfl = reinterpret_cast<unsigned*>(base + A.pflags);
+    const AdjArgs P0 = faces_args(L, A, base, V.state(A.states, 0), nullptr, grad_z, grad_z, grad_z, 1.0);
+    const long long* gcells = reinterpret_cast<const long long*>(gauges);
+    std::vector<unsigned> pf_host((size_t)nsteps);
+    std::vector<double> dt_host((size_t)nsteps);
+    cudaError_t e = cudaMemcpyAsync(dt_host.data(), dth, nsteps * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(pf_host.data(), pfl, nsteps * sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(grad_z, 0, pb, st);
+    double* lamb[2] = {V.state(A.lam, 0), V.state(A.lam, 1)};
+    if (e == cudaSuccess) e = cudaMemsetAsync(lamb[0], 0, 3 * pb, st);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_adj_faces<FAST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(AdjSmem));
+    if (e != cudaSuccess) return set_error(HX_ERR_CUDA, cudaGetErrorString(e));
+    const IBox vb{0, 0, L->nx - 1, L->ny - 1};
+    const dim3 grid = tile_grid(vb, ATX, ATY);
+    double* nxt = V.state(A.nxt, 0);
+    double* tmp[3] = {V.state(A.tmp, 0), V.state(A.tmp, 1), V.state(A.tmp, 2)};
+    int cur = 0, launches = 0;
+
+    auto finish = [&](int n, const double* Un, double* lam, int with_dt) {
+        const double* series_ref = n >= 1 ? href + (size_t)(n - 1) * ngauges : nullptr;
+        k_adj_finish<<<1, ANT, 0, st>>>(A.nblocks, P0.p_dt, P0.p_rate, P0.p_idx, P0.p_fl, cfl, L->dx, L->dy, Un,
+                                        Un + A.plane, Un + 2 * A.plane, lam, lam + A.plane, lam + 2 * A.plane, with_dt,
+                                        n >= 1 ? ngauges : 0, gcells, series_ref, seed);
+        ++launches;
+        return cudaGetLastError();
+    };
+    // forward from state a (in src) to state m into dst, with the recorded dt
+    auto advance = [&](long long a, const double* src, long long m, double* dst) -> cudaError_t {
+        cudaError_t r = cudaSuccess;
+        const double* from = src;
+        for (long long n = a; n < m && r == cudaSuccess; ++n) {
+            double* to = (n == m - 1) ? dst : tmp[(n - a) & 1];
+            double *in[3], *out[3];
+            for (int k = 0; k < 3; ++k) {
+                in[k] = const_cast<double*>(from) + k * A.plane;
+                out[k] = to + k * A.plane;
+            }
+            StepCtl<double> ctl{};
+            ctl.dx = L->dx; ctl.dy = L->dy;
+            r = forward_step<FAST>(L, in, out, ctl, &dth[n], nullptr, AdjRecord{}, st);
+            ++launches;
+            from = to;
+        }
+        return r;
+    };
+    // reverse step j from U^j (in Uj) and U^{j+1} (in nxt); then U^j becomes the next step's U^{j+1}
+    auto leaf = [&](long long j, const double* Uj) -> cudaError_t {
+        const double dt = dt_host[(size_t)j];
+        double* lam1 = lamb[cur];
+        double* lam0 = lamb[cur ^ 1];
+        const double* lam_for_faces = lam1;
+        const double* un1 = nxt;
+        cudaError_t r = cudaSuccess;
+        if (pf_host[(size_t)j]) {
+            double* lin = V.state(A.lin, 0);
+            double* ll = V.state(A.lamlin, 0);
+            r = linear_step<FAST>(L, Uj, A.plane, lin, &dth[j], st);
+            PostArgs P;
+            for (int k = 0; k < 3; ++k) {
+                P.lin[k] = lin + k * A.plane; P.un[k] = Uj + k * A.plane; P.lam[k] = lam1 + k * A.plane;
+                P.out[k] = ll + k * A.plane;
+            }
+            P.nman = L->n; P.dtbar = P0.p_dt; P.pitch = L->pitch; P.nx = L->nx; P.ny = L->ny; P.dt = dt;
+            k_adj_post<<<grid, ANT, 0, st>>>(P);
+            launches += 2;
+            lam_for_faces = ll;
+            un1 = nullptr;
+        }
+        const AdjArgs B = faces_args(L, A, base, Uj, un1, lam_for_faces, lam0, grad_z, dt);
+        k_adj_faces<FAST><<<grid, ANT, sizeof(AdjSmem), st>>>(B);
+        ++launches;
+        if (r == cudaSuccess) r = cudaGetLastError();
+        if (r == cudaSuccess) r = finish((int)j, Uj, lam0, 1);
+        if (r == cudaSuccess && j > 0) r = cudaMemcpyAsync(nxt, Uj, 3 * pb, cudaMemcpyDeviceToDevice, st);
+        cur ^= 1;
+        return r;
+    };
+    // slots: 0 holds U^0; the forward sweep left chain[k] in slot k + 1
+    std::vector<long long> slot_pos((size_t)A.binom, -1);
+    slot_pos[0] = 0;
+    const std::vector<long long> chain = binom_chain(nsteps, A.binom);
+    for (size_t k = 0; k < chain.size(); ++k) slot_pos[k + 1] = chain[k];
+    std::vector<int> pool;  // free slots, taken from the back
+    for (int k = A.binom - 1; k >= 1; --k) pool.push_back(k);
+    std::function<cudaError_t(long long, long long, int)> rev = [&](long long a, long long b, int slot_a) {
+        const double* Ua = V.state(A.states, slot_a);
+        if (b - a == 1) return leaf(a, Ua);
+        if (pool.empty()) {  // no free slot: recompute each state from U^a
+            for (long long j = b - 1; j >= a; --j) {
+                cudaError_t r = j == a ? cudaSuccess : advance(a, Ua, j, tmp[2]);
+                if (r == cudaSuccess) r = leaf(j, j == a ? Ua : tmp[2]);
+                if (r != cudaSuccess) return r;
+            }
+            return cudaSuccess;
+        }
+        const long long m = a + binom_split(b - a, (int)pool.size() + 1);
+        const int slot_m = pool.back();
+        pool.pop_back();
+        cudaError_t r = cudaSuccess;
+        if (slot_pos[(size_t)slot_m] != m) {
+            r = advance(a, Ua, m, V.state(A.states, slot_m));
+            slot_pos[(size_t)slot_m] = m;
+        }
+        if (r == cudaSuccess) r = rev(m, b, slot_m);
+        pool.push_back(slot_m);
+        if (r == cudaSuccess) r = rev(a, m, slot_a);
+        return r;
+    };
+    e = finish(nsteps, nxt, lamb[cur], 0);  // lambda^N: the misfit of the final state
+    if (e == cudaSuccess) e = rev(0, nsteps, 0);
+    for (int k = 0; k < 3 && e == cudaSuccess; ++k)
+        e = cudaMemcpyAsync(grad[k], lamb[cur] + k * A.plane, pb, cudaMemcpyDeviceToDevice, st);
+    note_launches(launches);
+    if (e != cudaSuccess) return set_error(HX_ERR_LAUNCH, cudaGetErrorString(e));
+    return HX_OK;
+}
+
 template <bool FAST>
 int adjoint_reverse(const hx_level_f64* L, int nsteps, double cfl, int ngauges, const int64_t* gauges,
                     const double* href, double seed, int checkpoint_every, void* work, double* grad_h, double* grad_hu,
                     double* grad_hv, double* grad_z, cudaStream_t st) {
     const AdjLayout A = adj_layout(L->nx, L->ny, L->pitch, nsteps, checkpoint_every);
+    if (A.binom) {
+        double* grad[3] = {grad_h, grad_hu, grad_hv};
+        return adjoint_reverse_binomial<FAST>(L, nsteps, cfl, ngauges, gauges, href, seed, work, A, grad, grad_z, st);
+    }
     Views V{static_cast<double*>(work), A.plane};
     char* base = static_cast<char*>(work);
     const size_t pb = A.plane * sizeof(double);
@@ -1277,6 +1497,16 @@ int adjoint_step(const hx_level_f64* L, double dt, const double* const* lam, dou
 bool arith_ok(int arith) { return arith == HX_ARITH_EXACT || arith == HX_ARITH_FAST; }
 
 }  // namespace
+
+extern "C" int64_t hx_adjoint_recompute_steps(int nsteps, int checkpoint_every) {
+    if (nsteps < 1) return -1;
+    if (checkpoint_every > 0) return checkpoint_every < nsteps ? nsteps : 0;
+    if (checkpoint_every == 0) return 0;
+    int c = -checkpoint_every < nsteps + 1 ? -checkpoint_every : nsteps + 1;
+    if (c < 2) c = 2;
+    const std::vector<long long> chain = binom_chain(nsteps, c);  // advanced by the forward sweep already
+    return binom_cost(nsteps, c) - (chain.empty() ? 0 : chain.back());
+}
 
 extern "C" int64_t hx_adjoint_work_bytes_f64(int nx, int ny, int64_t pitch, int nsteps, int checkpoint_every) {
     if (nx < 2 || ny < 2 || pitch < nx || nsteps < 1) return 0;

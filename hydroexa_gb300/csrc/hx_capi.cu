@@ -37,6 +37,7 @@ template <class A> struct Elem;
 template <> struct Elem<hx_array4_f64> { using T = double; };
 template <> struct Elem<hx_array4_f32> { using T = float; };
 template <> struct Elem<hx_array4_i8> { using T = signed char; };
+template <> struct Elem<hx_array4_i32> { using T = int; };
 
 template <class A> V4<typename Elem<A>::T> to_v4(const A& a) {
     V4<typename Elem<A>::T> v;
@@ -113,7 +114,8 @@ template <class R> StepCtl<R> host_ctl(R dt, R dx, R dy, hx_dt_accum* next_dt, u
 // ---------------------------------------------------------------- box forms
 template <class R, class A>
 int advance_box_hydro(const A* eta, const A* Ue, const A* Te, const A* Uo, A* Un, hx_box vb, R dt, R dx, R dy,
-                      const A* FL, const A* FR, hx_dt_accum* nd, uint32_t* status, int arith, cudaStream_t st) {
+                      const A* FL, const A* FR, hx_dt_accum* nd, uint32_t* status, int arith, cudaStream_t st,
+                      const A* Fm = nullptr) {
     if (!box_ok(vb)) return HX_ERR_ARG;
     if (!covers(eta, vb, 2, 1, "eta_ext") || !covers(Ue, vb, 2, 3, "U_ext") || !covers(Te, vb, 2, 2, "T_ext") ||
         !covers(Uo, vb, 0, 3, "U_old") || !covers(Un, vb, 0, 3, "U_new"))
@@ -131,6 +133,13 @@ int advance_box_hydro(const A* eta, const A* Ue, const A* Te, const A* Uo, A* Un
         for (int d = 0; d < 2; ++d) { fo.FL[d] = to_v4(FL[d]); fo.FR[d] = to_v4(FR[d]); }
         fo.on = 1;
     }
+    if (Fm) {
+        hx_box bx{{vb.lo[0], vb.lo[1]}, {vb.hi[0] + 1, vb.hi[1]}};
+        hx_box by{{vb.lo[0], vb.lo[1]}, {vb.hi[0], vb.hi[1] + 1}};
+        if (!covers(&Fm[0], bx, 0, 3, "Freg[x]") || !covers(&Fm[1], by, 0, 3, "Freg[y]")) return HX_ERR_ARG;
+        for (int d = 0; d < 2; ++d) fo.Fm[d] = to_v4(Fm[d]);
+        fo.mean = 1;
+    }
     BoxSrc<R> src;
     src.eta = to_v4(*eta);
     src.U = to_v4(*Ue);
@@ -145,7 +154,9 @@ int advance_box_hydro(const A* eta, const A* Ue, const A* Te, const A* Uo, A* Un
 
 template <class R, class A>
 int advance_box_roe(const A* eta, A* Uo, const A* T, A* Un, hx_box vb, R dt, R dx, R dy, const A* F, const A* Sm,
-                    const A* Sp, hx_dt_accum* nd, uint32_t* status, int arith, cudaStream_t st) {
+                    const A* Sp, hx_dt_accum* nd, uint32_t* status, int arith, cudaStream_t st,
+                    const hx_array4_i32* mask = nullptr, const hx_box* grid = nullptr, const A* fc = nullptr,
+                    const A* ff = nullptr) {
     if (!box_ok(vb)) return HX_ERR_ARG;
     if (!covers(eta, vb, 1, 1, "eta") || !covers(Uo, vb, 1, 3, "U_old") || !covers(T, vb, 1, 2, "T") ||
         !covers(Un, vb, 0, 3, "U_new"))
@@ -164,6 +175,28 @@ int advance_box_roe(const A* eta, A* Uo, const A* T, A* Un, hx_box vb, R dt, R d
             fo.F[d] = to_v4(F[d]); fo.Sm[d] = to_v4(Sm[d]); fo.Sp[d] = to_v4(Sp[d]);
         }
         fo.on = 1;
+    }
+    if (fc || ff) {
+        hx_box bx{{vb.lo[0], vb.lo[1]}, {vb.hi[0] + 1, vb.hi[1]}};
+        hx_box by{{vb.lo[0], vb.lo[1]}, {vb.hi[0], vb.hi[1] + 1}};
+        if (fc) {
+            if (!mask) return fail(HX_ERR_ARG, "flux_crse needs fine_mask");
+            if (!covers(mask, vb, 1, 1, "fine_mask") || !covers(&fc[0], bx, 0, 3, "flux_crse[x]") ||
+                !covers(&fc[1], by, 0, 3, "flux_crse[y]"))
+                return HX_ERR_ARG;
+            fo.mask = to_v4(*mask);
+            for (int d = 0; d < 2; ++d) fo.fc[d] = to_v4(fc[d]);
+            fo.crse_on = 1;
+        }
+        if (ff) {
+            if (!grid || grid->hi[0] < grid->lo[0] || grid->hi[1] < grid->lo[1])
+                return fail(HX_ERR_ARG, "flux_fine needs the grid box");
+            if (!covers(&ff[0], bx, 0, 3, "flux_fine[x]") || !covers(&ff[1], by, 0, 3, "flux_fine[y]"))
+                return HX_ERR_ARG;
+            fo.grid = ibox(*grid);
+            for (int d = 0; d < 2; ++d) fo.ff[d] = to_v4(ff[d]);
+            fo.fine_on = 1;
+        }
     }
     BoxSrc<R> src;
     src.eta = to_v4(*eta);
@@ -214,6 +247,33 @@ int mavg_box(const A* fine, A* crse, hx_box cb, int scomp, int ccomp, int ncomp,
                     "hx_masked_average_down_box");
 }
 
+template <class R, class A>
+int eta_box(const A* U, const A* T, A* eta, hx_box b, cudaStream_t st) {
+    if (!box_ok(b)) return HX_ERR_ARG;
+    if (!covers(U, b, 0, 1, "U") || !covers(T, b, 0, 1, "terrain") || !covers(eta, b, 0, 1, "eta")) return HX_ERR_ARG;
+    return launched(launch_derive_eta<R>(to_v4(*U), to_v4(*T), to_v4(*eta), ibox(b), st), "hx_derive_eta_box");
+}
+
+template <class R, class A>
+Plane<R> comp_plane(const A* a, int c) {
+    return Plane<R>{a->p + (long long)c * a->nstride, a->jstride, a->lo[0], a->lo[1]};
+}
+
+long long diag_blocks(hx_box b) {
+    return (long long)((b.hi[0] - b.lo[0] + TX) / TX) * (long long)((b.hi[1] - b.lo[1] + TY) / TY);
+}
+
+template <class R, class A>
+int diag_box(const A* U, const A* T, hx_box b, R dx, R dy, double* out, void* work, cudaStream_t st) {
+    if (!box_ok(b)) return HX_ERR_ARG;
+    if (!out || !work) return fail(HX_ERR_ARG, "hx_diagnostics: null output or work");
+    if (!covers(U, b, 0, 3, "U") || !covers(T, b, 0, 2, "terrain")) return HX_ERR_ARG;
+    const R dA = dx * dy;
+    return launched(launch_diagnostics<R>(comp_plane<R>(U, 0), comp_plane<R>(U, 1), comp_plane<R>(U, 2),
+                                          comp_plane<R>(T, 1), ibox(b), dA, static_cast<double*>(work), out, st),
+                    "hx_diagnostics_box");
+}
+
 // ---------------------------------------------------------------- level forms
 template <class L> bool level_ok(const L* lv) {
     if (!lv || !lv->h || !lv->hu || !lv->hv || !lv->z || !lv->n) { fail(HX_ERR_ARG, "level: null plane"); return false; }
@@ -233,9 +293,12 @@ template <class R, class L> LevelSrc<R> level_src(const L* lv, int g) {
     return s;
 }
 
+// One step of the level, or of its rows j0..j1 (the rest of the level is read
+// as halo, nothing outside the rows is written).
 template <class R, class L>
-int level_advance(int method, const L* lv, const StepCtl<R>& ctl, R* ho, R* huo, R* hvo, int arith, cudaStream_t st) {
-    const IBox vb{0, 0, lv->nx - 1, lv->ny - 1};
+int level_advance(int method, const L* lv, const StepCtl<R>& ctl, R* ho, R* huo, R* hvo, int arith, cudaStream_t st,
+                  int j0 = 0, int j1 = -1) {
+    const IBox vb{0, j0, lv->nx - 1, j1 < 0 ? lv->ny - 1 : j1};
     Cells3W<R> out;
     out.p[0] = ho; out.p[1] = huo; out.p[2] = hvo;
     out.js = lv->pitch; out.lo0 = 0; out.lo1 = 0;
@@ -333,10 +396,35 @@ template <class R> int accum_read(const hx_dt_accum* acc, R* dtmin, R* maxvel, c
 }
 
 // ---------------------------------------------------------------- host form
+// Device buffers of the host-buffer entry, kept between calls, and two copy
+// streams (transfers in both directions overlap each other and the step).
+constexpr int kHostBands = 8;
 struct HostCache {
     void* base = nullptr;
     size_t bytes = 0;
-    ~HostCache() { if (base) cudaFree(base); }
+    cudaStream_t cs[2] = {nullptr, nullptr};
+    cudaEvent_t ev[4 + kHostBands] = {};
+    bool streams_ok = false;
+    bool ensure_streams() {
+        if (streams_ok) return true;
+        for (int k = 0; k < 2; ++k)
+            if (cudaStreamCreateWithFlags(&cs[k], cudaStreamNonBlocking) != cudaSuccess) return false;
+        for (auto& e : ev)
+            if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return false;
+        streams_ok = true;
+        return true;
+    }
+    void release() {
+        if (base) cudaFree(base);
+        base = nullptr;
+        bytes = 0;
+        if (streams_ok) {
+            for (auto& e : ev) cudaEventDestroy(e);
+            for (auto& c : cs) cudaStreamDestroy(c);
+        }
+        streams_ok = false;
+    }
+    ~HostCache() { release(); }
 };
 thread_local HostCache g_host;
 
@@ -408,6 +496,40 @@ int hx_advance_box_roe_f32(const hx_array4_f32* eta, hx_array4_f32* Uo, const hx
                            const hx_array4_f32* Sp, hx_dt_accum* nd, uint32_t* status, int arith, hx_stream_t st) {
     return advance_box_roe<float>(eta, Uo, T, Un, vb, dt, dx, dy, F, Sm, Sp, nd, status, arith, (cudaStream_t)st);
 }
+int hx_advance_box_hydrostatic_reflux_f64(const hx_array4_f64* eta, const hx_array4_f64* Ue,
+                                          const hx_array4_f64* Te, const hx_array4_f64* Uo, hx_array4_f64* Un,
+                                          hx_box vb, double dt, double dx, double dy, const hx_array4_f64* Freg,
+                                          hx_dt_accum* nd, uint32_t* status, int arith, hx_stream_t st) {
+    if (!Freg) return fail(HX_ERR_ARG, "hx_advance_box_hydrostatic_reflux: null Freg");
+    return advance_box_hydro<double, hx_array4_f64>(eta, Ue, Te, Uo, Un, vb, dt, dx, dy, nullptr, nullptr, nd, status,
+                                                    arith, (cudaStream_t)st, Freg);
+}
+int hx_advance_box_hydrostatic_reflux_f32(const hx_array4_f32* eta, const hx_array4_f32* Ue,
+                                          const hx_array4_f32* Te, const hx_array4_f32* Uo, hx_array4_f32* Un,
+                                          hx_box vb, float dt, float dx, float dy, const hx_array4_f32* Freg,
+                                          hx_dt_accum* nd, uint32_t* status, int arith, hx_stream_t st) {
+    if (!Freg) return fail(HX_ERR_ARG, "hx_advance_box_hydrostatic_reflux: null Freg");
+    return advance_box_hydro<float, hx_array4_f32>(eta, Ue, Te, Uo, Un, vb, dt, dx, dy, nullptr, nullptr, nd, status,
+                                                   arith, (cudaStream_t)st, Freg);
+}
+int hx_advance_box_roe_reflux_f64(const hx_array4_f64* eta, hx_array4_f64* Uo, const hx_array4_f64* T,
+                                  hx_array4_f64* Un, hx_box vb, double dt, double dx, double dy,
+                                  const hx_array4_i32* fine_mask, hx_box grid_box, const hx_array4_f64* flux_crse,
+                                  const hx_array4_f64* flux_fine, hx_dt_accum* nd, uint32_t* status, int arith,
+                                  hx_stream_t st) {
+    if (!flux_crse && !flux_fine) return fail(HX_ERR_ARG, "hx_advance_box_roe_reflux: no register output");
+    return advance_box_roe<double, hx_array4_f64>(eta, Uo, T, Un, vb, dt, dx, dy, nullptr, nullptr, nullptr, nd, status,
+                                                  arith, (cudaStream_t)st, fine_mask, &grid_box, flux_crse, flux_fine);
+}
+int hx_advance_box_roe_reflux_f32(const hx_array4_f32* eta, hx_array4_f32* Uo, const hx_array4_f32* T,
+                                  hx_array4_f32* Un, hx_box vb, float dt, float dx, float dy,
+                                  const hx_array4_i32* fine_mask, hx_box grid_box, const hx_array4_f32* flux_crse,
+                                  const hx_array4_f32* flux_fine, hx_dt_accum* nd, uint32_t* status, int arith,
+                                  hx_stream_t st) {
+    if (!flux_crse && !flux_fine) return fail(HX_ERR_ARG, "hx_advance_box_roe_reflux: no register output");
+    return advance_box_roe<float, hx_array4_f32>(eta, Uo, T, Un, vb, dt, dx, dy, nullptr, nullptr, nullptr, nd, status,
+                                                 arith, (cudaStream_t)st, fine_mask, &grid_box, flux_crse, flux_fine);
+}
 int hx_dt_reduce_box_f64(const hx_array4_f64* U, const hx_array4_f64* T, hx_box vb, double dx, double dy,
                          hx_dt_accum* acc, hx_stream_t st) {
     return dt_reduce_box<double>(U, T, vb, dx, dy, acc, (cudaStream_t)st);
@@ -431,6 +553,36 @@ int hx_masked_average_down_box_f64(const hx_array4_f64* fine, hx_array4_f64* crs
 int hx_masked_average_down_box_f32(const hx_array4_f32* fine, hx_array4_f32* crse, hx_box cb, int scomp, int ccomp,
                                    int ncomp, int rx, int ry, float fv, float nodata, hx_stream_t st) {
     return mavg_box<float>(fine, crse, cb, scomp, ccomp, ncomp, rx, ry, fv, nodata, (cudaStream_t)st);
+}
+
+int hx_derive_eta_box_f64(const hx_array4_f64* U, const hx_array4_f64* T, hx_array4_f64* eta, hx_box b,
+                          hx_stream_t st) {
+    return eta_box<double>(U, T, eta, b, (cudaStream_t)st);
+}
+int hx_derive_eta_box_f32(const hx_array4_f32* U, const hx_array4_f32* T, hx_array4_f32* eta, hx_box b,
+                          hx_stream_t st) {
+    return eta_box<float>(U, T, eta, b, (cudaStream_t)st);
+}
+int64_t hx_diagnostics_work_bytes(hx_box b) {
+    if (b.hi[0] < b.lo[0] || b.hi[1] < b.lo[1]) return 0;
+    return 5 * (int64_t)sizeof(double) * diag_blocks(b);
+}
+int hx_diagnostics_box_f64(const hx_array4_f64* U, const hx_array4_f64* T, hx_box b, double dx, double dy,
+                           double* out, void* work, hx_stream_t st) {
+    return diag_box<double>(U, T, b, dx, dy, out, work, (cudaStream_t)st);
+}
+int hx_diagnostics_box_f32(const hx_array4_f32* U, const hx_array4_f32* T, hx_box b, float dx, float dy,
+                           double* out, void* work, hx_stream_t st) {
+    return diag_box<float>(U, T, b, dx, dy, out, work, (cudaStream_t)st);
+}
+int hx_level_diagnostics_f64(const hx_level_f64* L, double* out, void* work, hx_stream_t st) {
+    if (!level_ok(L)) return HX_ERR_ARG;
+    if (!out || !work) return fail(HX_ERR_ARG, "hx_level_diagnostics: null output or work");
+    const IBox b{0, 0, L->nx - 1, L->ny - 1};
+    auto pl = [&](const double* p) { return Plane<double>{p, L->pitch, 0, 0}; };
+    return launched(launch_diagnostics<double>(pl(L->h), pl(L->hu), pl(L->hv), pl(L->n), b, L->dx * L->dy,
+                                               static_cast<double*>(work), out, (cudaStream_t)st),
+                    "hx_level_diagnostics_f64");
 }
 
 int hx_level_advance_f64(int method, const hx_level_f64* L, double dt, double* ho, double* huo, double* hvo,
@@ -475,6 +627,9 @@ int hx_level_run_host_f64(int method, int nx, int ny, double dx, double dy, cons
     cudaStream_t st = (cudaStream_t)stream;
     if (nx < 2 || ny < 2) return fail(HX_ERR_ARG, "nx, ny must be >= 2");
     if (!h || !hu || !hv || !z || !n || !bc_lo || !bc_hi) return fail(HX_ERR_ARG, "null host buffer");
+    if (nsteps < 0) return fail(HX_ERR_ARG, "nsteps < 0");
+    if (!(cfl > 0)) return fail(HX_ERR_ARG, "cfl must be positive");
+    if (method != HX_METHOD_ROE && method != HX_METHOD_HYDROSTATIC_ROE) return fail(HX_ERR_ARG, "unknown method");
     const size_t N = (size_t)nx * ny, pb = N * sizeof(double);
     const size_t need = 8 * pb + 512;
     if (g_host.bytes < need) {
@@ -485,25 +640,81 @@ int hx_level_run_host_f64(int method, int nx, int ny, double dx, double dy, cons
         if (e != cudaSuccess) return fail(HX_ERR_CUDA, "device buffers: %s", cudaGetErrorString(e));
         g_host.bytes = need;
     }
+    if (!g_host.ensure_streams()) return fail(HX_ERR_CUDA, "copy streams could not be created");
+    cudaStream_t* cs = g_host.cs;
+    cudaEvent_t* ev = g_host.ev;
     double* d = (double*)g_host.base;
     double* P[8];
     for (int k = 0; k < 8; ++k) P[k] = d + k * N;
     char* tail = (char*)(d + 8 * N);
     uint32_t* status = (uint32_t*)tail;
     double* tdev = (double*)(tail + 64);
-    void* work = tail + 128;
+    DtAccum* slot = reinterpret_cast<DtAccum*>(tail + 128);
     const double* src[5] = {h, hu, hv, z, n};
-    cudaError_t e = cudaSuccess;
-    for (int k = 0; k < 5 && e == cudaSuccess; ++k) e = cudaMemcpyAsync(P[k], src[k], pb, cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(tail, 0, 128, st);
+    // upload: each plane in row chunks over the two copy streams, after the caller's earlier work
+    cudaError_t e = cudaEventRecord(ev[0], st);
+    for (int k = 0; k < 2 && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(cs[k], ev[0], 0);
+    const int chunks = 4;
+    for (int k = 0; k < 5 && e == cudaSuccess; ++k)
+        for (int c = 0; c < chunks && e == cudaSuccess; ++c) {
+            const size_t r0 = (size_t)ny * c / chunks, r1 = (size_t)ny * (c + 1) / chunks;
+            e = cudaMemcpyAsync(P[k] + r0 * nx, src[k] + r0 * nx, (r1 - r0) * nx * sizeof(double),
+                                cudaMemcpyHostToDevice, cs[(k * chunks + c) & 1]);
+        }
+    for (int k = 0; k < 2 && e == cudaSuccess; ++k) e = cudaEventRecord(ev[1 + k], cs[k]);
+    for (int k = 0; k < 2 && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(st, ev[1 + k], 0);
+    if (e == cudaSuccess) e = cudaMemsetAsync(tail, 0, 128 + 3 * sizeof(DtAccum), st);
     if (e != cudaSuccess) return fail(HX_ERR_CUDA, "upload: %s", cudaGetErrorString(e));
     hx_level_f64 L{P[0], P[1], P[2], P[3], P[4], (int64_t)nx, nx, ny, dx, dy, {bc_lo[0], bc_lo[1]}, {bc_hi[0], bc_hi[1]}};
-    int fin = 0;
-    int rc = level_run<double>(method, &L, P[5], P[6], P[7], nsteps, cfl, work, status, tdev, arith, &fin, st);
+    int rc = level_dt<double>(&L, reinterpret_cast<hx_dt_accum*>(&slot[0]), st, arith);
     if (rc) return rc;
-    double* res[3] = {fin ? P[5] : P[0], fin ? P[6] : P[1], fin ? P[7] : P[2]};
-    double* dst[3] = {h, hu, hv};
-    for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = cudaMemcpyAsync(dst[k], res[k], pb, cudaMemcpyDeviceToHost, st);
+    // steps: all but the last in one launch each; the last in row bands, each band's rows downloaded (on the
+    // copy streams) while the next band computes
+    const double* A[3] = {P[0], P[1], P[2]};
+    double* B[3] = {P[5], P[6], P[7]};
+    hx_level_f64 cur = L;
+    const double* res[3] = {P[0], P[1], P[2]};
+    for (int s = 0; s < nsteps; ++s) {
+        StepCtl<double> ctl;
+        ctl.dt_host = 0.0; ctl.cfl = cfl;
+        ctl.dt_in = &slot[s % 3]; ctl.dt_out = &slot[(s + 1) % 3]; ctl.dt_reset = &slot[(s + 2) % 3];
+        ctl.status = status; ctl.time = tdev; ctl.dx = dx; ctl.dy = dy;
+        const bool even = (s % 2) == 0;
+        cur.h = even ? A[0] : B[0];
+        cur.hu = even ? A[1] : B[1];
+        cur.hv = even ? A[2] : B[2];
+        double* o[3] = {even ? B[0] : const_cast<double*>(A[0]), even ? B[1] : const_cast<double*>(A[1]),
+                        even ? B[2] : const_cast<double*>(A[2])};
+        res[0] = o[0]; res[1] = o[1]; res[2] = o[2];
+        if (s < nsteps - 1) {
+            rc = level_advance<double>(method, &cur, ctl, o[0], o[1], o[2], arith, st);
+            if (rc) return rc;
+            continue;
+        }
+        const int band = ((ny + kHostBands - 1) / kHostBands + TY - 1) / TY * TY;
+        for (int b = 0; b * band < ny; ++b) {
+            const int j0 = b * band, j1 = (j0 + band < ny ? j0 + band : ny) - 1;
+            StepCtl<double> cb = ctl;
+            if (b > 0) { cb.time = nullptr; cb.dt_reset = nullptr; }  // once per step
+            rc = level_advance<double>(method, &cur, cb, o[0], o[1], o[2], arith, st, j0, j1);
+            if (rc) return rc;
+            cudaStream_t c = cs[b & 1];
+            e = cudaEventRecord(ev[4 + b], st);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(c, ev[4 + b], 0);
+            double* dst[3] = {h, hu, hv};
+            for (int k = 0; k < 3 && e == cudaSuccess; ++k)
+                e = cudaMemcpyAsync(dst[k] + (size_t)j0 * nx, o[k] + (size_t)j0 * nx,
+                                    (size_t)(j1 - j0 + 1) * nx * sizeof(double), cudaMemcpyDeviceToHost, c);
+            if (e != cudaSuccess) return fail(HX_ERR_CUDA, "download: %s", cudaGetErrorString(e));
+        }
+    }
+    if (nsteps == 0) {
+        double* dst[3] = {h, hu, hv};
+        for (int k = 0; k < 3 && e == cudaSuccess; ++k)
+            e = cudaMemcpyAsync(dst[k], res[k], pb, cudaMemcpyDeviceToHost, cs[k & 1]);
+    }
+    for (int k = 0; k < 2 && e == cudaSuccess; ++k) e = cudaEventRecord(ev[1 + k], cs[k]);
+    for (int k = 0; k < 2 && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(st, ev[1 + k], 0);
     uint32_t sv = 0;
     double tv = 0;
     if (e == cudaSuccess) e = cudaMemcpyAsync(&sv, status, 4, cudaMemcpyDeviceToHost, st);
@@ -514,11 +725,7 @@ int hx_level_run_host_f64(int method, int nx, int ny, double dx, double dy, cons
     return (int)sv;
 }
 
-void hx_host_cache_release(void) {
-    if (g_host.base) cudaFree(g_host.base);
-    g_host.base = nullptr;
-    g_host.bytes = 0;
-}
+void hx_host_cache_release(void) { g_host.release(); }
 
 int hx_level_tangent_f64(const hx_level_f64* L, double dt, double ddt, double* oh, double* ohu, double* ohv,
                          hx_stream_t s) {

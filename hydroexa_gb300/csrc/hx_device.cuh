@@ -32,6 +32,7 @@ template <> struct Cst<double> {
     // IEEE bit patterns of the positive tolerances (for integer comparisons)
     static constexpr long long toldry_bits = 0x3eb0c6f7a0b5ed8dll;
     static constexpr long long tol12_bits = 0x3d719799812dea11ll;
+    static constexpr double max_value = 1.7976931348623157e308;  // std::numeric_limits<double>::max()
 };
 template <> struct Cst<float> {
     static constexpr float g = 9.81f;
@@ -42,6 +43,7 @@ template <> struct Cst<float> {
     static constexpr float tol10 = 1e-10f;
     static constexpr int toldry_bits = 0x358637bd;
     static constexpr int tol12_bits = 0x2b8cbccc;
+    static constexpr float max_value = 3.40282347e38f;  // std::numeric_limits<float>::max()
 };
 
 template <> struct Cst<Dual> {

@@ -23,7 +23,11 @@ namespace hx {
     template cudaError_t launch_tag<R>(int, const V4<R>&, const V4<R>&, const V4<signed char>&, const IBox&, R, \
                                        R, R, R, R, R, signed char, cudaStream_t);                              \
     template cudaError_t launch_masked_avgdown<R>(const V4<R>&, const V4<R>&, const IBox&, int, int, int, int,  \
-                                                  int, R, R, cudaStream_t);
+                                                  int, R, R, cudaStream_t);                                     \
+    template cudaError_t launch_derive_eta<R>(const V4<R>&, const V4<R>&, const V4<R>&, const IBox&,          \
+                                              cudaStream_t);                                                    \
+    template cudaError_t launch_diagnostics<R>(const Plane<R>&, const Plane<R>&, const Plane<R>&,             \
+                                               const Plane<R>&, const IBox&, R, double*, double*, cudaStream_t);
 HX_INST(double)
 HX_INST(float)
 #undef HX_INST

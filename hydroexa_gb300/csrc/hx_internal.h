@@ -6,6 +6,12 @@
 
 namespace hx {
 
+// The level kernels' tile: 32 x 8 cells, one thread per cell.
+constexpr int TX = 32;
+constexpr int TY = 8;
+constexpr int NT = TX * TY;
+
+
 // Read-only load: through the read-only data cache for plain reals, a plain
 // load for other element types (the dual numbers of the tangent model).
 template <class T> __device__ __forceinline__ T ld_ro(const T* p) { return *p; }
@@ -63,48 +69,88 @@ template <class R> struct Cells3W {
 };
 
 // Optional hydrostatic face output: FL/FR nodal arrays per direction, 3 comps.
+// Optional hydrostatic face outputs: the FL/FR arrays (on), and/or the reflux
+// flux 0.5 FL + 0.5 FR the flux registers receive (mean,
+// src/solvers/HydrostaticRoe.cpp:612-627; the halves are exact, so the one
+// rounding of the sum gives the reference's value with or without contraction).
 template <class R> struct FaceOut {
-    V4<R> FL[2], FR[2];
-    int on;
+    V4<R> FL[2], FR[2], Fm[2];
+    int on, mean;
+    __device__ __forceinline__ void put(int d, int gi, int gj, const R* l, const R* r) const {
+        if (on)
+            for (int k = 0; k < 3; ++k) { FL[d].ref(gi, gj, k) = l[k]; FR[d].ref(gi, gj, k) = r[k]; }
+        if (mean)
+            for (int k = 0; k < 3; ++k) Fm[d].ref(gi, gj, k) = R(0.5) * l[k] + R(0.5) * r[k];
+    }
     // x face (gi, gj): FL = (F0, Fa, Fc), FR = (F0, Fb, Fc)
     __device__ __forceinline__ void store_x(int gi, int gj, const IBox& vb, R F0, R Fa, R Fb, R Fc, bool extra) const {
-        if (!on) return;
+        if (!on && !mean) return;
         if (gi < vb.lo0 || gi > vb.hi0 + 1 || gj < vb.lo1 || gj > vb.hi1) return;
         if (extra && gi != vb.hi0 + 1) return;
-        FL[0].ref(gi, gj, 0) = F0; FL[0].ref(gi, gj, 1) = Fa; FL[0].ref(gi, gj, 2) = Fc;
-        FR[0].ref(gi, gj, 0) = F0; FR[0].ref(gi, gj, 1) = Fb; FR[0].ref(gi, gj, 2) = Fc;
+        const R l[3] = {F0, Fa, Fc}, r[3] = {F0, Fb, Fc};
+        put(0, gi, gj, l, r);
     }
     // y face: FL = (F0, Fa, Fb), FR = (F0, Fa, Fc)
     __device__ __forceinline__ void store_y(int gi, int gj, const IBox& vb, R F0, R Fa, R Fb, R Fc, bool extra) const {
-        if (!on) return;
+        if (!on && !mean) return;
         if (gi < vb.lo0 || gi > vb.hi0 || gj < vb.lo1 || gj > vb.hi1 + 1) return;
         if (extra && gj != vb.hi1 + 1) return;
-        FL[1].ref(gi, gj, 0) = F0; FL[1].ref(gi, gj, 1) = Fa; FL[1].ref(gi, gj, 2) = Fb;
-        FR[1].ref(gi, gj, 0) = F0; FR[1].ref(gi, gj, 1) = Fa; FR[1].ref(gi, gj, 2) = Fc;
+        const R l[3] = {F0, Fa, Fb}, r[3] = {F0, Fa, Fc};
+        put(1, gi, gj, l, r);
     }
 };
 
-// Optional classic face output: F, S-, S+ nodal arrays per direction.
+// Optional classic face outputs: the F, S-, S+ nodal arrays per direction
+// (on), and/or the side-selected effective fluxes of the flux registers
+// (src/solvers/Roe.cpp:369-388, 447-566): D- = F - S- (seen by the right
+// cell), D+ = F + S+ (seen by the left cell).  Coarse register (crse_on): D+
+// where the left cell is coarse and the right one covered by the finer level
+// (mask 0 | 1), D- for 1 | 0, else 0.  Fine register (fine_on): D- on the
+// grid box's low face, D+ on its high face, else 0.
 template <class R> struct FaceOut9 {
     V4<R> F[2], Sm[2], Sp[2];
-    int on;
+    V4<R> fc[2], ff[2];
+    V4<int> mask;
+    IBox grid;
+    int on, crse_on, fine_on;
     __device__ __forceinline__ void put(int d, int gi, int gj, const R* f, const R* m, const R* p) const {
-        for (int k = 0; k < 3; ++k) {
-            F[d].ref(gi, gj, k) = f[k];
-            Sm[d].ref(gi, gj, k) = m[k];
-            Sp[d].ref(gi, gj, k) = p[k];
+        if (on)
+            for (int k = 0; k < 3; ++k) {
+                F[d].ref(gi, gj, k) = f[k];
+                Sm[d].ref(gi, gj, k) = m[k];
+                Sp[d].ref(gi, gj, k) = p[k];
+            }
+        if (!crse_on && !fine_on) return;
+        R Dm[3], Dp[3];
+        for (int k = 0; k < 3; ++k) {  // LinComb(1.0, F, -1.0, S-) and LinComb(1.0, F, 1.0, S+): exact products
+            Dm[k] = R(1.0) * f[k] + R(-1.0) * m[k];
+            Dp[k] = R(1.0) * f[k] + R(1.0) * p[k];
+        }
+        if (crse_on) {
+            const int left_is_fine = d == 0 ? mask.ld(gi - 1, gj, 0) : mask.ld(gi, gj - 1, 0);
+            const int right_is_fine = mask.ld(gi, gj, 0);
+            for (int k = 0; k < 3; ++k)
+                fc[d].ref(gi, gj, k) = (left_is_fine == 0 && right_is_fine == 1)   ? Dp[k]
+                                       : (left_is_fine == 1 && right_is_fine == 0) ? Dm[k]
+                                                                                   : R(0.0);
+        }
+        if (fine_on) {
+            const int face_idx = d == 0 ? gi : gj;
+            const int i_low = d == 0 ? grid.lo0 : grid.lo1, i_high = (d == 0 ? grid.hi0 : grid.hi1) + 1;
+            for (int k = 0; k < 3; ++k)
+                ff[d].ref(gi, gj, k) = face_idx == i_low ? Dm[k] : (face_idx == i_high ? Dp[k] : R(0.0));
         }
     }
     __device__ __forceinline__ void store_x(int gi, int gj, const IBox& vb, const R* f, const R* m, const R* p,
                                             bool extra) const {
-        if (!on) return;
+        if (!on && !crse_on && !fine_on) return;
         if (gi < vb.lo0 || gi > vb.hi0 + 1 || gj < vb.lo1 || gj > vb.hi1) return;
         if (extra && gi != vb.hi0 + 1) return;
         put(0, gi, gj, f, m, p);
     }
     __device__ __forceinline__ void store_y(int gi, int gj, const IBox& vb, const R* f, const R* m, const R* p,
                                             bool extra) const {
-        if (!on) return;
+        if (!on && !crse_on && !fine_on) return;
         if (gi < vb.lo0 || gi > vb.hi0 || gj < vb.lo1 || gj > vb.hi1 + 1) return;
         if (extra && gj != vb.hi1 + 1) return;
         put(1, gi, gj, f, m, p);

@@ -16,10 +16,6 @@
 
 namespace hx {
 
-constexpr int TX = 32;
-constexpr int TY = 8;
-constexpr int NT = TX * TY;
-
 // ---------------------------------------------------------------------------
 // Hydrostatic-Roe tile kernel.
 // ---------------------------------------------------------------------------
@@ -586,6 +582,87 @@ __global__ void __launch_bounds__(NT) k_masked_avgdown(V4<R> fine, V4<R> crse, I
 }
 
 // ---------------------------------------------------------------------------
+// Level diagnostics and eta (src/state/AmrMeshState_Utils.cpp:213-298,
+// src/state/AmrMeshState_AMR.cpp:203-224).
+// ---------------------------------------------------------------------------
+// eta = h + z on any box of the views (ghosts included).
+template <class R>
+__global__ void __launch_bounds__(NT) k_derive_eta(V4<R> U, V4<R> T, V4<R> eta, IBox b) {
+    const int i = b.lo0 + blockIdx.x * TX + (threadIdx.x & (TX - 1));
+    const int j = b.lo1 + blockIdx.y * TY + threadIdx.x / TX;
+    if (i > b.hi0 || j > b.hi1) return;
+    eta.ref(i, j, 0) = U.ld(i, j, 0) + T.ld(i, j, 0);
+}
+
+// Per-block sums of the conservation diagnostics over the valid cells that are
+// not NODATA (roughness == -9999) and wet (h > 0): mass = h dA, momenta hu dA,
+// hv dA, kinetic energy 0.5 (hu^2 + hv^2) / h dA, and min h.  Each cell's terms
+// take the reference's types and order (the 0.5 literal is double, so a float
+// build evaluates the kinetic term in double and rounds it to float); sums are
+// carried in double.  part: 5 doubles per block.
+template <class R>
+__global__ void __launch_bounds__(NT) k_diag_partial(Plane<R> h, Plane<R> hu, Plane<R> hv, Plane<R> nr, IBox b, R dA,
+                                                     double* part) {
+    __shared__ double sh[5][NT / 32];
+    const int i = b.lo0 + blockIdx.x * TX + (threadIdx.x & (TX - 1));
+    const int j = b.lo1 + blockIdx.y * TY + threadIdx.x / TX;
+    double m = 0.0, px = 0.0, py = 0.0, ke = 0.0, mn = (double)Cst<R>::max_value;
+    if (i <= b.hi0 && j <= b.hi1) {
+        const R hh = h.ld(i, j), a = hu.ld(i, j), c = hv.ld(i, j);
+        const R nodata_val = R(-9999.0);
+        if (!(nr.ld(i, j) == nodata_val) && hh > R(0)) {
+            const R s_mass = hh * dA, s_mx = a * dA, s_my = c * dA;
+            const R s_ke = 0.5 * (a * a + c * c) / hh * dA;
+            m = s_mass; px = s_mx; py = s_my; ke = s_ke; mn = hh;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        m += __shfl_xor_sync(0xffffffffu, m, o);
+        px += __shfl_xor_sync(0xffffffffu, px, o);
+        py += __shfl_xor_sync(0xffffffffu, py, o);
+        ke += __shfl_xor_sync(0xffffffffu, ke, o);
+        mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+    }
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) { sh[0][w] = m; sh[1][w] = px; sh[2][w] = py; sh[3][w] = ke; sh[4][w] = mn; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < NT / 32; ++k) {
+            m += sh[0][k]; px += sh[1][k]; py += sh[2][k]; ke += sh[3][k]; mn = fmin(mn, sh[4][k]);
+        }
+        double* q = part + 5 * (blockIdx.x + (long long)blockIdx.y * gridDim.x);
+        q[0] = m; q[1] = px; q[2] = py; q[3] = ke; q[4] = mn;
+    }
+}
+
+// The block partials folded in a fixed order into out[5] (one block; R only
+// ties the instance to the unit that instantiates launch_diagnostics<R>).
+template <class R>
+__global__ void __launch_bounds__(NT) k_diag_final(const double* part, long long nblocks, double* out) {
+    __shared__ double sh[5][NT / 32];
+    double v[5] = {0.0, 0.0, 0.0, 0.0, 1.7976931348623157e308};
+    for (long long k = threadIdx.x; k < nblocks; k += NT) {
+        for (int c = 0; c < 4; ++c) v[c] += part[5 * k + c];
+        v[4] = fmin(v[4], part[5 * k + 4]);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        for (int c = 0; c < 4; ++c) v[c] += __shfl_xor_sync(0xffffffffu, v[c], o);
+        v[4] = fmin(v[4], __shfl_xor_sync(0xffffffffu, v[4], o));
+    }
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0)
+        for (int c = 0; c < 5; ++c) sh[c][w] = v[c];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < NT / 32; ++k) {
+            for (int c = 0; c < 4; ++c) v[c] += sh[c][k];
+            v[4] = fmin(v[4], sh[4][k]);
+        }
+        for (int c = 0; c < 5; ++c) out[c] = v[c];
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Point evaluation of the Riemann solvers (diagnostic entry, golden vectors).
 // method 1: states (n, 6) = (hi hui hvi hj huj hvj), aux (n, 2) = normal;
 // method 0: states (n, 10), aux (n, 4) = (dt dx nx ny).  out: (n, 3) F then,
@@ -759,6 +836,23 @@ template <class R>
 cudaError_t launch_tag(int method, const V4<R>& U, const V4<R>& T, const V4<signed char>& tags, const IBox& vb, R dx,
                        R dy, R time, R h_th, R u_th, R z_th, signed char set_value, cudaStream_t st) {
     k_tag<R><<<tile_grid(vb, TX, TY), NT, 0, st>>>(method, U, T, tags, vb, dx, dy, time, h_th, u_th, z_th, set_value);
+    return cudaGetLastError();
+}
+
+template <class R>
+cudaError_t launch_derive_eta(const V4<R>& U, const V4<R>& T, const V4<R>& eta, const IBox& b, cudaStream_t st) {
+    k_derive_eta<R><<<tile_grid(b, TX, TY), NT, 0, st>>>(U, T, eta, b);
+    return cudaGetLastError();
+}
+
+template <class R>
+cudaError_t launch_diagnostics(const Plane<R>& h, const Plane<R>& hu, const Plane<R>& hv, const Plane<R>& nr,
+                               const IBox& b, R dA, double* part, double* out, cudaStream_t st) {
+    const dim3 g = tile_grid(b, TX, TY);
+    k_diag_partial<R><<<g, NT, 0, st>>>(h, hu, hv, nr, b, dA, part);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_diag_final<R><<<1, NT, 0, st>>>(part, (long long)g.x * g.y, out);
     return cudaGetLastError();
 }
 

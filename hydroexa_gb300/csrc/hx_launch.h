@@ -31,6 +31,13 @@ template <class R>
 cudaError_t launch_masked_avgdown(const V4<R>& fine, const V4<R>& crse, const IBox& cb, int scomp, int ccomp,
                                   int ncomp, int rx, int ry, R fv, R nodata, cudaStream_t st);
 
+template <class R>
+cudaError_t launch_derive_eta(const V4<R>& U, const V4<R>& T, const V4<R>& eta, const IBox& b, cudaStream_t st);
+
+template <class R>
+cudaError_t launch_diagnostics(const Plane<R>& h, const Plane<R>& hu, const Plane<R>& hv, const Plane<R>& nr,
+                               const IBox& b, R dA, double* part, double* out, cudaStream_t st);
+
 template <class R, bool FAST>
 cudaError_t launch_ensemble(const EnsInstance<R>* inst, int ninst, long long total_tiles, int step, R cfl,
                            unsigned long long* queue, int grid, cudaStream_t st);

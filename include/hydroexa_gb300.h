@@ -87,6 +87,15 @@ typedef struct hx_array4_i8 {
     int32_t ncomp;
 } hx_array4_i8;
 
+typedef struct hx_array4_i32 {
+    int32_t* p;
+    int64_t jstride;
+    int64_t nstride;
+    int32_t lo[2];
+    int32_t hi[2];
+    int32_t ncomp;
+} hx_array4_i32;
+
 /* Inclusive cell box, like amrex::Box in 2-D. */
 typedef struct hx_box {
     int32_t lo[2];
@@ -167,6 +176,51 @@ int hx_advance_box_roe_f32(const hx_array4_f32* eta, hx_array4_f32* U_old, const
                            const hx_array4_f32* F, const hx_array4_f32* Sm, const hx_array4_f32* Sp,
                            hx_dt_accum* next_dt, uint32_t* status, int arith, hx_stream_t stream);
 
+/* ---- reflux: the flux-register fluxes emitted by the advance kernels ------ */
+
+/*
+ * Hydrostatic advance that writes, instead of FL and FR, the one flux the
+ * registers receive, Freg[d] = 0.5 FL + 0.5 FR on the box's nodal faces ([0] x,
+ * [1] y) -- the flux-register preparation of HydrostaticRoe::compute_fluxes_Impl
+ * (src/solvers/HydrostaticRoe.cpp:612-627) fused into the face loop.  The
+ * caller passes Freg to FluxRegister::CrseInit (scale -dt dA) / FineAdd
+ * (scale dt dA) as the reference does.  Other arguments as
+ * hx_advance_box_hydrostatic_*.
+ */
+int hx_advance_box_hydrostatic_reflux_f64(const hx_array4_f64* eta_ext, const hx_array4_f64* U_ext,
+                                          const hx_array4_f64* T_ext, const hx_array4_f64* U_old,
+                                          hx_array4_f64* U_new, hx_box valid, double dt, double dx, double dy,
+                                          const hx_array4_f64* Freg, hx_dt_accum* next_dt, uint32_t* status,
+                                          int arith, hx_stream_t stream);
+int hx_advance_box_hydrostatic_reflux_f32(const hx_array4_f32* eta_ext, const hx_array4_f32* U_ext,
+                                          const hx_array4_f32* T_ext, const hx_array4_f32* U_old,
+                                          hx_array4_f32* U_new, hx_box valid, float dt, float dx, float dy,
+                                          const hx_array4_f32* Freg, hx_dt_accum* next_dt, uint32_t* status,
+                                          int arith, hx_stream_t stream);
+/*
+ * Classic Roe advance that writes the side-selected effective fluxes of the
+ * flux registers (src/solvers/Roe.cpp:369-388 and 447-566) instead of F, S-,
+ * S+, on the box's nodal faces ([0] x, [1] y, 3 comps):
+ *   D- = F - S- (the flux the right cell saw), D+ = F + S+ (the left cell's).
+ *   flux_crse (optional): with fine_mask (one int comp, 0 = coarse, 1 = covered
+ *     by the next finer level, >= 1 ghost: amrex::makeFineMask(U, fine grids,
+ *     ratio, 0, 1)), D+ where the left cell is coarse and the right covered,
+ *     D- where the left is covered and the right coarse, 0 elsewhere.
+ *   flux_fine (optional): D- on faces at the low end of grid_box (the box's
+ *     grid, which may extend beyond a tile), D+ at its high end, 0 elsewhere.
+ * Other arguments as hx_advance_box_roe_*.
+ */
+int hx_advance_box_roe_reflux_f64(const hx_array4_f64* eta, hx_array4_f64* U_old, const hx_array4_f64* T,
+                                  hx_array4_f64* U_new, hx_box valid, double dt, double dx, double dy,
+                                  const hx_array4_i32* fine_mask, hx_box grid_box, const hx_array4_f64* flux_crse,
+                                  const hx_array4_f64* flux_fine, hx_dt_accum* next_dt, uint32_t* status, int arith,
+                                  hx_stream_t stream);
+int hx_advance_box_roe_reflux_f32(const hx_array4_f32* eta, hx_array4_f32* U_old, const hx_array4_f32* T,
+                                  hx_array4_f32* U_new, hx_box valid, float dt, float dx, float dy,
+                                  const hx_array4_i32* fine_mask, hx_box grid_box, const hx_array4_f32* flux_crse,
+                                  const hx_array4_f32* flux_fine, hx_dt_accum* next_dt, uint32_t* status, int arith,
+                                  hx_stream_t stream);
+
 /*
  * Per-cell CFL bound of one box folded into acc (replaces the ReduceOps pass of
  * compute_dt_Impl, src/solvers/HydrostaticRoe.cpp:19-65 and
@@ -203,6 +257,36 @@ int hx_masked_average_down_box_f64(const hx_array4_f64* fine, hx_array4_f64* crs
 int hx_masked_average_down_box_f32(const hx_array4_f32* fine, hx_array4_f32* crse, hx_box crse_box, int scomp,
                                    int ccomp, int ncomp, int rx, int ry, float fine_volume, float nodata,
                                    hx_stream_t stream);
+
+/* ---- eta and the conservation diagnostics ---------------------------------- */
+
+/*
+ * eta = h + z on box b, ghosts included where the views cover them: the kernel
+ * of AmrMeshState::DeriveEtaFrom (src/state/AmrMeshState_AMR.cpp:203-224).
+ */
+int hx_derive_eta_box_f64(const hx_array4_f64* U, const hx_array4_f64* terrain, hx_array4_f64* eta, hx_box b,
+                          hx_stream_t stream);
+int hx_derive_eta_box_f32(const hx_array4_f32* U, const hx_array4_f32* terrain, hx_array4_f32* eta, hx_box b,
+                          hx_stream_t stream);
+
+/*
+ * The per-box reduction of AmrMeshState::ComputeMassDiagnostics
+ * (src/state/AmrMeshState_Utils.cpp:242-298) over the valid box b: out (device,
+ * 5 doubles) = {mass, x-momentum, y-momentum, kinetic energy, min h} summed
+ * over cells that are not NODATA (roughness == -9999) and wet (h > 0), each
+ * cell's terms in the reference's types and order, the sums carried in double
+ * in a fixed order (deterministic).  min h is DBL_MAX / FLT_MAX when no cell
+ * counts.  work: hx_diagnostics_work_bytes(b) bytes of device memory.  The
+ * reference assigns each box's result to the level's total instead of adding
+ * it (AmrMeshState_Utils.cpp:293-296), so with several boxes per level it
+ * reports the last box only; an adapter reproducing that keeps the last
+ * call's output, one summing the level adds the per-box outputs.
+ */
+int64_t hx_diagnostics_work_bytes(hx_box b);
+int hx_diagnostics_box_f64(const hx_array4_f64* U, const hx_array4_f64* terrain, hx_box b, double dx, double dy,
+                           double* out, void* work, hx_stream_t stream);
+int hx_diagnostics_box_f32(const hx_array4_f32* U, const hx_array4_f32* terrain, hx_box b, float dx, float dy,
+                           double* out, void* work, hx_stream_t stream);
 
 /* ---- single-box level with the physical boundary fused into the loader --- */
 
@@ -249,6 +333,9 @@ int hx_level_advance_f32(int method, const hx_level_f32* L, float dt, float* h_o
 /* compute_dt_Impl over the level (no ghosts needed). */
 int hx_level_dt_reduce_f64(const hx_level_f64* L, hx_dt_accum* acc, hx_stream_t stream);
 int hx_level_dt_reduce_f32(const hx_level_f32* L, hx_dt_accum* acc, hx_stream_t stream);
+/* hx_diagnostics_box_f64 over a whole single-box level (work: hx_diagnostics_work_bytes of
+ * the box (0,0)-(nx-1,ny-1)). */
+int hx_level_diagnostics_f64(const hx_level_f64* level, double* out, void* work, hx_stream_t stream);
 
 /*
  * nsteps of the single-level time loop of the reference driver
@@ -355,9 +442,14 @@ int hx_level_run_static_f64(int method, hx_level_f64* level, int nsteps, double 
  * flux taking the forward's entropy-fix and dry branches, the hydrostatic cap
  * and pressure correction, the update, Manning factor and dry clamp) plus the
  * dependence of each step's dt on the cell that set the CFL bound.
- *   checkpoint_every = 0: every state is kept (N + 1 states in work);
+ *   checkpoint_every = 0: every state is kept (N + 5 states in work);
  *   k > 0: every k-th state is kept and each k-step segment is recomputed once
- *   in the reverse sweep (N/k + k + 1 states in work).
+ *   in the reverse sweep, on a second stream while the previous segment is
+ *   reversed (N/k + 2k + 9 states in work);
+ *   k < 0: binomial checkpointing with -k snapshot slots (Griewank's revolve
+ *   schedule: the fewest recomputed steps for that memory; -k + 8 states in
+ *   work).  hx_adjoint_recompute_steps gives the forward steps the reverse
+ *   sweep recomputes under each choice.
  * hx_adjoint_forward_f64 runs the forward sweep: the level's planes are the
  * initial state (not modified); series (device, N x ngauges) receives h at the
  * gauge cells (cell index i + j * pitch) after every step.
@@ -371,6 +463,7 @@ int hx_level_run_static_f64(int method, hx_level_f64* level, int nsteps, double 
  * Restriction: nx % 32 != 1 and ny % 16 != 1.
  */
 int64_t hx_adjoint_work_bytes_f64(int nx, int ny, int64_t pitch, int nsteps, int checkpoint_every);
+int64_t hx_adjoint_recompute_steps(int nsteps, int checkpoint_every);
 int hx_adjoint_forward_f64(const hx_level_f64* level, int nsteps, double cfl, int ngauges, const int64_t* gauge_cells,
                            double* series, int checkpoint_every, int arith, void* work, uint32_t* status,
                            hx_stream_t stream);
@@ -397,6 +490,17 @@ int hx_adjoint_step_f64(const hx_level_f64* level, double dt, const double* lam_
  */
 int hx_level_tangent_f64(const hx_level_f64* level_pairs, double dt, double ddt, double* out_h, double* out_hu,
                          double* out_hv, hx_stream_t stream);
+
+/* ---- the FP64 roof --------------------------------------------------------- */
+
+/*
+ * Measured FMA issue rates of the current GPU (thread instructions per second,
+ * best of three launches of register-only FMA chains): DFMA, and FFMA when
+ * ffma_per_s is not NULL.  The fused FP64 kernels are bound by FP64 issue on
+ * GB300; bench.py reports their FP64-pipe fraction against this rate.
+ * Synchronises the stream; allocates a few MB for the duration of the call.
+ */
+int hx_measure_fp64_rate(double* dfma_per_s, double* ffma_per_s, hx_stream_t stream);
 
 /* ---- diagnostics (points) ------------------------------------------------ */
 

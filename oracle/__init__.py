@@ -224,6 +224,64 @@ def masked_average_down(fine: np.ndarray, rx: int, ry: int, fine_volume: float, 
     return c
 
 
+def mass_diagnostics(h, hu, hv, n, dx: float, dy: float) -> np.ndarray:
+    """{mass, x-momentum, y-momentum, kinetic energy, min h} of one box
+    (src/state/AmrMeshState_Utils.cpp:267-298); planes (ny, nx) of one dtype."""
+    planes = [np.ascontiguousarray(a) for a in (h, hu, hv, n)]
+    ny, nx = planes[0].shape
+    R = _real(planes[0].dtype)
+    out = np.zeros(5, dtype=np.float64)
+    getattr(lib(), "hxo_mass_diagnostics_" + _suffix(planes[0].dtype))(
+        ctypes.c_int(nx), ctypes.c_int(ny), ctypes.c_longlong(nx), *(_ptr(a) for a in planes), R(dx), R(dy),
+        out.ctypes.data_as(ctypes.c_void_p))
+    return out
+
+
+def derive_eta(h, z) -> np.ndarray:
+    """eta = h + z (src/state/AmrMeshState_AMR.cpp:217-219)."""
+    h = np.ascontiguousarray(h)
+    z = np.ascontiguousarray(z)
+    eta = np.empty_like(h)
+    getattr(lib(), "hxo_derive_eta_" + _suffix(h.dtype))(ctypes.c_longlong(h.size), _ptr(h), _ptr(z), _ptr(eta))
+    return eta
+
+
+def reflux_mean(FL, FR):
+    """The hydrostatic solver's flux-register flux, 0.5 FL + 0.5 FR
+    (src/solvers/HydrostaticRoe.cpp:619-626, MultiFab::LinComb); the halves
+    are exact, so the sum is rounded once in any evaluation order."""
+    FL, FR = np.asarray(FL), np.asarray(FR)
+    return FL.dtype.type(0.5) * FL + FR.dtype.type(0.5) * FR
+
+
+def roe_reflux_select(d, F, Sm, Sp, face_lo, mask=None, mask_lo=None, grid=None):
+    """Side-selected effective fluxes of the classic solver's flux registers
+    (src/solvers/Roe.cpp:369-388 for D- and D+, :447-566 for the selection)
+    on the nodal faces of direction d.  F, Sm, Sp: (3, nyf, nxf) with face
+    (i, j) at [:, j - face_lo[1], i - face_lo[0]].  mask: (ny, nx) ints with
+    cell (i, j) at [j - mask_lo[1], i - mask_lo[0]] (0 coarse, 1 covered);
+    grid: ((lo_x, lo_y), (hi_x, hi_y)).  Returns (flux_crse, flux_fine)."""
+    F, Sm, Sp = (np.asarray(a) for a in (F, Sm, Sp))
+    one = F.dtype.type(1.0)
+    Dm = one * F + F.dtype.type(-1.0) * Sm
+    Dp = one * F + one * Sp
+    _, nyf, nxf = F.shape
+    I, J = np.meshgrid(np.arange(nxf) + face_lo[0], np.arange(nyf) + face_lo[1])
+    zero = np.zeros_like(F)
+    fc = ff = None
+    if mask is not None:
+        m = np.asarray(mask)
+        li, lj = (I - 1, J) if d == 0 else (I, J - 1)
+        left = m[lj - mask_lo[1], li - mask_lo[0]]
+        right = m[J - mask_lo[1], I - mask_lo[0]]
+        fc = np.where(((left == 0) & (right == 1))[None], Dp, np.where(((left == 1) & (right == 0))[None], Dm, zero))
+    if grid is not None:
+        face_idx = I if d == 0 else J
+        i_low, i_high = grid[0][d], grid[1][d] + 1
+        ff = np.where((face_idx == i_low)[None], Dm, np.where((face_idx == i_high)[None], Dp, zero))
+    return fc, ff
+
+
 # --- reference kernels compiled verbatim (only where the reference tree exists) ---
 
 _ref = None

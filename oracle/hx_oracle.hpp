@@ -717,4 +717,43 @@ void masked_average_down(View<const R> fine, View<R> crse, int clo0, int clo1, i
             }
 }
 
+// Per-box reduction of AmrMeshState::ComputeMassDiagnostics,
+// src/state/AmrMeshState_Utils.cpp:267-298, over the valid cells of one box:
+// out = {mass, x-momentum, y-momentum, kinetic energy, min h}.  A cell counts
+// when its roughness (terrain comp 1) is not -9999 and h > 0 (:273, :281); its
+// terms keep the reference's expressions and types (:282-286; the 0.5 literal
+// is double).  The reference's ReduceOps fixes no summation order; here the
+// terms are summed in double, row by row.
+template <class R>
+void mass_diagnostics(int nx, int ny, long long pitch, const R* h, const R* hu, const R* hv, const R* n, R dx, R dy,
+                      double out[5]) {
+    const R dA = dx * dy;                // :239
+    const R nodata_val = R(-9999.0);     // :217
+    double m = 0.0, px = 0.0, py = 0.0, ke = 0.0;
+    R min_h = std::numeric_limits<R>::max();
+    for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+            const long long o = (long long)i + (long long)j * pitch;
+            const R hh = h[o], a = hu[o], c = hv[o];
+            const int is_nodata = (n[o] == nodata_val) ? 1 : 0;
+            if (is_nodata == 0 && hh > 0.0) {
+                const R s_mass = hh * dA;
+                const R s_mx = a * dA;
+                const R s_my = c * dA;
+                const R s_ke = 0.5 * (a * a + c * c) / hh * dA;
+                m += s_mass;
+                px += s_mx;
+                py += s_my;
+                ke += s_ke;
+                min_h = smin(min_h, hh);
+            }
+        }
+    out[0] = m; out[1] = px; out[2] = py; out[3] = ke; out[4] = (double)min_h;
+}
+
+// eta = h + z, the kernel of DeriveEtaFrom, src/state/AmrMeshState_AMR.cpp:217-219.
+template <class R> void derive_eta(long long count, const R* h, const R* z, R* eta) {
+    for (long long k = 0; k < count; ++k) eta[k] = h[k] + z[k];
+}
+
 }  // namespace hxo

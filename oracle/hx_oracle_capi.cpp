@@ -137,6 +137,13 @@ int run(int method, const Level<R>& L, R* h, R* hu, R* hv, const R* z, const R* 
         View<const R> Fv{fine, fjs, fns, flo0, flo1};                                                               \
         View<R> Cv{crse, cjs, cns, clo0, clo1};                                                                     \
         masked_average_down<R>(Fv, Cv, bx_lo0, bx_lo1, bx_hi0, bx_hi1, ncomp, rx, ry, fv, nodata);                 \
+    }                                                                                                               \
+    extern "C" void hxo_mass_diagnostics_##SUF(int nx, int ny, long long pitch, const R* h, const R* hu,            \
+                                               const R* hv, const R* n, R dx, R dy, double* out) {                  \
+        mass_diagnostics<R>(nx, ny, pitch, h, hu, hv, n, dx, dy, out);                                              \
+    }                                                                                                               \
+    extern "C" void hxo_derive_eta_##SUF(long long count, const R* h, const R* z, R* eta) {                         \
+        derive_eta<R>(count, h, z, eta);                                                                            \
     }
 
 HXO_DEFINE(double, f64)

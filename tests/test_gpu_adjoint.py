@@ -178,6 +178,27 @@ def test_checkpointed_reverse_equals_store_all(cuda, hxlib):
         assert torch.equal(a, b)
 
 
+@pytest.mark.parametrize("slots", [2, 3, 5, 9])
+def test_binomial_reverse_equals_store_all(cuda, hxlib, slots):
+    """Binomial checkpointing with few slots (2: no spare slot after the
+    first snapshot) recomputes states bit for bit and reverses the same
+    steps: gradients equal to the store-all sweep, Manning factor included."""
+    geom, z, h0, hu0, hv0, gauges, _, _ = misfit_problem(nsteps=23)
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(cuda)
+    base = [T(z), T(h0), T(hu0), T(hv0)]
+    nman = torch.zeros_like(base[0])
+    nman[:, : geom.nx // 2] = 0.03
+    href = torch.full((23, len(gauges)), 1.0, dtype=torch.float64, device=cuda)
+    grads, series = [], []
+    for every in (0, -slots):
+        prob = GaugeProblem(geom, nman, gauges, 23, 0.45, checkpoint_every=every)
+        series.append(prob.forward(*base))
+        grads.append(prob.reverse(href))
+    assert torch.equal(series[0], series[1])
+    for a, b in zip(*grads):
+        assert torch.equal(a, b)
+
+
 def test_autograd_function(cuda, hxlib):
     geom, z, h0, _, _, gauges, nsteps, _ = misfit_problem(nsteps=12)
     T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(cuda)

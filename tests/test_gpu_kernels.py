@@ -211,3 +211,109 @@ def test_nan_input_sets_status(cuda):
     torch.cuda.synchronize()
     assert lev.status.read() & capi.HX_STATUS_NAN
     assert torch.isnan(out).any()
+
+
+def _box_case(cuda, oracle_lib, method, seed):
+    case = workloads.fractal_dam_break(64, 48, seed=seed, amplitude=1.5, nodata_frac=0.1 if method else 0.0)
+    g = case.geom
+    L = oracle_lib.Level(g.nx, g.ny, g.dx, g.dy, g.bc_lo, g.bc_hi)
+    h, hu, hv, *_ = oracle_lib.run(L, method, case.h, case.hu, case.hv, case.z, case.n, 5, case.cfl)
+    mn, _ = oracle_lib.compute_dt(L, h, hu, hv, case.z)
+    return case, L, (h, hu, hv), mn * case.cfl
+
+
+def test_hydrostatic_reflux_flux_from_the_advance(cuda, hxlib, oracle_lib):
+    """The fused reflux output equals 0.5 FL + 0.5 FR of the reference's face
+    arrays, bit for bit, and the update is unchanged."""
+    case, L, (h, hu, hv), dt = _box_case(cuda, oracle_lib, 1, 41)
+    g = case.geom
+    (rh, rhu, rhv), F = oracle_lib.advance(L, 1, h, hu, hv, case.z, case.n, dt, faces=True)
+    G = 2
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(cuda)
+    Eta = dev(_bc_ext(h + case.z, G, "even", "even")[None])
+    Uext = dev(np.stack([np.zeros((g.ny + 2 * G, g.nx + 2 * G)), _bc_ext(hu, G, "odd", "even"),
+                         _bc_ext(hv, G, "even", "odd")]))
+    Text = dev(np.stack([_bc_ext(case.z, G, "edge", "edge"), _bc_ext(case.n, G, "edge", "edge")]))
+    Uold = dev(np.stack([h, hu, hv]))
+    Unew = torch.zeros_like(Uold)
+    Fx = torch.zeros((3, g.ny, g.nx + 1), dtype=torch.float64, device=cuda)
+    Fy = torch.zeros((3, g.ny + 1, g.nx), dtype=torch.float64, device=cuda)
+    for (x0, x1), (y0, y1) in [((0, 29), (0, 20)), ((30, 63), (0, 20)), ((0, 29), (21, 47)), ((30, 63), (21, 47))]:
+        Freg = (capi.Array4F64 * 2)(array4(Fx), array4(Fy))
+        rc = hxlib.lib().hx_advance_box_hydrostatic_reflux_f64(
+            ctypes.byref(array4(Eta, (-G, -G))), ctypes.byref(array4(Uext, (-G, -G))),
+            ctypes.byref(array4(Text, (-G, -G))), ctypes.byref(array4(Uold)), ctypes.byref(array4(Unew)),
+            box((x0, y0), (x1, y1)), dt, g.dx, g.dy, Freg, None, None, EXACT, None)
+        hxlib.check(rc, "reflux box")
+    got = Unew.cpu().numpy()
+    assert np.array_equal(got[0], rh) and np.array_equal(got[1], rhu) and np.array_equal(got[2], rhv)
+    assert np.array_equal(Fx.cpu().numpy(), oracle_lib.reflux_mean(F["FLx"], F["FRx"]))
+    assert np.array_equal(Fy.cpu().numpy(), oracle_lib.reflux_mean(F["FLy"], F["FRy"]))
+
+
+def test_classic_box_form_and_reflux_selection(cuda, hxlib, oracle_lib):
+    """Classic box form (FillPatch-style ghosts) equals the level form with its
+    F / S- / S+ faces; the reflux variant writes the reference's side-selected
+    D+ / D- for a coarse register (fine mask) and a fine register (grid box)."""
+    case, L, (h, hu, hv), dt = _box_case(cuda, oracle_lib, 0, 43)
+    g = case.geom
+    (rh, rhu, rhv), F = oracle_lib.advance(L, 0, h, hu, hv, case.z, case.n, dt, faces=True)
+    G = 1
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(cuda)
+
+    def inputs():
+        Eta = dev(_bc_ext(h + case.z, G, "even", "even")[None])
+        Uold = dev(np.stack([np.zeros((g.ny + 2 * G, g.nx + 2 * G)), _bc_ext(hu, G, "odd", "even"),
+                             _bc_ext(hv, G, "even", "odd")]))
+        T = dev(np.stack([_bc_ext(case.z, G, "edge", "edge"), _bc_ext(case.n, G, "edge", "edge")]))
+        return Eta, Uold, T
+
+    vb = box((0, 0), (g.nx - 1, g.ny - 1))
+    faces = lambda: [torch.zeros((3, g.ny, g.nx + 1), dtype=torch.float64, device=cuda),
+                     torch.zeros((3, g.ny + 1, g.nx), dtype=torch.float64, device=cuda)]
+    Eta, Uold, T = inputs()
+    Unew = torch.zeros((3, g.ny, g.nx), dtype=torch.float64, device=cuda)
+    Ff, Smf, Spf = faces(), faces(), faces()
+    arr = lambda fs: (capi.Array4F64 * 2)(array4(fs[0]), array4(fs[1]))
+    rc = hxlib.lib().hx_advance_box_roe_f64(ctypes.byref(array4(Eta, (-G, -G))), ctypes.byref(array4(Uold, (-G, -G))),
+                                            ctypes.byref(array4(T, (-G, -G))), ctypes.byref(array4(Unew)), vb, dt,
+                                            g.dx, g.dy, arr(Ff), arr(Smf), arr(Spf), None, None, EXACT, None)
+    hxlib.check(rc, "classic box")
+    got = Unew.cpu().numpy()
+    assert np.array_equal(got[0], rh) and np.array_equal(got[1], rhu) and np.array_equal(got[2], rhv)
+    for d, sfx in ((0, "x"), (1, "y")):
+        assert np.array_equal(Ff[d].cpu().numpy(), F["F" + sfx])
+        assert np.array_equal(Smf[d].cpu().numpy(), F["Sm" + sfx])
+        assert np.array_equal(Spf[d].cpu().numpy(), F["Sp" + sfx])
+    # reflux: a covered rectangle (and part of the ghost ring) for the coarse register, a grid box for the fine one
+    mask = np.zeros((g.ny + 2 * G, g.nx + 2 * G), dtype=np.int32)
+    mask[10:25, 20:45] = 1
+    mask[30:, :4] = 1
+    Mk = dev(mask)
+    grid = ((0, 0), (g.nx - 1, g.ny - 1))
+    Eta, Uold, T = inputs()
+    Unew2 = torch.zeros_like(Unew)
+    fc, ff = faces(), faces()
+    ma = capi.Array4I32()
+    ma.p = ctypes.cast(ctypes.c_void_p(Mk.data_ptr()), ctypes.POINTER(ctypes.c_int32))
+    ma.jstride, ma.nstride = g.nx + 2 * G, (g.nx + 2 * G) * (g.ny + 2 * G)
+    ma.lo[0], ma.lo[1], ma.hi[0], ma.hi[1], ma.ncomp = -G, -G, g.nx - 1 + G, g.ny - 1 + G, 1
+    rc = hxlib.lib().hx_advance_box_roe_reflux_f64(ctypes.byref(array4(Eta, (-G, -G))),
+                                                   ctypes.byref(array4(Uold, (-G, -G))),
+                                                   ctypes.byref(array4(T, (-G, -G))), ctypes.byref(array4(Unew2)),
+                                                   vb, dt, g.dx, g.dy, ctypes.byref(ma), box(*grid), arr(fc), arr(ff),
+                                                   None, None, EXACT, None)
+    hxlib.check(rc, "classic reflux box")
+    assert torch.equal(Unew2, Unew)
+    for d, sfx in ((0, "x"), (1, "y")):
+        ref_c, ref_f = oracle_lib.roe_reflux_select(d, F["F" + sfx], F["Sm" + sfx], F["Sp" + sfx], (0, 0), mask,
+                                                    (-G, -G), grid)
+        assert np.array_equal(fc[d].cpu().numpy(), ref_c), sfx
+        assert np.array_equal(ff[d].cpu().numpy(), ref_f), sfx
+        assert np.count_nonzero(ref_c) > 0 and np.count_nonzero(ref_f) > 0
+
+
+def test_fp64_rate_probe(cuda, hxlib):
+    """The FP64 roof probe measures positive rates, FP32 well above FP64."""
+    d, f = capi.fp64_rates()
+    assert d > 1e10 and f > d

@@ -158,21 +158,23 @@ def test_fp32_advance(cuda, oracle_lib):
     assert rel_err(got, ref) <= 1e-5
 
 
-def test_host_buffer_run(cuda, oracle_lib, hxlib):
-    """hx_level_run_host_f64 (host buffers in, host buffers out) equals the
-    device-resident run."""
+@pytest.mark.parametrize("method,nx,ny,nsteps", [(1, 64, 48, 10), (1, 64, 48, 1), (1, 70, 45, 3), (0, 53, 61, 1)])
+def test_host_buffer_run(cuda, oracle_lib, hxlib, method, nx, ny, nsteps):
+    """hx_level_run_host_f64 (host buffers in, host buffers out; the last
+    step in row bands downloaded as they finish) equals the device-resident
+    run, partial bands included."""
     import ctypes
-    case = workloads.fractal_dam_break(64, 48, seed=4, amplitude=1.0)
+    case = workloads.fractal_dam_break(nx, ny, seed=4, amplitude=1.0, nodata_frac=0.2 if method else 0.0)
     h, hu, hv = case.h.copy(), case.hu.copy(), case.hv.copy()
     t = ctypes.c_double()
     lo = (ctypes.c_int32 * 2)(*case.geom.bc_lo)
     hi = (ctypes.c_int32 * 2)(*case.geom.bc_hi)
     P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
-    rc = hxlib.lib().hx_level_run_host_f64(1, 64, 48, case.geom.dx, case.geom.dy, lo, hi, P(h), P(hu), P(hv),
-                                           P(case.z), P(case.n), 10, case.cfl, EXACT, ctypes.byref(t), None)
+    rc = hxlib.lib().hx_level_run_host_f64(method, nx, ny, case.geom.dx, case.geom.dy, lo, hi, P(h), P(hu), P(hv),
+                                           P(case.z), P(case.n), nsteps, case.cfl, EXACT, ctypes.byref(t), None)
     assert rc == 0
     lev = to_level(case, case.h, case.hu, case.hv, cuda)
-    lev.run(1, 10, case.cfl, arith=EXACT)
+    lev.run(method, nsteps, case.cfl, arith=EXACT)
     got = lev.state.cpu().numpy()
     assert np.array_equal(got[0], h) and np.array_equal(got[1], hu) and np.array_equal(got[2], hv)
     assert t.value == lev.time.item()

@@ -96,3 +96,38 @@ def test_workloads_are_seeded_and_shaped():
     assert all(64 <= s <= 1024 and s % 16 == 0 for s in sides)
     case, gauges = workloads.adjoint_case(64, 64, ngauges=16)
     assert len(set(gauges.tolist())) == 16 and np.abs(case.z).max() == pytest.approx(0.3)
+
+
+def test_binomial_schedule_recomputes_the_optimal_number_of_steps(hxlib):
+    """hx_adjoint_recompute_steps under binomial checkpointing equals an
+    exhaustive optimum of the recursive schedule, less the steps the forward
+    sweep advances while it places the first snapshots."""
+    from functools import lru_cache
+
+    @lru_cache(None)
+    def opt(n, free):  # least forward steps to reverse n steps from a stored state with `free` spare slots
+        if n <= 1:
+            return 0
+        if free == 0:
+            return n * (n - 1) // 2
+        return min(m + opt(n - m, free - 1) + opt(m, free) for m in range(1, n))
+
+    def split(n, c):  # the optimal first advance (c slots including the start state)
+        return min(range(1, n), key=lambda m: (m + opt(n - m, c - 2) + opt(m, c - 1), m))
+
+    def chain_last(n, c):
+        a = 0
+        while n > 1 and c > 1:
+            k = split(n, c)
+            a, n, c = a + k, n - k, c - 1
+        return a
+
+    L = hxlib.lib()
+    for n in (1, 2, 3, 7, 20, 41, 64):
+        for c in (2, 3, 4, 6, 9):
+            cc = min(c, n + 1)
+            got = L.hx_adjoint_recompute_steps(n, -c)
+            assert got == opt(n, cc - 1) - chain_last(n, cc), (n, c, got)
+    assert L.hx_adjoint_recompute_steps(30, 0) == 0
+    assert L.hx_adjoint_recompute_steps(30, 7) == 30
+    assert L.hx_adjoint_recompute_steps(30, 31) == 0

@@ -102,3 +102,20 @@ def test_dam_break_against_exact_solution(oracle_lib):
         t += dt
     err = np.abs(h[0] - g["h_t0.1"]).mean()
     assert err < 1.5e-2
+
+
+def test_mass_diagnostics_excludes_nodata_and_dry_cells(oracle_lib):
+    """ComputeMassDiagnostics counts cells that are not NODATA (roughness
+    -9999) and wet; its sums are the plain sums over those cells."""
+    oracle = oracle_lib
+    c = workloads.fractal_dam_break(64, 48, seed=5, amplitude=1.0, nodata_frac=0.2)
+    c.hu = c.h * 0.3
+    c.hv = -c.h * 0.1
+    c.h[3, 3:9] = 0.0
+    dA = c.geom.dx * c.geom.dy
+    out = oracle.mass_diagnostics(c.h, c.hu, c.hv, c.n, c.geom.dx, c.geom.dy)
+    m = (c.n != -9999.0) & (c.h > 0)
+    np.testing.assert_allclose(out[:4], [(c.h[m] * dA).sum(), (c.hu[m] * dA).sum(), (c.hv[m] * dA).sum(),
+                                         (0.5 * (c.hu[m] ** 2 + c.hv[m] ** 2) / c.h[m] * dA).sum()], rtol=1e-13)
+    assert out[4] == c.h[m].min()
+    assert np.array_equal(oracle.derive_eta(c.h, c.z), c.h + c.z)
