@@ -326,14 +326,14 @@ int level_advance(int method, const L* lv, const StepCtl<R>& ctl, R* ho, R* huo,
 }
 
 template <class R, class L>
-int level_dt(const L* lv, hx_dt_accum* acc, cudaStream_t st, int arith = HX_ARITH_EXACT) {
+int level_dt(const L* lv, hx_dt_accum* acc, cudaStream_t st, int arith = HX_ARITH_EXACT, int j0 = 0, int j1 = -1) {
     if (!level_ok(lv)) return HX_ERR_ARG;
     if (!acc) return fail(HX_ERR_ARG, "null accumulator");
     Cells3<R> U;
     U.p[0] = lv->h; U.p[1] = lv->hu; U.p[2] = lv->hv;
     U.js = lv->pitch; U.lo0 = 0; U.lo1 = 0;
     Plane<R> Z{lv->z, lv->pitch, 0, 0};
-    const IBox vb{0, 0, lv->nx - 1, lv->ny - 1};
+    const IBox vb{0, j0, lv->nx - 1, j1 < 0 ? lv->ny - 1 : j1};  // rows j0..j1 (all by default)
     DtAccum* a = reinterpret_cast<DtAccum*>(acc);
     return launched(arith == HX_ARITH_EXACT ? launch_dt_reduce<R, false>(U, Z, vb, lv->dx, lv->dy, a, st)
                                             : launch_dt_reduce<R, true>(U, Z, vb, lv->dx, lv->dy, a, st),
@@ -396,19 +396,21 @@ template <class R> int accum_read(const hx_dt_accum* acc, R* dtmin, R* maxvel, c
 }
 
 // ---------------------------------------------------------------- host form
-// Device buffers of the host-buffer entry, kept between calls, and two copy
-// streams (transfers in both directions overlap each other and the step).
+// Device buffers of the host-buffer entry, kept between calls, and three
+// streams: uploads and downloads (one each: a copy engine does not interleave
+// two streams' queues, so bands go in order on one) and the CFL reduction of
+// the uploaded level, which then does not wait behind the flux work.
 constexpr int kHostBands = 8;
 struct HostCache {
     void* base = nullptr;
     size_t bytes = 0;
-    cudaStream_t cs[2] = {nullptr, nullptr};
-    cudaEvent_t ev[4 + kHostBands] = {};
+    cudaStream_t cs[3] = {nullptr, nullptr, nullptr};  // uploads, downloads, CFL reduction
+    cudaEvent_t ev[4 + 2 * kHostBands] = {};
     bool streams_ok = false;
     bool ensure_streams() {
         if (streams_ok) return true;
-        for (int k = 0; k < 2; ++k)
-            if (cudaStreamCreateWithFlags(&cs[k], cudaStreamNonBlocking) != cudaSuccess) return false;
+        for (auto& c : cs)
+            if (cudaStreamCreateWithFlags(&c, cudaStreamNonBlocking) != cudaSuccess) return false;
         for (auto& e : ev)
             if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return false;
         streams_ok = true;
@@ -630,8 +632,10 @@ int hx_level_run_host_f64(int method, int nx, int ny, double dx, double dy, cons
     if (nsteps < 0) return fail(HX_ERR_ARG, "nsteps < 0");
     if (!(cfl > 0)) return fail(HX_ERR_ARG, "cfl must be positive");
     if (method != HX_METHOD_ROE && method != HX_METHOD_HYDROSTATIC_ROE) return fail(HX_ERR_ARG, "unknown method");
+    // the hydrostatic first step is split: flux differences as the rows land, the update once dt is known
+    const bool split = method == HX_METHOD_HYDROSTATIC_ROE && nsteps >= 1;
     const size_t N = (size_t)nx * ny, pb = N * sizeof(double);
-    const size_t need = 8 * pb + 512;
+    const size_t need = (split ? 14 : 8) * pb + 512;
     if (g_host.bytes < need) {
         if (g_host.base) cudaFree(g_host.base);
         g_host.base = nullptr;
@@ -644,41 +648,116 @@ int hx_level_run_host_f64(int method, int nx, int ny, double dx, double dy, cons
     cudaStream_t* cs = g_host.cs;
     cudaEvent_t* ev = g_host.ev;
     double* d = (double*)g_host.base;
-    double* P[8];
-    for (int k = 0; k < 8; ++k) P[k] = d + k * N;
-    char* tail = (char*)(d + 8 * N);
+    double* P[14];
+    for (int k = 0; k < 14; ++k) P[k] = d + k * N;
+    char* tail = (char*)(d + (split ? 14 : 8) * N);
     uint32_t* status = (uint32_t*)tail;
     double* tdev = (double*)(tail + 64);
     DtAccum* slot = reinterpret_cast<DtAccum*>(tail + 128);
     const double* src[5] = {h, hu, hv, z, n};
-    // upload: each plane in row chunks over the two copy streams, after the caller's earlier work
-    cudaError_t e = cudaEventRecord(ev[0], st);
-    for (int k = 0; k < 2 && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(cs[k], ev[0], 0);
-    const int chunks = 4;
-    for (int k = 0; k < 5 && e == cudaSuccess; ++k)
-        for (int c = 0; c < chunks && e == cudaSuccess; ++c) {
-            const size_t r0 = (size_t)ny * c / chunks, r1 = (size_t)ny * (c + 1) / chunks;
-            e = cudaMemcpyAsync(P[k] + r0 * nx, src[k] + r0 * nx, (r1 - r0) * nx * sizeof(double),
-                                cudaMemcpyHostToDevice, cs[(k * chunks + c) & 1]);
-        }
-    for (int k = 0; k < 2 && e == cudaSuccess; ++k) e = cudaEventRecord(ev[1 + k], cs[k]);
-    for (int k = 0; k < 2 && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(st, ev[1 + k], 0);
-    if (e == cudaSuccess) e = cudaMemsetAsync(tail, 0, 128 + 3 * sizeof(DtAccum), st);
-    if (e != cudaSuccess) return fail(HX_ERR_CUDA, "upload: %s", cudaGetErrorString(e));
     hx_level_f64 L{P[0], P[1], P[2], P[3], P[4], (int64_t)nx, nx, ny, dx, dy, {bc_lo[0], bc_lo[1]}, {bc_hi[0], bc_hi[1]}};
-    int rc = level_dt<double>(&L, reinterpret_cast<hx_dt_accum*>(&slot[0]), st, arith);
+    const bool fast = arith != HX_ARITH_EXACT;
+    DivOut<double> div{{P[8], P[9], P[10], P[11], P[12], P[13]}, (long long)nx, 0, 0};
+    Cells3<double> uo;
+    uo.p[0] = P[0]; uo.p[1] = P[1]; uo.p[2] = P[2];
+    uo.js = nx; uo.lo0 = 0; uo.lo1 = 0;
+    const Plane<double> np{P[4], (long long)nx, 0, 0}, zp{P[3], (long long)nx, 0, 0};
+    const int band = ((ny + kHostBands - 1) / kHostBands + TY - 1) / TY * TY;
+    const int nbands = (ny + band - 1) / band;
+    auto rows = [&](int b, int& j0, int& j1) { j0 = b * band; j1 = (j0 + band < ny ? j0 + band : ny) - 1; };
+    auto flux_band = [&](int b) -> int {  // flux differences of band b (rows b-1 .. b+1 must have landed)
+        int j0, j1;
+        rows(b, j0, j1);
+        const LevelSrc<double> lsrc = level_src<double>(&L, 2);
+        const IBox vb{0, j0, nx - 1, j1};
+        return launched(fast ? launch_hydro_split<double, true>(lsrc, uo, np, div, vb, dx, dy, st)
+                             : launch_hydro_split<double, false>(lsrc, uo, np, div, vb, dx, dy, st),
+                        "hx_level_run_host_f64 (flux differences)");
+    };
+    // Upload in row bands (stream up), after the caller's earlier work.  The CFL reduction of each band runs
+    // as soon as its rows have landed.  Split: on its own stream, while st runs each band's flux differences
+    // once the band after it has landed, then each band's update once dt is known, the band's rows then
+    // going down (stream down) under the flux work of later bands.
+    cudaStream_t up = cs[0], down = cs[1], dts = cs[2];
+    cudaEvent_t* ev_up = ev + 4;
+    cudaEvent_t* ev_k = ev + 4 + kHostBands;
+    cudaError_t e = cudaMemsetAsync(tail, 0, 128 + 3 * sizeof(DtAccum), st);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[0], st);
+    for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(cs[k], ev[0], 0);
+    int rc = HX_OK;
+    cudaStream_t dstream = split ? dts : st;
+    for (int b = 0; b < nbands && e == cudaSuccess && rc == HX_OK; ++b) {
+        int j0, j1;
+        rows(b, j0, j1);
+        for (int k = 0; k < 5 && e == cudaSuccess; ++k)
+            e = cudaMemcpyAsync(P[k] + (size_t)j0 * nx, src[k] + (size_t)j0 * nx,
+                                (size_t)(j1 - j0 + 1) * nx * sizeof(double), cudaMemcpyHostToDevice, up);
+        if (e == cudaSuccess) e = cudaEventRecord(ev_up[b], up);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(dstream, ev_up[b], 0);
+        if (e == cudaSuccess)
+            rc = level_dt<double>(&L, reinterpret_cast<hx_dt_accum*>(&slot[0]), dstream, arith, j0, j1);
+    }
+    if (e == cudaSuccess && split) e = cudaEventRecord(ev[3], dts);
+    if (e != cudaSuccess) return fail(HX_ERR_CUDA, "upload: %s", cudaGetErrorString(e));
     if (rc) return rc;
-    // steps: all but the last in one launch each; the last in row bands, each band's rows downloaded (on the
-    // copy streams) while the next band computes
     const double* A[3] = {P[0], P[1], P[2]};
     double* B[3] = {P[5], P[6], P[7]};
     hx_level_f64 cur = L;
     const double* res[3] = {P[0], P[1], P[2]};
-    for (int s = 0; s < nsteps; ++s) {
-        StepCtl<double> ctl;
-        ctl.dt_host = 0.0; ctl.cfl = cfl;
-        ctl.dt_in = &slot[s % 3]; ctl.dt_out = &slot[(s + 1) % 3]; ctl.dt_reset = &slot[(s + 2) % 3];
-        ctl.status = status; ctl.time = tdev; ctl.dx = dx; ctl.dy = dy;
+    double* dst[3] = {h, hu, hv};
+    // step s's controls; b > 0 leaves the clock and the slot reset to band 0
+    auto step_ctl = [&](int s, int b) {
+        StepCtl<double> c;
+        c.dt_host = 0.0; c.cfl = cfl;
+        c.dt_in = &slot[s % 3]; c.dt_out = &slot[(s + 1) % 3]; c.dt_reset = b ? nullptr : &slot[(s + 2) % 3];
+        c.status = status; c.time = b ? nullptr : tdev; c.dx = dx; c.dy = dy;
+        return c;
+    };
+    auto download = [&](int b, double* const* o) -> cudaError_t {  // band b's rows of o, after st's work so far
+        int j0, j1;
+        rows(b, j0, j1);
+        cudaError_t r = cudaEventRecord(ev_k[b], st);
+        if (r == cudaSuccess) r = cudaStreamWaitEvent(down, ev_k[b], 0);
+        for (int k = 0; k < 3 && r == cudaSuccess; ++k)
+            r = cudaMemcpyAsync(dst[k] + (size_t)j0 * nx, o[k] + (size_t)j0 * nx,
+                                (size_t)(j1 - j0 + 1) * nx * sizeof(double), cudaMemcpyDeviceToHost, down);
+        return r;
+    };
+    int s0 = 0;
+    if (split) {
+        double* o[3] = {B[0], B[1], B[2]};
+        Cells3W<double> ow;
+        ow.p[0] = o[0]; ow.p[1] = o[1]; ow.p[2] = o[2];
+        ow.js = nx; ow.lo0 = 0; ow.lo1 = 0;
+        auto update_band = [&](int b) -> int {
+            int j0, j1;
+            rows(b, j0, j1);
+            const IBox vb{0, j0, nx - 1, j1};
+            const StepCtl<double> cb = step_ctl(0, b);
+            int r = launched(fast ? launch_hydro_update<double, true>(uo, div, np, zp, ow, vb, cb, st)
+                                  : launch_hydro_update<double, false>(uo, div, np, zp, ow, vb, cb, st),
+                             "hx_level_run_host_f64 (update)");
+            if (r == HX_OK && nsteps == 1) {
+                const cudaError_t de = download(b, o);
+                if (de != cudaSuccess) r = fail(HX_ERR_CUDA, "download: %s", cudaGetErrorString(de));
+            }
+            return r;
+        };
+        for (int b = 0; b < nbands && rc == HX_OK && e == cudaSuccess; ++b) {
+            e = cudaStreamWaitEvent(st, ev_up[b + 1 < nbands ? b + 1 : b], 0);  // rows b-1 .. b+1 have landed
+            if (e == cudaSuccess) rc = flux_band(b);
+            if (rc == HX_OK && b == 1) e = cudaStreamWaitEvent(st, ev[3], 0);  // dt of the whole level
+            if (rc == HX_OK && e == cudaSuccess && b >= 1) rc = update_band(b - 1);
+        }
+        if (rc == HX_OK && e == cudaSuccess && nbands == 1) e = cudaStreamWaitEvent(st, ev[3], 0);
+        if (rc == HX_OK && e == cudaSuccess) rc = update_band(nbands - 1);
+        if (e != cudaSuccess) return fail(HX_ERR_CUDA, "split step: %s", cudaGetErrorString(e));
+        if (rc) return rc;
+        res[0] = o[0]; res[1] = o[1]; res[2] = o[2];
+        s0 = 1;
+    }
+    // the other steps; the last one in row bands, each band's rows going down while the next computes
+    for (int s = s0; s < nsteps; ++s) {
         const bool even = (s % 2) == 0;
         cur.h = even ? A[0] : B[0];
         cur.hu = even ? A[1] : B[1];
@@ -686,35 +765,25 @@ int hx_level_run_host_f64(int method, int nx, int ny, double dx, double dy, cons
         double* o[3] = {even ? B[0] : const_cast<double*>(A[0]), even ? B[1] : const_cast<double*>(A[1]),
                         even ? B[2] : const_cast<double*>(A[2])};
         res[0] = o[0]; res[1] = o[1]; res[2] = o[2];
-        if (s < nsteps - 1) {
-            rc = level_advance<double>(method, &cur, ctl, o[0], o[1], o[2], arith, st);
+        const bool last = s == nsteps - 1;
+        for (int b = 0; b < (last ? nbands : 1); ++b) {
+            int j0 = 0, j1 = ny - 1;
+            if (last) rows(b, j0, j1);
+            rc = level_advance<double>(method, &cur, step_ctl(s, b), o[0], o[1], o[2], arith, st, j0, j1);
             if (rc) return rc;
-            continue;
-        }
-        const int band = ((ny + kHostBands - 1) / kHostBands + TY - 1) / TY * TY;
-        for (int b = 0; b * band < ny; ++b) {
-            const int j0 = b * band, j1 = (j0 + band < ny ? j0 + band : ny) - 1;
-            StepCtl<double> cb = ctl;
-            if (b > 0) { cb.time = nullptr; cb.dt_reset = nullptr; }  // once per step
-            rc = level_advance<double>(method, &cur, cb, o[0], o[1], o[2], arith, st, j0, j1);
-            if (rc) return rc;
-            cudaStream_t c = cs[b & 1];
-            e = cudaEventRecord(ev[4 + b], st);
-            if (e == cudaSuccess) e = cudaStreamWaitEvent(c, ev[4 + b], 0);
-            double* dst[3] = {h, hu, hv};
-            for (int k = 0; k < 3 && e == cudaSuccess; ++k)
-                e = cudaMemcpyAsync(dst[k] + (size_t)j0 * nx, o[k] + (size_t)j0 * nx,
-                                    (size_t)(j1 - j0 + 1) * nx * sizeof(double), cudaMemcpyDeviceToHost, c);
+            if (!last) continue;
+            e = download(b, o);
             if (e != cudaSuccess) return fail(HX_ERR_CUDA, "download: %s", cudaGetErrorString(e));
         }
     }
     if (nsteps == 0) {
-        double* dst[3] = {h, hu, hv};
+        e = cudaEventRecord(ev[1], st);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(down, ev[1], 0);
         for (int k = 0; k < 3 && e == cudaSuccess; ++k)
-            e = cudaMemcpyAsync(dst[k], res[k], pb, cudaMemcpyDeviceToHost, cs[k & 1]);
+            e = cudaMemcpyAsync(dst[k], res[k], pb, cudaMemcpyDeviceToHost, down);
     }
-    for (int k = 0; k < 2 && e == cudaSuccess; ++k) e = cudaEventRecord(ev[1 + k], cs[k]);
-    for (int k = 0; k < 2 && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(st, ev[1 + k], 0);
+    for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = cudaEventRecord(ev[1 + k], cs[k]);  // join all three
+    for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(st, ev[1 + k], 0);
     uint32_t sv = 0;
     double tv = 0;
     if (e == cudaSuccess) e = cudaMemcpyAsync(&sv, status, 4, cudaMemcpyDeviceToHost, st);

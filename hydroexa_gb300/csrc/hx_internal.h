@@ -10,6 +10,10 @@ namespace hx {
 constexpr int TX = 32;
 constexpr int TY = 8;
 constexpr int NT = TX * TY;
+// Rows of cells per thread in the per-cell kernels (CFL reduction, split
+// update): four 32 x 8 layers per block cut the blocks, and with them the
+// block-level atomics on the one dt accumulator, by four.
+constexpr int ROWS_PER_THREAD = 4;
 
 
 // Read-only load: through the read-only data cache for plain reals, a plain
@@ -68,7 +72,24 @@ template <class R> struct Cells3W {
     }
 };
 
-// Optional hydrostatic face output: FL/FR nodal arrays per direction, 3 comps.
+// No flux-difference output (the fused step).
+struct NoDiv {
+    static constexpr bool on = false;
+    template <class R> __device__ void st(int, int, R, R, R, R, R, R) const {}
+};
+// The six flux differences of every valid cell (dx0 dx1 dx2 dy0 dy1 dy2), for
+// a step whose update runs once dt is known.
+template <class R> struct DivOut {
+    static constexpr bool on = true;
+    R* p[6];
+    long long js;
+    int lo0, lo1;
+    __device__ __forceinline__ void st(int i, int j, R a, R b, R c, R d, R e, R f) const {
+        const long long o = (long long)(i - lo0) + (long long)(j - lo1) * js;
+        p[0][o] = a; p[1][o] = b; p[2][o] = c; p[3][o] = d; p[4][o] = e; p[5][o] = f;
+    }
+};
+
 // Optional hydrostatic face outputs: the FL/FR arrays (on), and/or the reflux
 // flux 0.5 FL + 0.5 FR the flux registers receive (mean,
 // src/solvers/HydrostaticRoe.cpp:612-627; the halves are exact, so the one

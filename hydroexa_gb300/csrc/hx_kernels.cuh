@@ -27,6 +27,7 @@ template <class R, int TXv = TX, int TYv = TY> struct HydroSmem {
     R fx[4][TYv][TXv + 1];                                      // x faces: F0, FL1, FR1, F2
     R fy[4][TYv + 1][TXv];                                      // y faces: F0, F1, FL2, FR2
     unsigned char nod[GY][GX];                                  // NODATA predicate of each grown-tile cell
+    R kc[4];  // dt/dx, dt/dy, 1/dx, 1/dy: computed once per tile, not once per cell
 };
 
 // One hydrostatic face (src/solvers/HydrostaticRoe.cpp:218-396).  L and R are
@@ -122,15 +123,92 @@ template <class R> __device__ __forceinline__ void step_bookkeeping(const StepCt
 // LINEAR: store the state after the flux update but before friction and the
 // dry clamp (used by the adjoint).  post_flags (optional): OR-ed with 1 when a
 // cell of the tile took the friction branch and 2 when one took the dry clamp.
-template <class R, bool FAST, int TXv, int TYv, int NTv, class Src, bool LINEAR = false>
+// The per-cell end of a step: the update of the stored state by the flux
+// differences (HydrostaticRoe.cpp:554-564), Manning friction and the dry clamp
+// (:566-603), the store, and the cell's share of the next CFL bound.  One
+// function for the fused tile kernel and the split update kernel, so both do
+// the same arithmetic.  LINEAR stores the updated state before friction and
+// clamp.  pflags: 1 if the Manning factor applied, 2 if the clamp did.
+template <class R, bool FAST, bool LINEAR>
+__device__ __forceinline__ void step_cell(R o0, R o1, R o2, R dx0, R dx1, R dx2, R dy0, R dy1, R dy2, R cx, R cy,
+                                          R dt, const Plane<R>& nplane, const Cells3W<R>& out, int gi, int gj,
+                                          bool nod, R dx, R dy, R idx, R idy, bool fold_dt, R& rate, R& mv,
+                                          unsigned& flags, unsigned& pflags) {
+    R un[3];
+    un[0] = (o0 - cx * dx0) - cy * dy0;
+    un[1] = (o1 - cx * dx1) - cy * dy1;
+    un[2] = (o2 - cx * dx2) - cy * dy2;
+    if constexpr (LINEAR) {
+        out.st(gi, gj, un[0], un[1], un[2]);
+        return;
+    }
+    const R hh = un[0];
+    bool wet, rough;
+    if constexpr (FAST) wet = ge_bits(hh, Cst<R>::toldry_bits);
+    else wet = hh >= Cst<R>::toldry;
+    if (wet) {
+        const R nv = nplane.ld(gi, gj);
+        const R nsq = nv * nv;
+        if constexpr (FAST) rough = gt_bits(nsq, Cst<R>::tol12_bits);
+        else rough = nsq > Cst<R>::tol12;
+        if (rough) {  // the friction factor needs a rough bed
+            const R qx = un[1], qy = un[2];
+            R modM;
+            if constexpr (!FAST) {
+                const R inv_h = R(1.0) / hh;
+                const R uu = qx * inv_h, vv = qy * inv_h;
+                modM = sqrt(uu * uu + vv * vv);
+            } else {
+                modM = sqrt(qx * qx + qy * qy) * rcp_nr(hh);
+            }
+            if (modM > Cst<R>::tol12) {
+                pflags |= 1u;
+                const R h43 = hh * cbrt(hh);
+                const R tt = dt * Cst<R>::g * nsq * modM / h43;
+                const R ff = sqrt(R(1.0) + R(4.0) * tt);
+                const R fac = R(2.0) / (R(1.0) + ff);
+                un[1] = qx * fac;
+                un[2] = qy * fac;
+            }
+        }
+    } else {
+        pflags |= 2u;
+        if constexpr (FAST) un[0] = neg_i(hh) ? R(0) : hh;
+        else un[0] = smax(hh, R(0));
+        un[1] = R(0);
+        un[2] = R(0);
+    }
+    out.st(gi, gj, un[0], un[1], un[2]);
+    if (bits_nonfinite(un[0]) || bits_nonfinite(un[1]) || bits_nonfinite(un[2])) flags |= DTF_NAN;
+    if (fold_dt) {
+        R rc, mc;
+        dt_cell_contrib<R, FAST>(un[0], un[1], un[2], nod, dx, dy, idx, idy, rc, mc, flags);
+        if constexpr (FAST) {
+            rate = nnmax_i(rate, rc);
+            mv = nnmax_i(mv, mc);
+        } else {
+            rate = smax(rate, rc);
+            mv = smax(mv, mc);
+        }
+    }
+}
+
+template <class R, bool FAST, int TXv, int TYv, int NTv, class Src, bool LINEAR = false, class Div = NoDiv>
 __device__ __forceinline__ void hydro_tile_body(HydroSmem<R, TXv, TYv>& S, const Src& src, const Cells3<R>& uo,
                                                 const Plane<R>& nplane, const Cells3W<R>& out, const FaceOut<R>& fo,
                                                 const IBox& vb, int x0, int y0, R dt, R dx, R dy, DtAccum* dt_out,
-                                                unsigned* status, unsigned* post_flags = nullptr) {
+                                                unsigned* status, unsigned* post_flags = nullptr,
+                                                const Div& div = Div{}) {
     constexpr int GX = HydroSmem<R, TXv, TYv>::GX, GY = HydroSmem<R, TXv, TYv>::GY;
     constexpr int CELLS = TXv * TYv;
     const int t = threadIdx.x;
     __syncthreads();  // the previous tile of this block is done with S
+    if (t == 0) {     // read after the barriers below
+        S.kc[0] = dt / dx;
+        S.kc[1] = dt / dy;
+        S.kc[2] = R(1) / dx;
+        S.kc[3] = R(1) / dy;
+    }
 
     // --- A: grown tile -> h rebuilt, eta = h + z, velocities -----------------
     for (int idx = t; idx < GX * GY; idx += NTv) {
@@ -225,76 +303,25 @@ __device__ __forceinline__ void hydro_tile_body(HydroSmem<R, TXv, TYv>& S, const
     // --- D: update, Manning friction, dry clamp (HydrostaticRoe.cpp:551-604) --
     R rate = R(0), mv = R(0);
     unsigned flags = 0, pflags = 0;
-    const R cx = dt / dx, cy = dt / dy;
+    const R cx = S.kc[0], cy = S.kc[1], idx = S.kc[2], idy = S.kc[3];
     for (int k = t; k < CELLS; k += NTv) {
         const int tx = k % TXv, ty = k / TXv;
         const int gi = x0 + tx, gj = y0 + ty;
         if (gi > vb.hi0 || gj > vb.hi1) continue;
-        R un[3];
-        const R o0 = uo.ld(0, gi, gj), o1 = uo.ld(1, gi, gj), o2 = uo.ld(2, gi, gj);
         const R dx0 = S.fx[0][ty][tx + 1] - S.fx[0][ty][tx];
         const R dx1 = S.fx[1][ty][tx + 1] - S.fx[2][ty][tx];
         const R dx2 = S.fx[3][ty][tx + 1] - S.fx[3][ty][tx];
         const R dy0 = S.fy[0][ty + 1][tx] - S.fy[0][ty][tx];
         const R dy1 = S.fy[1][ty + 1][tx] - S.fy[1][ty][tx];
         const R dy2 = S.fy[2][ty + 1][tx] - S.fy[3][ty][tx];
-        un[0] = (o0 - cx * dx0) - cy * dy0;
-        un[1] = (o1 - cx * dx1) - cy * dy1;
-        un[2] = (o2 - cx * dx2) - cy * dy2;
-        if constexpr (LINEAR) {
-            out.st(gi, gj, un[0], un[1], un[2]);
+        if constexpr (Div::on) {  // the flux differences only: the update waits for dt
+            div.st(gi, gj, dx0, dx1, dx2, dy0, dy1, dy2);
             continue;
         }
-        const R hh = un[0];
-        bool wet, rough;
-        if constexpr (FAST) wet = ge_bits(hh, Cst<R>::toldry_bits);
-        else wet = hh >= Cst<R>::toldry;
-        if (wet) {
-            const R nv = nplane.ld(gi, gj);
-            const R nsq = nv * nv;
-            if constexpr (FAST) rough = gt_bits(nsq, Cst<R>::tol12_bits);
-            else rough = nsq > Cst<R>::tol12;
-            if (rough) {  // the friction factor needs a rough bed
-                const R qx = un[1], qy = un[2];
-                R modM;
-                if constexpr (!FAST) {
-                    const R inv_h = R(1.0) / hh;
-                    const R uu = qx * inv_h, vv = qy * inv_h;
-                    modM = sqrt(uu * uu + vv * vv);
-                } else {
-                    modM = sqrt(qx * qx + qy * qy) * rcp_nr(hh);
-                }
-                if (modM > Cst<R>::tol12) {
-                    pflags |= 1u;
-                    const R h43 = hh * cbrt(hh);
-                    const R tt = dt * Cst<R>::g * nsq * modM / h43;
-                    const R ff = sqrt(R(1.0) + R(4.0) * tt);
-                    const R fac = R(2.0) / (R(1.0) + ff);
-                    un[1] = qx * fac;
-                    un[2] = qy * fac;
-                }
-            }
-        } else {
-            pflags |= 2u;
-            if constexpr (FAST) un[0] = neg_i(hh) ? R(0) : hh;
-            else un[0] = smax(hh, R(0));
-            un[1] = R(0);
-            un[2] = R(0);
-        }
-        out.st(gi, gj, un[0], un[1], un[2]);
-        if (bits_nonfinite(un[0]) || bits_nonfinite(un[1]) || bits_nonfinite(un[2])) flags |= DTF_NAN;
-        if (dt_out) {
-            R rc, mc;
-            dt_cell_contrib<R, FAST>(un[0], un[1], un[2], S.nod[ty + 2][tx + 2] != 0, dx, dy, R(1) / dx, R(1) / dy,
-                                     rc, mc, flags);
-            if constexpr (FAST) {
-                rate = nnmax_i(rate, rc);
-                mv = nnmax_i(mv, mc);
-            } else {
-                rate = smax(rate, rc);
-                mv = smax(mv, mc);
-            }
-        }
+        const R o0 = uo.ld(0, gi, gj), o1 = uo.ld(1, gi, gj), o2 = uo.ld(2, gi, gj);
+        step_cell<R, FAST, LINEAR>(o0, o1, o2, dx0, dx1, dx2, dy0, dy1, dy2, cx, cy, dt, nplane, out, gi, gj,
+                                   S.nod[ty + 2][tx + 2] != 0, dx, dy, idx, idy, dt_out != nullptr, rate, mv, flags,
+                                   pflags);
     }
     if (dt_out) block_fold_dt<R, NTv>(rate, mv, flags, dt_out);
     if ((flags & DTF_NAN) && status) atomicOr(status, (unsigned)HX_STATUS_NAN);
@@ -314,6 +341,50 @@ __global__ void __launch_bounds__(NT) k_hydro_tile(Src src, Cells3<R> uo, Plane<
     step_bookkeeping(ctl, dt);
     hydro_tile_body<R, FAST, TX, TY, NT>(S, src, uo, nplane, out, fo, vb, vb.lo0 + (int)blockIdx.x * TX,
                                          vb.lo1 + (int)blockIdx.y * TY, dt, ctl.dx, ctl.dy, ctl.dt_out, ctl.status);
+}
+
+// ---------------------------------------------------------------------------
+// A hydrostatic step split in two, for a caller that receives its level while
+// the step starts (the host-buffer entry): the flux differences of every cell
+// need no dt and run band by band as the rows arrive; the update applies dt
+// once the CFL bound of the whole level is known.  Together they do exactly
+// the fused kernel's arithmetic.
+// ---------------------------------------------------------------------------
+template <class R, bool FAST>
+__global__ void __launch_bounds__(NT) k_hydro_div(LevelSrc<R> src, Cells3<R> uo, Plane<R> nplane, DivOut<R> div,
+                                                  IBox vb, R dx, R dy) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    HydroSmem<R>& S = *reinterpret_cast<HydroSmem<R>*>(smem_raw);
+    FaceOut<R> fo{};
+    Cells3W<R> none{};
+    hydro_tile_body<R, FAST, TX, TY, NT, LevelSrc<R>, false, DivOut<R>>(
+        S, src, uo, nplane, none, fo, vb, vb.lo0 + (int)blockIdx.x * TX, vb.lo1 + (int)blockIdx.y * TY, R(0), dx, dy,
+        nullptr, nullptr, nullptr, div);
+}
+
+template <class R, bool FAST>
+__global__ void __launch_bounds__(NT) k_hydro_update(Cells3<R> uo, DivOut<R> div, Plane<R> nplane, Plane<R> zplane,
+                                                     Cells3W<R> out, IBox vb, StepCtl<R> ctl) {
+    __shared__ R kc[4];
+    R dt;
+    if (!resolve_dt(ctl, dt)) return;
+    step_bookkeeping(ctl, dt);
+    if (threadIdx.x == 0) { kc[0] = dt / ctl.dx; kc[1] = dt / ctl.dy; kc[2] = R(1) / ctl.dx; kc[3] = R(1) / ctl.dy; }
+    __syncthreads();
+    R rate = R(0), mv = R(0);
+    unsigned flags = 0, pflags = 0;
+    const int gi = vb.lo0 + (int)blockIdx.x * TX + (threadIdx.x % TX);
+    for (int r = 0; r < ROWS_PER_THREAD; ++r) {  // a 32 x (8 ROWS) block: fewer blocks, fewer dt atomics
+        const int gj = vb.lo1 + ((int)blockIdx.y * ROWS_PER_THREAD + r) * TY + (threadIdx.x / TX);
+        if (gi > vb.hi0 || gj > vb.hi1) continue;
+        const long long o = (long long)(gi - div.lo0) + (long long)(gj - div.lo1) * div.js;
+        step_cell<R, FAST, false>(uo.ld(0, gi, gj), uo.ld(1, gi, gj), uo.ld(2, gi, gj), div.p[0][o], div.p[1][o],
+                                  div.p[2][o], div.p[3][o], div.p[4][o], div.p[5][o], kc[0], kc[1], dt, nplane, out,
+                                  gi, gj, is_nodata(zplane.ld(gi, gj)), ctl.dx, ctl.dy, kc[2], kc[3],
+                                  ctl.dt_out != nullptr, rate, mv, flags, pflags);
+    }
+    if (ctl.dt_out) block_fold_dt<R, NT>(rate, mv, flags, ctl.dt_out);
+    if ((flags & DTF_NAN) && ctl.status) atomicOr(ctl.status, (unsigned)HX_STATUS_NAN);
 }
 
 // ---------------------------------------------------------------------------
@@ -411,6 +482,7 @@ template <class R> struct ClassicSmem {
     R h[GY][GX], hu[GY][GX], hv[GY][GX], z[GY][GX], n[GY][GX];
     R fx[9][TY][TX + 1];  // F0..2, S-0..2, S+0..2
     R fy[9][TY + 1][TX];
+    R kc[4];  // dt/dx, dt/dy, 1/dx, 1/dy: computed once per tile
 };
 
 template <class R, bool FAST, class Src>
@@ -425,6 +497,12 @@ __global__ void __launch_bounds__(NT) k_classic_tile(Src src, Cells3W<R> out, Fa
     step_bookkeeping(ctl, dt);
 
     const int t = threadIdx.x;
+    if (t == 0) {  // read after the loader's barrier
+        S.kc[0] = dt / ctl.dx;
+        S.kc[1] = dt / ctl.dy;
+        S.kc[2] = R(1) / ctl.dx;
+        S.kc[3] = R(1) / ctl.dy;
+    }
     const int tx = t & (TX - 1), ty = t / TX;
     const int x0 = vb.lo0 + blockIdx.x * TX;
     const int y0 = vb.lo1 + blockIdx.y * TY;
@@ -478,7 +556,7 @@ __global__ void __launch_bounds__(NT) k_classic_tile(Src src, Cells3W<R> out, Fa
     R rate = R(0), mv = R(0);
     unsigned flags = 0;
     if (valid) {
-        const R cx = dt / ctl.dx, cy = dt / ctl.dy;
+        const R cx = S.kc[0], cy = S.kc[1];
         const R uo[3] = {S.h[ty + 1][tx + 1], S.hu[ty + 1][tx + 1], S.hv[ty + 1][tx + 1]};
         R un[3];
 #pragma unroll
@@ -492,7 +570,7 @@ __global__ void __launch_bounds__(NT) k_classic_tile(Src src, Cells3W<R> out, Fa
         if (bits_nonfinite(un[0]) || bits_nonfinite(un[1]) || bits_nonfinite(un[2])) flags |= DTF_NAN;
         if (ctl.dt_out) {
             dt_cell_contrib<R, FAST>(un[0], un[1], un[2], is_nodata(S.z[ty + 1][tx + 1]), ctl.dx, ctl.dy,
-                                     R(1) / ctl.dx, R(1) / ctl.dy, rate, mv, flags);
+                                     S.kc[2], S.kc[3], rate, mv, flags);
         }
     }
     if (ctl.dt_out) block_fold_dt<R, NT>(rate, mv, flags, ctl.dt_out);
@@ -503,14 +581,25 @@ __global__ void __launch_bounds__(NT) k_classic_tile(Src src, Cells3W<R> out, Fa
 // compute_dt_Impl over a box (HydrostaticRoe.cpp:19-65, Roe.cpp:20-76).
 // ---------------------------------------------------------------------------
 template <class R, bool FAST>
-__global__ void __launch_bounds__(NT) k_dt_reduce(Cells3<R> U, Plane<R> Z, IBox vb, R dx, R dy, DtAccum* acc) {
+__global__ void __launch_bounds__(NT) k_dt_reduce(Cells3<R> U, Plane<R> Z, IBox vb, R dx, R dy, R idx, R idy,
+                                                  DtAccum* acc) {
     const int i = vb.lo0 + blockIdx.x * TX + (threadIdx.x & (TX - 1));
-    const int j = vb.lo1 + blockIdx.y * TY + threadIdx.x / TX;
     R rate = R(0), mv = R(0);
     unsigned flags = 0;
-    if (i <= vb.hi0 && j <= vb.hi1)
-        dt_cell_contrib<R, FAST>(U.ld(0, i, j), U.ld(1, i, j), U.ld(2, i, j), is_nodata(Z.ld(i, j)), dx, dy,
-                                 R(1) / dx, R(1) / dy, rate, mv, flags);
+    for (int r = 0; r < ROWS_PER_THREAD; ++r) {  // a 32 x (8 ROWS) block: fewer blocks, fewer atomics
+        const int j = vb.lo1 + ((int)blockIdx.y * ROWS_PER_THREAD + r) * TY + threadIdx.x / TX;
+        if (i > vb.hi0 || j > vb.hi1) continue;
+        R rc, mc;
+        dt_cell_contrib<R, FAST>(U.ld(0, i, j), U.ld(1, i, j), U.ld(2, i, j), is_nodata(Z.ld(i, j)), dx, dy, idx,
+                                 idy, rc, mc, flags);
+        if constexpr (FAST) {
+            rate = nnmax_i(rate, rc);
+            mv = nnmax_i(mv, mc);
+        } else {
+            rate = smax(rate, rc);
+            mv = smax(mv, mc);
+        }
+    }
     block_fold_dt<R, NT>(rate, mv, flags, acc);
 }
 
@@ -797,9 +886,28 @@ int ensemble_blocks_per_sm() {
 }
 
 template <class R, bool FAST>
+cudaError_t launch_hydro_split(const LevelSrc<R>& src, const Cells3<R>& uo, const Plane<R>& np, const DivOut<R>& div,
+                               const IBox& vb, R dx, R dy, cudaStream_t st) {
+    const size_t sm = sizeof(HydroSmem<R>);
+    cudaError_t e = ensure_smem(k_hydro_div<R, FAST>, sm);
+    if (e != cudaSuccess) return e;
+    k_hydro_div<R, FAST><<<tile_grid(vb, TX, TY), NT, sm, st>>>(src, uo, np, div, vb, dx, dy);
+    return cudaGetLastError();
+}
+
+template <class R, bool FAST>
+cudaError_t launch_hydro_update(const Cells3<R>& uo, const DivOut<R>& div, const Plane<R>& np, const Plane<R>& zp,
+                                const Cells3W<R>& out, const IBox& vb, const StepCtl<R>& ctl, cudaStream_t st) {
+    k_hydro_update<R, FAST><<<tile_grid(vb, TX, TY * ROWS_PER_THREAD), NT, 0, st>>>(uo, div, np, zp, out, vb, ctl);
+    return cudaGetLastError();
+}
+
+template <class R, bool FAST>
 cudaError_t launch_dt_reduce(const Cells3<R>& U, const Plane<R>& Z, const IBox& vb, R dx, R dy, DtAccum* acc,
                              cudaStream_t st) {
-    k_dt_reduce<R, FAST><<<tile_grid(vb, TX, TY), NT, 0, st>>>(U, Z, vb, dx, dy, acc);
+    // 1/dx, 1/dy correctly rounded on the host: the same values the device would compute
+    k_dt_reduce<R, FAST><<<tile_grid(vb, TX, TY * ROWS_PER_THREAD), NT, 0, st>>>(U, Z, vb, dx, dy, R(1) / dx,
+                                                                                 R(1) / dy, acc);
     return cudaGetLastError();
 }
 

@@ -16,6 +16,15 @@ template <class R, bool FAST, class Src>
 cudaError_t launch_classic(const Src& src, const Cells3W<R>& out, const FaceOut9<R>& fo, const RebuildOut<R>& hb,
                            const IBox& vb, const StepCtl<R>& ctl, cudaStream_t st);
 
+// The hydrostatic step in two launches: flux differences (no dt), then the
+// update once dt is known (same arithmetic as launch_hydro).
+template <class R, bool FAST>
+cudaError_t launch_hydro_split(const LevelSrc<R>& src, const Cells3<R>& uo, const Plane<R>& np, const DivOut<R>& div,
+                               const IBox& vb, R dx, R dy, cudaStream_t st);
+template <class R, bool FAST>
+cudaError_t launch_hydro_update(const Cells3<R>& uo, const DivOut<R>& div, const Plane<R>& np, const Plane<R>& zp,
+                                const Cells3W<R>& out, const IBox& vb, const StepCtl<R>& ctl, cudaStream_t st);
+
 template <class R, bool FAST>
 cudaError_t launch_dt_reduce(const Cells3<R>& U, const Plane<R>& Z, const IBox& vb, R dx, R dy, DtAccum* acc,
                              cudaStream_t st);
