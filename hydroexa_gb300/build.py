@@ -1,6 +1,6 @@
 """Build the CUDA library ``hydroexa_gb300/libhydroexa_gb300.so`` for sm_103a.
 
-Seven translation units compiled in parallel, then linked:
+Eight translation units compiled in parallel, then linked:
 
 * ``hx_exact.cu``  -- exact arithmetic form, ``--fmad=false`` (no multiply-add
   contraction, the reference's host rounding); tags and restriction kernels.
@@ -10,6 +10,7 @@ Seven translation units compiled in parallel, then linked:
 * ``hx_ensemble.cu`` -- the batched-ensemble plan, dt initialisation and CUDA-graph replay.
 * ``hx_adjoint.cu`` -- the hand-written adjoint of the hydrostatic-Roe time loop and its drivers.
 * ``hx_roofs.cu`` -- the FP64 issue-rate probe (the roof the FP64-bound kernels are reported against).
+* ``hx_boxlevel.cu`` -- the multi-box level (same-level ghosts read from neighbouring boxes).
 
 The build is in-tree (objects in ``_build/``), takes well under a minute, and
 needs only nvcc; the CUDA runtime is linked statically so the library loads
@@ -39,6 +40,7 @@ UNITS = {
     "hx_ensemble": [],
     "hx_adjoint": [],
     "hx_roofs": [],
+    "hx_boxlevel": [],
 }
 
 

@@ -61,6 +61,12 @@ LevelF64 = _level(c_double)
 LevelF32 = _level(c_float)
 
 
+class LevelBoxF64(Structure):
+    _fields_ = [("h", c_void_p), ("hu", c_void_p), ("hv", c_void_p), ("h_alt", c_void_p), ("hu_alt", c_void_p),
+                ("hv_alt", c_void_p), ("z", c_void_p), ("n", c_void_p), ("pitch", c_int64), ("lo", c_int32 * 2),
+                ("hi", c_int32 * 2)]
+
+
 class EnsembleMemberF64(Structure):
     _fields_ = [("level", LevelF64), ("h_alt", c_void_p), ("hu_alt", c_void_p), ("hv_alt", c_void_p),
                 ("tile_shape", c_int32)]
@@ -137,6 +143,11 @@ def _declare(L):
                                          c_void_p, c_void_p]
     L.hx_level_diagnostics_f64.argtypes = [POINTER(LevelF64), c_void_p, c_void_p, c_void_p]
     L.hx_measure_fp64_rate.argtypes = [POINTER(c_double), POINTER(c_double), c_void_p]
+    L.hx_boxlevel_work_bytes.restype = c_int64
+    L.hx_boxlevel_work_bytes.argtypes = [c_int, POINTER(LevelBoxF64), c_int, c_int]
+    L.hx_boxlevel_run_f64.argtypes = [c_int, POINTER(LevelBoxF64), c_int, c_int, c_double, c_double,
+                                      POINTER(c_int32), POINTER(c_int32), c_int, c_double, c_int, c_void_p, c_void_p,
+                                      c_void_p, POINTER(c_int), c_void_p]
     L.hx_adjoint_work_bytes_f64.restype = c_int64
     L.hx_adjoint_work_bytes_f64.argtypes = [c_int, c_int, c_int64, c_int, c_int]
     L.hx_adjoint_recompute_steps.restype = c_int64
@@ -185,7 +196,8 @@ EXPORTED = [
     "hx_advance_box_roe_reflux_f64", "hx_advance_box_roe_reflux_f32", "hx_dt_reduce_box_f64", "hx_dt_reduce_box_f32", "hx_tag_box_f64", "hx_tag_box_f32",
     "hx_masked_average_down_box_f64", "hx_masked_average_down_box_f32", "hx_derive_eta_box_f64",
     "hx_derive_eta_box_f32", "hx_diagnostics_work_bytes", "hx_diagnostics_box_f64", "hx_diagnostics_box_f32",
-    "hx_level_diagnostics_f64", "hx_measure_fp64_rate", "hx_level_advance_f64",
+    "hx_level_diagnostics_f64", "hx_measure_fp64_rate", "hx_boxlevel_work_bytes", "hx_boxlevel_run_f64",
+    "hx_level_advance_f64",
     "hx_level_advance_f32", "hx_level_dt_reduce_f64", "hx_level_dt_reduce_f32", "hx_level_run_work_bytes",
     "hx_level_run_f64", "hx_level_run_f32", "hx_level_run_host_f64", "hx_host_cache_release",
     "hx_debug_roe_points_f64", "hx_debug_roe_points_f32", "hx_level_run_static_f64",

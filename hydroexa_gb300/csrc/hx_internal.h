@@ -240,6 +240,57 @@ template <class R> struct LevelSrc {
     }
 };
 
+// A level of several boxes (a same-level BoxArray).  Each box keeps its own
+// valid-cell arrays; a ghost of one box inside the domain is read from the
+// box that owns that cell, found through a map of the domain at the boxes'
+// common granularity, and one outside the domain follows the physical rules
+// of LevelSrc (reflect / extrapolate, terrain always extrapolated) before the
+// lookup.  This replaces the FillPatch of same-level and physical ghosts.
+struct DevBox {
+    const double *h[2], *hu[2], *hv[2];  // the two states of the time loop
+    const double *z, *n;
+    long long pitch;
+    int lo0, lo1, hi0, hi1;
+};
+struct BoxSetSrc {
+    const DevBox* boxes;
+    const int* map;   // box index of each g x g block of the domain
+    int g, mnx;       // granularity, map row length
+    int nx, ny;
+    int bc_xlo, bc_xhi, bc_ylo, bc_yhi;
+    int self, phase;  // the tile's box, which state is current
+    int glo0, glo1, ghi0, ghi1;
+    __device__ __forceinline__ bool inside(int i, int j) const {
+        return i >= glo0 && i <= ghi0 && j >= glo1 && j <= ghi1;
+    }
+    __device__ __forceinline__ int owner(int i, int j) const {
+        const DevBox& b = boxes[self];
+        if (i >= b.lo0 && i <= b.hi0 && j >= b.lo1 && j <= b.hi1) return self;
+        return ld_ro(map + (long long)(j / g) * mnx + i / g);
+    }
+    __device__ __forceinline__ void fetch(int i, int j, double& eta, double& zz, double& qx, double& qy,
+                                          double& nn) const {
+        int mi = i, mj = j;
+        bool nx_neg = false, ny_neg = false;
+        if (i < 0) { if (bc_xlo == 0) { mi = -1 - i; nx_neg = true; } else mi = 0; }
+        else if (i >= nx) { if (bc_xhi == 0) { mi = 2 * nx - 1 - i; nx_neg = true; } else mi = nx - 1; }
+        if (j < 0) { if (bc_ylo == 0) { mj = -1 - j; ny_neg = true; } else mj = 0; }
+        else if (j >= ny) { if (bc_yhi == 0) { mj = 2 * ny - 1 - j; ny_neg = true; } else mj = ny - 1; }
+        const int ei = i < 0 ? 0 : (i >= nx ? nx - 1 : i);
+        const int ej = j < 0 ? 0 : (j >= ny ? ny - 1 : j);
+        const DevBox& bm = boxes[owner(mi, mj)];
+        const DevBox& be = boxes[owner(ei, ej)];
+        const long long pm = (long long)(mi - bm.lo0) + (long long)(mj - bm.lo1) * bm.pitch;
+        const long long pe = (long long)(ei - be.lo0) + (long long)(ej - be.lo1) * be.pitch;
+        eta = ld_ro(bm.h[phase] + pm) + ld_ro(bm.z + pm);
+        zz = ld_ro(be.z + pe);
+        nn = ld_ro(be.n + pe);
+        const double a = ld_ro(bm.hu[phase] + pm), b = ld_ro(bm.hv[phase] + pm);
+        qx = nx_neg ? -a : a;
+        qy = ny_neg ? -b : b;
+    }
+};
+
 // A box whose ghosts were filled by AMReX (FillPatch): read them as they are.
 template <class R> struct BoxSrc {
     V4<R> eta, U, T;  // eta comp 0; U comps 1,2 (hu, hv); T comps 0,1 (z, n)

@@ -388,6 +388,36 @@ __global__ void __launch_bounds__(NT) k_hydro_update(Cells3<R> uo, DivOut<R> div
 }
 
 // ---------------------------------------------------------------------------
+// One step of a multi-box level: one block per tile of any box (tiles[k] =
+// box, x0, y0), ghosts from the neighbouring boxes (BoxSetSrc), one dt chain.
+// ---------------------------------------------------------------------------
+template <bool FAST>
+__global__ void __launch_bounds__(NT) k_boxlevel_hydro(BoxSetSrc base, const int* tiles, StepCtl<double> ctl) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    HydroSmem<double>& S = *reinterpret_cast<HydroSmem<double>*>(smem_raw);
+    double dt;
+    if (!resolve_dt(ctl, dt)) return;
+    step_bookkeeping(ctl, dt);
+    const int b = tiles[3 * blockIdx.x], x0 = tiles[3 * blockIdx.x + 1], y0 = tiles[3 * blockIdx.x + 2];
+    const DevBox& B = base.boxes[b];
+    BoxSetSrc src = base;
+    src.self = b;
+    const int cur = base.phase, nxt = 1 - base.phase;
+    Cells3<double> uo;
+    uo.p[0] = B.h[cur]; uo.p[1] = B.hu[cur]; uo.p[2] = B.hv[cur];
+    uo.js = B.pitch; uo.lo0 = B.lo0; uo.lo1 = B.lo1;
+    Cells3W<double> out;
+    out.p[0] = const_cast<double*>(B.h[nxt]); out.p[1] = const_cast<double*>(B.hu[nxt]);
+    out.p[2] = const_cast<double*>(B.hv[nxt]);
+    out.js = B.pitch; out.lo0 = B.lo0; out.lo1 = B.lo1;
+    const Plane<double> np{B.n, B.pitch, B.lo0, B.lo1};
+    const IBox vb{B.lo0, B.lo1, B.hi0, B.hi1};
+    FaceOut<double> fo{};
+    hydro_tile_body<double, FAST, TX, TY, NT>(S, src, uo, np, out, fo, vb, x0, y0, dt, ctl.dx, ctl.dy, ctl.dt_out,
+                                              ctl.status);
+}
+
+// ---------------------------------------------------------------------------
 // Batched ensemble: many independent single-box levels advanced by one
 // persistent launch per step.  The launch drains a queue of tiles that spans
 // every instance; each instance keeps its own dt chain (three rotating
@@ -883,6 +913,17 @@ int ensemble_blocks_per_sm() {
         cudaSuccess)
         return 0;
     return n;
+}
+
+template <bool FAST>
+cudaError_t launch_boxlevel(const BoxSetSrc& src, const int* tiles, int ntiles, const StepCtl<double>& ctl,
+                            cudaStream_t st) {
+    if (ntiles <= 0) return cudaSuccess;
+    const size_t sm = sizeof(HydroSmem<double>);
+    cudaError_t e = ensure_smem(k_boxlevel_hydro<FAST>, sm);
+    if (e != cudaSuccess) return e;
+    k_boxlevel_hydro<FAST><<<ntiles, NT, sm, st>>>(src, tiles, ctl);
+    return cudaGetLastError();
 }
 
 template <class R, bool FAST>

@@ -16,6 +16,11 @@ template <class R, bool FAST, class Src>
 cudaError_t launch_classic(const Src& src, const Cells3W<R>& out, const FaceOut9<R>& fo, const RebuildOut<R>& hb,
                            const IBox& vb, const StepCtl<R>& ctl, cudaStream_t st);
 
+// One hydrostatic step of a multi-box level (one block per tile of the tile table).
+template <bool FAST>
+cudaError_t launch_boxlevel(const BoxSetSrc& src, const int* tiles, int ntiles, const StepCtl<double>& ctl,
+                            cudaStream_t st);
+
 // The hydrostatic step in two launches: flux differences (no dt), then the
 // update once dt is known (same arithmetic as launch_hydro).
 template <class R, bool FAST>

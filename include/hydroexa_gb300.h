@@ -491,6 +491,40 @@ int hx_adjoint_step_f64(const hx_level_f64* level, double dt, const double* lam_
 int hx_level_tangent_f64(const hx_level_f64* level_pairs, double dt, double ddt, double* out_h, double* out_hu,
                          double* out_hv, hx_stream_t stream);
 
+/* ---- multi-box level (same-level ghosts without FillPatch) ------------------- */
+
+/*
+ * One box of a level: its valid cells lo..hi (level cell coordinates), state
+ * (h, hu, hv) and a second state for the time loop, terrain (z, n), planes of
+ * (hi[1]-lo[1]+1) rows x pitch elements.
+ */
+typedef struct hx_levelbox_f64 {
+    double *h, *hu, *hv;
+    double *h_alt, *hu_alt, *hv_alt;
+    const double *z, *n;
+    int64_t pitch;
+    int32_t lo[2], hi[2];
+} hx_levelbox_f64;
+
+/*
+ * The single-level time loop of hx_level_run_f64 (hydrostatic-Roe) on a level
+ * given as several boxes that tile the domain (0,0)-(nx-1,ny-1) -- the
+ * same-level BoxArray of AMReX.  The ghosts a box needs are read straight
+ * from the boxes that own those cells, and physical-boundary ghosts follow
+ * the BCFill rules: the FillPatch of same-level and physical ghosts
+ * (src/state/AmrMeshState_AMR.cpp:667-767, include/boundaries/BCFill.H:211-296)
+ * and the U_ext / Terrain_ext / Eta_ext copies (HydrostaticRoe.cpp:456-500)
+ * are not needed.  Each step is one launch over the tiles of all boxes with
+ * one CFL chain for the level; results equal the single-box run bit for bit.
+ * Boxes must not overlap and must cover the domain (coarse-fine ghosts still
+ * need FillPatch).  On return *final_in_alt says which state of each box
+ * holds the result.  work: hx_boxlevel_work_bytes bytes of device memory.
+ */
+int64_t hx_boxlevel_work_bytes(int nboxes, const hx_levelbox_f64* boxes, int nx, int ny);
+int hx_boxlevel_run_f64(int nboxes, const hx_levelbox_f64* boxes, int nx, int ny, double dx, double dy,
+                        const int32_t bc_lo[2], const int32_t bc_hi[2], int nsteps, double cfl, int arith, void* work,
+                        uint32_t* status, double* time_dev, int* final_in_alt, hx_stream_t stream);
+
 /* ---- the FP64 roof --------------------------------------------------------- */
 
 /*
