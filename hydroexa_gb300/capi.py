@@ -113,6 +113,8 @@ def _declare(L):
                                                    real, real, ctypes.c_byte, c_void_p]
         getattr(L, f"hx_masked_average_down_box_{sfx}").argtypes = [P4, P4, Box, c_int, c_int, c_int, c_int, c_int,
                                                                     real, real, c_void_p]
+        getattr(L, f"hx_average_down_box_{sfx}").argtypes = [P4, P4, Box, c_int, c_int, c_int, c_int, c_int,
+                                                             c_void_p]
         getattr(L, f"hx_level_advance_{sfx}").argtypes = [c_int, POINTER(Lv), real, c_void_p, c_void_p, c_void_p,
                                                          c_void_p, c_void_p, c_int, c_void_p]
         getattr(L, f"hx_level_dt_reduce_{sfx}").argtypes = [POINTER(Lv), c_void_p, c_void_p]
@@ -194,7 +196,8 @@ EXPORTED = [
     "hx_advance_box_hydrostatic_f64", "hx_advance_box_hydrostatic_f32", "hx_advance_box_roe_f64",
     "hx_advance_box_roe_f32", "hx_advance_box_hydrostatic_reflux_f64", "hx_advance_box_hydrostatic_reflux_f32",
     "hx_advance_box_roe_reflux_f64", "hx_advance_box_roe_reflux_f32", "hx_dt_reduce_box_f64", "hx_dt_reduce_box_f32", "hx_tag_box_f64", "hx_tag_box_f32",
-    "hx_masked_average_down_box_f64", "hx_masked_average_down_box_f32", "hx_derive_eta_box_f64",
+    "hx_masked_average_down_box_f64", "hx_masked_average_down_box_f32", "hx_average_down_box_f64",
+    "hx_average_down_box_f32", "hx_derive_eta_box_f64",
     "hx_derive_eta_box_f32", "hx_diagnostics_work_bytes", "hx_diagnostics_box_f64", "hx_diagnostics_box_f32",
     "hx_level_diagnostics_f64", "hx_measure_fp64_rate", "hx_boxlevel_work_bytes", "hx_boxlevel_run_f64",
     "hx_level_advance_f64",

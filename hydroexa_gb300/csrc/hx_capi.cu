@@ -236,6 +236,16 @@ int tag_box(int method, const A* U, const A* T, hx_array4_i8* tags, hx_box vb, R
 }
 
 template <class R, class A>
+int avgdown_box(const A* fine, A* crse, hx_box cb, int scomp, int ccomp, int ncomp, int rx, int ry, cudaStream_t st) {
+    if (!box_ok(cb)) return HX_ERR_ARG;
+    if (rx < 1 || ry < 1 || ncomp < 1 || scomp < 0 || ccomp < 0) return fail(HX_ERR_ARG, "bad ratio or components");
+    hx_box fb{{cb.lo[0] * rx, cb.lo[1] * ry}, {cb.hi[0] * rx + rx - 1, cb.hi[1] * ry + ry - 1}};
+    if (!covers(fine, fb, 0, scomp + ncomp, "fine") || !covers(crse, cb, 0, ccomp + ncomp, "crse")) return HX_ERR_ARG;
+    return launched(launch_average_down<R>(to_v4(*fine), to_v4(*crse), ibox(cb), scomp, ccomp, ncomp, rx, ry, st),
+                    "hx_average_down_box");
+}
+
+template <class R, class A>
 int mavg_box(const A* fine, A* crse, hx_box cb, int scomp, int ccomp, int ncomp, int rx, int ry, R fv, R nodata,
              cudaStream_t st) {
     if (!box_ok(cb)) return HX_ERR_ARG;
@@ -555,6 +565,15 @@ int hx_masked_average_down_box_f64(const hx_array4_f64* fine, hx_array4_f64* crs
 int hx_masked_average_down_box_f32(const hx_array4_f32* fine, hx_array4_f32* crse, hx_box cb, int scomp, int ccomp,
                                    int ncomp, int rx, int ry, float fv, float nodata, hx_stream_t st) {
     return mavg_box<float>(fine, crse, cb, scomp, ccomp, ncomp, rx, ry, fv, nodata, (cudaStream_t)st);
+}
+
+int hx_average_down_box_f64(const hx_array4_f64* fine, hx_array4_f64* crse, hx_box cb, int scomp, int ccomp,
+                            int ncomp, int rx, int ry, hx_stream_t st) {
+    return avgdown_box<double>(fine, crse, cb, scomp, ccomp, ncomp, rx, ry, (cudaStream_t)st);
+}
+int hx_average_down_box_f32(const hx_array4_f32* fine, hx_array4_f32* crse, hx_box cb, int scomp, int ccomp,
+                            int ncomp, int rx, int ry, hx_stream_t st) {
+    return avgdown_box<float>(fine, crse, cb, scomp, ccomp, ncomp, rx, ry, (cudaStream_t)st);
 }
 
 int hx_derive_eta_box_f64(const hx_array4_f64* U, const hx_array4_f64* T, hx_array4_f64* eta, hx_box b,

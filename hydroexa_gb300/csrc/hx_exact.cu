@@ -24,6 +24,8 @@ namespace hx {
                                        R, R, R, R, R, signed char, cudaStream_t);                              \
     template cudaError_t launch_masked_avgdown<R>(const V4<R>&, const V4<R>&, const IBox&, int, int, int, int,  \
                                                   int, R, R, cudaStream_t);                                     \
+    template cudaError_t launch_average_down<R>(const V4<R>&, const V4<R>&, const IBox&, int, int, int, int, int,  \
+                                                cudaStream_t);                                                    \
     template cudaError_t launch_derive_eta<R>(const V4<R>&, const V4<R>&, const V4<R>&, const IBox&,          \
                                               cudaStream_t);                                                    \
     template cudaError_t launch_diagnostics<R>(const Plane<R>&, const Plane<R>&, const Plane<R>&,             \

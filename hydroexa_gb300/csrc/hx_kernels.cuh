@@ -701,6 +701,28 @@ __global__ void __launch_bounds__(NT) k_masked_avgdown(V4<R> fine, V4<R> crse, I
 }
 
 // ---------------------------------------------------------------------------
+// Conservative restriction of the state over a coarse box: amrex::average_down
+// as AmrMeshState::AverageDownTo calls it (src/state/AmrMeshState_AMR.cpp:
+// 838-844), Cartesian.  AMReX's amrex_avgdown sums the rx*ry fine values rows
+// outer, columns inner, from 0, and multiplies by 1/(rx*ry); the same order
+// here keeps the result bit-equal.  One thread per coarse cell and component
+// loop inside, so a warp reads rx*32 consecutive fine values per fine row.
+// ---------------------------------------------------------------------------
+template <class R>
+__global__ void __launch_bounds__(NT) k_average_down(V4<R> fine, V4<R> crse, IBox cb, int scomp, int ccomp,
+                                                     int ncomp, int rx, int ry, R volfrac) {
+    const int i = cb.lo0 + blockIdx.x * TX + (threadIdx.x & (TX - 1));
+    const int j = cb.lo1 + blockIdx.y * TY + threadIdx.x / TX;
+    if (i > cb.hi0 || j > cb.hi1) return;
+    for (int n = 0; n < ncomp; ++n) {
+        R c = R(0);
+        for (int jr = 0; jr < ry; ++jr)
+            for (int ir = 0; ir < rx; ++ir) c += fine.ld(i * rx + ir, j * ry + jr, scomp + n);
+        crse.ref(i, j, ccomp + n) = volfrac * c;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Level diagnostics and eta (src/state/AmrMeshState_Utils.cpp:213-298,
 // src/state/AmrMeshState_AMR.cpp:203-224).
 // ---------------------------------------------------------------------------
@@ -1002,6 +1024,14 @@ cudaError_t launch_diagnostics(const Plane<R>& h, const Plane<R>& hu, const Plan
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     k_diag_final<R><<<1, NT, 0, st>>>(part, (long long)g.x * g.y, out);
+    return cudaGetLastError();
+}
+
+template <class R>
+cudaError_t launch_average_down(const V4<R>& fine, const V4<R>& crse, const IBox& cb, int scomp, int ccomp,
+                                int ncomp, int rx, int ry, cudaStream_t st) {
+    const R volfrac = R(1.0) / R(rx * ry);
+    k_average_down<R><<<tile_grid(cb, TX, TY), NT, 0, st>>>(fine, crse, cb, scomp, ccomp, ncomp, rx, ry, volfrac);
     return cudaGetLastError();
 }
 

@@ -46,6 +46,10 @@ cudaError_t launch_masked_avgdown(const V4<R>& fine, const V4<R>& crse, const IB
                                   int ncomp, int rx, int ry, R fv, R nodata, cudaStream_t st);
 
 template <class R>
+cudaError_t launch_average_down(const V4<R>& fine, const V4<R>& crse, const IBox& cb, int scomp, int ccomp,
+                                int ncomp, int rx, int ry, cudaStream_t st);
+
+template <class R>
 cudaError_t launch_derive_eta(const V4<R>& U, const V4<R>& T, const V4<R>& eta, const IBox& b, cudaStream_t st);
 
 template <class R>

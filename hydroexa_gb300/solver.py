@@ -220,5 +220,20 @@ def masked_average_down(S_fine: torch.Tensor, S_crse: torch.Tensor, fgeom: Geome
     capi.check(rc, "hx_masked_average_down_box")
 
 
+def average_down(S_fine: torch.Tensor, S_crse: torch.Tensor, scomp: int, ncomp: int, ratio) -> None:
+    """amrex::average_down of the state as AmrMeshState::AverageDownTo calls it
+    (src/state/AmrMeshState_AMR.cpp:838-844), for single-box levels:
+    components scomp.. of S_fine (ncomp, ny, nx) restricted into S_crse."""
+    rx, ry = int(ratio[0]), int(ratio[1])
+    nc, nyc, nxc = S_crse.shape
+    if S_fine.shape[1] != nyc * ry or S_fine.shape[2] != nxc * rx:
+        raise ValueError("fine and coarse boxes do not match the ratio")
+    sfx = "f64" if S_fine.dtype == torch.float64 else "f32"
+    rc = getattr(capi.lib(), f"hx_average_down_box_{sfx}")(
+        ctypes.byref(array4(S_fine)), ctypes.byref(array4(S_crse)), box((0, 0), (nxc - 1, nyc - 1)), scomp, scomp,
+        ncomp, rx, ry, ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    capi.check(rc, "hx_average_down_box")
+
+
 __all__ = ["BaseSolver", "Roe", "HydrostaticRoe", "SolverVariant", "SolverContext", "HydroExaAbort", "make_solver",
-           "masked_average_down", "DtAccum"]
+           "masked_average_down", "average_down", "DtAccum"]

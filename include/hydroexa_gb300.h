@@ -258,6 +258,18 @@ int hx_masked_average_down_box_f32(const hx_array4_f32* fine, hx_array4_f32* crs
                                    int ccomp, int ncomp, int rx, int ry, float fine_volume, float nodata,
                                    hx_stream_t stream);
 
+/*
+ * Conservative restriction of the coarse box crse_box: each coarse value is the
+ * mean of its rx*ry fine values, summed rows outer, columns inner, times
+ * 1/(rx*ry) (replaces amrex::average_down as AmrMeshState::AverageDownTo and
+ * AverageDown call it on the state, src/state/AmrMeshState_AMR.cpp:828-844;
+ * Cartesian geometry).  Components scomp.. of fine go to ccomp.. of crse.
+ */
+int hx_average_down_box_f64(const hx_array4_f64* fine, hx_array4_f64* crse, hx_box crse_box, int scomp, int ccomp,
+                            int ncomp, int rx, int ry, hx_stream_t stream);
+int hx_average_down_box_f32(const hx_array4_f32* fine, hx_array4_f32* crse, hx_box crse_box, int scomp, int ccomp,
+                            int ncomp, int rx, int ry, hx_stream_t stream);
+
 /* ---- eta and the conservation diagnostics ---------------------------------- */
 
 /*

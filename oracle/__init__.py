@@ -224,6 +224,22 @@ def masked_average_down(fine: np.ndarray, rx: int, ry: int, fine_volume: float, 
     return c
 
 
+def average_down(fine: np.ndarray, rx: int, ry: int):
+    """Conservative restriction (amrex::average_down as called by
+    src/state/AmrMeshState_AMR.cpp:838-844): fine (ncomp, nyf, nxf) ->
+    crse (ncomp, nyf//ry, nxf//rx)."""
+    f = np.ascontiguousarray(fine)
+    nc, nyf, nxf = f.shape
+    nxc, nyc = nxf // rx, nyf // ry
+    c = np.empty((nc, nyc, nxc), dtype=f.dtype)
+    getattr(lib(), "hxo_average_down_" + _suffix(f.dtype))(
+        _ptr(f), ctypes.c_longlong(nxf), ctypes.c_longlong(nxf * nyf), ctypes.c_int(0), ctypes.c_int(0),
+        _ptr(c), ctypes.c_longlong(nxc), ctypes.c_longlong(nxc * nyc), ctypes.c_int(0), ctypes.c_int(0),
+        ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(nxc - 1), ctypes.c_int(nyc - 1),
+        ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(nc), ctypes.c_int(rx), ctypes.c_int(ry))
+    return c
+
+
 def mass_diagnostics(h, hu, hv, n, dx: float, dy: float) -> np.ndarray:
     """{mass, x-momentum, y-momentum, kinetic energy, min h} of one box
     (src/state/AmrMeshState_Utils.cpp:267-298); planes (ny, nx) of one dtype."""

@@ -717,6 +717,26 @@ void masked_average_down(View<const R> fine, View<R> crse, int clo0, int clo1, i
             }
 }
 
+// Conservative restriction of the state, amrex::average_down as
+// AmrMeshState::AverageDownTo calls it (src/state/AmrMeshState_AMR.cpp:838-844)
+// on a Cartesian geometry.  The kernel is AMReX's amrex_avgdown
+// (AMReX_MultiFabUtil_2D_C.H; AMReX is an un-vendored submodule with no pinned
+// version): the rx*ry fine values are summed, rows outer and columns inner,
+// starting from 0, and the sum is multiplied by volfrac = 1/(rx*ry).
+template <class R>
+void average_down(View<const R> fine, View<R> crse, int clo0, int clo1, int chi0, int chi1, int scomp, int ccomp,
+                  int ncomp, int rx, int ry) {
+    const R volfrac = R(1.0) / R(rx * ry);
+    for (int n = 0; n < ncomp; ++n)
+        for (int j = clo1; j <= chi1; ++j)
+            for (int i = clo0; i <= chi0; ++i) {
+                R c = R(0);
+                for (int jr = 0; jr < ry; ++jr)
+                    for (int ir = 0; ir < rx; ++ir) c += fine(i * rx + ir, j * ry + jr, scomp + n);
+                crse(i, j, ccomp + n) = volfrac * c;
+            }
+}
+
 // Per-box reduction of AmrMeshState::ComputeMassDiagnostics,
 // src/state/AmrMeshState_Utils.cpp:267-298, over the valid cells of one box:
 // out = {mass, x-momentum, y-momentum, kinetic energy, min h}.  A cell counts

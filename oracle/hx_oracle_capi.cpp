@@ -138,6 +138,14 @@ int run(int method, const Level<R>& L, R* h, R* hu, R* hv, const R* z, const R* 
         View<R> Cv{crse, cjs, cns, clo0, clo1};                                                                     \
         masked_average_down<R>(Fv, Cv, bx_lo0, bx_lo1, bx_hi0, bx_hi1, ncomp, rx, ry, fv, nodata);                 \
     }                                                                                                               \
+    extern "C" void hxo_average_down_##SUF(const R* fine, long long fjs, long long fns, int flo0, int flo1,          \
+                                           R* crse, long long cjs, long long cns, int clo0, int clo1, int bx_lo0,    \
+                                           int bx_lo1, int bx_hi0, int bx_hi1, int scomp, int ccomp, int ncomp,      \
+                                           int rx, int ry) {                                                         \
+        View<const R> Fv{fine, fjs, fns, flo0, flo1};                                                               \
+        View<R> Cv{crse, cjs, cns, clo0, clo1};                                                                     \
+        average_down<R>(Fv, Cv, bx_lo0, bx_lo1, bx_hi0, bx_hi1, scomp, ccomp, ncomp, rx, ry);                       \
+    }                                                                                                               \
     extern "C" void hxo_mass_diagnostics_##SUF(int nx, int ny, long long pitch, const R* h, const R* hu,            \
                                                const R* hv, const R* n, R dx, R dy, double* out) {                  \
         mass_diagnostics<R>(nx, ny, pitch, h, hu, hv, n, dx, dy, out);                                              \

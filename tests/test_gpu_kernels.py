@@ -124,6 +124,35 @@ def test_masked_average_down_bit_exact(cuda, hxlib, oracle_lib, r):
     assert np.array_equal(got, g[f"crse_r{r}"], equal_nan=True)
 
 
+@pytest.mark.parametrize("rx,ry,dtype", [(2, 2, torch.float64), (4, 4, torch.float64), (2, 4, torch.float64),
+                                         (3, 3, torch.float64), (2, 2, torch.float32)])
+def test_average_down_bit_exact(cuda, hxlib, oracle_lib, rx, ry, dtype):
+    """The state restriction (amrex::average_down of AverageDownTo) equals the
+    oracle bit for bit on a coarse sub-box of an offset view with ghosts,
+    components 1..2 into 0..1; cells outside the box are left alone."""
+    rng = np.random.default_rng(7 * rx + ry)
+    npd = np.float64 if dtype == torch.float64 else np.float32
+    nxc, nyc = 21, 17
+    fine = rng.uniform(-2.0, 3.0, size=(3, nyc * ry, nxc * rx)).astype(npd)
+    ref = oracle_lib.average_down(fine[1:], rx, ry)
+    # fine view indexed from (0,0); coarse view with one ghost, lo = (-1,-1)
+    F = torch.from_numpy(fine).to(cuda)
+    C = torch.full((2, nyc + 2, nxc + 2), 123.0, dtype=dtype, device=cuda)
+    sfx = "f64" if dtype == torch.float64 else "f32"
+    cv = array4(C, lo=(-1, -1))
+    rc = getattr(hxlib.lib(), f"hx_average_down_box_{sfx}")(ctypes.byref(array4(F)), ctypes.byref(cv),
+                                                             box((2, 3), (nxc - 1, nyc - 2)), 1, 0, 2, rx, ry, None)
+    hxlib.check(rc, "avgdown")
+    got = C.cpu().numpy()
+    assert np.array_equal(got[:, 4:nyc, 3:nxc + 1], ref[:, 3:nyc - 1, 2:nxc])
+    inner = np.ones_like(got, dtype=bool)
+    inner[:, 4:nyc, 3:nxc + 1] = False
+    assert (got[inner] == 123.0).all()
+    bad = getattr(hxlib.lib(), f"hx_average_down_box_{sfx}")(ctypes.byref(array4(F)), ctypes.byref(cv),
+                                                              box((0, 0), (nxc, nyc - 1)), 1, 0, 2, rx, ry, None)
+    assert bad == capi.HX_ERR_ARG
+
+
 def test_box_form_matches_level_form(cuda, hxlib, oracle_lib):
     """The AMReX drop-in (ghost-filled per-box views, four boxes) equals the
     single-box level form, including the FL/FR face arrays the reflux needs."""

@@ -119,3 +119,23 @@ def test_mass_diagnostics_excludes_nodata_and_dry_cells(oracle_lib):
                                          (0.5 * (c.hu[m] ** 2 + c.hv[m] ** 2) / c.h[m] * dA).sum()], rtol=1e-13)
     assert out[4] == c.h[m].min()
     assert np.array_equal(oracle.derive_eta(c.h, c.z), c.h + c.z)
+
+
+@pytest.mark.parametrize("rx,ry,dtype", [(2, 2, np.float64), (4, 4, np.float64), (2, 4, np.float64),
+                                         (3, 3, np.float64), (2, 2, np.float32)])
+def test_average_down_is_the_ordered_mean(oracle_lib, rx, ry, dtype):
+    """average_down: coarse = (1 / (rx ry)) * sum of the fine block, summed
+    rows outer, columns inner; the mean of a constant is that constant and the
+    restriction conserves the integral to round-off."""
+    rng = np.random.default_rng(rx * 10 + ry)
+    fine = rng.uniform(-2.0, 3.0, size=(3, 12 * ry, 10 * rx)).astype(dtype)
+    got = oracle_lib.average_down(fine, rx, ry)
+    acc = np.zeros((3, 12, 10), dtype=dtype)
+    for jr in range(ry):
+        for ir in range(rx):
+            acc = acc + fine[:, jr::ry, ir::rx]
+    assert np.array_equal(got, (dtype(1.0) / dtype(rx * ry)) * acc)
+    const = np.full_like(fine, 0.7)
+    assert np.allclose(oracle_lib.average_down(const, rx, ry), dtype(0.7), rtol=4 * np.finfo(dtype).eps)
+    np.testing.assert_allclose(got.sum(axis=(1, 2)) * rx * ry, fine.sum(axis=(1, 2)),
+                               rtol=50 * np.finfo(dtype).eps, atol=1e-3 if dtype == np.float32 else 1e-9)
