@@ -44,22 +44,37 @@ def _plane(t: torch.Tensor, geom: Geometry):
     return t.contiguous()
 
 
+# Face records are kept when they take at most this much device memory.
+RECORD_BUDGET = 16 << 30
+
+
 class GaugeProblem:
     """Geometry, roughness, gauges and step count of a misfit problem.
     gauges: (G,) flat cell indices i + j * nx.  checkpoint_every: 0 keeps every
-    state; k > 0 keeps every k-th and recomputes segments in the reverse sweep."""
+    state; k > 0 keeps every k-th and recomputes segments in the reverse sweep;
+    k < 0 binomial checkpointing with -k slots.  records (fast form, k > 0):
+    the segment recompute records each face's Roe intermediates for the
+    reverse sweep; None keeps them when they fit RECORD_BUDGET."""
 
     def __init__(self, geom: Geometry, n: torch.Tensor, gauges, nsteps: int, cfl: float, checkpoint_every: int = 0,
-                 arith: int = capi.HX_ARITH_FAST):
+                 arith: int = capi.HX_ARITH_FAST, records=None):
         self.geom = geom
         self.arith = int(arith)
         self.n = _plane(n, geom)
         dev = self.n.device
         self.gauges = torch.as_tensor(gauges, dtype=torch.int64, device=dev).contiguous()
         self.nsteps, self.cfl, self.every = int(nsteps), float(cfl), int(checkpoint_every)
-        nbytes = capi.lib().hx_adjoint_work_bytes_f64(geom.nx, geom.ny, geom.nx, self.nsteps, self.every)
-        if nbytes <= 0:
+        L = capi.lib()
+        plain = L.hx_adjoint_work_bytes_f64(geom.nx, geom.ny, geom.nx, self.nsteps, self.every, 0)
+        if plain <= 0:
             raise capi.HxError("bad adjoint problem size")
+        self.options = 0
+        if self.arith == capi.HX_ARITH_FAST and self.every > 0 and records is not False:
+            with_rec = L.hx_adjoint_work_bytes_f64(geom.nx, geom.ny, geom.nx, self.nsteps, self.every,
+                                                   capi.HX_ADJ_FACE_RECORDS)
+            if records or with_rec - plain <= RECORD_BUDGET:
+                self.options = capi.HX_ADJ_FACE_RECORDS
+        nbytes = L.hx_adjoint_work_bytes_f64(geom.nx, geom.ny, geom.nx, self.nsteps, self.every, self.options)
         self.work = torch.empty(int(nbytes), dtype=torch.uint8, device=dev)
         self.status = torch.zeros(1, dtype=torch.int32, device=dev)
         self._inputs = None
@@ -95,7 +110,7 @@ class GaugeProblem:
         d = _level(g, h0, hu0, hv0, z, self.n)
         capi.check(capi.lib().hx_adjoint_reverse_f64(
             ctypes.byref(d), self.nsteps, self.cfl, self.gauges.numel(), _vp(self.gauges), _vp(href), float(seed),
-            self.every, self.arith, _vp(self.work), _vp(gh), _vp(ghu), _vp(ghv), _vp(gz),
+            self.every, self.arith | self.options, _vp(self.work), _vp(gh), _vp(ghu), _vp(ghv), _vp(gz),
             ctypes.c_void_p(s.cuda_stream)),
             "hx_adjoint_reverse_f64")
         return gz, gh, ghu, ghv
@@ -194,7 +209,7 @@ def adjoint_step(geom: Geometry, state, z, n, dt, lam, arith: int = capi.HX_ARIT
     out = [torch.empty_like(st[0]) for _ in range(3)]
     zbar = torch.zeros_like(z)
     dtbar = torch.zeros(1, dtype=torch.float64, device=z.device)
-    nbytes = capi.lib().hx_adjoint_work_bytes_f64(geom.nx, geom.ny, geom.nx, 1, 0)
+    nbytes = capi.lib().hx_adjoint_work_bytes_f64(geom.nx, geom.ny, geom.nx, 1, 0, 0)
     work = torch.empty(int(nbytes), dtype=torch.uint8, device=z.device)
     d = _level(geom, st[0], st[1], st[2], z.contiguous(), n.contiguous())
     capi.check(capi.lib().hx_adjoint_step_f64(ctypes.byref(d), float(dt), *(_vp(t) for t in lm),

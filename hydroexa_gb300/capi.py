@@ -24,6 +24,7 @@ HX_STATUS_BOUNDS = 4
 HX_STATUS_TIMEOUT = 8
 HX_ARITH_EXACT = 0
 HX_ARITH_FAST = 1
+HX_ADJ_FACE_RECORDS = 0x100
 HX_METHOD_ROE = 0
 HX_METHOD_HYDROSTATIC_ROE = 1
 
@@ -151,7 +152,7 @@ def _declare(L):
                                       POINTER(c_int32), POINTER(c_int32), c_int, c_double, c_int, c_void_p, c_void_p,
                                       c_void_p, POINTER(c_int), c_void_p]
     L.hx_adjoint_work_bytes_f64.restype = c_int64
-    L.hx_adjoint_work_bytes_f64.argtypes = [c_int, c_int, c_int64, c_int, c_int]
+    L.hx_adjoint_work_bytes_f64.argtypes = [c_int, c_int, c_int64, c_int, c_int, c_int]
     L.hx_adjoint_recompute_steps.restype = c_int64
     L.hx_adjoint_recompute_steps.argtypes = [c_int, c_int]
     L.hx_adjoint_forward_f64.argtypes = [POINTER(LevelF64), c_int, c_double, c_int, c_void_p, c_void_p, c_int,

@@ -39,6 +39,10 @@ extern template cudaError_t launch_adj_forward<true>(const LevelSrc<double>&, co
                                                      const Plane<double>&, const Cells3W<double>&, const IBox&,
                                                      const StepCtl<double>&, const double*, unsigned*,
                                                      const AdjRecord&, cudaStream_t);
+extern template cudaError_t launch_adj_forward_rec<true>(const LevelSrc<double>&, const Cells3<double>&,
+                                                         const Plane<double>&, const Cells3W<double>&, const IBox&,
+                                                         double, double, const double*, unsigned*, const FaceRec&,
+                                                         cudaStream_t);
 extern template cudaError_t launch_adj_forward_linear<false>(const LevelSrc<double>&, const Cells3<double>&,
                                                              const Plane<double>&, const Cells3W<double>&,
                                                              const IBox&, double, double, const double*, cudaStream_t);
@@ -167,56 +171,116 @@ __device__ void roe_rev(double hi, double ui, double vi, double hj, double uj, d
     if (wj) { ghj += gHj; guj += gUj; gvj += gVj; }
 }
 
-// Fast form of roe_rev: the forward quantities that decide branches (wet
-// tests, sonic fixes) are recomputed as roe_hydrostatic_fast computes them,
-// and every division of the reverse becomes a product with one of five
-// reciprocals (1/sden, 1/den, 1/cm, 1/si, 1/sj) obtained from a single
-// rcp_nr of their product.
-__device__ void roe_rev_fast(double hi, double ui, double vi, double hj, double uj, double vj, double b0, double b1,
-                             double b2, double& ghi, double& gui, double& gvi, double& ghj, double& guj, double& gvj) {
+// Fast form of roe_rev, in two parts.  The forward section gives the
+// quantities the reverse needs: either recomputed (roe_fwd_fast, taking the
+// branches roe_hydrostatic_fast takes, every division of the reverse turned
+// into a product with one of five reciprocals 1/sden, 1/den, 1/cm, 1/si, 1/sj
+// from a single rcp_nr of their product), or read from the record the segment
+// recompute wrote for the face (roe_fwd_rec: square roots, Roe averages,
+// entropy-fixed speeds and wave strengths as the forward step computed them;
+// only 1/si and 1/sj are formed).  roe_rev_core then runs the reverse.
+struct RoeFwd {
+    double Hi, Hj, Ui, Uj, Vi, Vj, si, sj, rsi, rsj, cm, rs, rden, rcm, um, vm, l0, l2, a0, a1, a2, w0, w1, w2, dh;
+    double e0i, e0j, e2i, e2j, l0a, l2a, rD0, rD2;
+    bool wi, wj, hmb, fix0, fix2;
+};
+
+__device__ __forceinline__ void roe_fwd_fast(double hi, double ui, double vi, double hj, double uj, double vj,
+                                             RoeFwd& F) {
     using C = Cst<double>;
     const bool wi = ge_bits(hi, C::toldry_bits), wj = ge_bits(hj, C::toldry_bits);
+    F.wi = wi; F.wj = wj;
     const double Hi = wi ? hi : 0.0, Hj = wj ? hj : 0.0;
     const double Ui = wi ? ui : 0.0, Vi = wi ? vi : 0.0, Uj = wj ? uj : 0.0, Vj = wj ? vj : 0.0;
+    F.Hi = Hi; F.Hj = Hj; F.Ui = Ui; F.Uj = Uj; F.Vi = Vi; F.Vj = Vj;
     const double si = sqrt(Hi), sj = sqrt(Hj);
+    F.si = si; F.sj = sj;
     const double hh = 0.5 * (Hi + Hj);
-    const bool hmb = gt_bits(hh, C::toldry_bits);
-    const double hm = hmb ? hh : TD;
+    F.hmb = gt_bits(hh, C::toldry_bits);
+    const double hm = F.hmb ? hh : TD;
     const double cm = sqrt(G * hm);
+    F.cm = cm;
     const double den = 2.0 * cm + T12;
     const double sden = si + sj + T12;
     const double cd = cm * den, S3 = sden * cd;
-    double q3, rsi = 0.0, rsj = 0.0;
+    double q3;
+    F.rsi = 0.0; F.rsj = 0.0;
     if (wi && wj) {
         const double pij = si * sj;
         const double q = rcp_nr(S3 * pij);
         q3 = pij * q;
-        rsi = (sj * S3) * q;
-        rsj = (si * S3) * q;
+        F.rsi = (sj * S3) * q;
+        F.rsj = (si * S3) * q;
     } else {
         q3 = rcp_nr(S3);
-        if (wi) rsi = rcp_nr(si);
-        if (wj) rsj = rcp_nr(sj);
+        if (wi) F.rsi = rcp_nr(si);
+        if (wj) F.rsj = rcp_nr(sj);
     }
-    const double rs = cd * q3, rden = (sden * cm) * q3, rcm = (sden * den) * q3;
-    const double um = (Ui * si + Uj * sj) * rs;
-    const double vm = (Vi * si + Vj * sj) * rs;
-    const double l0a = um - cm, l2a = um + cm;
+    F.rs = cd * q3; F.rden = (sden * cm) * q3; F.rcm = (sden * den) * q3;
+    const double um = (Ui * si + Uj * sj) * F.rs;
+    const double vm = (Vi * si + Vj * sj) * F.rs;
+    F.um = um; F.vm = vm;
+    F.l0a = um - cm; F.l2a = um + cm;
     const double ci = C::sqrt_g * si, cj = C::sqrt_g * sj;
-    const double e0i = Ui - ci, e0j = Uj - cj;
-    const bool fix0 = neg_i(e0i) && pos_i(e0j);
-    const double e2i = Ui + ci, e2j = Uj + cj;
-    const bool fix2 = neg_i(e2i) && pos_i(e2j);
-    double l0 = l0a, l2 = l2a, rD0 = 0.0, rD2 = 0.0;
-    if (fix0) { rD0 = rcp_nr(e0j - e0i); l0 = e0i * (e0j - l0a) * rD0; }
-    if (fix2) { rD2 = rcp_nr(e2j - e2i); l2 = e2j * (l2a - e2i) * rD2; }
-    const double l1 = um;
+    F.e0i = Ui - ci; F.e0j = Uj - cj;
+    F.fix0 = neg_i(F.e0i) && pos_i(F.e0j);
+    F.e2i = Ui + ci; F.e2j = Uj + cj;
+    F.fix2 = neg_i(F.e2i) && pos_i(F.e2j);
+    F.l0 = F.l0a; F.l2 = F.l2a; F.rD0 = 0.0; F.rD2 = 0.0;
+    if (F.fix0) { F.rD0 = rcp_nr(F.e0j - F.e0i); F.l0 = F.e0i * (F.e0j - F.l0a) * F.rD0; }
+    if (F.fix2) { F.rD2 = rcp_nr(F.e2j - F.e2i); F.l2 = F.e2j * (F.l2a - F.e2i) * F.rD2; }
     const double dh = Hj - Hi;
+    F.dh = dh;
     const double dhu = Hj * Uj - Hi * Ui;
     const double dhv = Hj * Vj - Hi * Vi;
-    const double a0 = (l2 * dh - dhu) * rden, a1 = (dhv - vm * dh) * rcm, a2 = (dhu - l0 * dh) * rden;
-    const double w0 = 0.5 * fabs(l0) * a0, w1 = 0.5 * fabs(l1) * a1, w2 = 0.5 * fabs(l2) * a2;
+    F.a0 = (F.l2 * dh - dhu) * F.rden; F.a1 = (dhv - vm * dh) * F.rcm; F.a2 = (dhu - F.l0 * dh) * F.rden;
+    F.w0 = 0.5 * fabs(F.l0) * F.a0; F.w1 = 0.5 * fabs(um) * F.a1; F.w2 = 0.5 * fabs(F.l2) * F.a2;
+}
 
+__device__ __forceinline__ void roe_fwd_rec(double hi, double ui, double vi, double hj, double uj, double vj,
+                                            const RoeRecVals& R, RoeFwd& F) {
+    using C = Cst<double>;
+    const bool wi = (R.fl & RR_WI) != 0, wj = (R.fl & RR_WJ) != 0;
+    F.wi = wi; F.wj = wj;
+    const double Hi = wi ? hi : 0.0, Hj = wj ? hj : 0.0;
+    const double Ui = wi ? ui : 0.0, Vi = wi ? vi : 0.0, Uj = wj ? uj : 0.0, Vj = wj ? vj : 0.0;
+    F.Hi = Hi; F.Hj = Hj; F.Ui = Ui; F.Uj = Uj; F.Vi = Vi; F.Vj = Vj;
+    const double si = R.si, sj = R.sj, cm = R.cm;
+    F.si = si; F.sj = sj; F.cm = cm;
+    F.hmb = (R.fl & RR_HM) != 0;
+    const double den = 2.0 * cm + T12;
+    const double sden = si + sj + T12;
+    F.rs = (cm * den) * R.q; F.rden = (sden * cm) * R.q; F.rcm = (sden * den) * R.q;
+    F.rsi = 0.0; F.rsj = 0.0;
+    if (wi && wj) {
+        const double r = rcp_nr(si * sj);
+        F.rsi = sj * r;
+        F.rsj = si * r;
+    } else {
+        if (wi) F.rsi = rcp_nr(si);
+        if (wj) F.rsj = rcp_nr(sj);
+    }
+    F.um = R.um; F.vm = R.vm; F.l0 = R.l0; F.l2 = R.l2;
+    F.fix0 = (R.fl & RR_FIX0) != 0;
+    F.fix2 = (R.fl & RR_FIX2) != 0;
+    if (F.fix0 | F.fix2) {  // the sonic-fix derivatives need the one-sided speeds
+        const double ci = C::sqrt_g * si, cj = C::sqrt_g * sj;
+        F.l0a = R.um - cm; F.l2a = R.um + cm;
+        F.e0i = Ui - ci; F.e0j = Uj - cj; F.e2i = Ui + ci; F.e2j = Uj + cj;
+        F.rD0 = F.fix0 ? rcp_nr(F.e0j - F.e0i) : 0.0;
+        F.rD2 = F.fix2 ? rcp_nr(F.e2j - F.e2i) : 0.0;
+    }
+    F.dh = Hj - Hi;
+    F.a0 = 2.0 * R.a0h; F.a1 = 2.0 * R.a1h; F.a2 = 2.0 * R.a2h;
+    F.w0 = fabs(R.l0) * R.a0h; F.w1 = fabs(R.um) * R.a1h; F.w2 = fabs(R.l2) * R.a2h;
+}
+
+__device__ __forceinline__ void roe_rev_core(const RoeFwd& F, double b0, double b1, double b2, double& ghi,
+                                             double& gui, double& gvi, double& ghj, double& guj, double& gvj) {
+    using C = Cst<double>;
+    const double Hi = F.Hi, Hj = F.Hj, Ui = F.Ui, Uj = F.Uj, Vi = F.Vi, Vj = F.Vj;
+    const double l0 = F.l0, l1 = F.um, l2 = F.l2, vm = F.vm, cm = F.cm, dh = F.dh;
+    const double a0 = F.a0, a1 = F.a1, a2 = F.a2, w0 = F.w0, w1 = F.w1, w2 = F.w2;
     double gHi = 0.5 * (b0 * Ui + b1 * (Ui * Ui + 2.0 * HG * Hi) + b2 * Ui * Vi);
     double gHj = 0.5 * (b0 * Uj + b1 * (Uj * Uj + 2.0 * HG * Hj) + b2 * Uj * Vj);
     double gUi = 0.5 * b0 * Hi + b1 * Hi * Ui + 0.5 * b2 * Hi * Vi;
@@ -229,9 +293,9 @@ __device__ void roe_rev_fast(double hi, double ui, double vi, double hj, double 
     double gl2 = -b1 * w2 + gw2 * 0.5 * sgn(l2) * a2;
     double gvm = -b2 * (w0 + w2), gcm = -b2 * w1;
     const double gl1 = gw1 * 0.5 * sgn(l1) * a1;
-    const double ga0 = gw0 * 0.5 * fabs(l0) * rden;  // already divided by den
-    const double ga1 = gw1 * 0.5 * fabs(l1) * rcm;   // already divided by cm
-    const double ga2 = gw2 * 0.5 * fabs(l2) * rden;
+    const double ga0 = gw0 * 0.5 * fabs(l0) * F.rden;  // already divided by den
+    const double ga1 = gw1 * 0.5 * fabs(l1) * F.rcm;   // already divided by cm
+    const double ga2 = gw2 * 0.5 * fabs(l2) * F.rden;
     gl2 += ga0 * dh;
     double gdh = ga0 * l2 - ga1 * vm - ga2 * l0;
     double gdhu = ga2 - ga0;
@@ -244,39 +308,39 @@ __device__ void roe_rev_fast(double hi, double ui, double vi, double hj, double 
     gUj += gdhu * Hj; gUi -= gdhu * Hi;
     gVj += gdhv * Hj; gVi -= gdhv * Hi;
     double gum = gl1, gci = 0.0, gcj = 0.0;
-    if (fix2) {
-        const double t = gl2 * rD2;
-        const double gl2a = t * e2j;
-        const double ge2i = t * e2j * (l2a - e2j) * rD2;
-        const double ge2j = -t * (l2a - e2i) * e2i * rD2;
+    if (F.fix2) {
+        const double t = gl2 * F.rD2;
+        const double gl2a = t * F.e2j;
+        const double ge2i = t * F.e2j * (F.l2a - F.e2j) * F.rD2;
+        const double ge2j = -t * (F.l2a - F.e2i) * F.e2i * F.rD2;
         gUi += ge2i; gci += ge2i; gUj += ge2j; gcj += ge2j;
         gum += gl2a; gcm += gl2a;
     } else {
         gum += gl2; gcm += gl2;
     }
-    if (fix0) {
-        const double t = gl0 * rD0;
-        const double gl0a = -t * e0i;
-        const double ge0i = t * (e0j - l0a) * e0j * rD0;
-        const double ge0j = t * e0i * (l0a - e0i) * rD0;
+    if (F.fix0) {
+        const double t = gl0 * F.rD0;
+        const double gl0a = -t * F.e0i;
+        const double ge0i = t * (F.e0j - F.l0a) * F.e0j * F.rD0;
+        const double ge0j = t * F.e0i * (F.l0a - F.e0i) * F.rD0;
         gUi += ge0i; gci -= ge0i; gUj += ge0j; gcj -= ge0j;
         gum += gl0a; gcm -= gl0a;
     } else {
         gum += gl0; gcm -= gl0;
     }
-    const double gnu = gum * rs, gnv = gvm * rs, gsden = -(gnu * um + gnv * vm);
-    gUi += gnu * si; gUj += gnu * sj; gVi += gnv * si; gVj += gnv * sj;
+    const double gnu = gum * F.rs, gnv = gvm * F.rs, gsden = -(gnu * F.um + gnv * vm);
+    gUi += gnu * F.si; gUj += gnu * F.sj; gVi += gnv * F.si; gVj += gnv * F.sj;
     // s = sqrt(H) and c = sqrt(g) s: d/dH = (gs + sqrt(g) gc) / (2 s)
     const double gsi = gnu * Ui + gnv * Vi + gsden + C::sqrt_g * gci;
     const double gsj = gnu * Uj + gnv * Vj + gsden + C::sqrt_g * gcj;
-    if (hmb) {
-        const double ghm = 0.5 * gcm * G * rcm;
+    if (F.hmb) {
+        const double ghm = 0.5 * gcm * G * F.rcm;
         gHi += 0.5 * ghm; gHj += 0.5 * ghm;
     }
-    gHi += 0.5 * gsi * rsi;
-    gHj += 0.5 * gsj * rsj;
-    if (wi) { ghi += gHi; gui += gUi; gvi += gVi; }
-    if (wj) { ghj += gHj; guj += gUj; gvj += gVj; }
+    gHi += 0.5 * gsi * F.rsi;
+    gHj += 0.5 * gsj * F.rsj;
+    if (F.wi) { ghi += gHi; gui += gUi; gvi += gVi; }
+    if (F.wj) { ghj += gHj; guj += gUj; gvj += gVj; }
 }
 
 // Inputs and adjoints of one hydrostatic face: eta, z, u, v of the two cells
@@ -287,8 +351,9 @@ struct FaceVals {
 
 // Reverse of the hydrostatic face (HydrostaticRoe.cpp:247-396) for direction
 // DIR, given the adjoints of FL and FR (global frame).  Adds to g.
-template <int DIR, bool FAST>
-__device__ void face_rev(const FaceVals& f, const double gFL[3], const double gFR[3], FaceVals& g) {
+template <int DIR, bool FAST, bool REC = false>
+__device__ void face_rev(const FaceVals& f, const double gFL[3], const double gFR[3], FaceVals& g,
+                         const RoeRecVals* rec = nullptr) {
     const bool zLmax = okey(f.zL) >= okey(f.zR);  // std::max(zL, zR) keeps zL on ties
     const double zf = zLmax ? f.zL : f.zR;
     const double etaLf = f.eL + 0.5 * f.seL, etaRf = f.eR - 0.5 * f.seR;
@@ -305,8 +370,15 @@ __device__ void face_rev(const FaceVals& f, const double gFL[3], const double gF
     if (DIR == 0) { gpL = gFL[1]; gpR = gFR[1]; b1 = gf1; b2 = gf2; }
     else { gpL = gFL[2]; gpR = gFR[2]; b1 = gf2; b2 = -gf1; }
     double ghLs = 0, gunL = 0, gutL = 0, ghRs = 0, gunR = 0, gutR = 0;
-    if constexpr (FAST) roe_rev_fast(hLs, unL, utL, hRs, unR, utR, gf0, b1, b2, ghLs, gunL, gutL, ghRs, gunR, gutR);
-    else roe_rev(hLs, unL, utL, hRs, unR, utR, gf0, b1, b2, ghLs, gunL, gutL, ghRs, gunR, gutR);
+    if constexpr (FAST) {
+        RoeFwd F;
+        if constexpr (REC) roe_fwd_rec(hLs, unL, utL, hRs, unR, utR, *rec, F);
+        else roe_fwd_fast(hLs, unL, utL, hRs, unR, utR, F);
+        roe_rev_core(F, gf0, b1, b2, ghLs, gunL, gutL, ghRs, gunR, gutR);
+    } else {
+        static_assert(!REC, "face records are kept for the fast form");
+        roe_rev(hLs, unL, utL, hRs, unR, utR, gf0, b1, b2, ghLs, gunL, gutL, ghRs, gunR, gutR);
+    }
     // pressure correction p = HG (hu^2 - hs^2)
     const double ghLu = gpL * 2.0 * HG * hLu, ghRu = gpR * 2.0 * HG * hRu;
     ghLs += -gpL * 2.0 * HG * hLs;
@@ -422,11 +494,23 @@ struct AdjArgs {
     double *p_dt, *p_rate;
     long long* p_idx;
     unsigned* p_fl;
+    FaceRec rec;  // the step's face records (k_adj_faces<true, true>)
 };
+
+// The record of x face (f, j) (d = 0) or y face (i, f) (d = 1).
+__device__ __forceinline__ RoeRecVals load_rec(const FaceRec& R, int d, long long o) {
+    const double* b = R.f[d] + o;
+    const long long ps = R.plane[d];
+    RoeRecVals r;
+    r.si = b[0]; r.sj = b[ps]; r.cm = b[2 * ps]; r.q = b[3 * ps]; r.um = b[4 * ps]; r.vm = b[5 * ps];
+    r.l0 = b[6 * ps]; r.l2 = b[7 * ps]; r.a0h = b[8 * ps]; r.a1h = b[9 * ps]; r.a2h = b[10 * ps];
+    r.fl = R.fl[d][o];
+    return r;
+}
 
 __device__ __forceinline__ double fget(const FaceVals& f, int k) { return (&f.eL)[k]; }
 
-template <bool FAST>
+template <bool FAST, bool REC = false>
 __global__ void __launch_bounds__(ANT) k_adj_faces(AdjArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     AdjSmem& S = *reinterpret_cast<AdjSmem*>(smem_raw);
@@ -500,7 +584,12 @@ __global__ void __launch_bounds__(ANT) k_adj_faces(AdjArgs A) {
                     gFL[c] = -A.cx * S.lam[c][r][cl];
                     gFR[c] = A.cx * S.lam[c][r][cr];
                 }
-                face_rev<0, FAST>(fv, gFL, gFR, g);
+                if constexpr (REC) {
+                    const RoeRecVals rv = load_rec(A.rec, 0, (long long)f + (long long)gj * (nx + 1));
+                    face_rev<0, FAST, true>(fv, gFL, gFR, g, &rv);
+                } else {
+                    face_rev<0, FAST>(fv, gFL, gFR, g);
+                }
             }
             for (int q = 0; q < 14; ++q) P.fa[q][row][fcol + 1] = fget(g, q);
         }
@@ -608,7 +697,12 @@ __global__ void __launch_bounds__(ANT) k_adj_faces(AdjArgs A) {
                     gFL[q] = -A.cy * S.lam[q][rl][c];
                     gFR[q] = A.cy * S.lam[q][rr][c];
                 }
-                face_rev<1, FAST>(fv, gFL, gFR, g);
+                if constexpr (REC) {
+                    const RoeRecVals rv = load_rec(A.rec, 1, (long long)gi + (long long)f * nx);
+                    face_rev<1, FAST, true>(fv, gFL, gFR, g, &rv);
+                } else {
+                    face_rev<1, FAST>(fv, gFL, gFR, g);
+                }
             }
             for (int q = 0; q < 14; ++q) P.fa[q][frow + 1][col] = fget(g, q);
         }
@@ -893,6 +987,9 @@ struct AdjLayout {
     int nslots, seg, binom;       // stored states; segment length (uniform); snapshot slots (binomial)
     size_t states, segbuf, segbuf_stride, lam, lamlin, lin, tmp, nxt, dthist, pflags, slots, status, part, total;
     int nblocks;
+    // face records (uniform checkpoints, fast form, on request): one set per step of the two segments in
+    // flight, after everything else so the layout is otherwise the same with and without them
+    size_t rec, rec_step, rec_plane[2];
 };
 
 size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
@@ -967,7 +1064,7 @@ std::vector<long long> binom_chain(long long n, int c) {
     return pos;
 }
 
-AdjLayout adj_layout(int nx, int ny, long long pitch, int nsteps, int every) {
+AdjLayout adj_layout(int nx, int ny, long long pitch, int nsteps, int every, bool records = false) {
     AdjLayout L{};
     L.plane = (size_t)ny * (size_t)pitch;
     const size_t st = 3 * L.plane * sizeof(double);
@@ -990,8 +1087,30 @@ AdjLayout adj_layout(int nx, int ny, long long pitch, int nsteps, int every) {
     L.status = o; o += 256;
     L.nblocks = ((nx + ATX - 1) / ATX) * ((ny + ATY - 1) / ATY);
     L.part = o; o += al256((size_t)L.nblocks * (2 * sizeof(double) + sizeof(long long) + sizeof(unsigned)));
+    if (records && L.seg) {
+        L.rec_plane[0] = al256((size_t)(nx + 1) * ny * sizeof(double)) / sizeof(double);
+        L.rec_plane[1] = al256((size_t)nx * (ny + 1) * sizeof(double)) / sizeof(double);
+        L.rec_step = NREC * (L.rec_plane[0] + L.rec_plane[1]) * sizeof(double) + al256((size_t)(nx + 1) * ny) +
+                     al256((size_t)nx * (ny + 1));
+        L.rec = o; o += 2 * (size_t)L.seg * L.rec_step;
+    }
     L.total = o;
     return L;
+}
+
+// The face records of step slot k (0 .. 2 seg - 1) of the layout.
+FaceRec rec_at(const AdjLayout& A, char* base, int k, int nx, int ny) {
+    FaceRec R;
+    char* p = base + A.rec + (size_t)k * A.rec_step;
+    R.f[0] = reinterpret_cast<double*>(p);
+    R.f[1] = R.f[0] + NREC * A.rec_plane[0];
+    R.fl[0] = reinterpret_cast<unsigned char*>(R.f[1] + NREC * A.rec_plane[1]);
+    R.fl[1] = R.fl[0] + al256((size_t)(nx + 1) * ny);
+    R.plane[0] = (long long)A.rec_plane[0];
+    R.plane[1] = (long long)A.rec_plane[1];
+    R.nx = nx;
+    R.ny = ny;
+    return R;
 }
 
 struct Views {
@@ -1043,6 +1162,22 @@ cudaError_t forward_step(const hx_level_f64* L, double* const* in, double* const
     o.js = L->pitch; o.lo0 = 0; o.lo1 = 0;
     Plane<double> np{L->n, L->pitch, 0, 0};
     return launch_adj_forward<FAST>(src, uo, np, o, vb, ctl, dt_fixed, pflags, rec, st);
+}
+
+// A recompute step at the recorded dt that also writes the step's face records.
+cudaError_t forward_step_rec(const hx_level_f64* L, double* const* in, double* const* out, const double* dt_fixed,
+                             const FaceRec& rec, cudaStream_t st) {
+    const double* cin[3] = {in[0], in[1], in[2]};
+    LevelSrc<double> src = make_src(L, cin, 2);
+    Cells3<double> uo;
+    for (int k = 0; k < 3; ++k) uo.p[k] = in[k];
+    uo.js = L->pitch; uo.lo0 = 0; uo.lo1 = 0;
+    Cells3W<double> o;
+    for (int k = 0; k < 3; ++k) o.p[k] = out[k];
+    o.js = L->pitch; o.lo0 = 0; o.lo1 = 0;
+    Plane<double> np{L->n, L->pitch, 0, 0};
+    return launch_adj_forward_rec<true>(src, uo, np, o, IBox{0, 0, L->nx - 1, L->ny - 1}, L->dx, L->dy, dt_fixed,
+                                        nullptr, rec, st);
 }
 
 // The flux update of U^n alone (before friction and clamp) into lin.
@@ -1315,9 +1450,10 @@ int adjoint_reverse_binomial(const hx_level_f64* L, int nsteps, double cfl, int 
 
 template <bool FAST>
 int adjoint_reverse(const hx_level_f64* L, int nsteps, double cfl, int ngauges, const int64_t* gauges,
-                    const double* href, double seed, int checkpoint_every, void* work, double* grad_h, double* grad_hu,
-                    double* grad_hv, double* grad_z, cudaStream_t st) {
-    const AdjLayout A = adj_layout(L->nx, L->ny, L->pitch, nsteps, checkpoint_every);
+                    const double* href, double seed, int checkpoint_every, bool records, void* work, double* grad_h,
+                    double* grad_hu, double* grad_hv, double* grad_z, cudaStream_t st) {
+    const AdjLayout A = adj_layout(L->nx, L->ny, L->pitch, nsteps, checkpoint_every, FAST && records);
+    const bool use_rec = A.rec_step != 0;  // uniform checkpoints, fast form, records requested
     if (A.binom) {
         double* grad[3] = {grad_h, grad_hu, grad_hv};
         return adjoint_reverse_binomial<FAST>(L, nsteps, cfl, ngauges, gauges, href, seed, work, A, grad, grad_z, st);
@@ -1340,6 +1476,11 @@ int adjoint_reverse(const hx_level_f64* L, int nsteps, double cfl, int ngauges, 
     if (e == cudaSuccess) e = cudaMemsetAsync(lamb[0], 0, 3 * pb, st);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_adj_faces<FAST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(AdjSmem));
+    if constexpr (FAST) {
+        if (e == cudaSuccess && use_rec)
+            e = cudaFuncSetAttribute(k_adj_faces<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)sizeof(AdjSmem));
+    }
     SideStream side;
     if (e == cudaSuccess && A.seg) e = side.init();
     if (e == cudaSuccess && A.seg) e = cudaEventRecord(side.start, st);
@@ -1376,9 +1517,14 @@ int adjoint_reverse(const hx_level_f64* L, int nsteps, double cfl, int ngauges, 
             double* b = segstate(sg, n - n0 + 1);
             double *in[3], *out[3];
             for (int k = 0; k < 3; ++k) { in[k] = a + k * A.plane; out[k] = b + k * A.plane; }
-            StepCtl<double> ctl{};
-            ctl.dx = L->dx; ctl.dy = L->dy;
-            r = forward_step<FAST>(L, in, out, ctl, &dth[n], nullptr, AdjRecord{}, side.s);
+            if (use_rec) {
+                r = forward_step_rec(L, in, out, &dth[n], rec_at(A, base, (sg & 1) * L_seg + (n - n0), L->nx, L->ny),
+                                     side.s);
+            } else {
+                StepCtl<double> ctl{};
+                ctl.dx = L->dx; ctl.dy = L->dy;
+                r = forward_step<FAST>(L, in, out, ctl, &dth[n], nullptr, AdjRecord{}, side.s);
+            }
             ++launches;
         }
         if (r == cudaSuccess) r = cudaEventRecord(side.rec[sg & 1], side.s);
@@ -1423,8 +1569,17 @@ int adjoint_reverse(const hx_level_f64* L, int nsteps, double cfl, int ngauges, 
                 lam_for_faces = ll;
                 un1 = nullptr;  // the post kernel wrote the dt partials
             }
-            const AdjArgs B = faces_args(L, A, base, Un, un1, lam_for_faces, lam0, grad_z, dt);
-            k_adj_faces<FAST><<<grid, ANT, sizeof(AdjSmem), st>>>(B);
+            AdjArgs B = faces_args(L, A, base, Un, un1, lam_for_faces, lam0, grad_z, dt);
+            if constexpr (FAST) {
+                if (use_rec) {
+                    B.rec = rec_at(A, base, (sg & 1) * L_seg + (n - n0), L->nx, L->ny);
+                    k_adj_faces<true, true><<<grid, ANT, sizeof(AdjSmem), st>>>(B);
+                } else {
+                    k_adj_faces<FAST><<<grid, ANT, sizeof(AdjSmem), st>>>(B);
+                }
+            } else {
+                k_adj_faces<FAST><<<grid, ANT, sizeof(AdjSmem), st>>>(B);
+            }
             ++launches;
             if (e == cudaSuccess) e = cudaGetLastError();
             if (e == cudaSuccess) e = finish(n, Un, lam0, 1);
@@ -1508,9 +1663,10 @@ extern "C" int64_t hx_adjoint_recompute_steps(int nsteps, int checkpoint_every) 
     return binom_cost(nsteps, c) - (chain.empty() ? 0 : chain.back());
 }
 
-extern "C" int64_t hx_adjoint_work_bytes_f64(int nx, int ny, int64_t pitch, int nsteps, int checkpoint_every) {
-    if (nx < 2 || ny < 2 || pitch < nx || nsteps < 1) return 0;
-    return (int64_t)adj_layout(nx, ny, pitch, nsteps, checkpoint_every).total;
+extern "C" int64_t hx_adjoint_work_bytes_f64(int nx, int ny, int64_t pitch, int nsteps, int checkpoint_every,
+                                             int options) {
+    if (nx < 2 || ny < 2 || pitch < nx || nsteps < 1 || (options & ~HX_ADJ_FACE_RECORDS)) return 0;
+    return (int64_t)adj_layout(nx, ny, pitch, nsteps, checkpoint_every, (options & HX_ADJ_FACE_RECORDS) != 0).total;
 }
 
 extern "C" int hx_adjoint_forward_f64(const hx_level_f64* L, int nsteps, double cfl, int ngauges,
@@ -1518,6 +1674,7 @@ extern "C" int hx_adjoint_forward_f64(const hx_level_f64* L, int nsteps, double 
                                       void* work, uint32_t* status, hx_stream_t stream) {
     int rc = adj_check(L, nsteps, ngauges, gauges);
     if (rc) return rc;
+    arith &= ~HX_ADJ_FACE_RECORDS;  // the forward sweep writes no records
     if (!work || !(cfl > 0) || (ngauges > 0 && !series) || !arith_ok(arith))
         return set_error(HX_ERR_ARG, "adjoint forward: bad arguments");
     return arith == HX_ARITH_FAST
@@ -1533,13 +1690,15 @@ extern "C" int hx_adjoint_reverse_f64(const hx_level_f64* L, int nsteps, double 
                                       double* grad_z, hx_stream_t stream) {
     int rc = adj_check(L, nsteps, ngauges, gauges);
     if (rc) return rc;
+    const bool records = (arith & HX_ADJ_FACE_RECORDS) != 0;
+    arith &= ~HX_ADJ_FACE_RECORDS;
     if (!work || !grad_h || !grad_hu || !grad_hv || !grad_z || (ngauges > 0 && !href) || !arith_ok(arith))
         return set_error(HX_ERR_ARG, "adjoint reverse: bad arguments");
     return arith == HX_ARITH_FAST
-               ? adjoint_reverse<true>(L, nsteps, cfl, ngauges, gauges, href, seed, checkpoint_every, work, grad_h,
-                                       grad_hu, grad_hv, grad_z, (cudaStream_t)stream)
-               : adjoint_reverse<false>(L, nsteps, cfl, ngauges, gauges, href, seed, checkpoint_every, work, grad_h,
-                                        grad_hu, grad_hv, grad_z, (cudaStream_t)stream);
+               ? adjoint_reverse<true>(L, nsteps, cfl, ngauges, gauges, href, seed, checkpoint_every, records, work,
+                                       grad_h, grad_hu, grad_hv, grad_z, (cudaStream_t)stream)
+               : adjoint_reverse<false>(L, nsteps, cfl, ngauges, gauges, href, seed, checkpoint_every, records, work,
+                                        grad_h, grad_hu, grad_hv, grad_z, (cudaStream_t)stream);
 }
 
 // One reverse step with a given dt (no CFL dependence, no gauges): the

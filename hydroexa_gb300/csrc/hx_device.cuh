@@ -61,7 +61,8 @@ template <class R> __host__ __device__ __forceinline__ R smax(R a, R b) { return
 
 // NODATA predicate of the hydrostatic face kernel and compute_dt_Impl
 // (HydrostaticRoe.cpp:41,238): |z + 9999| < 1e-10, evaluated in double as the
-// reference's literal -9999.0 forces.
+// reference's literal -9999.0 forces.  Generic form (dual numbers); double and
+// float have integer forms below.
 template <class R> __host__ __device__ __forceinline__ bool is_nodata(R z) {
     return fabs((double)z + 9999.0) < 1e-10;
 }
@@ -105,6 +106,18 @@ __host__ __device__ __forceinline__ int sbits(float x) {
     return b;
 #endif
 }
+// is_nodata on the bit pattern.  A double z with |z + 9999| < 1e-10 lies in
+// [-19998, -4999.5], where z + 9999 is exact (Sterbenz), and there the doubles
+// are spaced 2^-39 apart; 1e-10 / 2^-39 = 54.98, so the predicate holds exactly
+// for the 109 doubles -9999 + k 2^-39, |k| <= 54, whose patterns are
+// bits(-9999.0) + k.  One integer range check replaces an FP64 add and compare.
+// A float converted to double and added to 9999 is exact too, and the float
+// spacing near 9999 (2^-10) leaves -9999.0f as the only float that qualifies.
+__host__ __device__ __forceinline__ bool is_nodata(double z) {
+    return (unsigned long long)sbits(z) - (0xC0C3878000000000ull - 54ull) <= 108ull;
+}
+__host__ __device__ __forceinline__ bool is_nodata(float z) { return sbits(z) == (int)0xC61C3C00u; }
+
 template <class R> __host__ __device__ __forceinline__ bool gt_bits(R x, decltype(sbits(R(0))) cb) {
     return sbits(x) > cb;
 }
@@ -242,13 +255,26 @@ __host__ __device__ __forceinline__ void roe_hydrostatic_exact(R hi, R hui, R hv
     else { F1 = -f2; F2 = f1; }
 }
 
+// Intermediates of one fast-form face flux that its reverse needs: square
+// roots, the shared reciprocal, Roe averages, the entropy-fixed speeds and the
+// half wave strengths, with the branch flags.  Recorded by the adjoint's
+// segment recompute so the reverse sweep does not evaluate them again.
+struct RoeRecVals {
+    double si, sj, cm, q, um, vm, l0, l2, a0h, a1h, a2h;
+    unsigned fl;  // RR_WI | RR_WJ | RR_HM | RR_FIX0 | RR_FIX2
+};
+constexpr int NREC = 11;  // doubles of a RoeRecVals
+constexpr unsigned RR_WI = 1u, RR_WJ = 2u, RR_HM = 4u, RR_FIX0 = 8u, RR_FIX2 = 16u;
+
 // Fast form: inputs are the face depths and face velocities (the reference
 // rebuilds the velocity as (h u)/h, which equals u to an ulp).  One division
 // serves both Roe-average quotients and one serves the three wave strengths;
-// the wave speeds sqrt(g h) reuse sqrt(h).
-template <class R, int DIR>
+// the wave speeds sqrt(g h) reuse sqrt(h).  With REC the intermediates go to
+// *rv (values only stored: the arithmetic is the same instruction for
+// instruction).
+template <class R, int DIR, bool REC = false>
 __host__ __device__ __forceinline__ void roe_hydrostatic_fast(R hi, R ui, R vi, R hj, R uj, R vj, R& F0, R& F1,
-                                                             R& F2) {
+                                                             R& F2, RoeRecVals* rv = nullptr) {
     using C = Cst<R>;
     // depths arrive non-negative (capped with max(0, .)), so bit comparisons apply
     const bool wi = ge_bits(hi, C::toldry_bits), wj = ge_bits(hj, C::toldry_bits);
@@ -263,7 +289,8 @@ __host__ __device__ __forceinline__ void roe_hydrostatic_fast(R hi, R ui, R vi, 
     if (DIR == 0) { uni = ui; uti = vi; unj = uj; utj = vj; }
     else { uni = vi; uti = -ui; unj = vj; utj = -uj; }
     const R hh = R(0.5) * (hi + hj);
-    const R hm = gt_bits(hh, C::toldry_bits) ? hh : C::toldry;
+    const bool hmb = gt_bits(hh, C::toldry_bits);
+    const R hm = hmb ? hh : C::toldry;
     const R cm = sqrt(C::g * hm);
     const R den = R(2) * cm + C::tol12;
     const R sden = si + sj + C::tol12;
@@ -278,13 +305,16 @@ __host__ __device__ __forceinline__ void roe_hydrostatic_fast(R hi, R ui, R vi, 
     R l0 = um - cm;
     const R l1 = um;
     R l2 = um + cm;
+    bool fix0, fix2;
     {
         const R ci = C::sqrt_g * si, cj = C::sqrt_g * sj;
         R ei = uni - ci, ej = unj - cj;
-        if (neg_i(ei) && pos_i(ej)) l0 = ei * (ej - l0) / (ej - ei);
+        fix0 = neg_i(ei) && pos_i(ej);
+        if (fix0) l0 = ei * (ej - l0) / (ej - ei);
         ei = uni + ci;
         ej = unj + cj;
-        if (neg_i(ei) && pos_i(ej)) l2 = ej * (l2 - ei) / (ej - ei);
+        fix2 = neg_i(ei) && pos_i(ej);
+        if (fix2) l2 = ej * (l2 - ei) / (ej - ei);
     }
     const R dh = hj - hi;
     const R qi = hi * uni, qj = hj * unj;
@@ -303,6 +333,12 @@ __host__ __device__ __forceinline__ void roe_hydrostatic_fast(R hi, R ui, R vi, 
     F0 = f0;
     if (DIR == 0) { F1 = f1; F2 = f2; }
     else { F1 = -f2; F2 = f1; }
+    if constexpr (REC) {
+        rv->si = si; rv->sj = sj; rv->cm = cm; rv->q = q; rv->um = um; rv->vm = vm; rv->l0 = l0; rv->l2 = l2;
+        rv->a0h = a0h; rv->a1h = a1h; rv->a2h = a2h;
+        rv->fl = (wi ? RR_WI : 0u) | (wj ? RR_WJ : 0u) | (hmb ? RR_HM : 0u) | (fix0 ? RR_FIX0 : 0u) |
+                 (fix2 ? RR_FIX2 : 0u);
+    }
 }
 
 // ----------------------------------------------------------------------------

@@ -35,6 +35,9 @@ template cudaError_t launch_hydro_update<double, true>(const Cells3<double>&, co
 template cudaError_t launch_adj_forward<true>(const LevelSrc<double>&, const Cells3<double>&, const Plane<double>&,
                                               const Cells3W<double>&, const IBox&, const StepCtl<double>&,
                                               const double*, unsigned*, const AdjRecord&, cudaStream_t);
+template cudaError_t launch_adj_forward_rec<true>(const LevelSrc<double>&, const Cells3<double>&, const Plane<double>&,
+                                                  const Cells3W<double>&, const IBox&, double, double, const double*,
+                                                  unsigned*, const FaceRec&, cudaStream_t);
 template cudaError_t launch_adj_forward_linear<true>(const LevelSrc<double>&, const Cells3<double>&,
                                                      const Plane<double>&, const Cells3W<double>&, const IBox&, double,
                                                      double, const double*, cudaStream_t);

@@ -32,9 +32,10 @@ template <class R, int TXv = TX, int TYv = TY> struct HydroSmem {
 
 // One hydrostatic face (src/solvers/HydrostaticRoe.cpp:218-396).  L and R are
 // the cells on either side; sX are the cells' slopes along the face normal.
-template <class R, bool FAST, int DIR>
+template <class R, bool FAST, int DIR, bool REC = false>
 __device__ __forceinline__ void hydro_face(bool wall, R zL, R zR, R eL, R eR, R seL, R seR, R uL, R uR, R suL, R suR,
-                                           R vL, R vR, R svL, R svR, R& F0, R& Fa, R& Fb, R& Fc) {
+                                           R vL, R vR, R svL, R svR, R& F0, R& Fa, R& Fb, R& Fc,
+                                           RoeRecVals* rv = nullptr) {
     // wall: either side is NODATA (HydrostaticRoe.cpp:237-245)
     if (wall) {
         F0 = R(0); Fa = R(0); Fb = R(0); Fc = R(0);
@@ -69,7 +70,7 @@ __device__ __forceinline__ void hydro_face(bool wall, R zL, R zR, R eL, R eR, R 
         const R hvR = (hRs > R(0)) ? hRs * vRf : R(0);
         roe_hydrostatic_exact<DIR>(hLs, huL, hvL, hRs, huR, hvR, f0, f1, f2);
     } else {
-        roe_hydrostatic_fast<R, DIR>(hLs, uLf, vLf, hRs, uRf, vRf, f0, f1, f2);
+        roe_hydrostatic_fast<R, DIR, REC>(hLs, uLf, vLf, hRs, uRf, vRf, f0, f1, f2, rv);
     }
     // hydrostatic pressure correction, rotated with the normal
     R pL, pR;
@@ -193,12 +194,47 @@ __device__ __forceinline__ void step_cell(R o0, R o1, R o2, R dx0, R dx1, R dx2,
     }
 }
 
-template <class R, bool FAST, int TXv, int TYv, int NTv, class Src, bool LINEAR = false, class Div = NoDiv>
+// No face records (every step but the adjoint's segment recompute).
+struct NoRec {
+    static constexpr bool on = false;
+};
+// Face records of one step of the adjoint's segment recompute (fast form,
+// FP64): NREC field planes and one flag plane per direction.  x face (i, j),
+// i in 0..nx, j in 0..ny-1, at i + j (nx + 1); y face (i, j), i in 0..nx-1,
+// j in 0..ny, at i + j nx.  Each face is written once, by the tile of the cell
+// on its high side (the domain's last face by the last tile); wall faces are
+// not written (the reverse skips them).
+struct FaceRec {
+    static constexpr bool on = true;
+    double* f[2];
+    unsigned char* fl[2];
+    long long plane[2];  // doubles per field plane
+    int nx, ny;
+    __device__ __forceinline__ void put(int d, long long o, const RoeRecVals& r) const {
+        double* b = f[d] + o;
+        const long long ps = plane[d];
+        b[0] = r.si; b[ps] = r.sj; b[2 * ps] = r.cm; b[3 * ps] = r.q; b[4 * ps] = r.um; b[5 * ps] = r.vm;
+        b[6 * ps] = r.l0; b[7 * ps] = r.l2; b[8 * ps] = r.a0h; b[9 * ps] = r.a1h; b[10 * ps] = r.a2h;
+        fl[d][o] = (unsigned char)r.fl;
+    }
+    __device__ __forceinline__ void put_x(int gi, int gj, const RoeRecVals& r, bool extra) const {
+        if (gi < 0 || gi > nx || gj < 0 || gj >= ny || (extra && gi != nx)) return;
+        put(0, (long long)gi + (long long)gj * (nx + 1), r);
+    }
+    __device__ __forceinline__ void put_y(int gi, int gj, const RoeRecVals& r, bool extra) const {
+        if (gi < 0 || gi >= nx || gj < 0 || gj > ny || (extra && gj != ny)) return;
+        put(1, (long long)gi + (long long)gj * nx, r);
+    }
+};
+
+template <class R, bool FAST, int TXv, int TYv, int NTv, class Src, bool LINEAR = false, class Div = NoDiv,
+          class Rec = NoRec>
 __device__ __forceinline__ void hydro_tile_body(HydroSmem<R, TXv, TYv>& S, const Src& src, const Cells3<R>& uo,
                                                 const Plane<R>& nplane, const Cells3W<R>& out, const FaceOut<R>& fo,
                                                 const IBox& vb, int x0, int y0, R dt, R dx, R dy, DtAccum* dt_out,
                                                 unsigned* status, unsigned* post_flags = nullptr,
-                                                const Div& div = Div{}) {
+                                                const Div& div = Div{}, const Rec& rec = Rec{}) {
+    static_assert(!Rec::on || (FAST && sizeof(R) == 8), "face records are kept for the FP64 fast form");
     constexpr int GX = HydroSmem<R, TXv, TYv>::GX, GY = HydroSmem<R, TXv, TYv>::GY;
     constexpr int CELLS = TXv * TYv;
     const int t = threadIdx.x;
@@ -266,20 +302,38 @@ __device__ __forceinline__ void hydro_tile_body(HydroSmem<R, TXv, TYv>& S, const
     auto xface = [&](int fi, int fj) {
         const int r = fj + 2, cl = fi + 1, cr = fi + 2;
         R F0, Fa, Fb, Fc;
-        hydro_face<R, FAST, 0>(S.nod[r][cl] | S.nod[r][cr], S.z[r][cl], S.z[r][cr], S.eta[r][cl], S.eta[r][cr],
-                               S.sxe[fj][fi], S.sxe[fj][fi + 1], S.u[r][cl], S.u[r][cr], S.sxu[fj][fi],
-                               S.sxu[fj][fi + 1], S.v[r][cl], S.v[r][cr], S.sxv[fj][fi], S.sxv[fj][fi + 1], F0, Fa,
-                               Fb, Fc);
+        const bool wall = S.nod[r][cl] | S.nod[r][cr];
+        if constexpr (Rec::on) {
+            RoeRecVals rv;
+            hydro_face<R, FAST, 0, true>(wall, S.z[r][cl], S.z[r][cr], S.eta[r][cl], S.eta[r][cr], S.sxe[fj][fi],
+                                         S.sxe[fj][fi + 1], S.u[r][cl], S.u[r][cr], S.sxu[fj][fi], S.sxu[fj][fi + 1],
+                                         S.v[r][cl], S.v[r][cr], S.sxv[fj][fi], S.sxv[fj][fi + 1], F0, Fa, Fb, Fc,
+                                         &rv);
+            if (!wall) rec.put_x(x0 + fi, y0 + fj, rv, fi == TXv);
+        } else {
+            hydro_face<R, FAST, 0>(wall, S.z[r][cl], S.z[r][cr], S.eta[r][cl], S.eta[r][cr], S.sxe[fj][fi],
+                                   S.sxe[fj][fi + 1], S.u[r][cl], S.u[r][cr], S.sxu[fj][fi], S.sxu[fj][fi + 1],
+                                   S.v[r][cl], S.v[r][cr], S.sxv[fj][fi], S.sxv[fj][fi + 1], F0, Fa, Fb, Fc);
+        }
         S.fx[0][fj][fi] = F0; S.fx[1][fj][fi] = Fa; S.fx[2][fj][fi] = Fb; S.fx[3][fj][fi] = Fc;
         fo.store_x(x0 + fi, y0 + fj, vb, F0, Fa, Fb, Fc, fi == TXv);
     };
     auto yface = [&](int fi, int fj) {
         const int c = fi + 2, rl = fj + 1, rr = fj + 2;
         R F0, Fa, Fb, Fc;
-        hydro_face<R, FAST, 1>(S.nod[rl][c] | S.nod[rr][c], S.z[rl][c], S.z[rr][c], S.eta[rl][c], S.eta[rr][c],
-                               S.sye[fj][fi], S.sye[fj + 1][fi], S.u[rl][c], S.u[rr][c], S.syu[fj][fi],
-                               S.syu[fj + 1][fi], S.v[rl][c], S.v[rr][c], S.syv[fj][fi], S.syv[fj + 1][fi], F0, Fa,
-                               Fb, Fc);
+        const bool wall = S.nod[rl][c] | S.nod[rr][c];
+        if constexpr (Rec::on) {
+            RoeRecVals rv;
+            hydro_face<R, FAST, 1, true>(wall, S.z[rl][c], S.z[rr][c], S.eta[rl][c], S.eta[rr][c], S.sye[fj][fi],
+                                         S.sye[fj + 1][fi], S.u[rl][c], S.u[rr][c], S.syu[fj][fi], S.syu[fj + 1][fi],
+                                         S.v[rl][c], S.v[rr][c], S.syv[fj][fi], S.syv[fj + 1][fi], F0, Fa, Fb, Fc,
+                                         &rv);
+            if (!wall) rec.put_y(x0 + fi, y0 + fj, rv, fj == TYv);
+        } else {
+            hydro_face<R, FAST, 1>(wall, S.z[rl][c], S.z[rr][c], S.eta[rl][c], S.eta[rr][c], S.sye[fj][fi],
+                                   S.sye[fj + 1][fi], S.u[rl][c], S.u[rr][c], S.syu[fj][fi], S.syu[fj + 1][fi],
+                                   S.v[rl][c], S.v[rr][c], S.syv[fj][fi], S.syv[fj + 1][fi], F0, Fa, Fb, Fc);
+        }
         S.fy[0][fj][fi] = F0; S.fy[1][fj][fi] = Fa; S.fy[2][fj][fi] = Fb; S.fy[3][fj][fi] = Fc;
         fo.store_y(x0 + fi, y0 + fj, vb, F0, Fa, Fb, Fc, fj == TYv);
     };
@@ -868,6 +922,22 @@ __global__ void __launch_bounds__(NT) k_adj_forward(LevelSrc<double> src, Cells3
                                               dt_fixed ? nullptr : ctl.dt_out, ctl.status, post_flags);
 }
 
+// A recompute step (dt given) that also records every face's intermediates
+// (FAST must be true: records exist for the fast form only).
+template <bool FAST>
+__global__ void __launch_bounds__(NT) k_adj_forward_rec(LevelSrc<double> src, Cells3<double> uo, Plane<double> np,
+                                                         Cells3W<double> out, IBox vb, double dx, double dy,
+                                                         const double* dt_fixed, unsigned* post_flags, FaceRec rec) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    HydroSmem<double>& S = *reinterpret_cast<HydroSmem<double>*>(smem_raw);
+    FaceOut<double> fo{};
+    fo.on = 0;
+    static_assert(FAST, "face records are kept for the fast form");
+    hydro_tile_body<double, FAST, TX, TY, NT, LevelSrc<double>, false, NoDiv, FaceRec>(
+        S, src, uo, np, out, fo, vb, vb.lo0 + (int)blockIdx.x * TX, vb.lo1 + (int)blockIdx.y * TY, *dt_fixed, dx, dy,
+        nullptr, nullptr, post_flags, NoDiv{}, rec);
+}
+
 template <bool FAST>
 __global__ void __launch_bounds__(NT) k_adj_forward_linear(LevelSrc<double> src, Cells3<double> uo, Plane<double> np,
                                                             Cells3W<double> out, IBox vb, double dx, double dy,
@@ -982,6 +1052,18 @@ cudaError_t launch_adj_forward(const LevelSrc<double>& src, const Cells3<double>
     cudaError_t e = ensure_smem(k_adj_forward<FAST>, sm);
     if (e != cudaSuccess) return e;
     k_adj_forward<FAST><<<tile_grid(vb, TX, TY), NT, sm, st>>>(src, uo, np, out, vb, ctl, dt_fixed, post_flags, rec);
+    return cudaGetLastError();
+}
+
+template <bool FAST>
+cudaError_t launch_adj_forward_rec(const LevelSrc<double>& src, const Cells3<double>& uo, const Plane<double>& np,
+                                   const Cells3W<double>& out, const IBox& vb, double dx, double dy,
+                                   const double* dt_fixed, unsigned* post_flags, const FaceRec& rec, cudaStream_t st) {
+    const size_t sm = sizeof(HydroSmem<double>);
+    cudaError_t e = ensure_smem(k_adj_forward_rec<FAST>, sm);
+    if (e != cudaSuccess) return e;
+    k_adj_forward_rec<FAST><<<tile_grid(vb, TX, TY), NT, sm, st>>>(src, uo, np, out, vb, dx, dy, dt_fixed, post_flags,
+                                                                   rec);
     return cudaGetLastError();
 }
 

@@ -472,9 +472,17 @@ int hx_level_run_static_f64(int method, hx_level_f64* level, int nsteps, double 
  * it takes the same branches.  HX_ARITH_EXACT runs the trajectory of
  * hx_level_run_f64 with HX_ARITH_EXACT bit for bit (and of the tangent-linear
  * step's value part).
+ * options of hx_adjoint_work_bytes_f64, and the same bit OR-ed into arith of
+ * the reverse: HX_ADJ_FACE_RECORDS (fast form, k > 0) makes the segment
+ * recompute record each face's Roe intermediates (square roots, shared
+ * reciprocal, Roe averages, fixed speeds, wave strengths; 11 doubles and a
+ * flag byte per face, 2 k steps' worth in work) so the reverse reads them
+ * instead of evaluating them again; the gradient agrees with the unrecorded
+ * reverse to rounding.  Ignored for k <= 0 and the exact form.
  * Restriction: nx % 32 != 1 and ny % 16 != 1.
  */
-int64_t hx_adjoint_work_bytes_f64(int nx, int ny, int64_t pitch, int nsteps, int checkpoint_every);
+#define HX_ADJ_FACE_RECORDS 0x100
+int64_t hx_adjoint_work_bytes_f64(int nx, int ny, int64_t pitch, int nsteps, int checkpoint_every, int options);
 int64_t hx_adjoint_recompute_steps(int nsteps, int checkpoint_every);
 int hx_adjoint_forward_f64(const hx_level_f64* level, int nsteps, double cfl, int ngauges, const int64_t* gauge_cells,
                            double* series, int checkpoint_every, int arith, void* work, uint32_t* status,
@@ -486,7 +494,7 @@ int hx_adjoint_reverse_f64(const hx_level_f64* level, int nsteps, double cfl, in
 /*
  * One reverse step at a fixed dt: (lam_h, lam_hu, lam_hv) = lambda^{n+1}
  * (device planes) -> out = lambda^n, zbar += dJ/dz, *dtbar (device) = dJ/d dt.
- * work: hx_adjoint_work_bytes_f64(nx, ny, pitch, 1, 0) bytes.
+ * work: hx_adjoint_work_bytes_f64(nx, ny, pitch, 1, 0, 0) bytes.
  */
 int hx_adjoint_step_f64(const hx_level_f64* level, double dt, const double* lam_h, const double* lam_hu,
                         const double* lam_hv, double* out_h, double* out_hu, double* out_hv, double* zbar,

@@ -171,11 +171,37 @@ def test_checkpointed_reverse_equals_store_all(cuda, hxlib):
     href = torch.zeros((nsteps, len(gauges)), dtype=torch.float64, device=cuda)
     grads = []
     for every in (0, 5):
-        prob = GaugeProblem(geom, torch.zeros_like(ht), gauges, nsteps, 0.45, checkpoint_every=every)
+        prob = GaugeProblem(geom, torch.zeros_like(ht), gauges, nsteps, 0.45, checkpoint_every=every, records=False)
         prob.forward(zt, ht, zero, zero)
         grads.append(prob.reverse(href))
     for a, b in zip(*grads):
         assert torch.equal(a, b)
+
+
+@pytest.mark.parametrize("every", [1, 5, 11])
+def test_face_records_reverse_matches(cuda, hxlib, every):
+    """Uniform checkpoints with face records (the reverse reads the Roe
+    intermediates the segment recompute wrote, Manning and dry-clamp steps
+    included) against the same sweep evaluating them again: equal to rounding.
+    The two differ in the last bits only: the forward forms 1/den, 1/cm and
+    1/sden from one reciprocal and the sonic-fixed speeds by division, the
+    recomputation from a reciprocal of a longer product."""
+    geom, z, h0, hu0, hv0, gauges, _, _ = misfit_problem(nsteps=23)
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(cuda)
+    base = [T(z), T(h0), T(hu0), T(hv0)]
+    nman = torch.zeros_like(base[0])
+    nman[:, : geom.nx // 2] = 0.03
+    href = torch.full((23, len(gauges)), 1.0, dtype=torch.float64, device=cuda)
+    grads = []
+    for rec in (False, True):
+        prob = GaugeProblem(geom, nman, gauges, 23, 0.45, checkpoint_every=every, records=rec)
+        assert (prob.options == capi.HX_ADJ_FACE_RECORDS) == rec
+        prob.forward(*base)
+        grads.append(prob.reverse(href))
+    for a, b in zip(*grads):
+        scale = float(b.abs().max())
+        assert scale > 0
+        assert float((a - b).abs().max()) <= 1e-12 * scale
 
 
 @pytest.mark.parametrize("slots", [2, 3, 5, 9])

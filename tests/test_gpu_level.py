@@ -188,3 +188,39 @@ def test_host_buffer_run(cuda, oracle_lib, hxlib, method, nx, ny, nsteps, arith)
         for k, a in enumerate((h, hu, hv)):
             assert rel_err(a, got[k]) <= 1e-13
         assert abs(t.value - lev.time.item()) <= 1e-13 * lev.time.item()
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_nodata_predicate_at_its_edges(cuda, oracle_lib, dtype):
+    """The NODATA test |z + 9999| < 1e-10 at the edge of its interval: beds a
+    few representable steps either side of -9999 (double: |k| <= 54 steps of
+    2^-39 qualify; float: -9999 alone) give the oracle's walls, dt and state."""
+    rng = np.random.default_rng(17)
+    case = workloads.fractal_dam_break(64, 48, seed=23, amplitude=1.0, nodata_frac=0.0)
+    z = case.z.astype(dtype)
+    sel = rng.random(z.shape) < 0.08
+    k = rng.integers(-60, 61, size=z.shape)
+    if dtype == np.float64:
+        b = np.array(-9999.0).view(np.int64) + k
+        edge = b.view(np.float64)
+    else:
+        b = np.array(-9999.0, dtype=np.float32).view(np.int32) + (k % 3 - 1)
+        edge = b.astype(np.int32).view(np.float32)
+    z[sel] = edge[sel]
+    g = case.geom
+    L = oracle_lib.Level(g.nx, g.ny, g.dx, g.dy, g.bc_lo, g.bc_hi)
+    f = [a.astype(dtype) for a in (case.h, case.hu, case.hv, z, case.n)]
+    mn, mx = oracle_lib.compute_dt(L, f[0], f[1], f[2], f[3])
+    tdt = torch.float64 if dtype == np.float64 else torch.float32
+    lev = Level.from_numpy(g, *f, dtype=tdt, device=cuda)
+    gmn, gmx = lev.compute_dt()
+    dt = float(dtype(mn * case.cfl))
+    ref = oracle_lib.advance(L, 1, f[0], f[1], f[2], f[3], f[4], dt)
+    got = lev.advance(1, dt, arith=EXACT).cpu().numpy()
+    if dtype == np.float64:
+        assert gmn == mn and gmx == mx
+        for c in range(3):
+            assert np.array_equal(got[c], ref[c]), c
+    else:  # a misplaced wall changes the state by O(1) next to it
+        assert gmn == pytest.approx(mn, rel=1e-6) and gmx == pytest.approx(mx, rel=1e-6)
+        assert rel_err(got, ref) <= 1e-5
