@@ -422,19 +422,7 @@ __device__ __forceinline__ void slope_rev(double qm, double q, double qp, double
     gqp = gdp;
 }
 
-// The fast van Leer slope (van_leer_slope<double, true>, same operations) that
-// also hands back the reciprocal 1 / (dm + dp) its reverse needs.
-__device__ __forceinline__ double vl_slope_rs(double qm, double q, double qp, double& rS) {
-    const double dm = q - qm, dp = qp - q;
-    rS = 0.0;
-    if (abs_le_bits(dp, Cst<double>::tol12_bits)) return 0.0;
-    const double p = dm * dp;
-    if (!pos_i(p)) return 0.0;
-    rS = rcp_nr(dm + dp);
-    return (p + p) * rS;
-}
-
-// slope_rev with the reciprocal from vl_slope_rs (rS == 0: the slope was 0 by a branch).
+// slope_rev with the reciprocal from van_leer_slope_rs (rS == 0: the slope was 0 by a branch).
 __device__ __forceinline__ void slope_rev_rs(double qm, double q, double qp, double rS, double gs, double& gqm,
                                              double& gq, double& gqp) {
     gqm = gq = gqp = 0.0;
@@ -555,10 +543,18 @@ __global__ void __launch_bounds__(ANT) k_adj_faces(AdjArgs A) {
         for (int k = t; k < ATY * (ATX + 4); k += ANT) {  // slopes, columns x0-2 .. x0+TX+1
             const int row = k / (ATX + 4), col = k % (ATX + 4) - 2;
             const int r = row + H3, c = col + H3;
-            if constexpr (FAST) {
-                P.s[0][row][col + 2] = vl_slope_rs(S.eta[r][c - 1], S.eta[r][c], S.eta[r][c + 1], P.rs[0][row][col + 2]);
-                P.s[1][row][col + 2] = vl_slope_rs(S.u[r][c - 1], S.u[r][c], S.u[r][c + 1], P.rs[1][row][col + 2]);
-                P.s[2][row][col + 2] = vl_slope_rs(S.v[r][c - 1], S.v[r][c], S.v[r][c + 1], P.rs[2][row][col + 2]);
+            if constexpr (REC) {  // recorded for cells -1..nx; others feed no face of the domain
+                const int gi = x0 + col, gj = y0 + row;
+                const bool in = gi >= -1 && gi <= nx && gj < ny;
+                const long long o = (long long)(gi + 1) + (long long)gj * (nx + 2), ps = A.rec.slplane[0];
+                for (int q = 0; q < 3; ++q) {
+                    P.s[q][row][col + 2] = in ? A.rec.sl[0][q * ps + o] : 0.0;
+                    P.rs[q][row][col + 2] = in ? A.rec.sl[0][(3 + q) * ps + o] : 0.0;
+                }
+            } else if constexpr (FAST) {
+                P.s[0][row][col + 2] = van_leer_slope_rs(S.eta[r][c - 1], S.eta[r][c], S.eta[r][c + 1], P.rs[0][row][col + 2]);
+                P.s[1][row][col + 2] = van_leer_slope_rs(S.u[r][c - 1], S.u[r][c], S.u[r][c + 1], P.rs[1][row][col + 2]);
+                P.s[2][row][col + 2] = van_leer_slope_rs(S.v[r][c - 1], S.v[r][c], S.v[r][c + 1], P.rs[2][row][col + 2]);
             } else {
                 P.s[0][row][col + 2] = van_leer_slope<double, false>(S.eta[r][c - 1], S.eta[r][c], S.eta[r][c + 1]);
                 P.s[1][row][col + 2] = van_leer_slope<double, false>(S.u[r][c - 1], S.u[r][c], S.u[r][c + 1]);
@@ -669,10 +665,18 @@ __global__ void __launch_bounds__(ANT) k_adj_faces(AdjArgs A) {
         for (int k = t; k < (ATY + 4) * ATX; k += ANT) {  // slopes, rows y0-2 .. y0+TY+1
             const int row = k / ATX - 2, col = k % ATX;
             const int r = row + H3, c = col + H3;
-            if constexpr (FAST) {
-                P.s[0][row + 2][col] = vl_slope_rs(S.eta[r - 1][c], S.eta[r][c], S.eta[r + 1][c], P.rs[0][row + 2][col]);
-                P.s[1][row + 2][col] = vl_slope_rs(S.u[r - 1][c], S.u[r][c], S.u[r + 1][c], P.rs[1][row + 2][col]);
-                P.s[2][row + 2][col] = vl_slope_rs(S.v[r - 1][c], S.v[r][c], S.v[r + 1][c], P.rs[2][row + 2][col]);
+            if constexpr (REC) {
+                const int gi = x0 + col, gj = y0 + row;
+                const bool in = gj >= -1 && gj <= ny && gi < nx;
+                const long long o = (long long)gi + (long long)(gj + 1) * nx, ps = A.rec.slplane[1];
+                for (int q = 0; q < 3; ++q) {
+                    P.s[q][row + 2][col] = in ? A.rec.sl[1][q * ps + o] : 0.0;
+                    P.rs[q][row + 2][col] = in ? A.rec.sl[1][(3 + q) * ps + o] : 0.0;
+                }
+            } else if constexpr (FAST) {
+                P.s[0][row + 2][col] = van_leer_slope_rs(S.eta[r - 1][c], S.eta[r][c], S.eta[r + 1][c], P.rs[0][row + 2][col]);
+                P.s[1][row + 2][col] = van_leer_slope_rs(S.u[r - 1][c], S.u[r][c], S.u[r + 1][c], P.rs[1][row + 2][col]);
+                P.s[2][row + 2][col] = van_leer_slope_rs(S.v[r - 1][c], S.v[r][c], S.v[r + 1][c], P.rs[2][row + 2][col]);
             } else {
                 P.s[0][row + 2][col] = van_leer_slope<double, false>(S.eta[r - 1][c], S.eta[r][c], S.eta[r + 1][c]);
                 P.s[1][row + 2][col] = van_leer_slope<double, false>(S.u[r - 1][c], S.u[r][c], S.u[r + 1][c]);
@@ -989,7 +993,7 @@ struct AdjLayout {
     int nblocks;
     // face records (uniform checkpoints, fast form, on request): one set per step of the two segments in
     // flight, after everything else so the layout is otherwise the same with and without them
-    size_t rec, rec_step, rec_plane[2];
+    size_t rec, rec_step, rec_plane[2], rec_slplane[2];
 };
 
 size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
@@ -1090,8 +1094,11 @@ AdjLayout adj_layout(int nx, int ny, long long pitch, int nsteps, int every, boo
     if (records && L.seg) {
         L.rec_plane[0] = al256((size_t)(nx + 1) * ny * sizeof(double)) / sizeof(double);
         L.rec_plane[1] = al256((size_t)nx * (ny + 1) * sizeof(double)) / sizeof(double);
-        L.rec_step = NREC * (L.rec_plane[0] + L.rec_plane[1]) * sizeof(double) + al256((size_t)(nx + 1) * ny) +
-                     al256((size_t)nx * (ny + 1));
+        L.rec_slplane[0] = al256((size_t)(nx + 2) * ny * sizeof(double)) / sizeof(double);
+        L.rec_slplane[1] = al256((size_t)nx * (ny + 2) * sizeof(double)) / sizeof(double);
+        L.rec_step = (NREC * (L.rec_plane[0] + L.rec_plane[1]) + 6 * (L.rec_slplane[0] + L.rec_slplane[1])) *
+                         sizeof(double) +
+                     al256((size_t)(nx + 1) * ny) + al256((size_t)nx * (ny + 1));
         L.rec = o; o += 2 * (size_t)L.seg * L.rec_step;
     }
     L.total = o;
@@ -1104,7 +1111,11 @@ FaceRec rec_at(const AdjLayout& A, char* base, int k, int nx, int ny) {
     char* p = base + A.rec + (size_t)k * A.rec_step;
     R.f[0] = reinterpret_cast<double*>(p);
     R.f[1] = R.f[0] + NREC * A.rec_plane[0];
-    R.fl[0] = reinterpret_cast<unsigned char*>(R.f[1] + NREC * A.rec_plane[1]);
+    R.sl[0] = R.f[1] + NREC * A.rec_plane[1];
+    R.sl[1] = R.sl[0] + 6 * A.rec_slplane[0];
+    R.slplane[0] = (long long)A.rec_slplane[0];
+    R.slplane[1] = (long long)A.rec_slplane[1];
+    R.fl[0] = reinterpret_cast<unsigned char*>(R.sl[1] + 6 * A.rec_slplane[1]);
     R.fl[1] = R.fl[0] + al256((size_t)(nx + 1) * ny);
     R.plane[0] = (long long)A.rec_plane[0];
     R.plane[1] = (long long)A.rec_plane[1];

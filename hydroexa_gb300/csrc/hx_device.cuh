@@ -192,6 +192,19 @@ template <class R, bool FAST> __host__ __device__ __forceinline__ R van_leer_slo
     }
 }
 
+// The fast van Leer slope (van_leer_slope<double, true>, same operations) that
+// also hands back the reciprocal 1 / (dm + dp) its reverse needs (0 where the
+// slope is 0 by a branch).
+__host__ __device__ __forceinline__ double van_leer_slope_rs(double qm, double q, double qp, double& rS) {
+    const double dm = q - qm, dp = qp - q;
+    rS = 0.0;
+    if (abs_le_bits(dp, Cst<double>::tol12_bits)) return 0.0;
+    const double p = dm * dp;
+    if (!pos_i(p)) return 0.0;
+    rS = rcp_nr(dm + dp);
+    return (p + p) * rS;
+}
+
 // ----------------------------------------------------------------------------
 // Homogeneous Roe flux (include/solvers/kernels/HydrostaticRoe.H:44-159) for a
 // face of direction DIR (0: normal +x, 1: normal +y).  The normal is fixed at

@@ -203,13 +203,35 @@ struct NoRec {
 // i in 0..nx, j in 0..ny-1, at i + j (nx + 1); y face (i, j), i in 0..nx-1,
 // j in 0..ny, at i + j nx.  Each face is written once, by the tile of the cell
 // on its high side (the domain's last face by the last tile); wall faces are
-// not written (the reverse skips them).
+// not written (the reverse skips them).  Slope records: per direction the
+// three van Leer slopes (eta, u, v) and their reciprocals 1 / (dm + dp), six
+// planes, of the cells the faces use: x slopes of cells i in -1..nx at
+// (i + 1) + j (nx + 2), y slopes of cells j in -1..ny at i + (j + 1) nx; each
+// written by the tile that owns the cell (ghost cells by the edge tiles).
 struct FaceRec {
     static constexpr bool on = true;
     double* f[2];
     unsigned char* fl[2];
     long long plane[2];  // doubles per field plane
+    double* sl[2];
+    long long slplane[2];
     int nx, ny;
+    __device__ __forceinline__ void put_sx(int col, int TXv, int gi, int gj, int k, double s, double rS) const {
+        if (gj < 0 || gj >= ny) return;
+        const bool own = (col >= 0 && col < TXv) ? (gi <= nx) : (col < 0 ? gi == -1 : gi == nx);
+        if (!own) return;
+        const long long o = (long long)(gi + 1) + (long long)gj * (nx + 2);
+        sl[0][k * slplane[0] + o] = s;
+        sl[0][(3 + k) * slplane[0] + o] = rS;
+    }
+    __device__ __forceinline__ void put_sy(int row, int TYv, int gi, int gj, int k, double s, double rS) const {
+        if (gi < 0 || gi >= nx) return;
+        const bool own = (row >= 0 && row < TYv) ? (gj <= ny) : (row < 0 ? gj == -1 : gj == ny);
+        if (!own) return;
+        const long long o = (long long)gi + (long long)(gj + 1) * nx;
+        sl[1][k * slplane[1] + o] = s;
+        sl[1][(3 + k) * slplane[1] + o] = rS;
+    }
     __device__ __forceinline__ void put(int d, long long o, const RoeRecVals& r) const {
         double* b = f[d] + o;
         const long long ps = plane[d];
@@ -274,15 +296,39 @@ __device__ __forceinline__ void hydro_tile_body(HydroSmem<R, TXv, TYv>& S, const
     // --- B: van Leer slopes, once per cell and direction ---------------------
     auto xslopes = [&](int row, int col) {  // tile cell (col, row), col in -1..TXv
         const int r = row + 2, c = col + 2;
-        S.sxe[row][col + 1] = van_leer_slope<R, FAST>(S.eta[r][c - 1], S.eta[r][c], S.eta[r][c + 1]);
-        S.sxu[row][col + 1] = van_leer_slope<R, FAST>(S.u[r][c - 1], S.u[r][c], S.u[r][c + 1]);
-        S.sxv[row][col + 1] = van_leer_slope<R, FAST>(S.v[r][c - 1], S.v[r][c], S.v[r][c + 1]);
+        if constexpr (Rec::on) {
+            double rs0, rs1, rs2;
+            const double s0 = van_leer_slope_rs(S.eta[r][c - 1], S.eta[r][c], S.eta[r][c + 1], rs0);
+            const double s1 = van_leer_slope_rs(S.u[r][c - 1], S.u[r][c], S.u[r][c + 1], rs1);
+            const double s2 = van_leer_slope_rs(S.v[r][c - 1], S.v[r][c], S.v[r][c + 1], rs2);
+            S.sxe[row][col + 1] = s0; S.sxu[row][col + 1] = s1; S.sxv[row][col + 1] = s2;
+            const int gi = x0 + col, gj = y0 + row;
+            rec.put_sx(col, TXv, gi, gj, 0, s0, rs0);
+            rec.put_sx(col, TXv, gi, gj, 1, s1, rs1);
+            rec.put_sx(col, TXv, gi, gj, 2, s2, rs2);
+        } else {
+            S.sxe[row][col + 1] = van_leer_slope<R, FAST>(S.eta[r][c - 1], S.eta[r][c], S.eta[r][c + 1]);
+            S.sxu[row][col + 1] = van_leer_slope<R, FAST>(S.u[r][c - 1], S.u[r][c], S.u[r][c + 1]);
+            S.sxv[row][col + 1] = van_leer_slope<R, FAST>(S.v[r][c - 1], S.v[r][c], S.v[r][c + 1]);
+        }
     };
     auto yslopes = [&](int row, int col) {  // row in -1..TYv
         const int r = row + 2, c = col + 2;
-        S.sye[row + 1][col] = van_leer_slope<R, FAST>(S.eta[r - 1][c], S.eta[r][c], S.eta[r + 1][c]);
-        S.syu[row + 1][col] = van_leer_slope<R, FAST>(S.u[r - 1][c], S.u[r][c], S.u[r + 1][c]);
-        S.syv[row + 1][col] = van_leer_slope<R, FAST>(S.v[r - 1][c], S.v[r][c], S.v[r + 1][c]);
+        if constexpr (Rec::on) {
+            double rs0, rs1, rs2;
+            const double s0 = van_leer_slope_rs(S.eta[r - 1][c], S.eta[r][c], S.eta[r + 1][c], rs0);
+            const double s1 = van_leer_slope_rs(S.u[r - 1][c], S.u[r][c], S.u[r + 1][c], rs1);
+            const double s2 = van_leer_slope_rs(S.v[r - 1][c], S.v[r][c], S.v[r + 1][c], rs2);
+            S.sye[row + 1][col] = s0; S.syu[row + 1][col] = s1; S.syv[row + 1][col] = s2;
+            const int gi = x0 + col, gj = y0 + row;
+            rec.put_sy(row, TYv, gi, gj, 0, s0, rs0);
+            rec.put_sy(row, TYv, gi, gj, 1, s1, rs1);
+            rec.put_sy(row, TYv, gi, gj, 2, s2, rs2);
+        } else {
+            S.sye[row + 1][col] = van_leer_slope<R, FAST>(S.eta[r - 1][c], S.eta[r][c], S.eta[r + 1][c]);
+            S.syu[row + 1][col] = van_leer_slope<R, FAST>(S.u[r - 1][c], S.u[r][c], S.u[r + 1][c]);
+            S.syv[row + 1][col] = van_leer_slope<R, FAST>(S.v[r - 1][c], S.v[r][c], S.v[r + 1][c]);
+        }
     };
     for (int k = t; k < CELLS; k += NTv) {
         xslopes(k / TXv, k % TXv);

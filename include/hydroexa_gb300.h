@@ -476,9 +476,10 @@ int hx_level_run_static_f64(int method, hx_level_f64* level, int nsteps, double 
  * the reverse: HX_ADJ_FACE_RECORDS (fast form, k > 0) makes the segment
  * recompute record each face's Roe intermediates (square roots, shared
  * reciprocal, Roe averages, fixed speeds, wave strengths; 11 doubles and a
- * flag byte per face, 2 k steps' worth in work) so the reverse reads them
- * instead of evaluating them again; the gradient agrees with the unrecorded
- * reverse to rounding.  Ignored for k <= 0 and the exact form.
+ * flag byte per face) and each cell's van Leer slopes with their reciprocals,
+ * 2 k steps' worth in work, so the reverse reads them instead of evaluating
+ * them again; the gradient agrees with the unrecorded reverse to rounding.
+ * Ignored for k <= 0 and the exact form.
  * Restriction: nx % 32 != 1 and ny % 16 != 1.
  */
 #define HX_ADJ_FACE_RECORDS 0x100
