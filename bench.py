@@ -200,7 +200,7 @@ def main():
     import torch
 
     import hydroexa_gb300
-    from hydroexa_gb300 import capi
+    from hydroexa_gb300 import capi, ranks
     from hydroexa_gb300.level import DtAccum, Level
 
     ws, rank, local = dist_env()
@@ -248,11 +248,7 @@ def main():
     launches = capi.launch_count() - n0
     status = lev.status.read()
     assert status == 0, f"device status {status}"
-    ms = e0.elapsed_time(e1)
-    if dist is not None:
-        t = torch.tensor([ms], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = ranks.reduce_real_max([e0.elapsed_time(e1)])[0]  # the slowest rank's time
     value = ws * cells * args.steps / (ms * 1e-3) / 1e6
 
     # ---- dominant kernel: per-launch duration with events on its stream
@@ -295,11 +291,7 @@ def main():
             e2e_step()
         f1.record(stream)
         f1.synchronize()
-        ems = f0.elapsed_time(f1)
-        if dist is not None:
-            t = torch.tensor([ems], device=dev, dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ems = float(t.item())
+        ems = ranks.reduce_real_max([f0.elapsed_time(f1)])[0]
         L.hx_host_cache_release()
         e2e = {"value": ws * cells * ke / (ems * 1e-3) / 1e6, "unit": UNIT, "h2d_bytes_per_step": 40 * cells,
                "d2h_bytes_per_step": 24 * cells + 12, "steps": ke,

@@ -19,7 +19,7 @@ from dataclasses import dataclass, field
 
 import torch
 
-from . import capi
+from . import capi, ranks
 from .level import DtAccum, Geometry, Level, array4, box
 from .params import PhysicsParameters
 
@@ -86,7 +86,8 @@ class BaseSolver:
     # BaseSolver.H:120-165
     def compute_dt(self, dt: list, U, terrain, geom, ref_ratio, finest_level: int, cfl: float) -> None:
         dt_tmp = [self.compute_dt_level(U, terrain, geom, lev, cfl) for lev in range(finest_level + 1)]
-        # (the MPI ReduceRealMin of the reference is the identity on one process)
+        # 1. minimum over the ranks first (ParallelDescriptor::ReduceRealMin, BaseSolver.H:133)
+        dt_tmp = ranks.reduce_real_min(dt_tmp)
         dt_0 = dt_tmp[0]
         factor = 1.0
         for lev in range(1, finest_level + 1):
