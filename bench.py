@@ -448,13 +448,13 @@ def adjoint_measure(dev, nsteps=2000, every=45, fd_eps=1e-6):
     prob_bytes = prob.work_bytes
     J0 = float(((series - href) ** 2).sum())
 
-    def fd_check(prob, base, href, grads, seeds, nx, ny):
+    def fd_check(prob, base, href, grads, seeds, nx, ny, steps=(fd_eps, fd_eps / 10)):
         out = {}
         for name, k, seed in seeds:
             d = T(workloads.smooth_field(nx, ny, seed=seed, amplitude=1.0))
             ad = float((grads[k] * d).sum())
             rec = {"adjoint": ad}
-            for eps in (fd_eps, fd_eps / 10):
+            for eps in steps:
                 plus, minus = list(base), list(base)
                 plus[k] = base[k] + eps * d
                 minus[k] = base[k] - eps * d
@@ -462,6 +462,7 @@ def adjoint_measure(dev, nsteps=2000, every=45, fd_eps=1e-6):
                 jm = float(((prob.forward(*minus) - href) ** 2).sum())
                 fdv = (jp - jm) / (2 * eps)
                 rec["step_%g" % eps] = {"central_difference": fdv, "rel_err": abs(ad - fdv) / max(abs(fdv), 1e-300)}
+            rec["best_rel_err"] = min(v["rel_err"] for key, v in rec.items() if key.startswith("step_"))
             out[name] = rec
         return out
 
@@ -514,8 +515,10 @@ def adjoint_measure(dev, nsteps=2000, every=45, fd_eps=1e-6):
         sref = sp.forward(base[0] + dz, *base[1:]).clone()
         sp.forward(*base)
         sgr = sp.reverse(sref)
+        # a central difference is exact to O(eps^2) only while no limiter or bed kink lies within eps; the
+        # usual step scan (1e-5 .. 1e-8) shows the V of truncation against kinks and rounding
         scan.append({"steps": hsteps, "fd": fd_check(sp, base, sref, sgr, (("z", 0, 7), ("h0", 1, 8), ("hu0", 2, 9)),
-                                                     g.nx, g.ny)})
+                                                     g.nx, g.ny, steps=(1e-5, 1e-6, 1e-7, 1e-8))})
         del sp
     return {"workload": "512x512 FP64 hydrostatic-Roe, %d steps, smooth bed (32 Gaussians, 0.3 m), 0.2 m hump, "
                         "64 gauges, reference series from a perturbed bed (seed 6, 0.02 m)" % nsteps,

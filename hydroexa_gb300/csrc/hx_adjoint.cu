@@ -1253,7 +1253,8 @@ int adjoint_forward(const hx_level_f64* L, int nsteps, double cfl, int ngauges, 
         for (int k = 0; k < 3; ++k) { in[k] = a + k * A.plane; out[k] = b + k * A.plane; }
         StepCtl<double> ctl;
         ctl.dt_host = 0.0; ctl.cfl = cfl;
-        ctl.dt_in = &slot[n % 3]; ctl.dt_out = &slot[(n + 1) % 3]; ctl.dt_reset = &slot[(n + 2) % 3];
+        ctl.dt_in = &slot[n % 3]; ctl.dt_out = n + 1 < nsteps ? &slot[(n + 1) % 3] : nullptr;
+        ctl.dt_reset = &slot[(n + 2) % 3];
         ctl.status = stw; ctl.time = nullptr; ctl.dx = L->dx; ctl.dy = L->dy;
         AdjRecord rec{&dth[n], (series && n >= 1) ? series + (size_t)(n - 1) * ngauges : nullptr,
                       (const long long*)gauges, ngauges};

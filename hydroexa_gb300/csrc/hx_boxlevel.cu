@@ -139,7 +139,8 @@ extern "C" int hx_boxlevel_run_f64(int nboxes, const hx_levelbox_f64* boxes, int
     for (int s = 0; s < nsteps && e == cudaSuccess; ++s) {
         StepCtl<double> ctl;
         ctl.dt_host = 0.0; ctl.cfl = cfl;
-        ctl.dt_in = &slot[s % 3]; ctl.dt_out = &slot[(s + 1) % 3]; ctl.dt_reset = &slot[(s + 2) % 3];
+        ctl.dt_in = &slot[s % 3]; ctl.dt_out = s + 1 < nsteps ? &slot[(s + 1) % 3] : nullptr;
+        ctl.dt_reset = &slot[(s + 2) % 3];
         ctl.status = status; ctl.time = time_dev; ctl.dx = dx; ctl.dy = dy;
         src.phase = s % 2;
         e = arith == HX_ARITH_EXACT ? launch_boxlevel<false>(src, tiles, ntiles, ctl, st)

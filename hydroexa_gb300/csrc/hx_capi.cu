@@ -374,7 +374,7 @@ int level_run(int method, L* lv, R* ha, R* hua, R* hva, int nsteps, R cfl, void*
         ctl.dt_host = R(0);
         ctl.cfl = cfl;
         ctl.dt_in = &slot[s % 3];
-        ctl.dt_out = &slot[(s + 1) % 3];
+        ctl.dt_out = s + 1 < nsteps ? &slot[(s + 1) % 3] : nullptr;  // no step reads the last one's bound
         ctl.dt_reset = &slot[(s + 2) % 3];
         ctl.status = status;
         ctl.time = time_dev;
@@ -728,7 +728,8 @@ int hx_level_run_host_f64(int method, int nx, int ny, double dx, double dy, cons
     auto step_ctl = [&](int s, int b) {
         StepCtl<double> c;
         c.dt_host = 0.0; c.cfl = cfl;
-        c.dt_in = &slot[s % 3]; c.dt_out = &slot[(s + 1) % 3]; c.dt_reset = b ? nullptr : &slot[(s + 2) % 3];
+        c.dt_in = &slot[s % 3]; c.dt_out = s + 1 < nsteps ? &slot[(s + 1) % 3] : nullptr;
+        c.dt_reset = b ? nullptr : &slot[(s + 2) % 3];
         c.status = status; c.time = b ? nullptr : tdev; c.dx = dx; c.dy = dy;
         return c;
     };

@@ -115,7 +115,7 @@ extern "C" int hx_level_run_static_f64(int method, hx_level_f64* L, int nsteps, 
         ctl.dt_host = 0.0;
         ctl.cfl = cfl;
         ctl.dt_in = &slot[s % 3];
-        ctl.dt_out = &slot[(s + 1) % 3];
+        ctl.dt_out = s + 1 < nsteps ? &slot[(s + 1) % 3] : nullptr;
         ctl.dt_reset = &slot[(s + 2) % 3];
         ctl.status = stw;
         ctl.time = time_dev;
