@@ -520,6 +520,18 @@ def adjoint_measure(dev, nsteps=2000, every=45, fd_eps=1e-6):
         scan.append({"steps": hsteps, "fd": fd_check(sp, base, sref, sgr, (("z", 0, 7), ("h0", 1, 8), ("hu0", 2, 9)),
                                                      g.nx, g.ny, steps=(1e-5, 1e-6, 1e-7, 1e-8))})
         del sp
+    # a state with no kink in the gauges' domain of dependence: the configured FD step, 1e-6
+    mono = {}
+    for hsteps in [h for h in (100, 300) if h <= nsteps]:
+        mc, mg = workloads.adjoint_monotone_case(nsteps=hsteps)
+        base = [T(mc.z), T(mc.h), T(mc.hu), T(mc.hv)]
+        mp = GaugeProblem(mc.geom, zero.clone(), mg, hsteps, mc.cfl, checkpoint_every=every)
+        mref = mp.forward(base[0] + dz, *base[1:]).clone()
+        mp.forward(*base)
+        mgr = mp.reverse(mref)
+        mono["steps_%d" % hsteps] = fd_check(mp, base, mref, mgr, (("z", 0, 7), ("h0", 1, 8), ("hu0", 2, 9)),
+                                             g.nx, g.ny, steps=(1e-6,))
+        del mp
     return {"workload": "512x512 FP64 hydrostatic-Roe, %d steps, smooth bed (32 Gaussians, 0.3 m), 0.2 m hump, "
                         "64 gauges, reference series from a perturbed bed (seed 6, 0.02 m)" % nsteps,
             "loss": J0, "checkpoint_every": every, "face_records": face_records,
@@ -534,6 +546,10 @@ def adjoint_measure(dev, nsteps=2000, every=45, fd_eps=1e-6):
             "fd_check_note": "the initial state is a lake at rest outside the hump: limiters there sit on their "
                              "flat-data branch (|dp| <= 1e-12), a kink that a 1e-6 step leaves, and the exact "
                              "linearisation of single-stage MUSCL + forward Euler grows by up to 1.064 per step",
+            "fd_kink_free": {"workload": "512x512, planar bed 0.2x + 0.1y, free surface and currents increasing "
+                                         "strictly in x and y, open boundaries, 64 gauges in the central "
+                                         "[0.3, 0.7]^2: no limiter, bed-maximum, sonic or CFL arg-max switch "
+                                         "within the gauges' domain of dependence", "runs": mono},
             "fd_horizon_scan": {"workload": "same bed and gauges, free surface 1.0 + 0.05 m undulation + 0.2 m hump, "
                                             "smooth currents up to 0.2 m/s (no quiescent region)",
                                 "runs": scan}}

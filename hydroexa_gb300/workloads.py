@@ -180,6 +180,29 @@ def adjoint_case(nx=512, ny=512, seed=5, ngauss=32, amplitude=0.3, hump=0.2, nga
     return case, gauges
 
 
+def adjoint_monotone_case(nx=512, ny=512, seed=5, ngauges=64, nsteps=100, cfl=0.45):
+    """A state on which the step map has no kink near the gauges' domain of
+    dependence: a planar bed (0.2 x + 0.1 y, so the face bed max(zL, zR) never
+    switches side), a free surface and currents increasing strictly in x and y
+    (every van Leer ratio positive, no limiter at r <= 0 or on the flat-data
+    branch), open boundaries (the edge copies hold the edge slopes at exactly
+    zero whatever the perturbation) and gauges in the central [0.3, 0.7]^2,
+    farther from the boundaries than any wave travels in nsteps."""
+    rng = np.random.default_rng(seed)
+    X, Y = _centres(nx, ny)
+    z = 0.2 * X + 0.1 * Y
+    eta = 1.0 + 0.03 * X + 0.02 * Y + 0.01 * X * Y
+    h = eta - z
+    u = 0.10 + 0.05 * X + 0.02 * Y
+    v = 0.05 + 0.03 * Y + 0.01 * X
+    gi = rng.integers(int(0.3 * nx), int(0.7 * nx), size=ngauges)
+    gj = rng.integers(int(0.3 * ny), int(0.7 * ny), size=ngauges)
+    gauges = np.unique(gi + gj * nx)
+    geom = Geometry(nx, ny, 1.0 / nx, 1.0 / ny, (1, 1), (1, 1))
+    case = Case("adjoint_monotone_%dx%d" % (nx, ny), geom, h, h * u, h * v, z, np.zeros_like(h), cfl, nsteps, 1)
+    return case, gauges
+
+
 def adjoint_smooth_case(nx=512, ny=512, seed=5, ngauges=64, nsteps=100, cfl=0.45):
     """The adjoint bed and gauges with a state that has no quiescent region:
     free surface 1.0 + 0.05 m undulation + 0.2 m hump (centre off the cell
