@@ -432,7 +432,7 @@ __device__ __forceinline__ void hydro_tile_body(HydroSmem<R, TXv, TYv>& S, const
 }
 
 template <class R, bool FAST, class Src>
-__global__ void __launch_bounds__(NT) k_hydro_tile(Src src, Cells3<R> uo, Plane<R> nplane, Cells3W<R> out,
+__global__ void __launch_bounds__(NT, 4) k_hydro_tile(Src src, Cells3<R> uo, Plane<R> nplane, Cells3W<R> out,
                                                    FaceOut<R> fo, IBox vb, StepCtl<R> ctl) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     HydroSmem<R>& S = *reinterpret_cast<HydroSmem<R>*>(smem_raw);
