@@ -41,6 +41,7 @@ UNITS = {
     "hx_adjoint": [],
     "hx_roofs": [],
     "hx_boxlevel": [],
+    "hx_plotfile": [],
 }
 
 

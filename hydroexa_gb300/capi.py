@@ -68,6 +68,17 @@ class LevelBoxF64(Structure):
                 ("hi", c_int32 * 2)]
 
 
+class PlotBoxF64(Structure):
+    _fields_ = [("h", c_void_p), ("hu", c_void_p), ("hv", c_void_p), ("z", c_void_p), ("n", c_void_p),
+                ("pitch", c_int64), ("lo", c_int32 * 2), ("hi", c_int32 * 2)]
+
+
+class PlotLevelF64(Structure):
+    _fields_ = [("boxes", POINTER(PlotBoxF64)), ("nboxes", c_int32), ("domain_lo", c_int32 * 2),
+                ("domain_hi", c_int32 * 2), ("dx", c_double), ("dy", c_double), ("ref_ratio", c_int32),
+                ("istep", c_int32)]
+
+
 class EnsembleMemberF64(Structure):
     _fields_ = [("level", LevelF64), ("h_alt", c_void_p), ("hu_alt", c_void_p), ("hv_alt", c_void_p),
                 ("tile_shape", c_int32)]
@@ -146,6 +157,8 @@ def _declare(L):
                                          c_void_p, c_void_p]
     L.hx_level_diagnostics_f64.argtypes = [POINTER(LevelF64), c_void_p, c_void_p, c_void_p]
     L.hx_measure_fp64_rate.argtypes = [POINTER(c_double), POINTER(c_double), c_void_p]
+    L.hx_write_plotfile_f64.argtypes = [ctypes.c_char_p, c_int, c_double, c_int, POINTER(PlotLevelF64),
+                                        POINTER(c_double), POINTER(c_double), c_void_p]
     L.hx_boxlevel_work_bytes.restype = c_int64
     L.hx_boxlevel_work_bytes.argtypes = [c_int, POINTER(LevelBoxF64), c_int, c_int]
     L.hx_boxlevel_run_f64.argtypes = [c_int, POINTER(LevelBoxF64), c_int, c_int, c_double, c_double,
@@ -200,7 +213,7 @@ EXPORTED = [
     "hx_masked_average_down_box_f64", "hx_masked_average_down_box_f32", "hx_average_down_box_f64",
     "hx_average_down_box_f32", "hx_derive_eta_box_f64",
     "hx_derive_eta_box_f32", "hx_diagnostics_work_bytes", "hx_diagnostics_box_f64", "hx_diagnostics_box_f32",
-    "hx_level_diagnostics_f64", "hx_measure_fp64_rate", "hx_boxlevel_work_bytes", "hx_boxlevel_run_f64",
+    "hx_level_diagnostics_f64", "hx_measure_fp64_rate", "hx_boxlevel_work_bytes", "hx_boxlevel_run_f64", "hx_write_plotfile_f64",
     "hx_level_advance_f64",
     "hx_level_advance_f32", "hx_level_dt_reduce_f64", "hx_level_dt_reduce_f32", "hx_level_run_work_bytes",
     "hx_level_run_f64", "hx_level_run_f32", "hx_level_run_host_f64", "hx_host_cache_release",

@@ -527,6 +527,41 @@ typedef struct hx_levelbox_f64 {
     int32_t lo[2], hi[2];
 } hx_levelbox_f64;
 
+/* ---- native plotfile ------------------------------------------------------ */
+
+/* One box of one level: device planes of the state and the terrain with a row
+ * pitch (doubles), covering cells lo..hi of the level's index space. */
+typedef struct hx_plotbox_f64 {
+    const double *h, *hu, *hv, *z, *n;
+    int64_t pitch;
+    int32_t lo[2], hi[2];
+} hx_plotbox_f64;
+
+/* One level: its boxes, domain box, cell size, step count and refinement ratio
+ * to the next finer level (unused on the finest). */
+typedef struct hx_plotlevel_f64 {
+    const hx_plotbox_f64* boxes;
+    int32_t nboxes;
+    int32_t domain_lo[2], domain_hi[2];
+    double dx, dy;
+    int32_t ref_ratio;
+    int32_t istep;
+} hx_plotlevel_f64;
+
+/*
+ * AMReX native plotfile (HyperCLaw-V1.1) of the levels' state and terrain
+ * (replaces WriteNativePlotfile, src/io/NativePlotFile.cpp:19-97, which calls
+ * amrex::WriteMultiLevelPlotfile): directory <prefix><iteration as 5 digits>
+ * with Header, Level_<l>/Cell_H and Level_<l>/Cell_D_00000; variables
+ * h_fluid, hu_momentum, hv_momentum, z_bathymetry, extra_comp_4 (terrain
+ * component 1, the Manning coefficient, as the reference names it).  Copies from
+ * the device on stream through pinned staging; returns once the files are
+ * written.
+ */
+int hx_write_plotfile_f64(const char* prefix, int iteration, double time, int nlevels,
+                          const hx_plotlevel_f64* levels, const double prob_lo[2], const double prob_hi[2],
+                          hx_stream_t stream);
+
 /*
  * The single-level time loop of hx_level_run_f64 (hydrostatic-Roe) on a level
  * given as several boxes that tile the domain (0,0)-(nx-1,ny-1) -- the
