@@ -325,13 +325,15 @@ def main():
                 "bound": "hbm", "achieved": achieved_gbs, "peak": HBM_GBS, "unit": "GB/s",
                 "frac": achieved_gbs / HBM_GBS, "traffic": profiled_traffic(profile, cells, args),
                 "peak_source": HBM_SRC,
-                "kernel": "%s<%s,%s,LevelSrc>" % ("k_hydro_tile" if args.method == "hydrostatic" else "k_classic_tile",
-                                                  "double" if args.precision == "f64" else "float",
-                                                  "true" if arith else "false"),
+                "kernel": "%s<%s,%s,LevelSrc%s>" % (
+                    "k_hydro_tile" if args.method == "hydrostatic" else "k_classic_tile",
+                    "double" if args.precision == "f64" else "float", "true" if arith else "false",
+                    ",32,32" if (args.method, args.precision) == ("hydrostatic", "f64") and cells >= 1 << 22 else ""),
                 "kernel_ms": kms, "algorithmic_bytes_per_launch": BYTES_PER_CELL[args.precision] * cells,
                 "note": "FP64-issue bound on GB300: see fp64_pipe",
-                "fp64_pipe": (fp64_pipe(profile, kms) if (args.precision, args.method, args.arith) == ("f64", "hydrostatic", "fast")
-                              else None),
+                "fp64_pipe": (fp64_pipe(profile, kms)
+                              if (args.precision, args.method, args.arith) == ("f64", "hydrostatic", "fast")
+                              and cells >= 1 << 22 else None),
             },
             "ensemble": ens,
             "adjoint": adj,
@@ -573,7 +575,8 @@ def profiled_traffic(profile, cells, args):
     cell count) times this run's cells.  The capture is of the FP64 fast-form
     hydrostatic kernel; other variants report null."""
     per_cell = profile.get("traffic_bytes_per_cell")
-    if per_cell is None or (args.method, args.precision, args.arith) != ("hydrostatic", "f64", "fast"):
+    if per_cell is None or (args.method, args.precision, args.arith) != ("hydrostatic", "f64", "fast") or \
+            cells < 1 << 22:  # the capture is of the 32 x 32 tile that levels of 2048^2 cells and more take
         return None
     return per_cell * cells
 

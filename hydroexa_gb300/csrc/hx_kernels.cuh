@@ -431,16 +431,38 @@ __device__ __forceinline__ void hydro_tile_body(HydroSmem<R, TXv, TYv>& S, const
     }
 }
 
-template <class R, bool FAST, class Src>
-__global__ void __launch_bounds__(NT, 4) k_hydro_tile(Src src, Cells3<R> uo, Plane<R> nplane, Cells3W<R> out,
-                                                   FaceOut<R> fo, IBox vb, StepCtl<R> ctl) {
+// Tile shapes of the level kernels, one cell per thread.  FP64 is bound by
+// FP64 issue: a 32 x 32 tile loads 1.27 cells, computes 6.4 slopes and 2.06
+// faces per cell (32 x 8: 1.69, 6.9, 2.16) and runs ~9% faster on large boxes
+// (one CTA of 1024 threads per SM).  On boxes of a few waves the four 32 x 8
+// CTAs per SM overlap each other's barriers and win, and FP32 (bound by issue
+// of every kind) always prefers them.
+template <class R> struct BigTile {
+    static constexpr int X = 32, Y = 32;
+};
+template <> struct BigTile<float> {
+    static constexpr int X = 32, Y = 8;
+};
+struct SmallTile {
+    static constexpr int X = TX, Y = TY;
+};
+constexpr long long kBigTileCells = 1ll << 22;  // boxes from 2048 x 2048 cells take the big tile
+template <class R> inline bool big_tile(const IBox& vb) {
+    return BigTile<R>::Y != TY &&
+           (long long)(vb.hi0 - vb.lo0 + 1) * (long long)(vb.hi1 - vb.lo1 + 1) >= kBigTileCells;
+}
+
+template <class R, bool FAST, class Src, int TXH = TX, int TYH = TY>
+__global__ void __launch_bounds__(TXH * TYH, 1024 / (TXH * TYH))
+    k_hydro_tile(Src src, Cells3<R> uo, Plane<R> nplane, Cells3W<R> out, FaceOut<R> fo, IBox vb, StepCtl<R> ctl) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    HydroSmem<R>& S = *reinterpret_cast<HydroSmem<R>*>(smem_raw);
+    HydroSmem<R, TXH, TYH>& S = *reinterpret_cast<HydroSmem<R, TXH, TYH>*>(smem_raw);
     R dt;
     if (!resolve_dt(ctl, dt)) return;
     step_bookkeeping(ctl, dt);
-    hydro_tile_body<R, FAST, TX, TY, NT>(S, src, uo, nplane, out, fo, vb, vb.lo0 + (int)blockIdx.x * TX,
-                                         vb.lo1 + (int)blockIdx.y * TY, dt, ctl.dx, ctl.dy, ctl.dt_out, ctl.status);
+    hydro_tile_body<R, FAST, TXH, TYH, TXH * TYH>(S, src, uo, nplane, out, fo, vb, vb.lo0 + (int)blockIdx.x * TXH,
+                                                  vb.lo1 + (int)blockIdx.y * TYH, dt, ctl.dx, ctl.dy, ctl.dt_out,
+                                                  ctl.status);
 }
 
 // ---------------------------------------------------------------------------
@@ -450,16 +472,16 @@ __global__ void __launch_bounds__(NT, 4) k_hydro_tile(Src src, Cells3<R> uo, Pla
 // once the CFL bound of the whole level is known.  Together they do exactly
 // the fused kernel's arithmetic.
 // ---------------------------------------------------------------------------
-template <class R, bool FAST>
-__global__ void __launch_bounds__(NT) k_hydro_div(LevelSrc<R> src, Cells3<R> uo, Plane<R> nplane, DivOut<R> div,
-                                                  IBox vb, R dx, R dy) {
+template <class R, bool FAST, int TXH = TX, int TYH = TY>
+__global__ void __launch_bounds__(TXH * TYH, 1024 / (TXH * TYH))
+    k_hydro_div(LevelSrc<R> src, Cells3<R> uo, Plane<R> nplane, DivOut<R> div, IBox vb, R dx, R dy) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    HydroSmem<R>& S = *reinterpret_cast<HydroSmem<R>*>(smem_raw);
+    HydroSmem<R, TXH, TYH>& S = *reinterpret_cast<HydroSmem<R, TXH, TYH>*>(smem_raw);
     FaceOut<R> fo{};
     Cells3W<R> none{};
-    hydro_tile_body<R, FAST, TX, TY, NT, LevelSrc<R>, false, DivOut<R>>(
-        S, src, uo, nplane, none, fo, vb, vb.lo0 + (int)blockIdx.x * TX, vb.lo1 + (int)blockIdx.y * TY, R(0), dx, dy,
-        nullptr, nullptr, nullptr, div);
+    hydro_tile_body<R, FAST, TXH, TYH, TXH * TYH, LevelSrc<R>, false, DivOut<R>>(
+        S, src, uo, nplane, none, fo, vb, vb.lo0 + (int)blockIdx.x * TXH, vb.lo1 + (int)blockIdx.y * TYH, R(0), dx,
+        dy, nullptr, nullptr, nullptr, div);
 }
 
 template <class R, bool FAST>
@@ -940,15 +962,16 @@ __global__ void k_points(int method, long n, const R* __restrict__ st, const R* 
 }  // namespace hx
 
 // ---------------------------------------------------------------------------
-// Forward steps of the adjoint's sweeps (see launch_adj_forward).
+// Forward steps of the adjoint's sweeps (see launch_adj_forward), on the level
+// kernel's tile for the box's size.
 // ---------------------------------------------------------------------------
 namespace hx {
-template <bool FAST>
-__global__ void __launch_bounds__(NT) k_adj_forward(LevelSrc<double> src, Cells3<double> uo, Plane<double> np,
+template <bool FAST, int AX = TX, int AY = TY>
+__global__ void __launch_bounds__(AX * AY, 1024 / (AX * AY)) k_adj_forward(LevelSrc<double> src, Cells3<double> uo, Plane<double> np,
                                                      Cells3W<double> out, IBox vb, StepCtl<double> ctl,
                                                      const double* dt_fixed, unsigned* post_flags, AdjRecord rec) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    HydroSmem<double>& S = *reinterpret_cast<HydroSmem<double>*>(smem_raw);
+    HydroSmem<double, AX, AY>& S = *reinterpret_cast<HydroSmem<double, AX, AY>*>(smem_raw);
     double dt;
     if (dt_fixed) {
         dt = *dt_fixed;
@@ -963,37 +986,37 @@ __global__ void __launch_bounds__(NT) k_adj_forward(LevelSrc<double> src, Cells3
     }
     FaceOut<double> fo{};
     fo.on = 0;
-    hydro_tile_body<double, FAST, TX, TY, NT>(S, src, uo, np, out, fo, vb, vb.lo0 + (int)blockIdx.x * TX,
-                                              vb.lo1 + (int)blockIdx.y * TY, dt, ctl.dx, ctl.dy,
-                                              dt_fixed ? nullptr : ctl.dt_out, ctl.status, post_flags);
+    hydro_tile_body<double, FAST, AX, AY, AX * AY>(S, src, uo, np, out, fo, vb, vb.lo0 + (int)blockIdx.x * AX,
+                                                   vb.lo1 + (int)blockIdx.y * AY, dt, ctl.dx, ctl.dy,
+                                                   dt_fixed ? nullptr : ctl.dt_out, ctl.status, post_flags);
 }
 
 // A recompute step (dt given) that also records every face's intermediates
 // (FAST must be true: records exist for the fast form only).
-template <bool FAST>
-__global__ void __launch_bounds__(NT) k_adj_forward_rec(LevelSrc<double> src, Cells3<double> uo, Plane<double> np,
+template <bool FAST, int AX = TX, int AY = TY>
+__global__ void __launch_bounds__(AX * AY, 1024 / (AX * AY)) k_adj_forward_rec(LevelSrc<double> src, Cells3<double> uo, Plane<double> np,
                                                          Cells3W<double> out, IBox vb, double dx, double dy,
                                                          const double* dt_fixed, unsigned* post_flags, FaceRec rec) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    HydroSmem<double>& S = *reinterpret_cast<HydroSmem<double>*>(smem_raw);
+    HydroSmem<double, AX, AY>& S = *reinterpret_cast<HydroSmem<double, AX, AY>*>(smem_raw);
     FaceOut<double> fo{};
     fo.on = 0;
     static_assert(FAST, "face records are kept for the fast form");
-    hydro_tile_body<double, FAST, TX, TY, NT, LevelSrc<double>, false, NoDiv, FaceRec>(
-        S, src, uo, np, out, fo, vb, vb.lo0 + (int)blockIdx.x * TX, vb.lo1 + (int)blockIdx.y * TY, *dt_fixed, dx, dy,
+    hydro_tile_body<double, FAST, AX, AY, AX * AY, LevelSrc<double>, false, NoDiv, FaceRec>(
+        S, src, uo, np, out, fo, vb, vb.lo0 + (int)blockIdx.x * AX, vb.lo1 + (int)blockIdx.y * AY, *dt_fixed, dx, dy,
         nullptr, nullptr, post_flags, NoDiv{}, rec);
 }
 
-template <bool FAST>
-__global__ void __launch_bounds__(NT) k_adj_forward_linear(LevelSrc<double> src, Cells3<double> uo, Plane<double> np,
+template <bool FAST, int AX = TX, int AY = TY>
+__global__ void __launch_bounds__(AX * AY, 1024 / (AX * AY)) k_adj_forward_linear(LevelSrc<double> src, Cells3<double> uo, Plane<double> np,
                                                             Cells3W<double> out, IBox vb, double dx, double dy,
                                                             const double* dt_fixed) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    HydroSmem<double>& S = *reinterpret_cast<HydroSmem<double>*>(smem_raw);
+    HydroSmem<double, AX, AY>& S = *reinterpret_cast<HydroSmem<double, AX, AY>*>(smem_raw);
     FaceOut<double> fo{};
     fo.on = 0;
-    hydro_tile_body<double, FAST, TX, TY, NT, LevelSrc<double>, true>(
-        S, src, uo, np, out, fo, vb, vb.lo0 + (int)blockIdx.x * TX, vb.lo1 + (int)blockIdx.y * TY, *dt_fixed, dx, dy,
+    hydro_tile_body<double, FAST, AX, AY, AX * AY, LevelSrc<double>, true>(
+        S, src, uo, np, out, fo, vb, vb.lo0 + (int)blockIdx.x * AX, vb.lo1 + (int)blockIdx.y * AY, *dt_fixed, dx, dy,
         nullptr, nullptr);
 }
 }  // namespace hx
@@ -1013,6 +1036,15 @@ template <class K> inline cudaError_t ensure_smem(K kernel, size_t bytes) {
 template <class R, bool FAST, class Src>
 cudaError_t launch_hydro(const Src& src, const Cells3<R>& uo, const Plane<R>& np, const Cells3W<R>& out,
                          const FaceOut<R>& fo, const IBox& vb, const StepCtl<R>& ctl, cudaStream_t st) {
+    if (big_tile<R>(vb)) {
+        constexpr int BX = BigTile<R>::X, BY = BigTile<R>::Y;
+        const size_t sm = sizeof(HydroSmem<R, BX, BY>);
+        auto k = k_hydro_tile<R, FAST, Src, BX, BY>;
+        cudaError_t e = ensure_smem(k, sm);
+        if (e != cudaSuccess) return e;
+        k<<<tile_grid(vb, BX, BY), BX * BY, sm, st>>>(src, uo, np, out, fo, vb, ctl);
+        return cudaGetLastError();
+    }
     const size_t sm = sizeof(HydroSmem<R>);
     auto k = k_hydro_tile<R, FAST, Src>;
     cudaError_t e = ensure_smem(k, sm);
@@ -1067,6 +1099,14 @@ cudaError_t launch_boxlevel(const BoxSetSrc& src, const int* tiles, int ntiles, 
 template <class R, bool FAST>
 cudaError_t launch_hydro_split(const LevelSrc<R>& src, const Cells3<R>& uo, const Plane<R>& np, const DivOut<R>& div,
                                const IBox& vb, R dx, R dy, cudaStream_t st) {
+    if (big_tile<R>(vb)) {
+        constexpr int BX = BigTile<R>::X, BY = BigTile<R>::Y;
+        const size_t sm = sizeof(HydroSmem<R, BX, BY>);
+        cudaError_t e = ensure_smem(k_hydro_div<R, FAST, BX, BY>, sm);
+        if (e != cudaSuccess) return e;
+        k_hydro_div<R, FAST, BX, BY><<<tile_grid(vb, BX, BY), BX * BY, sm, st>>>(src, uo, np, div, vb, dx, dy);
+        return cudaGetLastError();
+    }
     const size_t sm = sizeof(HydroSmem<R>);
     cudaError_t e = ensure_smem(k_hydro_div<R, FAST>, sm);
     if (e != cudaSuccess) return e;
@@ -1094,34 +1134,48 @@ template <bool FAST>
 cudaError_t launch_adj_forward(const LevelSrc<double>& src, const Cells3<double>& uo, const Plane<double>& np,
                                const Cells3W<double>& out, const IBox& vb, const StepCtl<double>& ctl,
                                const double* dt_fixed, unsigned* post_flags, const AdjRecord& rec, cudaStream_t st) {
-    const size_t sm = sizeof(HydroSmem<double>);
-    cudaError_t e = ensure_smem(k_adj_forward<FAST>, sm);
-    if (e != cudaSuccess) return e;
-    k_adj_forward<FAST><<<tile_grid(vb, TX, TY), NT, sm, st>>>(src, uo, np, out, vb, ctl, dt_fixed, post_flags, rec);
-    return cudaGetLastError();
+    auto go = [&](auto shape) -> cudaError_t {
+        constexpr int AX = decltype(shape)::X, AY = decltype(shape)::Y;
+        const size_t sm = sizeof(HydroSmem<double, AX, AY>);
+        cudaError_t e = ensure_smem(k_adj_forward<FAST, AX, AY>, sm);
+        if (e != cudaSuccess) return e;
+        k_adj_forward<FAST, AX, AY><<<tile_grid(vb, AX, AY), AX * AY, sm, st>>>(src, uo, np, out, vb, ctl, dt_fixed,
+                                                                              post_flags, rec);
+        return cudaGetLastError();
+    };
+    return big_tile<double>(vb) ? go(BigTile<double>{}) : go(SmallTile{});
 }
 
 template <bool FAST>
 cudaError_t launch_adj_forward_rec(const LevelSrc<double>& src, const Cells3<double>& uo, const Plane<double>& np,
                                    const Cells3W<double>& out, const IBox& vb, double dx, double dy,
                                    const double* dt_fixed, unsigned* post_flags, const FaceRec& rec, cudaStream_t st) {
-    const size_t sm = sizeof(HydroSmem<double>);
-    cudaError_t e = ensure_smem(k_adj_forward_rec<FAST>, sm);
-    if (e != cudaSuccess) return e;
-    k_adj_forward_rec<FAST><<<tile_grid(vb, TX, TY), NT, sm, st>>>(src, uo, np, out, vb, dx, dy, dt_fixed, post_flags,
-                                                                   rec);
-    return cudaGetLastError();
+    auto go = [&](auto shape) -> cudaError_t {
+        constexpr int AX = decltype(shape)::X, AY = decltype(shape)::Y;
+        const size_t sm = sizeof(HydroSmem<double, AX, AY>);
+        cudaError_t e = ensure_smem(k_adj_forward_rec<FAST, AX, AY>, sm);
+        if (e != cudaSuccess) return e;
+        k_adj_forward_rec<FAST, AX, AY><<<tile_grid(vb, AX, AY), AX * AY, sm, st>>>(src, uo, np, out, vb, dx, dy,
+                                                                                  dt_fixed, post_flags, rec);
+        return cudaGetLastError();
+    };
+    return big_tile<double>(vb) ? go(BigTile<double>{}) : go(SmallTile{});
 }
 
 template <bool FAST>
 cudaError_t launch_adj_forward_linear(const LevelSrc<double>& src, const Cells3<double>& uo, const Plane<double>& np,
                                       const Cells3W<double>& out, const IBox& vb, double dx, double dy,
                                       const double* dt_fixed, cudaStream_t st) {
-    const size_t sm = sizeof(HydroSmem<double>);
-    cudaError_t e = ensure_smem(k_adj_forward_linear<FAST>, sm);
-    if (e != cudaSuccess) return e;
-    k_adj_forward_linear<FAST><<<tile_grid(vb, TX, TY), NT, sm, st>>>(src, uo, np, out, vb, dx, dy, dt_fixed);
-    return cudaGetLastError();
+    auto go = [&](auto shape) -> cudaError_t {
+        constexpr int AX = decltype(shape)::X, AY = decltype(shape)::Y;
+        const size_t sm = sizeof(HydroSmem<double, AX, AY>);
+        cudaError_t e = ensure_smem(k_adj_forward_linear<FAST, AX, AY>, sm);
+        if (e != cudaSuccess) return e;
+        k_adj_forward_linear<FAST, AX, AY><<<tile_grid(vb, AX, AY), AX * AY, sm, st>>>(src, uo, np, out, vb, dx, dy,
+                                                                                     dt_fixed);
+        return cudaGetLastError();
+    };
+    return big_tile<double>(vb) ? go(BigTile<double>{}) : go(SmallTile{});
 }
 
 template <class R, bool FAST>

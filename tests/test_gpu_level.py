@@ -224,3 +224,41 @@ def test_nodata_predicate_at_its_edges(cuda, oracle_lib, dtype):
     else:  # a misplaced wall changes the state by O(1) next to it
         assert gmn == pytest.approx(mn, rel=1e-6) and gmx == pytest.approx(mx, rel=1e-6)
         assert rel_err(got, ref) <= 1e-5
+
+
+def test_big_tile_levels_match_oracle(cuda, oracle_lib, hxlib):
+    """Boxes of 2048 x 2048 cells and more take the 32 x 32 tile kernels (level
+    step, split first step of the host-buffer call): the exact form stays
+    bit-equal to the oracle and to the device loop, the fast form within 1e-12."""
+    import ctypes
+    n = 2048
+    case = workloads.fractal_dam_break(n, n, seed=31, amplitude=2.0, nodata_frac=0.2)
+    g = case.geom
+    L = oracle_lib.Level(g.nx, g.ny, g.dx, g.dy, g.bc_lo, g.bc_hi)
+    ref = oracle_lib.run(L, capi.HX_METHOD_HYDROSTATIC_ROE, case.h, case.hu, case.hv, case.z, case.n, 2, case.cfl)
+    assert ref[5] == 0
+    lev = to_level(case, case.h, case.hu, case.hv, cuda)
+    assert lev.run(capi.HX_METHOD_HYDROSTATIC_ROE, 2, case.cfl, arith=EXACT) == 0
+    got = lev.state.cpu().numpy()
+    for k in range(3):
+        assert np.array_equal(got[k], ref[k]), k
+    fast = to_level(case, case.h, case.hu, case.hv, cuda)
+    assert fast.run(capi.HX_METHOD_HYDROSTATIC_ROE, 2, case.cfl, arith=FAST) == 0
+    assert rel_err(fast.state.cpu().numpy(), ref[:3]) <= 1e-12
+    # the host-buffer call on 8192 x 4096 cells: its row bands (512 x 8192) take the big tile too, in the split
+    # first step and in the banded last step; bit-equal to the device loop
+    case = workloads.fractal_dam_break(8192, 4096, seed=32, amplitude=2.0, nodata_frac=0.2)
+    g = case.geom
+    h, hu, hv = case.h.copy(), case.hu.copy(), case.hv.copy()
+    t = ctypes.c_double()
+    lo = (ctypes.c_int32 * 2)(*g.bc_lo)
+    hi = (ctypes.c_int32 * 2)(*g.bc_hi)
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    rc = hxlib.lib().hx_level_run_host_f64(capi.HX_METHOD_HYDROSTATIC_ROE, g.nx, g.ny, g.dx, g.dy, lo, hi, P(h),
+                                           P(hu), P(hv), P(case.z), P(case.n), 2, case.cfl, EXACT, ctypes.byref(t),
+                                           None)
+    assert rc == 0
+    lev = to_level(case, case.h, case.hu, case.hv, cuda)
+    assert lev.run(capi.HX_METHOD_HYDROSTATIC_ROE, 2, case.cfl, arith=EXACT) == 0
+    got = lev.state.cpu().numpy()
+    assert np.array_equal(h, got[0]) and np.array_equal(hu, got[1]) and np.array_equal(hv, got[2])
