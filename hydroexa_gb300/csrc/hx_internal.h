@@ -6,7 +6,9 @@
 
 namespace hx {
 
-// The level kernels' tile: 32 x 8 cells, one thread per cell.
+// The level kernels' default tile: 32 x 8 cells, one thread per cell (FP64
+// boxes of 2048^2 cells and more take a 32 x 32 tile: BigTile in
+// hx_kernels.cuh; the ensemble picks its shapes per member).
 constexpr int TX = 32;
 constexpr int TY = 8;
 constexpr int NT = TX * TY;
