@@ -163,11 +163,30 @@ __host__ __device__ __forceinline__ double rcp_nr(double x) {
     return 1.0 / x;
 #endif
 }
+// Float: the hardware approximation alone (rcp.approx.ftz.f32, within an ulp);
+// the FP32 fast form is held to 1e-5 of the oracle in float, and is bound by
+// instruction issue, where the IEEE reciprocal's correction steps cost.
 __host__ __device__ __forceinline__ float rcp_nr(float x) {
 #ifdef __CUDA_ARCH__
-    return __frcp_rn(x);
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
 #else
     return 1.0f / x;
+#endif
+}
+
+// Square root of the fast form: IEEE in FP64 (CUDA's sqrt already issues fewer
+// FP64 instructions than a Goldschmidt iteration from rsqrt.approx), the
+// hardware approximation sqrt.approx.ftz.f32 in float.
+__host__ __device__ __forceinline__ double fast_sqrt(double x) { return sqrt(x); }
+__host__ __device__ __forceinline__ float fast_sqrt(float x) {
+#ifdef __CUDA_ARCH__
+    float y;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+#else
+    return sqrtf(x);
 #endif
 }
 
@@ -297,14 +316,14 @@ __host__ __device__ __forceinline__ void roe_hydrostatic_fast(R hi, R ui, R vi, 
     vi = wi ? vi : R(0);
     uj = wj ? uj : R(0);
     vj = wj ? vj : R(0);
-    const R si = sqrt(hi), sj = sqrt(hj);
+    const R si = fast_sqrt(hi), sj = fast_sqrt(hj);
     R uni, uti, unj, utj;
     if (DIR == 0) { uni = ui; uti = vi; unj = uj; utj = vj; }
     else { uni = vi; uti = -ui; unj = vj; utj = -uj; }
     const R hh = R(0.5) * (hi + hj);
     const bool hmb = gt_bits(hh, C::toldry_bits);
     const R hm = hmb ? hh : C::toldry;
-    const R cm = sqrt(C::g * hm);
+    const R cm = fast_sqrt(C::g * hm);
     const R den = R(2) * cm + C::tol12;
     const R sden = si + sj + C::tol12;
     // one reciprocal for 1/sden, 1/den and 1/cm
@@ -375,8 +394,8 @@ __host__ __device__ __forceinline__ void roe_classic(R hi, R hui, R hvi, R zi, R
         uj = (hj > R(0)) ? huj / hj : R(0);
         vj = (hj > R(0)) ? hvj / hj : R(0);
     } else {
-        si = sqrt(hi);
-        sj = sqrt(hj);
+        si = fast_sqrt(hi);
+        sj = fast_sqrt(hj);
         const R ri = (hi > R(0)) ? R(1) / hi : R(0);
         const R rj = (hj > R(0)) ? R(1) / hj : R(0);
         ui = hui * ri; vi = hvi * ri; uj = huj * rj; vj = hvj * rj;
@@ -386,7 +405,7 @@ __host__ __device__ __forceinline__ void roe_classic(R hi, R hui, R hvi, R zi, R
     else { uni = vi; uti = -ui; unj = vj; utj = -uj; }
     const R hsum = hi + hj;
     const R hm = (R(0.5) * hsum > TD) ? R(0.5) * hsum : TD;
-    const R cm = sqrt(C::g * hm);
+    const R cm = FAST ? fast_sqrt(C::g * hm) : sqrt(C::g * hm);
     const R sden = si + sj + T12;
     const R um = (uni * si + unj * sj) / sden;
     const R vm = (uti * si + utj * sj) / sden;
@@ -573,7 +592,7 @@ __device__ __forceinline__ void dt_cell_contrib(R h, R hu, R hv, bool nod, R dx,
         if (!gt_bits(h, Cst<R>::tol12_bits)) { flags |= DTF_DRY; return; }
         const R r = rcp_nr(h);
         const R u = hu * r, v = hv * r;
-        const R c = sqrt(Cst<R>::g * h);
+        const R c = fast_sqrt(Cst<R>::g * h);
         rate = (fabs(u) + c) * idx + (fabs(v) + c) * idy;
         mv = nnmax_i(fabs(u), fabs(v));
     }

@@ -160,7 +160,7 @@ __device__ __forceinline__ void step_cell(R o0, R o1, R o2, R dx0, R dx1, R dx2,
                 const R uu = qx * inv_h, vv = qy * inv_h;
                 modM = sqrt(uu * uu + vv * vv);
             } else {
-                modM = sqrt(qx * qx + qy * qy) * rcp_nr(hh);
+                modM = fast_sqrt(qx * qx + qy * qy) * rcp_nr(hh);
             }
             if (modM > Cst<R>::tol12) {
                 pflags |= 1u;
