@@ -262,3 +262,27 @@ def test_big_tile_levels_match_oracle(cuda, oracle_lib, hxlib):
     assert lev.run(capi.HX_METHOD_HYDROSTATIC_ROE, 2, case.cfl, arith=EXACT) == 0
     got = lev.state.cpu().numpy()
     assert np.array_equal(h, got[0]) and np.array_equal(hu, got[1]) and np.array_equal(hv, got[2])
+
+
+@pytest.mark.parametrize("arith", [EXACT, FAST])
+def test_full_size_properties(cuda, arith):
+    """The throughput size, 8192^2 FP64, through size-independent properties:
+    the lake at rest over the fractal bed (no NODATA) stays at rest (|u| <= 1e-13)
+    and a dam break on a flat bed between reflective walls conserves mass to
+    round-off, over 10 steps of the device loop (32 x 32 tiles)."""
+    n = 8192
+    case = workloads.fractal_dam_break(n, n, seed=3, nodata_frac=0.0)
+    h = np.maximum(0.0, 3.0 - case.z)
+    lev = Level.from_numpy(case.geom, h, np.zeros_like(h), np.zeros_like(h), case.z, case.n, device=cuda)
+    assert lev.run(capi.HX_METHOD_HYDROSTATIC_ROE, 10, case.cfl, arith=arith) == 0
+    s = lev.state
+    wet = s[0] > 1e-6
+    vel = torch.sqrt(s[1] ** 2 + s[2] ** 2)[wet] / s[0][wet]
+    assert vel.max().item() <= 1e-13
+    del lev, s, wet, vel
+    flat = workloads.dam_break(n, n)
+    lev = Level.from_numpy(flat.geom, flat.h, flat.hu, flat.hv, flat.z, flat.n, device=cuda)
+    m0 = lev.state[0].sum(dtype=torch.float64).item()
+    assert lev.run(capi.HX_METHOD_HYDROSTATIC_ROE, 10, flat.cfl, arith=arith) == 0
+    m1 = lev.state[0].sum(dtype=torch.float64).item()
+    assert abs(m1 - m0) <= 1e-12 * m0
