@@ -118,6 +118,43 @@ __host__ __device__ __forceinline__ bool is_nodata(double z) {
 }
 __host__ __device__ __forceinline__ bool is_nodata(float z) { return sbits(z) == (int)0xC61C3C00u; }
 
+// x / 2 on the integer pipe: decrementing the exponent field is exact, and
+// equals 0.5 * x, for normal x above the smallest normal exponent; zero is
+// kept; subnormals, the smallest normals, inf and NaN take the FP64 multiply.
+__host__ __device__ __forceinline__ double half_i(double x) {
+    const long long b = sbits(x);
+    const long long e = b & 0x7FF0000000000000ll;
+    if (e > 0x0010000000000000ll && e != 0x7FF0000000000000ll) {
+        const long long r = b - 0x0010000000000000ll;
+        double y;
+        memcpy(&y, &r, sizeof y);
+        return y;
+    }
+    if ((b << 1) == 0) return x;
+    return 0.5 * x;
+}
+__host__ __device__ __forceinline__ float half_i(float x) { return 0.5f * x; }
+
+// The leading 24 significand bits of a double as a float (truncated, so within
+// 2^-23 relative; 0 below the float range, inf above, NaN kept as NaN or inf),
+// made on the integer pipe: for decisions whose outcome is certain at that
+// precision, taken without FP64 instructions.
+__host__ __device__ __forceinline__ float f32_lead(double x) {
+    const unsigned long long b = (unsigned long long)sbits(x);
+    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+    const int de = (int)((hi >> 20) & 0x7FF);
+    const unsigned sign = hi & 0x80000000u, mant = ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+    const int fe = de - 1023 + 127;
+    unsigned f;
+    if (de == 0x7FF) f = sign | 0x7F800000u | mant;
+    else if (fe >= 255) f = sign | 0x7F800000u;
+    else if (fe <= 0) f = sign;
+    else f = sign | ((unsigned)fe << 23) | mant;
+    float y;
+    memcpy(&y, &f, sizeof y);
+    return y;
+}
+
 template <class R> __host__ __device__ __forceinline__ bool gt_bits(R x, decltype(sbits(R(0))) cb) {
     return sbits(x) > cb;
 }
@@ -147,18 +184,19 @@ template <class R> __host__ __device__ __forceinline__ R smax_i(R a, R b) { retu
 // max of two non-negative values
 template <class R> __host__ __device__ __forceinline__ R nnmax_i(R a, R b) { return sbits(a) < sbits(b) ? b : a; }
 
-// Reciprocal of a positive normal x by Newton-Raphson, y <- y + y (1 - x y)
-// (Markstein, IBM J. Res. Dev. 34, 1990), twice, from the hardware estimate
-// rcp.approx.ftz.f64: four FMAs instead of a full IEEE division.  Callers only
-// pass finite, positive, normal arguments.
+// Reciprocal of a finite normal x from the hardware estimate
+// rcp.approx.ftz.f64 by one third-order Newton step on f(y) = 1/y - x:
+// with e = 1 - x y, y <- y + y (e + e^2), which cubes the relative error
+// (Householder's method of order 3; see Markstein, IBM J. Res. Dev. 34, 1990,
+// for the FMA formulation of these iterations): three FMAs instead of a full
+// IEEE division.  Faithful (within an ulp), as the tests check against IEEE
+// division; callers pass finite normal arguments only.
 __host__ __device__ __forceinline__ double rcp_nr(double x) {
 #ifdef __CUDA_ARCH__
     double y;
     asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
-    double e = fma(-x, y, 1.0);
-    y = fma(y, e, y);
-    e = fma(-x, y, 1.0);
-    return fma(y, e, y);
+    const double e = fma(-x, y, 1.0);
+    return fma(y, fma(e, e, e), y);
 #else
     return 1.0 / x;
 #endif
@@ -320,7 +358,7 @@ __host__ __device__ __forceinline__ void roe_hydrostatic_fast(R hi, R ui, R vi, 
     R uni, uti, unj, utj;
     if (DIR == 0) { uni = ui; uti = vi; unj = uj; utj = vj; }
     else { uni = vi; uti = -ui; unj = vj; utj = -uj; }
-    const R hh = R(0.5) * (hi + hj);
+    const R hh = half_i(hi + hj);
     const bool hmb = gt_bits(hh, C::toldry_bits);
     const R hm = hmb ? hh : C::toldry;
     const R cm = fast_sqrt(C::g * hm);
@@ -337,24 +375,37 @@ __host__ __device__ __forceinline__ void roe_hydrostatic_fast(R hi, R ui, R vi, 
     R l0 = um - cm;
     const R l1 = um;
     R l2 = um + cm;
-    bool fix0, fix2;
-    {
+    bool fix0 = false, fix2 = false;
+    // Entropy fixes need e_i < 0 < e_j for e = u -+ c.  In FP64 the tests are
+    // first taken in float from the leading bits (error below 2^-20 of
+    // |u| + c, against a margin of 2^-16 of it): where a sign is certain the
+    // fix is ruled out without FP64 work (subsonic faces); otherwise the FP64
+    // tests decide, so the outcome is that of the FP64 tests everywhere.
+    bool rule0 = false, rule2 = false;
+    if constexpr (sizeof(R) == 8) {
+        const float ui32 = f32_lead(uni), uj32 = f32_lead(unj);
+        const float ci32 = 3.13209195f * f32_lead(si), cj32 = 3.13209195f * f32_lead(sj);
+        const float mi = 0x1p-16f * (fabsf(ui32) + ci32), mj = 0x1p-16f * (fabsf(uj32) + cj32);
+        rule0 = (ui32 - ci32 >= mi) || (uj32 - cj32 <= -mj);
+        rule2 = (ui32 + ci32 >= mi) || (uj32 + cj32 <= -mj);
+    }
+    if (!(rule0 && rule2)) {
         const R ci = C::sqrt_g * si, cj = C::sqrt_g * sj;
         R ei = uni - ci, ej = unj - cj;
-        fix0 = neg_i(ei) && pos_i(ej);
+        fix0 = !rule0 && neg_i(ei) && pos_i(ej);
         if (fix0) l0 = ei * (ej - l0) / (ej - ei);
         ei = uni + ci;
         ej = unj + cj;
-        fix2 = neg_i(ei) && pos_i(ej);
+        fix2 = !rule2 && neg_i(ei) && pos_i(ej);
         if (fix2) l2 = ej * (l2 - ei) / (ej - ei);
     }
     const R dh = hj - hi;
     const R qi = hi * uni, qj = hj * unj;
     const R dhu = qj - qi;
     const R dhv = hj * utj - hi * uti;
-    const R hrden = R(0.5) * rden;
+    const R hrden = half_i(rden);
     const R a0h = (l2 * dh - dhu) * hrden;  // alpha0 / 2
-    const R a1h = (dhv - vm * dh) * (R(0.5) * rcm);
+    const R a1h = (dhv - vm * dh) * half_i(rcm);
     const R a2h = (dhu - l0 * dh) * hrden;
     const R w0 = fabs(l0) * a0h;
     const R w1 = fabs(l1) * a1h;

@@ -130,11 +130,17 @@ template <class R> __device__ __forceinline__ void step_bookkeeping(const StepCt
 // function for the fused tile kernel and the split update kernel, so both do
 // the same arithmetic.  LINEAR stores the updated state before friction and
 // clamp.  pflags: 1 if the Manning factor applied, 2 if the clamp did.
+// A cell's updated state kept for the screened CFL fold (screened_fold).
+template <class R> struct ScreenCell {
+    R h = R(0), hu = R(0), hv = R(0);
+    bool nod = false, live = false;
+};
+
 template <class R, bool FAST, bool LINEAR>
 __device__ __forceinline__ void step_cell(R o0, R o1, R o2, R dx0, R dx1, R dx2, R dy0, R dy1, R dy2, R cx, R cy,
                                           R dt, const Plane<R>& nplane, const Cells3W<R>& out, int gi, int gj,
                                           bool nod, R dx, R dy, R idx, R idy, bool fold_dt, R& rate, R& mv,
-                                          unsigned& flags, unsigned& pflags) {
+                                          unsigned& flags, unsigned& pflags, ScreenCell<R>* sc = nullptr) {
     R un[3];
     un[0] = (o0 - cx * dx0) - cy * dy0;
     un[1] = (o1 - cx * dx1) - cy * dy1;
@@ -181,6 +187,9 @@ __device__ __forceinline__ void step_cell(R o0, R o1, R o2, R dx0, R dx1, R dx2,
     }
     out.st(gi, gj, un[0], un[1], un[2]);
     if (bits_nonfinite(un[0]) || bits_nonfinite(un[1]) || bits_nonfinite(un[2])) flags |= DTF_NAN;
+    if (sc) {
+        sc->h = un[0]; sc->hu = un[1]; sc->hv = un[2]; sc->nod = nod; sc->live = true;
+    }
     if (fold_dt) {
         R rc, mc;
         dt_cell_contrib<R, FAST>(un[0], un[1], un[2], nod, dx, dy, idx, idy, rc, mc, flags);
@@ -248,6 +257,72 @@ struct FaceRec {
         put(1, (long long)gi + (long long)gj * nx, r);
     }
 };
+
+// The next step's CFL bound of a block's cells (one cell per thread) with FP64
+// work only where it can decide the maximum.  Each wet cell's rate
+// (|u| + c)/dx + (|v| + c)/dy and speed max(|u|, |v|) are first estimated in
+// float from the leading bits of h, hu, hv (error below 2^-19 relative); the
+// cells within 2^-12 of the block's float maxima, and any whose estimate is not
+// finite, are the candidates.  A candidate whose state is bit-identical to the
+// first candidate's has that cell's exact contribution, so only the first
+// candidate and the candidates that differ from it compute the exact FP64
+// contribution (dt_cell_contrib).  The block maxima, flags and the fold are then
+// exactly those of computing every cell: the cell holding the true maximum is
+// always a candidate.  Warps without such a cell skip the FP64 work, which in
+// regions of uniform state (a lake at rest, the still water ahead of a wave)
+// is all warps but one.  Every thread of the block must call it.
+template <int NTv>
+__device__ __forceinline__ void screened_fold(const ScreenCell<double>& c, double dx, double dy, double idx,
+                                              double idy, double& rate, double& mv, unsigned& flags) {
+    __shared__ float s_r[NTv / 32], s_m[NTv / 32];
+    __shared__ int s_rep;
+    __shared__ long long s_bits[3];
+    const int t = threadIdx.x;
+    bool wet = false;
+    float r32 = 0.f, m32 = 0.f;
+    if (c.live) {
+        if (c.nod) flags |= DTF_NODATA;
+        else if (!gt_bits(c.h, Cst<double>::tol12_bits)) flags |= DTF_DRY;
+        else {
+            wet = true;
+            const float h = f32_lead(c.h), qx = fabsf(f32_lead(c.hu)), qy = fabsf(f32_lead(c.hv));
+            const float rh = rcp_nr(h);
+            const float u = qx * rh, v = qy * rh;
+            const float cc = fast_sqrt(9.81f * h);
+            r32 = (u + cc) * f32_lead(idx) + (v + cc) * f32_lead(idy);
+            m32 = fmaxf(u, v);
+        }
+    }
+    const bool bad = wet && !(r32 <= 3.0e38f && m32 <= 3.0e38f);  // inf or NaN: decided in FP64
+    float wr = (wet && !bad) ? r32 : 0.f, wm = (wet && !bad) ? m32 : 0.f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        wr = fmaxf(wr, __shfl_xor_sync(0xffffffffu, wr, o));
+        wm = fmaxf(wm, __shfl_xor_sync(0xffffffffu, wm, o));
+    }
+    if (t == 0) s_rep = NTv;
+    if ((t & 31) == 0) { s_r[t >> 5] = wr; s_m[t >> 5] = wm; }
+    __syncthreads();
+    float br = 0.f, bm = 0.f;
+#pragma unroll
+    for (int k = 0; k < NTv / 32; ++k) { br = fmaxf(br, s_r[k]); bm = fmaxf(bm, s_m[k]); }
+    const float kr = br * (1.f - 0x1p-12f), km = bm * (1.f - 0x1p-12f);
+    const bool cand = bad || (wet && (r32 >= kr || m32 >= km));
+    if (cand) atomicMin(&s_rep, t);
+    __syncthreads();
+    const int rep = s_rep;
+    if (t == rep) { s_bits[0] = sbits(c.h); s_bits[1] = sbits(c.hu); s_bits[2] = sbits(c.hv); }
+    __syncthreads();
+    const bool same = t != rep && sbits(c.h) == s_bits[0] && sbits(c.hu) == s_bits[1] && sbits(c.hv) == s_bits[2];
+    if (cand && !same) {
+        double rc, mc;
+        unsigned f = 0;
+        dt_cell_contrib<double, true>(c.h, c.hu, c.hv, false, dx, dy, idx, idy, rc, mc, f);
+        flags |= f;
+        rate = nnmax_i(rate, rc);
+        mv = nnmax_i(mv, mc);
+    }
+}
 
 template <class R, bool FAST, int TXv, int TYv, int NTv, class Src, bool LINEAR = false, class Div = NoDiv,
           class Rec = NoRec>
@@ -404,6 +479,9 @@ __device__ __forceinline__ void hydro_tile_body(HydroSmem<R, TXv, TYv>& S, const
     R rate = R(0), mv = R(0);
     unsigned flags = 0, pflags = 0;
     const R cx = S.kc[0], cy = S.kc[1], idx = S.kc[2], idy = S.kc[3];
+    // the FP64 fast form folds the next CFL bound through the float screen
+    constexpr bool SCREEN = FAST && sizeof(R) == 8 && CELLS == NTv && !LINEAR && !Div::on;
+    ScreenCell<R> sc;
     for (int k = t; k < CELLS; k += NTv) {
         const int tx = k % TXv, ty = k / TXv;
         const int gi = x0 + tx, gj = y0 + ty;
@@ -420,8 +498,11 @@ __device__ __forceinline__ void hydro_tile_body(HydroSmem<R, TXv, TYv>& S, const
         }
         const R o0 = uo.ld(0, gi, gj), o1 = uo.ld(1, gi, gj), o2 = uo.ld(2, gi, gj);
         step_cell<R, FAST, LINEAR>(o0, o1, o2, dx0, dx1, dx2, dy0, dy1, dy2, cx, cy, dt, nplane, out, gi, gj,
-                                   S.nod[ty + 2][tx + 2] != 0, dx, dy, idx, idy, dt_out != nullptr, rate, mv, flags,
-                                   pflags);
+                                   S.nod[ty + 2][tx + 2] != 0, dx, dy, idx, idy, dt_out != nullptr && !SCREEN, rate,
+                                   mv, flags, pflags, (SCREEN && dt_out) ? &sc : nullptr);
+    }
+    if constexpr (SCREEN) {
+        if (dt_out) screened_fold<NTv>(sc, dx, dy, idx, idy, rate, mv, flags);
     }
     if (dt_out) block_fold_dt<R, NTv>(rate, mv, flags, dt_out);
     if ((flags & DTF_NAN) && status) atomicOr(status, (unsigned)HX_STATUS_NAN);
@@ -443,6 +524,10 @@ template <class R> struct BigTile {
 template <> struct BigTile<float> {
     static constexpr int X = 32, Y = 8;
 };
+// Resident CTAs per SM the tile kernels are compiled for: 1024-thread tiles
+// one, 512-thread tiles two, 256-thread tiles three (85 registers; four would
+// cap them at 64 and spill).
+constexpr int min_ctas(int threads) { return threads >= 1024 ? 1 : (threads >= 512 ? 2 : 3); }
 struct SmallTile {
     static constexpr int X = TX, Y = TY;
 };
@@ -453,7 +538,7 @@ template <class R> inline bool big_tile(const IBox& vb) {
 }
 
 template <class R, bool FAST, class Src, int TXH = TX, int TYH = TY>
-__global__ void __launch_bounds__(TXH * TYH, 1024 / (TXH * TYH))
+__global__ void __launch_bounds__(TXH * TYH, min_ctas(TXH * TYH))
     k_hydro_tile(Src src, Cells3<R> uo, Plane<R> nplane, Cells3W<R> out, FaceOut<R> fo, IBox vb, StepCtl<R> ctl) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     HydroSmem<R, TXH, TYH>& S = *reinterpret_cast<HydroSmem<R, TXH, TYH>*>(smem_raw);
@@ -473,7 +558,7 @@ __global__ void __launch_bounds__(TXH * TYH, 1024 / (TXH * TYH))
 // the fused kernel's arithmetic.
 // ---------------------------------------------------------------------------
 template <class R, bool FAST, int TXH = TX, int TYH = TY>
-__global__ void __launch_bounds__(TXH * TYH, 1024 / (TXH * TYH))
+__global__ void __launch_bounds__(TXH * TYH, min_ctas(TXH * TYH))
     k_hydro_div(LevelSrc<R> src, Cells3<R> uo, Plane<R> nplane, DivOut<R> div, IBox vb, R dx, R dy) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     HydroSmem<R, TXH, TYH>& S = *reinterpret_cast<HydroSmem<R, TXH, TYH>*>(smem_raw);
@@ -967,7 +1052,7 @@ __global__ void k_points(int method, long n, const R* __restrict__ st, const R* 
 // ---------------------------------------------------------------------------
 namespace hx {
 template <bool FAST, int AX = TX, int AY = TY>
-__global__ void __launch_bounds__(AX * AY, 1024 / (AX * AY)) k_adj_forward(LevelSrc<double> src, Cells3<double> uo, Plane<double> np,
+__global__ void __launch_bounds__(AX * AY, min_ctas(AX * AY)) k_adj_forward(LevelSrc<double> src, Cells3<double> uo, Plane<double> np,
                                                      Cells3W<double> out, IBox vb, StepCtl<double> ctl,
                                                      const double* dt_fixed, unsigned* post_flags, AdjRecord rec) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -994,7 +1079,7 @@ __global__ void __launch_bounds__(AX * AY, 1024 / (AX * AY)) k_adj_forward(Level
 // A recompute step (dt given) that also records every face's intermediates
 // (FAST must be true: records exist for the fast form only).
 template <bool FAST, int AX = TX, int AY = TY>
-__global__ void __launch_bounds__(AX * AY, 1024 / (AX * AY)) k_adj_forward_rec(LevelSrc<double> src, Cells3<double> uo, Plane<double> np,
+__global__ void __launch_bounds__(AX * AY, min_ctas(AX * AY)) k_adj_forward_rec(LevelSrc<double> src, Cells3<double> uo, Plane<double> np,
                                                          Cells3W<double> out, IBox vb, double dx, double dy,
                                                          const double* dt_fixed, unsigned* post_flags, FaceRec rec) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1008,7 +1093,7 @@ __global__ void __launch_bounds__(AX * AY, 1024 / (AX * AY)) k_adj_forward_rec(L
 }
 
 template <bool FAST, int AX = TX, int AY = TY>
-__global__ void __launch_bounds__(AX * AY, 1024 / (AX * AY)) k_adj_forward_linear(LevelSrc<double> src, Cells3<double> uo, Plane<double> np,
+__global__ void __launch_bounds__(AX * AY, min_ctas(AX * AY)) k_adj_forward_linear(LevelSrc<double> src, Cells3<double> uo, Plane<double> np,
                                                             Cells3W<double> out, IBox vb, double dx, double dy,
                                                             const double* dt_fixed) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1176,6 +1261,18 @@ cudaError_t launch_adj_forward_linear(const LevelSrc<double>& src, const Cells3<
         return cudaGetLastError();
     };
     return big_tile<double>(vb) ? go(BigTile<double>{}) : go(SmallTile{});
+}
+
+// The fast form's reciprocal (rcp_nr) of n values, for checking it against IEEE division.
+template <bool FAST> __global__ void k_rcp_probe(long n, const double* x, double* y) {
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = rcp_nr(x[i]);
+}
+template <bool FAST> cudaError_t launch_rcp(long n, const double* x, double* y, cudaStream_t st) {
+    static_assert(FAST, "the reciprocal belongs to the fast form");
+    if (n <= 0) return cudaSuccess;
+    k_rcp_probe<FAST><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, x, y);
+    return cudaGetLastError();
 }
 
 template <class R, bool FAST>

@@ -607,6 +607,8 @@ int hx_debug_roe_points_f64(int method, int arith, long n, const double* states,
                             hx_stream_t stream);
 int hx_debug_roe_points_f32(int method, int arith, long n, const float* states, const float* aux, float* out,
                             hx_stream_t stream);
+/* The fast form's FP64 reciprocal of n device values (to check it against IEEE division). */
+int hx_debug_rcp_f64(long n, const double* x, double* y, hx_stream_t stream);
 
 #ifdef __cplusplus
 }

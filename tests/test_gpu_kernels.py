@@ -346,3 +346,21 @@ def test_fp64_rate_probe(cuda, hxlib):
     """The FP64 roof probe measures positive rates, FP32 well above FP64."""
     d, f = capi.fp64_rates()
     assert d > 1e10 and f > d
+
+
+def test_fast_reciprocal_is_faithful(cuda, hxlib):
+    """The fast form's reciprocal (hardware estimate + one third-order Newton
+    step) is within one ulp of IEEE division over 2^22 values spanning 1e-300 to
+    1e300 in magnitude, both signs; report the share that is correctly rounded."""
+    rng = np.random.default_rng(11)
+    n = 1 << 22
+    x = np.exp(rng.uniform(np.log(1e-300), np.log(1e300), n)) * rng.choice([-1.0, 1.0], n)
+    x[:1000] = 1.0 + np.arange(1000) * 2.0 ** -52  # just above 1
+    xt = torch.from_numpy(x).to(cuda)
+    yt = torch.empty_like(xt)
+    hxlib.check(hxlib.lib().hx_debug_rcp_f64(n, dptr(xt), dptr(yt), None), "rcp")
+    y = yt.cpu().numpy()
+    ref = 1.0 / x
+    ulps = np.abs(y.view(np.int64) - ref.view(np.int64))
+    assert ulps.max() <= 1, ulps.max()
+    assert (ulps == 0).mean() > 0.99

@@ -10,7 +10,7 @@ import pytest
 import torch
 
 from hydroexa_gb300 import capi, workloads
-from hydroexa_gb300.level import Level
+from hydroexa_gb300.level import DtAccum, Level
 
 pytestmark = pytest.mark.gpu
 
@@ -289,3 +289,44 @@ def test_full_size_properties(cuda, arith):
     assert lev.run(capi.HX_METHOD_HYDROSTATIC_ROE, 10, flat.cfl, arith=arith) == 0
     m1 = lev.state[0].sum(dtype=torch.float64).item()
     assert abs(m1 - m0) <= 1e-12 * m0
+
+
+def _fold_reference(state, z, dx, dy):
+    """(1 / max rate, max speed) of a state over its wet, non-NODATA cells,
+    evaluated in numpy: the bound every cell's contribution gives."""
+    h, hu, hv = (np.asarray(a, dtype=np.float64) for a in state)
+    live = (np.abs(z + 9999.0) >= 1e-10) & (h > 1e-12)
+    u, v = np.abs(hu[live] / h[live]), np.abs(hv[live] / h[live])
+    c = np.sqrt(9.81 * h[live])
+    rate = (u + c) / dx + (v + c) / dy
+    return 1.0 / rate.max(), max(u.max(), v.max())
+
+
+@pytest.mark.parametrize("n,kind", [(64, "varied"), (96, "uniform"), (2048, "varied"), (2048, "uniform")])
+def test_screened_cfl_fold_is_the_maximum(cuda, oracle_lib, n, kind):
+    """The fast form folds the next CFL bound through a float screen (FP64 only
+    for the cells that can hold the block maximum, and once per block for
+    bit-identical candidates).  The folded bound and speed equal those of every
+    cell (to the last few ulps of the fast form's own rate arithmetic), on an
+    evolved state with NODATA and dry cells and on a uniform lake (all ties);
+    2048^2 runs the 32 x 32 tile."""
+    if kind == "varied":
+        case = workloads.fractal_dam_break(n, n, seed=41, amplitude=1.0, nodata_frac=0.15)
+        g = case.geom
+        L = oracle_lib.Level(g.nx, g.ny, g.dx, g.dy, g.bc_lo, g.bc_hi)
+        h, hu, hv, *_ = oracle_lib.run(L, 1, case.h, case.hu, case.hv, case.z, case.n, 4, case.cfl)
+        h[5, 5:9] = 0.0  # dry cells
+    else:
+        case = workloads.fractal_dam_break(n, n, seed=42, amplitude=1.0, nodata_frac=0.0)
+        g = case.geom
+        h = np.full_like(case.h, 2.0)
+        case.z = np.zeros_like(case.z)
+        hu = np.zeros_like(h)
+        hv = np.zeros_like(h)
+    lev = to_level(case, h, hu, hv, cuda)
+    dt = 0.2 * lev.compute_dt()[0]
+    acc = DtAccum(cuda)
+    out = lev.advance(capi.HX_METHOD_HYDROSTATIC_ROE, dt, next_dt=acc, arith=FAST)
+    got_dt, got_v = acc.read()
+    ref_dt, ref_v = _fold_reference(out.cpu().numpy(), case.z, g.dx, g.dy)
+    assert got_dt == pytest.approx(ref_dt, rel=4e-16 * 8) and got_v == pytest.approx(ref_v, rel=4e-16 * 8)
