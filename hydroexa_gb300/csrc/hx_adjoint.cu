@@ -180,10 +180,12 @@ __device__ void roe_rev(double hi, double ui, double vi, double hj, double uj, d
 // entropy-fixed speeds and wave strengths as the forward step computed them;
 // only 1/si and 1/sj are formed).  roe_rev_core then runs the reverse.
 struct RoeFwd {
-    double Hi, Hj, Ui, Uj, Vi, Vj, si, sj, rsi, rsj, cm, rs, rden, rcm, um, vm, l0, l2, a0, a1, a2, w0, w1, w2, dh;
+    double Hi, Hj, Ui, Uj, Vi, Vj, si, sj, rsi, rsj, cm, rs, rden, rcm, um, vm, l0, l2, dh;
+    double a0h, a1h, a2h, w0, w1, w2, hrden, hrcm;  // half wave strengths, w = |l| ah, halves of 1/den, 1/cm
     double e0i, e0j, e2i, e2j, l0a, l2a, rD0, rD2;
     bool wi, wj, hmb, fix0, fix2;
 };
+
 
 __device__ __forceinline__ void roe_fwd_fast(double hi, double ui, double vi, double hj, double uj, double vj,
                                              RoeFwd& F) {
@@ -233,8 +235,11 @@ __device__ __forceinline__ void roe_fwd_fast(double hi, double ui, double vi, do
     F.dh = dh;
     const double dhu = Hj * Uj - Hi * Ui;
     const double dhv = Hj * Vj - Hi * Vi;
-    F.a0 = (F.l2 * dh - dhu) * F.rden; F.a1 = (dhv - vm * dh) * F.rcm; F.a2 = (dhu - F.l0 * dh) * F.rden;
-    F.w0 = 0.5 * fabs(F.l0) * F.a0; F.w1 = 0.5 * fabs(um) * F.a1; F.w2 = 0.5 * fabs(F.l2) * F.a2;
+    F.a0h = 0.5 * ((F.l2 * dh - dhu) * F.rden);
+    F.a1h = 0.5 * ((dhv - vm * dh) * F.rcm);
+    F.a2h = 0.5 * ((dhu - F.l0 * dh) * F.rden);
+    F.w0 = fabs(F.l0) * F.a0h; F.w1 = fabs(um) * F.a1h; F.w2 = fabs(F.l2) * F.a2h;
+    F.hrden = 0.5 * F.rden; F.hrcm = 0.5 * F.rcm;
 }
 
 __device__ __forceinline__ void roe_fwd_rec(double hi, double ui, double vi, double hj, double uj, double vj,
@@ -271,8 +276,9 @@ __device__ __forceinline__ void roe_fwd_rec(double hi, double ui, double vi, dou
         F.rD2 = F.fix2 ? rcp_nr(F.e2j - F.e2i) : 0.0;
     }
     F.dh = Hj - Hi;
-    F.a0 = 2.0 * R.a0h; F.a1 = 2.0 * R.a1h; F.a2 = 2.0 * R.a2h;
+    F.a0h = R.a0h; F.a1h = R.a1h; F.a2h = R.a2h;
     F.w0 = fabs(R.l0) * R.a0h; F.w1 = fabs(R.um) * R.a1h; F.w2 = fabs(R.l2) * R.a2h;
+    F.hrden = 0.5 * F.rden; F.hrcm = 0.5 * F.rcm;
 }
 
 __device__ __forceinline__ void roe_rev_core(const RoeFwd& F, double b0, double b1, double b2, double& ghi,
@@ -280,28 +286,32 @@ __device__ __forceinline__ void roe_rev_core(const RoeFwd& F, double b0, double 
     using C = Cst<double>;
     const double Hi = F.Hi, Hj = F.Hj, Ui = F.Ui, Uj = F.Uj, Vi = F.Vi, Vj = F.Vj;
     const double l0 = F.l0, l1 = F.um, l2 = F.l2, vm = F.vm, cm = F.cm, dh = F.dh;
-    const double a0 = F.a0, a1 = F.a1, a2 = F.a2, w0 = F.w0, w1 = F.w1, w2 = F.w2;
-    double gHi = 0.5 * (b0 * Ui + b1 * (Ui * Ui + 2.0 * HG * Hi) + b2 * Ui * Vi);
-    double gHj = 0.5 * (b0 * Uj + b1 * (Uj * Uj + 2.0 * HG * Hj) + b2 * Uj * Vj);
-    double gUi = 0.5 * b0 * Hi + b1 * Hi * Ui + 0.5 * b2 * Hi * Vi;
-    double gUj = 0.5 * b0 * Hj + b1 * Hj * Uj + 0.5 * b2 * Hj * Vj;
-    double gVi = 0.5 * b2 * Hi * Ui, gVj = 0.5 * b2 * Hj * Uj;
+    const double w0 = F.w0, w1 = F.w1, w2 = F.w2;
+    // central flux (F(U_i) + F(U_j)) / 2 with F = (H U, H U^2 + HG H^2, H U V):
+    // dF/dH = (U, U^2 + G H, U V), dF/dU = (H, 2 H U, H V), dF/dV = (0, 0, H U)
+    const double hb0 = 0.5 * b0, hb1 = 0.5 * b1, hb2 = 0.5 * b2;
+    double gHi = fma(hb0, Ui, fma(hb1, fma(Ui, Ui, G * Hi), hb2 * Ui * Vi));
+    double gHj = fma(hb0, Uj, fma(hb1, fma(Uj, Uj, G * Hj), hb2 * Uj * Vj));
+    double gUi = Hi * fma(hb2, Vi, fma(b1, Ui, hb0));
+    double gUj = Hj * fma(hb2, Vj, fma(b1, Uj, hb0));
+    double gVi = hb2 * Hi * Ui, gVj = hb2 * Hj * Uj;
     const double gw0 = -b0 - b1 * l0 - b2 * vm;
     const double gw1 = -b2 * cm;
     const double gw2 = -b0 - b1 * l2 - b2 * vm;
-    double gl0 = -b1 * w0 + gw0 * 0.5 * sgn(l0) * a0;
-    double gl2 = -b1 * w2 + gw2 * 0.5 * sgn(l2) * a2;
+    // w_k = |l_k| ah_k, ah_k = alpha_k / 2
+    double gl0 = fma(gw0, sgn(l0) * F.a0h, -b1 * w0);
+    double gl2 = fma(gw2, sgn(l2) * F.a2h, -b1 * w2);
     double gvm = -b2 * (w0 + w2), gcm = -b2 * w1;
-    const double gl1 = gw1 * 0.5 * sgn(l1) * a1;
-    const double ga0 = gw0 * 0.5 * fabs(l0) * F.rden;  // already divided by den
-    const double ga1 = gw1 * 0.5 * fabs(l1) * F.rcm;   // already divided by cm
-    const double ga2 = gw2 * 0.5 * fabs(l2) * F.rden;
+    const double gl1 = gw1 * (sgn(l1) * F.a1h);
+    const double ga0 = gw0 * fabs(l0) * F.hrden;  // d/d alpha0, already divided by den
+    const double ga1 = gw1 * fabs(l1) * F.hrcm;   // d/d alpha1, already divided by cm
+    const double ga2 = gw2 * fabs(l2) * F.hrden;
     gl2 += ga0 * dh;
     double gdh = ga0 * l2 - ga1 * vm - ga2 * l0;
     double gdhu = ga2 - ga0;
     const double gdhv = ga1;
     gvm -= ga1 * dh;
-    gcm -= ga1 * a1 + 2.0 * (ga0 * a0 + ga2 * a2);
+    gcm -= 2.0 * fma(ga1, F.a1h, 2.0 * fma(ga0, F.a0h, ga2 * F.a2h));  // ga1 a1 + 2 (ga0 a0 + ga2 a2)
     gl0 -= ga2 * dh;
     gHj += gdh + gdhu * Uj + gdhv * Vj;
     gHi -= gdh + gdhu * Ui + gdhv * Vi;
@@ -334,11 +344,11 @@ __device__ __forceinline__ void roe_rev_core(const RoeFwd& F, double b0, double 
     const double gsi = gnu * Ui + gnv * Vi + gsden + C::sqrt_g * gci;
     const double gsj = gnu * Uj + gnv * Vj + gsden + C::sqrt_g * gcj;
     if (F.hmb) {
-        const double ghm = 0.5 * gcm * G * F.rcm;
-        gHi += 0.5 * ghm; gHj += 0.5 * ghm;
+        const double hghm = gcm * (0.25 * G) * F.rcm;
+        gHi += hghm; gHj += hghm;
     }
-    gHi += 0.5 * gsi * F.rsi;
-    gHj += 0.5 * gsj * F.rsj;
+    gHi = fma(0.5 * gsi, F.rsi, gHi);
+    gHj = fma(0.5 * gsj, F.rsj, gHj);
     if (F.wi) { ghi += gHi; gui += gUi; gvi += gVi; }
     if (F.wj) { ghj += gHj; guj += gUj; gvj += gVj; }
 }
@@ -380,9 +390,9 @@ __device__ void face_rev(const FaceVals& f, const double gFL[3], const double gF
         roe_rev(hLs, unL, utL, hRs, unR, utR, gf0, b1, b2, ghLs, gunL, gutL, ghRs, gunR, gutR);
     }
     // pressure correction p = HG (hu^2 - hs^2)
-    const double ghLu = gpL * 2.0 * HG * hLu, ghRu = gpR * 2.0 * HG * hRu;
-    ghLs += -gpL * 2.0 * HG * hLs;
-    ghRs += -gpR * 2.0 * HG * hRs;
+    const double ghLu = gpL * (G * hLu), ghRu = gpR * (G * hRu);
+    ghLs = fma(-gpL, G * hLs, ghLs);
+    ghRs = fma(-gpR, G * hRs, ghRs);
     double getaL = 0, getaR = 0, gzL = 0, gzR = 0, gzf = 0;
     if (pos_i(dLu)) { getaL += ghLu; gzL -= ghLu; }
     if (pos_i(dRu)) { getaR += ghRu; gzR -= ghRu; }
