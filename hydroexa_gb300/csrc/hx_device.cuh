@@ -118,23 +118,6 @@ __host__ __device__ __forceinline__ bool is_nodata(double z) {
 }
 __host__ __device__ __forceinline__ bool is_nodata(float z) { return sbits(z) == (int)0xC61C3C00u; }
 
-// x / 2 on the integer pipe: decrementing the exponent field is exact, and
-// equals 0.5 * x, for normal x above the smallest normal exponent; zero is
-// kept; subnormals, the smallest normals, inf and NaN take the FP64 multiply.
-__host__ __device__ __forceinline__ double half_i(double x) {
-    const long long b = sbits(x);
-    const long long e = b & 0x7FF0000000000000ll;
-    if (e > 0x0010000000000000ll && e != 0x7FF0000000000000ll) {
-        const long long r = b - 0x0010000000000000ll;
-        double y;
-        memcpy(&y, &r, sizeof y);
-        return y;
-    }
-    if ((b << 1) == 0) return x;
-    return 0.5 * x;
-}
-__host__ __device__ __forceinline__ float half_i(float x) { return 0.5f * x; }
-
 // The leading 24 significand bits of a double as a float (truncated, so within
 // 2^-23 relative; 0 below the float range, inf above, NaN kept as NaN or inf),
 // made on the integer pipe: for decisions whose outcome is certain at that
@@ -358,7 +341,7 @@ __host__ __device__ __forceinline__ void roe_hydrostatic_fast(R hi, R ui, R vi, 
     R uni, uti, unj, utj;
     if (DIR == 0) { uni = ui; uti = vi; unj = uj; utj = vj; }
     else { uni = vi; uti = -ui; unj = vj; utj = -uj; }
-    const R hh = half_i(hi + hj);
+    const R hh = R(0.5) * (hi + hj);
     const bool hmb = gt_bits(hh, C::toldry_bits);
     const R hm = hmb ? hh : C::toldry;
     const R cm = fast_sqrt(C::g * hm);
@@ -403,9 +386,9 @@ __host__ __device__ __forceinline__ void roe_hydrostatic_fast(R hi, R ui, R vi, 
     const R qi = hi * uni, qj = hj * unj;
     const R dhu = qj - qi;
     const R dhv = hj * utj - hi * uti;
-    const R hrden = half_i(rden);
+    const R hrden = R(0.5) * rden;
     const R a0h = (l2 * dh - dhu) * hrden;  // alpha0 / 2
-    const R a1h = (dhv - vm * dh) * half_i(rcm);
+    const R a1h = (dhv - vm * dh) * (R(0.5) * rcm);
     const R a2h = (dhu - l0 * dh) * hrden;
     const R w0 = fabs(l0) * a0h;
     const R w1 = fabs(l1) * a1h;
