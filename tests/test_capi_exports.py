@@ -44,3 +44,61 @@ def test_argument_errors_need_no_gpu(hxlib):
     lv = hxlib.LevelF64()
     rc = L.hx_level_run_f64(1, ctypes.byref(lv), None, None, None, 1, 0.5, None, None, None, 0, None, None)
     assert rc == hxlib.HX_ERR_ARG
+
+
+def test_box_level_plan_checks_the_tiling(hxlib):
+    """The multi-box planner (host code) accepts boxes that tile the domain and
+    rejects overlaps, gaps and boxes outside it, with a message."""
+    L = hxlib.lib()
+
+    def boxes(spans):
+        arr = (hxlib.LevelBoxF64 * len(spans))()
+        for k, (x0, y0, x1, y1) in enumerate(spans):
+            b = arr[k]
+            for f in ("h", "hu", "hv", "h_alt", "hu_alt", "hv_alt", "z", "n"):
+                setattr(b, f, 4096)  # never dereferenced by the planner
+            b.pitch = x1 - x0 + 1
+            b.lo[0], b.lo[1], b.hi[0], b.hi[1] = x0, y0, x1, y1
+        return arr, len(spans)
+
+    ok = [(0, 0, 31, 23), (32, 0, 63, 23), (0, 24, 63, 47)]
+    assert L.hx_boxlevel_work_bytes(len(ok), boxes(ok)[0], 64, 48) > 0
+    for bad in ([(0, 0, 40, 23), (32, 0, 63, 23), (0, 24, 63, 47)],   # overlap
+                [(0, 0, 31, 23), (0, 24, 63, 47)],                    # gap
+                [(0, 0, 63, 47), (64, 0, 70, 47)]):                   # outside
+        arr, n = boxes(bad)
+        assert L.hx_boxlevel_work_bytes(n, arr, 64, 48) == 0
+        assert L.hx_last_error()
+
+
+def test_adjoint_work_bytes_options(hxlib):
+    """Face records add to the work buffer of checkpointed sweeps only; unknown
+    option bits are refused."""
+    L = hxlib.lib()
+    rec = hxlib.HX_ADJ_FACE_RECORDS
+    plain = L.hx_adjoint_work_bytes_f64(512, 512, 512, 2000, 45, 0)
+    with_rec = L.hx_adjoint_work_bytes_f64(512, 512, 512, 2000, 45, rec)
+    assert plain > 0 and with_rec - plain > 2 * 45 * 250 * 512 * 512
+    assert L.hx_adjoint_work_bytes_f64(512, 512, 512, 2000, 0, rec) == L.hx_adjoint_work_bytes_f64(512, 512, 512, 2000, 0, 0)
+    assert L.hx_adjoint_work_bytes_f64(512, 512, 512, 2000, -20, rec) == L.hx_adjoint_work_bytes_f64(512, 512, 512, 2000, -20, 0)
+    assert L.hx_adjoint_work_bytes_f64(512, 512, 512, 2000, 45, 0x4000) == 0
+
+
+def test_plotfile_arguments_checked_on_the_host(hxlib, tmp_path):
+    """A box outside its level's domain is refused before any copy or file."""
+    L = hxlib.lib()
+    box = hxlib.PlotBoxF64()
+    for f in ("h", "hu", "hv", "z", "n"):
+        setattr(box, f, 4096)
+    box.pitch = 16
+    box.lo[0], box.lo[1], box.hi[0], box.hi[1] = 0, 0, 15, 15
+    lev = hxlib.PlotLevelF64()
+    lev.boxes = ctypes.pointer(box)
+    lev.nboxes = 1
+    lev.domain_lo[0], lev.domain_lo[1], lev.domain_hi[0], lev.domain_hi[1] = 0, 0, 14, 15
+    lev.dx, lev.dy = 0.1, 0.1
+    lo = (ctypes.c_double * 2)(0.0, 0.0)
+    hi = (ctypes.c_double * 2)(1.0, 1.0)
+    rc = L.hx_write_plotfile_f64(str(tmp_path / "plt").encode(), 3, 0.0, 1, ctypes.byref(lev), lo, hi, None)
+    assert rc == hxlib.HX_ERR_ARG
+    assert not (tmp_path / "plt00003").exists()
