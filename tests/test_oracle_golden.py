@@ -25,11 +25,27 @@ def test_roe_hydrostatic_golden(oracle_lib, sfx):
     assert bits_equal(F, g["F"])
 
 
+def ulps(a, b):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    it = np.int64 if a.dtype == np.float64 else np.int32
+    return np.abs(a.view(it).astype(np.int64) - b.view(it).astype(np.int64))
+
+
 @pytest.mark.parametrize("sfx", ["f64", "f32"])
 def test_roe_classic_golden(oracle_lib, sfx):
+    """Bit-equal on x86-64, where the golden vectors were made.  The sources
+    S- and S+ carry Manning's h^(1/3) from the C library's cbrt, which is not
+    correctly rounded and differs by an ulp between the x86-64 and aarch64
+    builds of the C library; there they are held to 4 ulps."""
+    import platform
     g = np.load(GOLD / f"roe_classic_{sfx}.npz")
     F, Sm, Sp = oracle_lib.roe_classic_points(g["states"], g["aux"])
-    assert bits_equal(F, g["F"]) and bits_equal(Sm, g["Sm"]) and bits_equal(Sp, g["Sp"])
+    assert bits_equal(F, g["F"])
+    if platform.machine() in ("x86_64", "AMD64"):
+        assert bits_equal(Sm, g["Sm"]) and bits_equal(Sp, g["Sp"])
+    else:
+        assert ulps(Sm, g["Sm"]).max() <= 4 and ulps(Sp, g["Sp"]).max() <= 4
 
 
 def test_golden_covers_branches(oracle_lib):
