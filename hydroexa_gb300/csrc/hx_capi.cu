@@ -402,25 +402,32 @@ template <class R> int accum_read(const hx_dt_accum* acc, R* dtmin, R* maxvel, c
     if (e != cudaSuccess) return fail(HX_ERR_CUDA, "accumulator read: %s", cudaGetErrorString(e));
     if (dtmin) *dtmin = accum_dt_min<R>(h.rate_bits, h.flags);
     if (maxvel) *maxvel = from_bits<R>(h.maxvel_bits);
-    return (h.flags & DTF_NAN) ? HX_STATUS_NAN : HX_OK;
+    return (h.flags & DTF_NAN) ? (int)HX_STATUS_NAN : (int)HX_OK;
 }
 
 // ---------------------------------------------------------------- host form
-// Device buffers of the host-buffer entry, kept between calls, and three
+// Device buffers of the host-buffer entry, kept between calls, and four
 // streams: uploads and downloads (one each: a copy engine does not interleave
-// two streams' queues, so bands go in order on one) and the CFL reduction of
-// the uploaded level, which then does not wait behind the flux work.
+// two streams' queues, so bands go in order on one), the CFL reduction of the
+// uploaded level and the first step's per-band updates.  The last two run at
+// the highest priority, so that their few blocks are scheduled ahead of the
+// flux work queued on the caller's stream and the bands go down early.
 constexpr int kHostBands = 8;
+constexpr int kHeadRows = 2;  // rows of the next band the flux differences of a band read (the MUSCL reach)
 struct HostCache {
     void* base = nullptr;
     size_t bytes = 0;
-    cudaStream_t cs[3] = {nullptr, nullptr, nullptr};  // uploads, downloads, CFL reduction
-    cudaEvent_t ev[4 + 2 * kHostBands] = {};
+    cudaStream_t cs[4] = {nullptr, nullptr, nullptr, nullptr};  // uploads, downloads, CFL reduction, updates
+    // start, dt known, updates done, four joins; per band: landed, head landed, flux differences, computed
+    cudaEvent_t ev[7 + 4 * kHostBands] = {};
     bool streams_ok = false;
     bool ensure_streams() {
         if (streams_ok) return true;
-        for (auto& c : cs)
-            if (cudaStreamCreateWithFlags(&c, cudaStreamNonBlocking) != cudaSuccess) return false;
+        int least = 0, greatest = 0;
+        if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) return false;
+        for (int k = 0; k < 4; ++k)
+            if (cudaStreamCreateWithPriority(&cs[k], cudaStreamNonBlocking, k >= 2 ? greatest : least) != cudaSuccess)
+                return false;
         for (auto& e : ev)
             if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return false;
         streams_ok = true;
@@ -684,7 +691,7 @@ int hx_level_run_host_f64(int method, int nx, int ny, double dx, double dy, cons
     const int band = ((ny + kHostBands - 1) / kHostBands + TY - 1) / TY * TY;
     const int nbands = (ny + band - 1) / band;
     auto rows = [&](int b, int& j0, int& j1) { j0 = b * band; j1 = (j0 + band < ny ? j0 + band : ny) - 1; };
-    auto flux_band = [&](int b) -> int {  // flux differences of band b (rows b-1 .. b+1 must have landed)
+    auto flux_band = [&](int b) -> int {  // flux differences of band b (rows to the head of b+1 have landed)
         int j0, j1;
         rows(b, j0, j1);
         const LevelSrc<double> lsrc = level_src<double>(&L, 2);
@@ -693,30 +700,47 @@ int hx_level_run_host_f64(int method, int nx, int ny, double dx, double dy, cons
                              : launch_hydro_split<double, false>(lsrc, uo, np, div, vb, dx, dy, st),
                         "hx_level_run_host_f64 (flux differences)");
     };
-    // Upload in row bands (stream up), after the caller's earlier work.  The CFL reduction of each band runs
-    // as soon as its rows have landed.  Split: on its own stream, while st runs each band's flux differences
-    // once the band after it has landed, then each band's update once dt is known, the band's rows then
-    // going down (stream down) under the flux work of later bands.
-    cudaStream_t up = cs[0], down = cs[1], dts = cs[2];
-    cudaEvent_t* ev_up = ev + 4;
-    cudaEvent_t* ev_k = ev + 4 + kHostBands;
+    // Upload in row bands (stream up), after the caller's earlier work; from the second band on, a band's
+    // first kHeadRows rows go up ahead of the rest.  The CFL reduction of each band runs as soon as its rows
+    // have landed.  Split: the reduction on its own stream (dts), while st runs each band's flux differences
+    // once the head of the band after it has landed; the updates (stream upd) start when dt is known, each
+    // after its band's flux differences, and each band's rows go down (stream down) under the flux work of
+    // later bands.
+    cudaStream_t up = cs[0], down = cs[1], dts = cs[2], upd = cs[3];
+    cudaEvent_t ev_start = ev[0], ev_dt = ev[1], ev_upd = ev[2];
+    cudaEvent_t* ev_join = ev + 3;
+    cudaEvent_t* ev_up = ev + 7;
+    cudaEvent_t* ev_head = ev + 7 + kHostBands;
+    cudaEvent_t* ev_flux = ev + 7 + 2 * kHostBands;
+    cudaEvent_t* ev_k = ev + 7 + 3 * kHostBands;
     cudaError_t e = cudaMemsetAsync(tail, 0, 128 + 3 * sizeof(DtAccum), st);
-    if (e == cudaSuccess) e = cudaEventRecord(ev[0], st);
-    for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(cs[k], ev[0], 0);
+    if (e == cudaSuccess) e = cudaEventRecord(ev_start, st);
+    for (int k = 0; k < 4 && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(cs[k], ev_start, 0);
     int rc = HX_OK;
     cudaStream_t dstream = split ? dts : st;
+    auto upload = [&](int r0, int r1) -> cudaError_t {  // rows r0..r1 of the five planes
+        cudaError_t r = cudaSuccess;
+        for (int k = 0; k < 5 && r == cudaSuccess; ++k)
+            r = cudaMemcpyAsync(P[k] + (size_t)r0 * nx, src[k] + (size_t)r0 * nx,
+                                (size_t)(r1 - r0 + 1) * nx * sizeof(double), cudaMemcpyHostToDevice, up);
+        return r;
+    };
     for (int b = 0; b < nbands && e == cudaSuccess && rc == HX_OK; ++b) {
         int j0, j1;
         rows(b, j0, j1);
-        for (int k = 0; k < 5 && e == cudaSuccess; ++k)
-            e = cudaMemcpyAsync(P[k] + (size_t)j0 * nx, src[k] + (size_t)j0 * nx,
-                                (size_t)(j1 - j0 + 1) * nx * sizeof(double), cudaMemcpyHostToDevice, up);
+        int jr = j0;  // the rows after the head
+        if (b > 0) {
+            jr = j0 + kHeadRows <= j1 ? j0 + kHeadRows : j1 + 1;
+            e = upload(j0, jr - 1);
+            if (e == cudaSuccess) e = cudaEventRecord(ev_head[b], up);
+        }
+        if (e == cudaSuccess && jr <= j1) e = upload(jr, j1);
         if (e == cudaSuccess) e = cudaEventRecord(ev_up[b], up);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(dstream, ev_up[b], 0);
         if (e == cudaSuccess)
             rc = level_dt<double>(&L, reinterpret_cast<hx_dt_accum*>(&slot[0]), dstream, arith, j0, j1);
     }
-    if (e == cudaSuccess && split) e = cudaEventRecord(ev[3], dts);
+    if (e == cudaSuccess && split) e = cudaEventRecord(ev_dt, dts);
     if (e != cudaSuccess) return fail(HX_ERR_CUDA, "upload: %s", cudaGetErrorString(e));
     if (rc) return rc;
     const double* A[3] = {P[0], P[1], P[2]};
@@ -733,10 +757,11 @@ int hx_level_run_host_f64(int method, int nx, int ny, double dx, double dy, cons
         c.status = status; c.time = b ? nullptr : tdev; c.dx = dx; c.dy = dy;
         return c;
     };
-    auto download = [&](int b, double* const* o) -> cudaError_t {  // band b's rows of o, after st's work so far
+    // band b's rows of o, after the work queued so far on stream after
+    auto download = [&](int b, double* const* o, cudaStream_t after) -> cudaError_t {
         int j0, j1;
         rows(b, j0, j1);
-        cudaError_t r = cudaEventRecord(ev_k[b], st);
+        cudaError_t r = cudaEventRecord(ev_k[b], after);
         if (r == cudaSuccess) r = cudaStreamWaitEvent(down, ev_k[b], 0);
         for (int k = 0; k < 3 && r == cudaSuccess; ++k)
             r = cudaMemcpyAsync(dst[k] + (size_t)j0 * nx, o[k] + (size_t)j0 * nx,
@@ -749,28 +774,28 @@ int hx_level_run_host_f64(int method, int nx, int ny, double dx, double dy, cons
         Cells3W<double> ow;
         ow.p[0] = o[0]; ow.p[1] = o[1]; ow.p[2] = o[2];
         ow.js = nx; ow.lo0 = 0; ow.lo1 = 0;
-        auto update_band = [&](int b) -> int {
+        for (int b = 0; b < nbands && rc == HX_OK && e == cudaSuccess; ++b) {
+            // rows b-1 .. b and the head of b+1 have landed
+            e = cudaStreamWaitEvent(st, b + 1 < nbands ? ev_head[b + 1] : ev_up[b], 0);
+            if (e == cudaSuccess) rc = flux_band(b);
+            if (rc == HX_OK && e == cudaSuccess) e = cudaEventRecord(ev_flux[b], st);
+        }
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(upd, ev_dt, 0);  // dt of the whole level
+        for (int b = 0; b < nbands && rc == HX_OK && e == cudaSuccess; ++b) {
             int j0, j1;
             rows(b, j0, j1);
             const IBox vb{0, j0, nx - 1, j1};
             const StepCtl<double> cb = step_ctl(0, b);
-            int r = launched(fast ? launch_hydro_update<double, true>(uo, div, np, zp, ow, vb, cb, st)
-                                  : launch_hydro_update<double, false>(uo, div, np, zp, ow, vb, cb, st),
-                             "hx_level_run_host_f64 (update)");
-            if (r == HX_OK && nsteps == 1) {
-                const cudaError_t de = download(b, o);
-                if (de != cudaSuccess) r = fail(HX_ERR_CUDA, "download: %s", cudaGetErrorString(de));
-            }
-            return r;
-        };
-        for (int b = 0; b < nbands && rc == HX_OK && e == cudaSuccess; ++b) {
-            e = cudaStreamWaitEvent(st, ev_up[b + 1 < nbands ? b + 1 : b], 0);  // rows b-1 .. b+1 have landed
-            if (e == cudaSuccess) rc = flux_band(b);
-            if (rc == HX_OK && b == 1) e = cudaStreamWaitEvent(st, ev[3], 0);  // dt of the whole level
-            if (rc == HX_OK && e == cudaSuccess && b >= 1) rc = update_band(b - 1);
+            e = cudaStreamWaitEvent(upd, ev_flux[b], 0);
+            if (e != cudaSuccess) break;
+            rc = launched(fast ? launch_hydro_update<double, true>(uo, div, np, zp, ow, vb, cb, upd)
+                               : launch_hydro_update<double, false>(uo, div, np, zp, ow, vb, cb, upd),
+                          "hx_level_run_host_f64 (update)");
+            if (rc == HX_OK && nsteps == 1) e = download(b, o, upd);
         }
-        if (rc == HX_OK && e == cudaSuccess && nbands == 1) e = cudaStreamWaitEvent(st, ev[3], 0);
-        if (rc == HX_OK && e == cudaSuccess) rc = update_band(nbands - 1);
+        // the later steps read every band's update
+        if (rc == HX_OK && e == cudaSuccess) e = cudaEventRecord(ev_upd, upd);
+        if (rc == HX_OK && e == cudaSuccess) e = cudaStreamWaitEvent(st, ev_upd, 0);
         if (e != cudaSuccess) return fail(HX_ERR_CUDA, "split step: %s", cudaGetErrorString(e));
         if (rc) return rc;
         res[0] = o[0]; res[1] = o[1]; res[2] = o[2];
@@ -792,18 +817,18 @@ int hx_level_run_host_f64(int method, int nx, int ny, double dx, double dy, cons
             rc = level_advance<double>(method, &cur, step_ctl(s, b), o[0], o[1], o[2], arith, st, j0, j1);
             if (rc) return rc;
             if (!last) continue;
-            e = download(b, o);
+            e = download(b, o, st);
             if (e != cudaSuccess) return fail(HX_ERR_CUDA, "download: %s", cudaGetErrorString(e));
         }
     }
     if (nsteps == 0) {
-        e = cudaEventRecord(ev[1], st);
-        if (e == cudaSuccess) e = cudaStreamWaitEvent(down, ev[1], 0);
+        e = cudaEventRecord(ev_k[0], st);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(down, ev_k[0], 0);
         for (int k = 0; k < 3 && e == cudaSuccess; ++k)
             e = cudaMemcpyAsync(dst[k], res[k], pb, cudaMemcpyDeviceToHost, down);
     }
-    for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = cudaEventRecord(ev[1 + k], cs[k]);  // join all three
-    for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(st, ev[1 + k], 0);
+    for (int k = 0; k < 4 && e == cudaSuccess; ++k) e = cudaEventRecord(ev_join[k], cs[k]);  // join all four
+    for (int k = 0; k < 4 && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(st, ev_join[k], 0);
     uint32_t sv = 0;
     double tv = 0;
     if (e == cudaSuccess) e = cudaMemcpyAsync(&sv, status, 4, cudaMemcpyDeviceToHost, st);

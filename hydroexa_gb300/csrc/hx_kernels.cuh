@@ -258,8 +258,8 @@ struct FaceRec {
     }
 };
 
-// The next step's CFL bound of a block's cells (one cell per thread) with FP64
-// work only where it can decide the maximum.  Each wet cell's rate
+// The CFL bound of a block's cells (K cells per thread) with FP64 work only
+// where it can decide the maximum.  Each wet cell's rate
 // (|u| + c)/dx + (|v| + c)/dy and speed max(|u|, |v|) are first estimated in
 // float from the leading bits of h, hu, hv (error below 2^-19 relative); the
 // cells within 2^-12 of the block's float maxima, and any whose estimate is not
@@ -270,57 +270,76 @@ struct FaceRec {
 // exactly those of computing every cell: the cell holding the true maximum is
 // always a candidate.  Warps without such a cell skip the FP64 work, which in
 // regions of uniform state (a lake at rest, the still water ahead of a wave)
-// is all warps but one.  Every thread of the block must call it.
-template <int NTv>
-__device__ __forceinline__ void screened_fold(const ScreenCell<double>& c, double dx, double dy, double idx,
+// is all warps but one.  Cell k of thread t is candidate number k * NTv + t.
+// Every thread of the block must call it.
+template <int NTv, int K = 1>
+__device__ __forceinline__ void screened_fold(const ScreenCell<double>* c, double dx, double dy, double idx,
                                               double idy, double& rate, double& mv, unsigned& flags) {
     __shared__ float s_r[NTv / 32], s_m[NTv / 32];
     __shared__ int s_rep;
     __shared__ long long s_bits[3];
     const int t = threadIdx.x;
-    bool wet = false;
-    float r32 = 0.f, m32 = 0.f;
-    if (c.live) {
-        if (c.nod) flags |= DTF_NODATA;
-        else if (!gt_bits(c.h, Cst<double>::tol12_bits)) flags |= DTF_DRY;
-        else {
-            wet = true;
-            const float h = f32_lead(c.h), qx = fabsf(f32_lead(c.hu)), qy = fabsf(f32_lead(c.hv));
-            const float rh = rcp_nr(h);
-            const float u = qx * rh, v = qy * rh;
-            const float cc = fast_sqrt(9.81f * h);
-            r32 = (u + cc) * f32_lead(idx) + (v + cc) * f32_lead(idy);
-            m32 = fmaxf(u, v);
+    bool wet[K], bad[K];
+    float r32[K], m32[K], wr = 0.f, wm = 0.f;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        wet[k] = false;
+        r32[k] = 0.f;
+        m32[k] = 0.f;
+        if (c[k].live) {
+            if (c[k].nod) flags |= DTF_NODATA;
+            else if (!gt_bits(c[k].h, Cst<double>::tol12_bits)) flags |= DTF_DRY;
+            else {
+                wet[k] = true;
+                const float h = f32_lead(c[k].h), qx = fabsf(f32_lead(c[k].hu)), qy = fabsf(f32_lead(c[k].hv));
+                const float rh = rcp_nr(h);
+                const float u = qx * rh, v = qy * rh;
+                const float cc = fast_sqrt(9.81f * h);
+                r32[k] = (u + cc) * f32_lead(idx) + (v + cc) * f32_lead(idy);
+                m32[k] = fmaxf(u, v);
+            }
         }
+        bad[k] = wet[k] && !(r32[k] <= 3.0e38f && m32[k] <= 3.0e38f);  // inf or NaN: decided in FP64
+        const float ar = (wet[k] && !bad[k]) ? r32[k] : 0.f, am = (wet[k] && !bad[k]) ? m32[k] : 0.f;
+        wr = k ? fmaxf(wr, ar) : ar;
+        wm = k ? fmaxf(wm, am) : am;
     }
-    const bool bad = wet && !(r32 <= 3.0e38f && m32 <= 3.0e38f);  // inf or NaN: decided in FP64
-    float wr = (wet && !bad) ? r32 : 0.f, wm = (wet && !bad) ? m32 : 0.f;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         wr = fmaxf(wr, __shfl_xor_sync(0xffffffffu, wr, o));
         wm = fmaxf(wm, __shfl_xor_sync(0xffffffffu, wm, o));
     }
-    if (t == 0) s_rep = NTv;
+    if (t == 0) s_rep = K * NTv;
     if ((t & 31) == 0) { s_r[t >> 5] = wr; s_m[t >> 5] = wm; }
     __syncthreads();
     float br = 0.f, bm = 0.f;
 #pragma unroll
     for (int k = 0; k < NTv / 32; ++k) { br = fmaxf(br, s_r[k]); bm = fmaxf(bm, s_m[k]); }
     const float kr = br * (1.f - 0x1p-12f), km = bm * (1.f - 0x1p-12f);
-    const bool cand = bad || (wet && (r32 >= kr || m32 >= km));
-    if (cand) atomicMin(&s_rep, t);
+    bool cand[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        cand[k] = bad[k] || (wet[k] && (r32[k] >= kr || m32[k] >= km));
+        if (cand[k]) atomicMin(&s_rep, k * NTv + t);
+    }
     __syncthreads();
     const int rep = s_rep;
-    if (t == rep) { s_bits[0] = sbits(c.h); s_bits[1] = sbits(c.hu); s_bits[2] = sbits(c.hv); }
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+        if (k * NTv + t == rep) { s_bits[0] = sbits(c[k].h); s_bits[1] = sbits(c[k].hu); s_bits[2] = sbits(c[k].hv); }
     __syncthreads();
-    const bool same = t != rep && sbits(c.h) == s_bits[0] && sbits(c.hu) == s_bits[1] && sbits(c.hv) == s_bits[2];
-    if (cand && !same) {
-        double rc, mc;
-        unsigned f = 0;
-        dt_cell_contrib<double, true>(c.h, c.hu, c.hv, false, dx, dy, idx, idy, rc, mc, f);
-        flags |= f;
-        rate = nnmax_i(rate, rc);
-        mv = nnmax_i(mv, mc);
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const bool same = k * NTv + t != rep && sbits(c[k].h) == s_bits[0] && sbits(c[k].hu) == s_bits[1] &&
+                          sbits(c[k].hv) == s_bits[2];
+        if (cand[k] && !same) {
+            double rc, mc;
+            unsigned f = 0;
+            dt_cell_contrib<double, true>(c[k].h, c[k].hu, c[k].hv, false, dx, dy, idx, idy, rc, mc, f);
+            flags |= f;
+            rate = nnmax_i(rate, rc);
+            mv = nnmax_i(mv, mc);
+        }
     }
 }
 
@@ -502,7 +521,7 @@ __device__ __forceinline__ void hydro_tile_body(HydroSmem<R, TXv, TYv>& S, const
                                    mv, flags, pflags, (SCREEN && dt_out) ? &sc : nullptr);
     }
     if constexpr (SCREEN) {
-        if (dt_out) screened_fold<NTv>(sc, dx, dy, idx, idy, rate, mv, flags);
+        if (dt_out) screened_fold<NTv>(&sc, dx, dy, idx, idy, rate, mv, flags);
     }
     if (dt_out) block_fold_dt<R, NTv>(rate, mv, flags, dt_out);
     if ((flags & DTF_NAN) && status) atomicOr(status, (unsigned)HX_STATUS_NAN);
@@ -823,18 +842,33 @@ __global__ void __launch_bounds__(NT) k_dt_reduce(Cells3<R> U, Plane<R> Z, IBox 
     const int i = vb.lo0 + blockIdx.x * TX + (threadIdx.x & (TX - 1));
     R rate = R(0), mv = R(0);
     unsigned flags = 0;
-    for (int r = 0; r < ROWS_PER_THREAD; ++r) {  // a 32 x (8 ROWS) block: fewer blocks, fewer atomics
-        const int j = vb.lo1 + ((int)blockIdx.y * ROWS_PER_THREAD + r) * TY + threadIdx.x / TX;
-        if (i > vb.hi0 || j > vb.hi1) continue;
-        R rc, mc;
-        dt_cell_contrib<R, FAST>(U.ld(0, i, j), U.ld(1, i, j), U.ld(2, i, j), is_nodata(Z.ld(i, j)), dx, dy, idx,
-                                 idy, rc, mc, flags);
-        if constexpr (FAST) {
-            rate = nnmax_i(rate, rc);
-            mv = nnmax_i(mv, mc);
-        } else {
-            rate = smax(rate, rc);
-            mv = smax(mv, mc);
+    if constexpr (FAST && sizeof(R) == 8) {  // through the float screen: FP64 for the candidates only
+        ScreenCell<double> c[ROWS_PER_THREAD];
+#pragma unroll
+        for (int r = 0; r < ROWS_PER_THREAD; ++r) {
+            const int j = vb.lo1 + ((int)blockIdx.y * ROWS_PER_THREAD + r) * TY + threadIdx.x / TX;
+            if (i > vb.hi0 || j > vb.hi1) continue;
+            c[r].h = U.ld(0, i, j);
+            c[r].hu = U.ld(1, i, j);
+            c[r].hv = U.ld(2, i, j);
+            c[r].nod = is_nodata(Z.ld(i, j));
+            c[r].live = true;
+        }
+        screened_fold<NT, ROWS_PER_THREAD>(c, dx, dy, idx, idy, rate, mv, flags);
+    } else {
+        for (int r = 0; r < ROWS_PER_THREAD; ++r) {  // a 32 x (8 ROWS) block: fewer blocks, fewer atomics
+            const int j = vb.lo1 + ((int)blockIdx.y * ROWS_PER_THREAD + r) * TY + threadIdx.x / TX;
+            if (i > vb.hi0 || j > vb.hi1) continue;
+            R rc, mc;
+            dt_cell_contrib<R, FAST>(U.ld(0, i, j), U.ld(1, i, j), U.ld(2, i, j), is_nodata(Z.ld(i, j)), dx, dy,
+                                     idx, idy, rc, mc, flags);
+            if constexpr (FAST) {
+                rate = nnmax_i(rate, rc);
+                mv = nnmax_i(mv, mc);
+            } else {
+                rate = smax(rate, rc);
+                mv = smax(mv, mc);
+            }
         }
     }
     block_fold_dt<R, NT>(rate, mv, flags, acc);

@@ -160,14 +160,17 @@ def test_fp32_advance(cuda, oracle_lib):
 
 @pytest.mark.parametrize("method,nx,ny,nsteps,arith", [(1, 64, 48, 10, EXACT), (1, 64, 48, 1, EXACT),
                                                       (1, 70, 45, 3, EXACT), (0, 53, 61, 1, EXACT),
-                                                      (1, 96, 130, 2, FAST)])
+                                                      (1, 96, 130, 2, FAST), (1, 40, 65, 1, EXACT),
+                                                      (1, 40, 66, 2, FAST), (1, 64, 2053, 1, EXACT)])
 def test_host_buffer_run(cuda, oracle_lib, hxlib, method, nx, ny, nsteps, arith):
     """hx_level_run_host_f64 (host buffers in, host buffers out: the upload in
     row bands with the CFL reduction and, for the hydrostatic solver, the first
     step's flux differences running under it; the last step in row bands
     downloaded as they finish) equals the device-resident run: bit for bit in
     the exact form, to 1e-13 in the fast form (multiply-add contraction may
-    differ between the split and the fused kernels); partial bands included."""
+    differ between the split and the fused kernels); partial bands included,
+    down to last bands of one and two rows (the head rows a band's flux
+    differences wait for)."""
     import ctypes
     case = workloads.fractal_dam_break(nx, ny, seed=4, amplitude=1.0, nodata_frac=0.2 if method else 0.0)
     h, hu, hv = case.h.copy(), case.hu.copy(), case.hv.copy()
@@ -330,3 +333,35 @@ def test_screened_cfl_fold_is_the_maximum(cuda, oracle_lib, n, kind):
     got_dt, got_v = acc.read()
     ref_dt, ref_v = _fold_reference(out.cpu().numpy(), case.z, g.dx, g.dy)
     assert got_dt == pytest.approx(ref_dt, rel=4e-16 * 8) and got_v == pytest.approx(ref_v, rel=4e-16 * 8)
+
+
+@pytest.mark.parametrize("n,kind", [(70, "varied"), (96, "uniform"), (2048, "varied")])
+def test_screened_dt_reduce_equals_the_fused_fold(cuda, oracle_lib, n, kind):
+    """The fast FP64 CFL reduction of a level (hx_level_run_f64 with no steps:
+    the bound of the state into the first work slot; 4 rows per thread) goes
+    through the same float screen as the fold fused into the advance.  Over the
+    state that advance wrote, both give the same bits: bound, speed and the
+    dry / NODATA flags, on an evolved state and on a uniform lake (all ties)."""
+    if kind == "varied":
+        case = workloads.fractal_dam_break(n, n + 3, seed=43, amplitude=1.0, nodata_frac=0.15)
+        g = case.geom
+        L = oracle_lib.Level(g.nx, g.ny, g.dx, g.dy, g.bc_lo, g.bc_hi)
+        h, hu, hv, *_ = oracle_lib.run(L, 1, case.h, case.hu, case.hv, case.z, case.n, 3, case.cfl)
+        h[7, 3:11] = 0.0  # dry cells
+    else:
+        case = workloads.fractal_dam_break(n, n, seed=44, amplitude=1.0, nodata_frac=0.0)
+        h = np.full_like(case.h, 1.5)
+        case.z = np.zeros_like(case.z)
+        hu = np.zeros_like(h)
+        hv = np.zeros_like(h)
+    lev = to_level(case, h, hu, hv, cuda)
+    dt = 0.2 * lev.compute_dt()[0]
+    acc = DtAccum(cuda)
+    out = lev.advance(capi.HX_METHOD_HYDROSTATIC_ROE, dt, next_dt=acc, arith=FAST).cpu().numpy()
+    nxt = to_level(case, out[0], out[1], out[2], cuda)
+    assert nxt.run(capi.HX_METHOD_HYDROSTATIC_ROE, 0, case.cfl, arith=FAST) == 0
+    torch.cuda.synchronize()
+    got, ref = nxt.work[:20].cpu(), acc.buf[:20].cpu()
+    assert torch.equal(got, ref), (got.tolist(), ref.tolist())
+    flags = int(ref[16])
+    assert (flags & 2) == (2 if kind == "varied" else 0) and (kind == "varied" or flags == 0)
