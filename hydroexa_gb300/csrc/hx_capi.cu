@@ -412,7 +412,7 @@ template <class R> int accum_read(const hx_dt_accum* acc, R* dtmin, R* maxvel, c
 // uploaded level and the first step's per-band updates.  The last two run at
 // the highest priority, so that their few blocks are scheduled ahead of the
 // flux work queued on the caller's stream and the bands go down early.
-constexpr int kHostBands = 8;
+constexpr int kHostBands = 10;  // at most: a short first and last band, up to eight between
 constexpr int kHeadRows = 2;  // rows of the next band the flux differences of a band read (the MUSCL reach)
 struct HostCache {
     void* base = nullptr;
@@ -688,9 +688,21 @@ int hx_level_run_host_f64(int method, int nx, int ny, double dx, double dy, cons
     uo.p[0] = P[0]; uo.p[1] = P[1]; uo.p[2] = P[2];
     uo.js = nx; uo.lo0 = 0; uo.lo1 = 0;
     const Plane<double> np{P[4], (long long)nx, 0, 0}, zp{P[3], (long long)nx, 0, 0};
-    const int band = ((ny + kHostBands - 1) / kHostBands + TY - 1) / TY * TY;
-    const int nbands = (ny + band - 1) / band;
-    auto rows = [&](int b, int& j0, int& j1) { j0 = b * band; j1 = (j0 + band < ny ? j0 + band : ny) - 1; };
+    // Row bands: a short first band (the only upload the flux work waits for in full) and a short last band
+    // (the only download not hidden under flux work), each ~1/32 of the rows, and up to eight between them;
+    // band b is rows starts[b] .. starts[b + 1] - 1.
+    int starts[kHostBands + 1];
+    int nbands = 0;
+    {
+        const int edge = ((ny + 31) / 32 + TY - 1) / TY * TY;
+        const int mid = ny - 2 * edge;
+        const int m = mid > 0 ? ((mid + 7) / 8 + TY - 1) / TY * TY : TY;  // a multiple of TY, >= TY
+        starts[nbands++] = 0;
+        for (int s = edge; s < ny - edge; s += m) starts[nbands++] = s;
+        if (ny - edge > starts[nbands - 1]) starts[nbands++] = ny - edge;
+        starts[nbands] = ny;
+    }
+    auto rows = [&](int b, int& j0, int& j1) { j0 = starts[b]; j1 = starts[b + 1] - 1; };
     auto flux_band = [&](int b) -> int {  // flux differences of band b (rows to the head of b+1 have landed)
         int j0, j1;
         rows(b, j0, j1);

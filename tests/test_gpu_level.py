@@ -169,8 +169,8 @@ def test_host_buffer_run(cuda, oracle_lib, hxlib, method, nx, ny, nsteps, arith)
     downloaded as they finish) equals the device-resident run: bit for bit in
     the exact form, to 1e-13 in the fast form (multiply-add contraction may
     differ between the split and the fused kernels); partial bands included,
-    down to last bands of one and two rows (the head rows a band's flux
-    differences wait for)."""
+    down to bands of one and two rows (the head rows a band's flux
+    differences wait for), with short first and last bands."""
     import ctypes
     case = workloads.fractal_dam_break(nx, ny, seed=4, amplitude=1.0, nodata_frac=0.2 if method else 0.0)
     h, hu, hv = case.h.copy(), case.hu.copy(), case.hv.copy()
