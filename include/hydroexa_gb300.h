@@ -374,7 +374,10 @@ int hx_level_run_f32(int method, hx_level_f32* L, float* h_alt, float* hu_alt, f
  * memory: copies h, hu, hv, z, n (host, pitch nx) to the device, runs nsteps,
  * copies the state back.  Device buffers are allocated by the call and cached
  * per thread for the next call of the same size (hx_host_cache_release frees
- * them).  Returns the status bits (>= 0) or a negative error.
+ * them).  The copies overlap the computation in row bands, and they can only
+ * when the host buffers are page-locked (cudaHostAlloc or cudaHostRegister).
+ * The call returns once the state is back in h, hu, hv: the status bits
+ * (>= 0) or a negative error.
  */
 int hx_level_run_host_f64(int method, int nx, int ny, double dx, double dy, const int32_t bc_lo[2],
                           const int32_t bc_hi[2], double* h, double* hu, double* hv, const double* z,
