@@ -673,6 +673,12 @@ int hx_level_run_host_f64(int method, int nx, int ny, double dx, double dy, cons
     if (!g_host.ensure_streams()) return fail(HX_ERR_CUDA, "copy streams could not be created");
     cudaStream_t* cs = g_host.cs;
     cudaEvent_t* ev = g_host.ev;
+    // an error after work was queued returns once the queued copies have finished with the caller's buffers
+    auto drain = [&](int r) -> int {
+        for (int k = 0; k < 4; ++k) cudaStreamSynchronize(cs[k]);
+        cudaStreamSynchronize(st);
+        return r;
+    };
     double* d = (double*)g_host.base;
     double* P[14];
     for (int k = 0; k < 14; ++k) P[k] = d + k * N;
@@ -753,8 +759,8 @@ int hx_level_run_host_f64(int method, int nx, int ny, double dx, double dy, cons
             rc = level_dt<double>(&L, reinterpret_cast<hx_dt_accum*>(&slot[0]), dstream, arith, j0, j1);
     }
     if (e == cudaSuccess && split) e = cudaEventRecord(ev_dt, dts);
-    if (e != cudaSuccess) return fail(HX_ERR_CUDA, "upload: %s", cudaGetErrorString(e));
-    if (rc) return rc;
+    if (e != cudaSuccess) return drain(fail(HX_ERR_CUDA, "upload: %s", cudaGetErrorString(e)));
+    if (rc) return drain(rc);
     const double* A[3] = {P[0], P[1], P[2]};
     double* B[3] = {P[5], P[6], P[7]};
     hx_level_f64 cur = L;
@@ -808,8 +814,8 @@ int hx_level_run_host_f64(int method, int nx, int ny, double dx, double dy, cons
         // the later steps read every band's update
         if (rc == HX_OK && e == cudaSuccess) e = cudaEventRecord(ev_upd, upd);
         if (rc == HX_OK && e == cudaSuccess) e = cudaStreamWaitEvent(st, ev_upd, 0);
-        if (e != cudaSuccess) return fail(HX_ERR_CUDA, "split step: %s", cudaGetErrorString(e));
-        if (rc) return rc;
+        if (e != cudaSuccess) return drain(fail(HX_ERR_CUDA, "split step: %s", cudaGetErrorString(e)));
+        if (rc) return drain(rc);
         res[0] = o[0]; res[1] = o[1]; res[2] = o[2];
         s0 = 1;
     }
@@ -827,10 +833,10 @@ int hx_level_run_host_f64(int method, int nx, int ny, double dx, double dy, cons
             int j0 = 0, j1 = ny - 1;
             if (last) rows(b, j0, j1);
             rc = level_advance<double>(method, &cur, step_ctl(s, b), o[0], o[1], o[2], arith, st, j0, j1);
-            if (rc) return rc;
+            if (rc) return drain(rc);
             if (!last) continue;
             e = download(b, o, st);
-            if (e != cudaSuccess) return fail(HX_ERR_CUDA, "download: %s", cudaGetErrorString(e));
+            if (e != cudaSuccess) return drain(fail(HX_ERR_CUDA, "download: %s", cudaGetErrorString(e)));
         }
     }
     if (nsteps == 0) {
@@ -846,7 +852,7 @@ int hx_level_run_host_f64(int method, int nx, int ny, double dx, double dy, cons
     if (e == cudaSuccess) e = cudaMemcpyAsync(&sv, status, 4, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(&tv, tdev, 8, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) return fail(HX_ERR_CUDA, "download: %s", cudaGetErrorString(e));
+    if (e != cudaSuccess) return drain(fail(HX_ERR_CUDA, "download: %s", cudaGetErrorString(e)));
     if (time_out) *time_out = tv;
     return (int)sv;
 }
