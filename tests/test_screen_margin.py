@@ -107,3 +107,52 @@ def test_the_true_maximum_is_always_a_candidate():
             kr, km = r32.max() * np.float32(1 - MARGIN), m32.max() * np.float32(1 - MARGIN)
             assert r32[np.argmax(r64)] >= kr
             assert m32[np.argmax(m64)] >= km
+
+
+SQRT_G = 3.1320919526731650  # sqrt(9.81) correctly rounded, the FP64 constant of the Roe flux
+
+
+def sonic_rules(ui, si, uj, sj):
+    """The float rules of the hydrostatic Roe flux (roe_hydrostatic_fast in
+    hydroexa_gb300/csrc/hx_device.cuh): rule0 (rule2) true means the entropy
+    fix of the slow (fast) wave is ruled out without FP64 work."""
+    ui32, uj32 = f32_lead(ui), f32_lead(uj)
+    ci32 = np.float32(3.13209195) * f32_lead(si)
+    cj32 = np.float32(3.13209195) * f32_lead(sj)
+    mi = np.float32(2.0 ** -16) * (np.abs(ui32) + ci32)
+    mj = np.float32(2.0 ** -16) * (np.abs(uj32) + cj32)
+    rule0 = (ui32 - ci32 >= mi) | (uj32 - cj32 <= -mj)
+    rule2 = (ui32 + ci32 >= mi) | (uj32 + cj32 <= -mj)
+    return rule0, rule2
+
+
+def test_sonic_screen_rules_out_only_impossible_fixes():
+    """Each entropy fix needs e_i < 0 < e_j (e = u -+ sqrt(g) s, s = sqrt(h)).
+    Where a float rule rules a fix out, the exact signs agree: e_i >= 0 or
+    e_j <= 0.  Wet sides (h >= 1e-6, so |u| + c >= 3e-3) and dry sides
+    (h = u = 0), velocities at, near (to 2^-50) and away from the sonic point;
+    the rules decide most subsonic faces."""
+    rng = np.random.default_rng(5)
+    n = 400_000
+    wet_i, wet_j = rng.random(n) > 0.05, rng.random(n) > 0.05
+    si = np.where(wet_i, np.sqrt(10.0 ** rng.uniform(-6, 4, n)), 0.0)
+    sj = np.where(wet_j, np.sqrt(10.0 ** rng.uniform(-6, 4, n)), 0.0)
+
+    def speeds(s, wet):
+        c = SQRT_G * s
+        kind = rng.integers(0, 4, n)
+        near = c * (1 + rng.choice([-1.0, 1.0], n) * 2.0 ** rng.uniform(-50, -8, n))
+        u = np.select([kind == 0, kind == 1, kind == 2], [c, near, rng.uniform(-5, 5, n) * c],
+                      rng.uniform(-1e-3, 1e-3, n))
+        u = u * rng.choice([-1.0, 1.0], n)
+        return np.where(wet, u, 0.0)
+
+    ui, uj = speeds(si, wet_i), speeds(sj, wet_j)
+    rule0, rule2 = sonic_rules(ui, si, uj, sj)
+    L = np.longdouble
+    ci, cj = L(SQRT_G) * si.astype(L), L(SQRT_G) * sj.astype(L)
+    for rule, ei, ej in ((rule0, ui.astype(L) - ci, uj.astype(L) - cj), (rule2, ui.astype(L) + ci, uj.astype(L) + cj)):
+        possible = (ei < 0) & (ej > 0)
+        assert not (rule & possible).any()
+    subsonic = wet_i & wet_j & (np.abs(ui) < 0.9 * SQRT_G * si) & (np.abs(uj) < 0.9 * SQRT_G * sj)
+    assert (rule0 & rule2)[subsonic].mean() > 0.99
