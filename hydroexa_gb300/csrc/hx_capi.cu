@@ -447,6 +447,23 @@ struct HostCache {
 };
 thread_local HostCache g_host;
 
+// Row bands of the host-buffer run over ny rows: a short first band (the only
+// upload the flux work waits for in full) and a short last band (the only
+// download not hidden under flux work), each ~1/32 of the rows, and up to
+// eight between them.  Band b is rows starts[b] .. starts[b + 1] - 1; starts
+// has room for kHostBands + 1 entries.  Returns the number of bands.
+int host_bands(int ny, int* starts) {
+    const int edge = ((ny + 31) / 32 + TY - 1) / TY * TY;
+    const int mid = ny - 2 * edge;
+    const int m = mid > 0 ? ((mid + 7) / 8 + TY - 1) / TY * TY : TY;  // a multiple of TY, >= TY
+    int nb = 0;
+    starts[nb++] = 0;
+    for (int s = edge; s < ny - edge; s += m) starts[nb++] = s;
+    if (ny - edge > starts[nb - 1]) starts[nb++] = ny - edge;
+    starts[nb] = ny;
+    return nb;
+}
+
 }  // namespace
 
 namespace hx {
@@ -694,20 +711,8 @@ int hx_level_run_host_f64(int method, int nx, int ny, double dx, double dy, cons
     uo.p[0] = P[0]; uo.p[1] = P[1]; uo.p[2] = P[2];
     uo.js = nx; uo.lo0 = 0; uo.lo1 = 0;
     const Plane<double> np{P[4], (long long)nx, 0, 0}, zp{P[3], (long long)nx, 0, 0};
-    // Row bands: a short first band (the only upload the flux work waits for in full) and a short last band
-    // (the only download not hidden under flux work), each ~1/32 of the rows, and up to eight between them;
-    // band b is rows starts[b] .. starts[b + 1] - 1.
     int starts[kHostBands + 1];
-    int nbands = 0;
-    {
-        const int edge = ((ny + 31) / 32 + TY - 1) / TY * TY;
-        const int mid = ny - 2 * edge;
-        const int m = mid > 0 ? ((mid + 7) / 8 + TY - 1) / TY * TY : TY;  // a multiple of TY, >= TY
-        starts[nbands++] = 0;
-        for (int s = edge; s < ny - edge; s += m) starts[nbands++] = s;
-        if (ny - edge > starts[nbands - 1]) starts[nbands++] = ny - edge;
-        starts[nbands] = ny;
-    }
+    const int nbands = host_bands(ny, starts);
     auto rows = [&](int b, int& j0, int& j1) { j0 = starts[b]; j1 = starts[b + 1] - 1; };
     auto flux_band = [&](int b) -> int {  // flux differences of band b (rows to the head of b+1 have landed)
         int j0, j1;
@@ -858,6 +863,12 @@ int hx_level_run_host_f64(int method, int nx, int ny, double dx, double dy, cons
 }
 
 void hx_host_cache_release(void) { g_host.release(); }
+
+int hx_debug_host_bands(int ny, int* starts, int max_bands) {
+    if (ny < 2) return fail(HX_ERR_ARG, "ny must be >= 2");
+    if (!starts || max_bands < kHostBands) return fail(HX_ERR_ARG, "starts needs room for %d bands", kHostBands);
+    return host_bands(ny, starts);
+}
 
 int hx_level_tangent_f64(const hx_level_f64* L, double dt, double ddt, double* oh, double* ohu, double* ohv,
                          hx_stream_t s) {

@@ -102,3 +102,23 @@ def test_plotfile_arguments_checked_on_the_host(hxlib, tmp_path):
     rc = L.hx_write_plotfile_f64(str(tmp_path / "plt").encode(), 3, 0.0, 1, ctypes.byref(lev), lo, hi, None)
     assert rc == hxlib.HX_ERR_ARG
     assert not (tmp_path / "plt00003").exists()
+
+
+def test_host_run_row_bands(hxlib):
+    """The row bands of hx_level_run_host_f64 cover every row once, in at most
+    ten bands, with short first and last bands (~1/32 of the rows each) on
+    tall levels; every ny from 2 to 20000 and the bench's 8192."""
+    L = hxlib.lib()
+    st = (ctypes.c_int * 11)()
+    assert L.hx_debug_host_bands(100, st, 9) == hxlib.HX_ERR_ARG
+    assert L.hx_debug_host_bands(1, st, 10) == hxlib.HX_ERR_ARG
+    for ny in list(range(2, 20001)) + [8192]:
+        n = L.hx_debug_host_bands(ny, st, 10)
+        assert 1 <= n <= 10, (ny, n)
+        s = list(st[:n + 1])
+        assert s[0] == 0 and s[-1] == ny and all(a < b for a, b in zip(s, s[1:])), (ny, s)
+        if ny >= 1024:
+            edge = -(-ny // 32)
+            assert s[1] <= edge + 7 and ny - s[-2] <= edge + 7, (ny, s)
+    n = L.hx_debug_host_bands(8192, st, 10)
+    assert list(st[:n + 1]) == [0, 256, 1216, 2176, 3136, 4096, 5056, 6016, 6976, 7936, 8192]
