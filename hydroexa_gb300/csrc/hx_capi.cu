@@ -414,7 +414,10 @@ template <class R> int accum_read(const hx_dt_accum* acc, R* dtmin, R* maxvel, c
 // flux work queued on the caller's stream and the bands go down early.
 constexpr int kHostBands = 10;  // at most: a short first and last band, up to eight between
 constexpr int kHeadRows = 2;  // rows of the next band the flux differences of a band read (the MUSCL reach)
+// One cache per device and thread: the buffers, streams and events are created
+// with their device current and used only while it is current.
 struct HostCache {
+    int device = -1;  // ordinal the resources belong to
     void* base = nullptr;
     size_t bytes = 0;
     cudaStream_t cs[4] = {nullptr, nullptr, nullptr, nullptr};  // uploads, downloads, CFL reduction, updates
@@ -433,7 +436,14 @@ struct HostCache {
         streams_ok = true;
         return true;
     }
+    // Frees with the owning device current, then restores the caller's device.
+    // At thread or process exit the CUDA runtime may already be shut down;
+    // the calls then fail harmlessly and the driver reclaims the memory.
     void release() {
+        if (!base && !streams_ok) return;
+        int prev = -1;
+        const bool switched = device >= 0 && cudaGetDevice(&prev) == cudaSuccess && prev != device &&
+                              cudaSetDevice(device) == cudaSuccess;
         if (base) cudaFree(base);
         base = nullptr;
         bytes = 0;
@@ -442,16 +452,28 @@ struct HostCache {
             for (auto& c : cs) cudaStreamDestroy(c);
         }
         streams_ok = false;
+        if (switched) cudaSetDevice(prev);
     }
     ~HostCache() { release(); }
 };
-thread_local HostCache g_host;
+constexpr int kMaxHostDevices = 64;
+thread_local HostCache g_host[kMaxHostDevices];
+
+// The calling thread's cache for the current device (null: no usable device).
+HostCache* host_cache() {
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxHostDevices) return nullptr;
+    g_host[dev].device = dev;
+    return &g_host[dev];
+}
 
 // Row bands of the host-buffer run over ny rows: a short first band (the only
 // upload the flux work waits for in full) and a short last band (the only
 // download not hidden under flux work), each ~1/32 of the rows, and up to
 // eight between them.  Band b is rows starts[b] .. starts[b + 1] - 1; starts
-// has room for kHostBands + 1 entries.  Returns the number of bands.
+// has room for kHostBands + 1 entries.  Returns the number of bands.  Every
+// band but the last holds at least kHeadRows rows: a remainder shorter than
+// that before the last band joins the band ahead of it.
 int host_bands(int ny, int* starts) {
     const int edge = ((ny + 31) / 32 + TY - 1) / TY * TY;
     const int mid = ny - 2 * edge;
@@ -459,9 +481,19 @@ int host_bands(int ny, int* starts) {
     int nb = 0;
     starts[nb++] = 0;
     for (int s = edge; s < ny - edge; s += m) starts[nb++] = s;
-    if (ny - edge > starts[nb - 1]) starts[nb++] = ny - edge;
+    if (ny - edge > starts[nb - 1]) {
+        if (ny - edge - starts[nb - 1] >= kHeadRows) starts[nb++] = ny - edge;
+        else if (nb > 1) starts[nb - 1] = ny - edge;  // (a first band that short: no split at all)
+    }
     starts[nb] = ny;
     return nb;
+}
+
+// The band holding row r (rows 0 .. ny - 1).
+int band_of(int r, int nb, const int* starts) {
+    int b = 0;
+    while (b + 1 < nb && starts[b + 1] <= r) ++b;
+    return b;
 }
 
 }  // namespace
@@ -679,24 +711,26 @@ int hx_level_run_host_f64(int method, int nx, int ny, double dx, double dy, cons
     const bool split = method == HX_METHOD_HYDROSTATIC_ROE && nsteps >= 1;
     const size_t N = (size_t)nx * ny, pb = N * sizeof(double);
     const size_t need = (split ? 14 : 8) * pb + 512;
-    if (g_host.bytes < need) {
-        if (g_host.base) cudaFree(g_host.base);
-        g_host.base = nullptr;
-        g_host.bytes = 0;
-        cudaError_t e = cudaMalloc(&g_host.base, need);
+    HostCache* hc = host_cache();
+    if (!hc) return fail(HX_ERR_CUDA, "hx_level_run_host_f64: no current CUDA device");
+    if (hc->bytes < need) {
+        if (hc->base) cudaFree(hc->base);
+        hc->base = nullptr;
+        hc->bytes = 0;
+        cudaError_t e = cudaMalloc(&hc->base, need);
         if (e != cudaSuccess) return fail(HX_ERR_CUDA, "device buffers: %s", cudaGetErrorString(e));
-        g_host.bytes = need;
+        hc->bytes = need;
     }
-    if (!g_host.ensure_streams()) return fail(HX_ERR_CUDA, "copy streams could not be created");
-    cudaStream_t* cs = g_host.cs;
-    cudaEvent_t* ev = g_host.ev;
+    if (!hc->ensure_streams()) return fail(HX_ERR_CUDA, "copy streams could not be created");
+    cudaStream_t* cs = hc->cs;
+    cudaEvent_t* ev = hc->ev;
     // an error after work was queued returns once the queued copies have finished with the caller's buffers
     auto drain = [&](int r) -> int {
         for (int k = 0; k < 4; ++k) cudaStreamSynchronize(cs[k]);
         cudaStreamSynchronize(st);
         return r;
     };
-    double* d = (double*)g_host.base;
+    double* d = (double*)hc->base;
     double* P[14];
     for (int k = 0; k < 14; ++k) P[k] = d + k * N;
     char* tail = (char*)(d + (split ? 14 : 8) * N);
@@ -798,8 +832,14 @@ int hx_level_run_host_f64(int method, int nx, int ny, double dx, double dy, cons
         ow.p[0] = o[0]; ow.p[1] = o[1]; ow.p[2] = o[2];
         ow.js = nx; ow.lo0 = 0; ow.lo1 = 0;
         for (int b = 0; b < nbands && rc == HX_OK && e == cudaSuccess; ++b) {
-            // rows b-1 .. b and the head of b+1 have landed
-            e = cudaStreamWaitEvent(st, b + 1 < nbands ? ev_head[b + 1] : ev_up[b], 0);
+            // the flux differences of band b read rows up to kHeadRows past its last row: wait for the upload
+            // event that covers the last of them (the head of the band holding it, or that whole band; rows
+            // go up in order on one stream, so every earlier row has landed too)
+            int j0, j1;
+            rows(b, j0, j1);
+            const int r = j1 + kHeadRows < ny ? j1 + kHeadRows : ny - 1;
+            const int c = band_of(r, nbands, starts);
+            e = cudaStreamWaitEvent(st, (c > b && r < starts[c] + kHeadRows) ? ev_head[c] : ev_up[c], 0);
             if (e == cudaSuccess) rc = flux_band(b);
             if (rc == HX_OK && e == cudaSuccess) e = cudaEventRecord(ev_flux[b], st);
         }
@@ -862,7 +902,9 @@ int hx_level_run_host_f64(int method, int nx, int ny, double dx, double dy, cons
     return (int)sv;
 }
 
-void hx_host_cache_release(void) { g_host.release(); }
+void hx_host_cache_release(void) {
+    for (auto& c : g_host) c.release();
+}
 
 int hx_debug_host_bands(int ny, int* starts, int max_bands) {
     if (ny < 2) return fail(HX_ERR_ARG, "ny must be >= 2");

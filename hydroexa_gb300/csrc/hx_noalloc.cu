@@ -100,7 +100,9 @@ extern "C" int hx_level_run_static_f64(int method, hx_level_f64* L, int nsteps, 
         U.p[0] = L->h; U.p[1] = L->hu; U.p[2] = L->hv;
         U.js = L->pitch; U.lo0 = 0; U.lo1 = 0;
         Plane<double> Z{L->z, L->pitch, 0, 0};
-        e = launch_dt_reduce<double, false>(U, Z, vb, L->dx, L->dy, &slot[0], st);
+        // the same arithmetic form as the steps, as hx_level_run_f64 does
+        e = arith == HX_ARITH_EXACT ? launch_dt_reduce<double, false>(U, Z, vb, L->dx, L->dy, &slot[0], st)
+                                    : launch_dt_reduce<double, true>(U, Z, vb, L->dx, L->dy, &slot[0], st);
         if (e != cudaSuccess) return set_error(HX_ERR_LAUNCH, cudaGetErrorString(e));
         note_launches(1);
     }
@@ -150,10 +152,13 @@ extern "C" int hx_level_run_static_f64(int method, hx_level_f64* L, int nsteps, 
         if (e != cudaSuccess) return set_error(HX_ERR_LAUNCH, cudaGetErrorString(e));
         note_launches(1);
     }
-    // An odd number of steps leaves the result in the scratch: copy it back.
+    // An odd number of steps leaves the result in the scratch: copy its valid
+    // cells back (nx of every pitch-long row; the caller's row padding is left
+    // as it was).
     if (nsteps % 2) {
+        const size_t row = (size_t)L->nx * sizeof(double), pitch = (size_t)L->pitch * sizeof(double);
         for (int k = 0; k < 3 && e == cudaSuccess; ++k)
-            e = cudaMemcpyAsync(A[k], B[k], (size_t)cells * sizeof(double), cudaMemcpyDeviceToDevice, st);
+            e = cudaMemcpy2DAsync(A[k], pitch, B[k], pitch, row, (size_t)L->ny, cudaMemcpyDeviceToDevice, st);
         if (e != cudaSuccess) return set_error(HX_ERR_CUDA, cudaGetErrorString(e));
     }
     return HX_OK;

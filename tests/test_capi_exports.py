@@ -107,7 +107,9 @@ def test_plotfile_arguments_checked_on_the_host(hxlib, tmp_path):
 def test_host_run_row_bands(hxlib):
     """The row bands of hx_level_run_host_f64 cover every row once, in at most
     ten bands, with short first and last bands (~1/32 of the rows each) on
-    tall levels; every ny from 2 to 20000 and the bench's 8192."""
+    tall levels; every band but the last holds at least the two rows its
+    predecessor's flux differences read past their own (so a band's flux work
+    waits for the rows it reads); every ny from 2 to 20000 and the bench's 8192."""
     L = hxlib.lib()
     st = (ctypes.c_int * 11)()
     assert L.hx_debug_host_bands(100, st, 9) == hxlib.HX_ERR_ARG
@@ -117,6 +119,7 @@ def test_host_run_row_bands(hxlib):
         assert 1 <= n <= 10, (ny, n)
         s = list(st[:n + 1])
         assert s[0] == 0 and s[-1] == ny and all(a < b for a, b in zip(s, s[1:])), (ny, s)
+        assert all(b - a >= 2 for a, b in zip(s[:-2], s[1:-1])), (ny, s)
         if ny >= 1024:
             edge = -(-ny // 32)
             assert s[1] <= edge + 7 and ny - s[-2] <= edge + 7, (ny, s)
