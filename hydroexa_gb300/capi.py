@@ -20,13 +20,15 @@ HX_ERR_LAUNCH = -2
 HX_ERR_CUDA = -3
 HX_STATUS_DT_COLLAPSE = 1
 HX_STATUS_NAN = 2
-HX_STATUS_BOUNDS = 4
-HX_STATUS_TIMEOUT = 8
 HX_ARITH_EXACT = 0
 HX_ARITH_FAST = 1
 HX_ADJ_FACE_RECORDS = 0x100
 HX_METHOD_ROE = 0
 HX_METHOD_HYDROSTATIC_ROE = 1
+# boundary codes of the level calls: 0 the reference's wall, 1 open, 2 a closed wall (see the C header)
+HX_BC_REFLECTIVE = 0
+HX_BC_TRANSMISSIVE = 1
+HX_BC_CLOSED_WALL = 2
 
 
 class HxError(RuntimeError):

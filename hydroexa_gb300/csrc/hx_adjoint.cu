@@ -652,14 +652,16 @@ __global__ void __launch_bounds__(ANT) k_adj_faces(AdjArgs A) {
                     double geta = 0;
                     if (pos_i(hp)) { geta = ghp; gzt -= ghp; }
                     const int edge = lo ? 0 : nx - 1;
-                    const int src = code == 0 ? (lo ? -1 - gi : 2 * nx - 1 - gi) : edge;
-                    const double sx = code == 0 ? -1.0 : 1.0;
+                    const bool wall = bc_is_wall(code);
+                    const int src = wall ? (lo ? -1 - gi : 2 * nx - 1 - gi) : edge;
+                    bool neg_u, neg_v;  // the forward's sign flips of this ghost's momenta (ghost_source)
+                    ghost_momentum_signs(wall, code, false, -1, neg_u, neg_v);
                     const int sc = src - x0, ec = edge - x0;
                     if (sc >= 0 && sc < ATX) {
                         S.fold[0][row][sc] += geta;
                         S.fold[3][row][sc] += geta;
-                        S.fold[1][row][sc] += sx * ghu;
-                        S.fold[2][row][sc] += ghv;
+                        S.fold[1][row][sc] += neg_u ? -ghu : ghu;
+                        S.fold[2][row][sc] += neg_v ? -ghv : ghv;
                     }
                     if (ec >= 0 && ec < ATX) S.fold[3][row][ec] += gzt;
                     (void)gj;
@@ -770,14 +772,16 @@ __global__ void __launch_bounds__(ANT) k_adj_faces(AdjArgs A) {
                     double geta = 0;
                     if (pos_i(hp)) { geta = ghp; gzt -= ghp; }
                     const int edge = lo ? 0 : ny - 1;
-                    const int src = code == 0 ? (lo ? -1 - gj : 2 * ny - 1 - gj) : edge;
-                    const double sy = code == 0 ? -1.0 : 1.0;
+                    const bool wall = bc_is_wall(code);
+                    const int src = wall ? (lo ? -1 - gj : 2 * ny - 1 - gj) : edge;
+                    bool neg_u, neg_v;
+                    ghost_momentum_signs(false, -1, wall, code, neg_u, neg_v);
                     const int sr = src - y0, er = edge - y0;
                     if (sr >= 0 && sr < ATY) {
                         S.fold[0][sr][col] += geta;
                         S.fold[3][sr][col] += geta;
-                        S.fold[1][sr][col] += ghu;
-                        S.fold[2][sr][col] += sy * ghv;
+                        S.fold[1][sr][col] += neg_u ? -ghu : ghu;
+                        S.fold[2][sr][col] += neg_v ? -ghv : ghv;
                     }
                     if (er >= 0 && er < ATY) S.fold[3][er][col] += gzt;
                 }

@@ -207,10 +207,51 @@ template <class R> struct RebuildOut {
 // Sources of the grown tile.
 // ---------------------------------------------------------------------------
 
+// Physical-boundary codes of one side of the level (inputs file
+// HydroEXA.lo_bc / hi_bc, include/boundaries/BCFill.H:35-138): 0 and 2 are
+// walls (depth, eta mirrored; terrain always copied from the edge), anything
+// else is open (every field copied from the edge cell).  The two walls differ
+// in the BC records the momentum ghosts take:
+//  - 0, the reference's wall: its per-step FillPatch fills hu, hv (components
+//    1, 2) with BC-record offset 0 (include/utils/FillPatchUtils.H:128-129,
+//    BCFill.H:244-264), so hu takes the scalar record (mirrored, never
+//    negated) and hv the x-momentum record (negated across x walls only);
+//  - 2, a closed wall (no counterpart in the reference's inputs): hu takes the
+//    x-momentum record, hv the y-momentum record, each negated across the
+//    walls normal to it.
+// A cell outside in both directions takes the y rule applied to the x ghost,
+// so its signs multiply (no stencil here reads such a corner cell).
+constexpr int kBcWall = 0;
+constexpr int kBcClosedWall = 2;
+__host__ __device__ __forceinline__ bool bc_is_wall(int code) { return code == kBcWall || code == kBcClosedWall; }
+// Sign flips of the momentum ghost read through an x mirror (xm, at a side of
+// code cx) and/or a y mirror (ym, code cy).
+__host__ __device__ __forceinline__ void ghost_momentum_signs(bool xm, int cx, bool ym, int cy, bool& neg_u,
+                                                              bool& neg_v) {
+    neg_u = xm && cx == kBcClosedWall;
+    neg_v = (xm && cx == kBcWall) != (ym && cy == kBcClosedWall);
+}
+// The cell a ghost (i, j) reads its state from (mi, mj) and its terrain from
+// (ei, ej), with the momentum sign flips.
+__host__ __device__ __forceinline__ void ghost_source(int i, int j, int nx, int ny, int bc_xlo, int bc_xhi,
+                                                      int bc_ylo, int bc_yhi, int& mi, int& mj, int& ei, int& ej,
+                                                      bool& neg_u, bool& neg_v) {
+    mi = i; mj = j;
+    bool xm = false, ym = false;
+    int cx = -1, cy = -1;
+    if (i < 0) { cx = bc_xlo; if (bc_is_wall(cx)) { mi = -1 - i; xm = true; } else mi = 0; }
+    else if (i >= nx) { cx = bc_xhi; if (bc_is_wall(cx)) { mi = 2 * nx - 1 - i; xm = true; } else mi = nx - 1; }
+    if (j < 0) { cy = bc_ylo; if (bc_is_wall(cy)) { mj = -1 - j; ym = true; } else mj = 0; }
+    else if (j >= ny) { cy = bc_yhi; if (bc_is_wall(cy)) { mj = 2 * ny - 1 - j; ym = true; } else mj = ny - 1; }
+    ei = i < 0 ? 0 : (i >= nx ? nx - 1 : i);
+    ej = j < 0 ? 0 : (j >= ny ? ny - 1 : j);
+    ghost_momentum_signs(xm, cx, ym, cy, neg_u, neg_v);
+}
+
 // A whole level as one box with no stored ghosts: the physical-boundary ghost
-// values of include/boundaries/BCFill.H:35-86 are generated here.  Wall (code
-// 0): eta and tangential momentum mirrored, normal momentum mirrored and
-// negated.  Open: the edge cell copied.  Terrain always copies the edge.
+// values of include/boundaries/BCFill.H:35-86 are generated here, by the
+// rules of ghost_source (walls mirror, open sides copy the edge; momentum
+// signs by the wall's BC records; terrain always copies the edge).
 template <class R> struct LevelSrc {
     const R* h; const R* hu; const R* hv; const R* z; const R* n;
     long long pitch;
@@ -223,22 +264,17 @@ template <class R> struct LevelSrc {
     }
     // (eta, z, hu, hv, n) of any cell in the grown region.
     __device__ __forceinline__ void fetch(int i, int j, R& eta, R& zz, R& qx, R& qy, R& nn) const {
-        int mi = i, mj = j;
-        bool nx_neg = false, ny_neg = false;
-        if (i < 0) { if (bc_xlo == 0) { mi = -1 - i; nx_neg = true; } else mi = 0; }
-        else if (i >= nx) { if (bc_xhi == 0) { mi = 2 * nx - 1 - i; nx_neg = true; } else mi = nx - 1; }
-        if (j < 0) { if (bc_ylo == 0) { mj = -1 - j; ny_neg = true; } else mj = 0; }
-        else if (j >= ny) { if (bc_yhi == 0) { mj = 2 * ny - 1 - j; ny_neg = true; } else mj = ny - 1; }
-        const int ei = i < 0 ? 0 : (i >= nx ? nx - 1 : i);
-        const int ej = j < 0 ? 0 : (j >= ny ? ny - 1 : j);
+        int mi, mj, ei, ej;
+        bool neg_u, neg_v;
+        ghost_source(i, j, nx, ny, bc_xlo, bc_xhi, bc_ylo, bc_yhi, mi, mj, ei, ej, neg_u, neg_v);
         const long long pm = (long long)mi + (long long)mj * pitch;
         const long long pe = (long long)ei + (long long)ej * pitch;
         eta = ld_ro(h + pm) + ld_ro(z + pm);
         zz = ld_ro(z + pe);
         nn = ld_ro(n + pe);
         const R a = ld_ro(hu + pm), b = ld_ro(hv + pm);
-        qx = nx_neg ? -a : a;
-        qy = ny_neg ? -b : b;
+        qx = neg_u ? -a : a;
+        qy = neg_v ? -b : b;
     }
 };
 
@@ -272,14 +308,9 @@ struct BoxSetSrc {
     }
     __device__ __forceinline__ void fetch(int i, int j, double& eta, double& zz, double& qx, double& qy,
                                           double& nn) const {
-        int mi = i, mj = j;
-        bool nx_neg = false, ny_neg = false;
-        if (i < 0) { if (bc_xlo == 0) { mi = -1 - i; nx_neg = true; } else mi = 0; }
-        else if (i >= nx) { if (bc_xhi == 0) { mi = 2 * nx - 1 - i; nx_neg = true; } else mi = nx - 1; }
-        if (j < 0) { if (bc_ylo == 0) { mj = -1 - j; ny_neg = true; } else mj = 0; }
-        else if (j >= ny) { if (bc_yhi == 0) { mj = 2 * ny - 1 - j; ny_neg = true; } else mj = ny - 1; }
-        const int ei = i < 0 ? 0 : (i >= nx ? nx - 1 : i);
-        const int ej = j < 0 ? 0 : (j >= ny ? ny - 1 : j);
+        int mi, mj, ei, ej;
+        bool neg_u, neg_v;
+        ghost_source(i, j, nx, ny, bc_xlo, bc_xhi, bc_ylo, bc_yhi, mi, mj, ei, ej, neg_u, neg_v);
         const DevBox& bm = boxes[owner(mi, mj)];
         const DevBox& be = boxes[owner(ei, ej)];
         const long long pm = (long long)(mi - bm.lo0) + (long long)(mj - bm.lo1) * bm.pitch;
@@ -288,8 +319,8 @@ struct BoxSetSrc {
         zz = ld_ro(be.z + pe);
         nn = ld_ro(be.n + pe);
         const double a = ld_ro(bm.hu[phase] + pm), b = ld_ro(bm.hv[phase] + pm);
-        qx = nx_neg ? -a : a;
-        qy = ny_neg ? -b : b;
+        qx = neg_u ? -a : a;
+        qy = neg_v ? -b : b;
     }
 };
 

@@ -14,10 +14,18 @@
  *  - Every call is stream-ordered and asynchronous on the given stream and
  *    allocates nothing.  Calls on different streams are independent.
  *  - Return value: HX_OK, or a negative argument/launch error detected on the
- *    host (HX_ERR_ARG, HX_ERR_LAUNCH).  Numerical conditions found on the
- *    device (dt collapse, NaN) are OR-ed into a device status word, read with
- *    hx_status_read(); the adapter maps a nonzero status to amrex::Abort,
- *    as the reference does (src/solvers/HydrostaticRoe.cpp:77-80).
+ *    host (HX_ERR_ARG, HX_ERR_LAUNCH).  Every view is checked on the host
+ *    against the stencil the call reads (the valid box grown by the ghosts it
+ *    needs, the components, the row stride): a view that falls short returns
+ *    HX_ERR_ARG with the reason in hx_last_error(), before anything is
+ *    launched -- the role of AMREX_ASSERT_WITH_MESSAGE in
+ *    src/solvers/HydrostaticRoe.cpp:411-413.  Numerical conditions found on
+ *    the device (dt collapse, NaN) are OR-ed into a device status word, read
+ *    with hx_status_read(); the adapter maps a nonzero status to amrex::Abort,
+ *    as the reference does (src/solvers/HydrostaticRoe.cpp:77-80).  Where a
+ *    call takes the status word as optional and it is passed as NULL, those
+ *    conditions are not reported (a collapsed dt chain still stops the later
+ *    steps of a device time loop).
  *  - The dt reduction is a device accumulator (hx_dt_accum) so a whole time
  *    loop can run without a host round trip; hx_dt_accum_read() is the
  *    synchronising read that replaces ReduceOps::value().
@@ -51,14 +59,27 @@ enum {
 enum {
     HX_STATUS_DT_COLLAPSE = 1, /* min CFL bound < 1e-12 (HydrostaticRoe.cpp:77, Roe.cpp:88) */
     HX_STATUS_NAN = 2,         /* a NaN or Inf appeared in an updated state */
-    HX_STATUS_BOUNDS = 4,      /* a view did not cover the stencil the call needs */
-    HX_STATUS_TIMEOUT = 8,     /* a bounded device-side wait gave up */
 };
 
 enum { HX_ARITH_EXACT = 0, HX_ARITH_FAST = 1 };
 enum { HX_METHOD_ROE = 0, HX_METHOD_HYDROSTATIC_ROE = 1 };
-/* Inputs-file boundary codes (HydroEXA.lo_bc / hi_bc): 0 wall, else open. */
-enum { HX_BC_REFLECTIVE = 0, HX_BC_TRANSMISSIVE = 1 };
+/*
+ * Physical-boundary codes of the level calls, one per side (bc_lo[dir],
+ * bc_hi[dir]), as the inputs file gives them (HydroEXA.lo_bc / hi_bc,
+ * include/boundaries/BCFill.H:35-138): 0 a wall, anything else open (every
+ * field copied from the edge cell).  At a wall eta and depth are mirrored and
+ * the terrain copied from the edge, and the momenta follow the BC records the
+ * reference's time loop applies to them: its per-step FillPatch fills hu, hv
+ * with BC-record offset 0 (include/utils/FillPatchUtils.H:128-129,
+ * BCFill.H:244-264), so hu is mirrored without a sign change on every wall
+ * and hv is negated across x walls only -- mass and momentum cross such a
+ * wall once flow reaches it, as in the reference.
+ * HX_BC_CLOSED_WALL (no counterpart in the reference's inputs) is the wall
+ * with each momentum's own record: hu negated across x walls, hv across y
+ * walls, so nothing crosses it.  The box calls read the ghosts the caller
+ * filled and take no codes.
+ */
+enum { HX_BC_REFLECTIVE = 0, HX_BC_TRANSMISSIVE = 1, HX_BC_CLOSED_WALL = 2 };
 
 typedef struct hx_array4_f64 {
     double* p;
@@ -372,9 +393,10 @@ int hx_level_run_f32(int method, hx_level_f32* L, float* h_alt, float* hu_alt, f
 /*
  * Host-buffer form of hx_level_run for callers whose level lives in host
  * memory: copies h, hu, hv, z, n (host, pitch nx) to the device, runs nsteps,
- * copies the state back.  Device buffers are allocated by the call and cached
- * per thread for the next call of the same size (hx_host_cache_release frees
- * them).  The copies overlap the computation in row bands, and they can only
+ * copies the state back.  Device buffers, streams and events are created by
+ * the call on the current device and cached per thread and per device for
+ * the next call of that size on that device (hx_host_cache_release frees the
+ * calling thread's caches on every device).  The copies overlap the computation in row bands, and they can only
  * when the host buffers are page-locked (cudaHostAlloc or cudaHostRegister).
  * The call returns once the state is back in h, hu, hv: the status bits
  * (>= 0) or a negative error.
@@ -432,9 +454,13 @@ int hx_ensemble_run_f64(int n, const hx_ensemble_member_f64* members, int nsteps
  *   - The level must satisfy ny * pitch <= HX_STATIC_RUN_MAX_CELLS (512 x 512);
  *     a larger one is rejected with HX_ERR_ARG and an explanatory
  *     hx_last_error().  Use hx_level_run_f64 with your own scratch for it.
- *   - The state is advanced in place: level->h, hu, hv hold the result.
- *     status and time_dev are optional caller-owned device words as in
- *     hx_level_run_f64.
+ *   - The state is advanced in place: level->h, hu, hv hold the result in
+ *     their valid cells (nx of each pitch-long row; row padding is not
+ *     touched).  The arithmetic form applies to the first CFL reduction and to
+ *     every step, as in hx_level_run_f64, and the result is that call's.
+ *     status and time_dev are optional caller-owned device words; without a
+ *     status word a dt collapse goes to a word inside the array and is not
+ *     reported.
  *   - The first call on a device looks up the array's device address
  *     (cudaGetSymbolAddress) with that device current and caches it; make that
  *     first call before any stream capture.

@@ -47,11 +47,28 @@ def build(force: bool = False) -> Path:
     return LIB_PATH
 
 
-def build_ref() -> Path | None:
-    """Compile the reference's point kernels if the reference tree is present."""
-    ref_root = Path(os.environ.get("HX_REFERENCE_ROOT", "/root/reference"))
-    if not (ref_root / "include" / "solvers" / "kernels").is_dir():
+def reference_root() -> Path | None:
+    """The reference source tree, as the recipe ``build_ref.sh`` locates it
+    ($HX_REFERENCE_ROOT or the recipe's default), or None where there is none."""
+    r = subprocess.run(["sh", str(HERE / "build_ref.sh"), "--root"], capture_output=True, text=True)
+    return Path(r.stdout.strip()) if r.returncode == 0 and r.stdout.strip() else None
+
+
+REF_OUTPUTS = ["libhx_ref.so"] + ["libhx_ref_level_%s%s.so" % (a, p) for a in ("", "fabs_") for p in ("f64", "f32")]
+
+
+def build_ref(force: bool = False) -> Path | None:
+    """Compile the reference's point kernels and per-box drivers (oracle/build_ref.sh)
+    if the reference tree is present; a no-op when every output is newer than
+    the recipe, the AMReX stand-in and the driver harness."""
+    if reference_root() is None:
         return None
+    outs = [HERE / "_ref" / n for n in REF_OUTPUTS]
+    srcs = [HERE / "build_ref.sh", *HERE.glob("ref_*.cpp"), *HERE.glob("ref_*.h"), *(HERE / "ref_shim").glob("*")]
+    if not force and all(o.exists() for o in outs):
+        oldest = min(o.stat().st_mtime for o in outs)
+        if all(p.stat().st_mtime <= oldest for p in srcs):
+            return REF_LIB_PATH
     subprocess.run(["sh", str(HERE / "build_ref.sh")], check=True, stdout=subprocess.DEVNULL)
     return REF_LIB_PATH
 
@@ -172,11 +189,18 @@ def compute_dt(level: Level, h, hu, hv, z):
     return float(mn.value), float(mx.value)
 
 
-def run(level: Level, method: int, h, hu, hv, z, n, nsteps, cfl, mode=LIMITER_FLOAT_ABS):
-    """nsteps of the single-level time loop in place on copies; returns (h, hu, hv, t, dt_last, status)."""
+def run(level: Level, method: int, h, hu, hv, z, n, nsteps, cfl, mode=LIMITER_FLOAT_ABS, copy=True):
+    """nsteps of the single-level time loop; returns (h, hu, hv, t, dt_last, status).
+
+    The loop runs on copies of h, hu, hv, or with ``copy=False`` in place on
+    the given arrays (C-contiguous, of one floating dtype)."""
     dtype = np.asarray(h).dtype
     R = _real(dtype)
-    st = [np.array(a, dtype=dtype, copy=True, order="C") for a in (h, hu, hv)]
+    if copy:
+        st = [np.array(a, dtype=dtype, copy=True, order="C") for a in (h, hu, hv)]
+    else:
+        st = [h, hu, hv]
+        assert all(a.dtype == dtype and a.flags.c_contiguous for a in st), "in-place run needs C-contiguous planes"
     zz = np.ascontiguousarray(z, dtype=dtype)
     nn = np.ascontiguousarray(n, dtype=dtype)
     t, dtl = R(), R()
@@ -342,3 +366,87 @@ def ref_masked_average_down(fine, rx, ry, fine_volume, nodata=-9999.0):
         ctypes.c_int(nxf), ctypes.c_int(nyf), ctypes.c_int(nc), _ptr(f), ctypes.c_int(rx), ctypes.c_int(ry),
         R(fine_volume), R(nodata), _ptr(c))
     return c
+
+
+# --- the reference's per-box drivers compiled verbatim (ref_level.cpp) ---------
+
+_ref_level = {}
+
+
+def ref_level_lib(dtype=np.float64, float_abs: bool = True) -> ctypes.CDLL:
+    """The reference's solver drivers at one level (oracle/_ref).  float_abs
+    picks the build whose limiter abs() is the floating one; otherwise C's
+    int abs(int), what the host headers alone give."""
+    key = (np.dtype(dtype).name, bool(float_abs))
+    if key not in _ref_level:
+        name = "libhx_ref_level_%s%s.so" % ("fabs_" if float_abs else "", _suffix(dtype))
+        path = HERE / "_ref" / name
+        if not path.exists():
+            if build_ref() is None:
+                raise FileNotFoundError("reference tree not available to build oracle/_ref")
+        _ref_level[key] = ctypes.CDLL(str(path))
+    return _ref_level[key]
+
+
+def _ref_call(fn, *args):
+    err = ctypes.create_string_buffer(256)
+    rc = fn(*args, err)
+    if rc == 2:
+        raise RuntimeError("reference driver: " + err.value.decode(errors="replace"))
+    return rc
+
+
+def ref_run(level: Level, method: int, h, hu, hv, z, n, nsteps, cfl, float_abs=True):
+    """The reference's single-level time loop: (h, hu, hv, t, dt_last, status)."""
+    dtype = np.asarray(h).dtype
+    R = _real(dtype)
+    st = [np.array(a, dtype=dtype, copy=True, order="C") for a in (h, hu, hv)]
+    zz, nn = (np.ascontiguousarray(a, dtype=dtype) for a in (z, n))
+    t, dtl = R(), R()
+    lib_ = ref_level_lib(dtype, float_abs)
+    rc = _ref_call(getattr(lib_, "hxref_level_run_" + _suffix(dtype)), ctypes.c_int(method), ctypes.c_int(level.nx),
+                   ctypes.c_int(level.ny), R(level.dx), R(level.dy), _ptr(level.bc_lo), _ptr(level.bc_hi),
+                   *[_ptr(a) for a in st], _ptr(zz), _ptr(nn), ctypes.c_int(nsteps), R(cfl), ctypes.byref(t),
+                   ctypes.byref(dtl))
+    return st[0], st[1], st[2], float(t.value), float(dtl.value), int(rc)
+
+
+def ref_advance(level: Level, method: int, h, hu, hv, z, n, dt, float_abs=True):
+    """One level advance of the reference by dt: (h, hu, hv)."""
+    dtype = np.asarray(h).dtype
+    R = _real(dtype)
+    arrs = [np.ascontiguousarray(a, dtype=dtype) for a in (h, hu, hv, z, n)]
+    out = [np.empty_like(arrs[0]) for _ in range(3)]
+    lib_ = ref_level_lib(dtype, float_abs)
+    _ref_call(getattr(lib_, "hxref_level_advance_" + _suffix(dtype)), ctypes.c_int(method), ctypes.c_int(level.nx),
+              ctypes.c_int(level.ny), R(level.dx), R(level.dy), _ptr(level.bc_lo), _ptr(level.bc_hi),
+              *[_ptr(a) for a in arrs], R(dt), *[_ptr(o) for o in out])
+    return tuple(out)
+
+
+def ref_compute_dt(level: Level, method: int, h, hu, hv, z, cfl=1.0, float_abs=True):
+    """The reference's compute_dt_level (cfl applied); None when it aborts on a collapsed dt."""
+    dtype = np.asarray(h).dtype
+    R = _real(dtype)
+    arrs = [np.ascontiguousarray(a, dtype=dtype) for a in (h, hu, hv, z)]
+    out = R()
+    lib_ = ref_level_lib(dtype, float_abs)
+    rc = _ref_call(getattr(lib_, "hxref_level_dt_" + _suffix(dtype)), ctypes.c_int(method), ctypes.c_int(level.nx),
+                   ctypes.c_int(level.ny), R(level.dx), R(level.dy), *[_ptr(a) for a in arrs], R(cfl),
+                   ctypes.byref(out))
+    return None if rc == 1 else float(out.value)
+
+
+def ref_tag_cells(method: int, Ug, Tg, dx, dy, time, h_th, u_th, z_th):
+    """The reference's tag_cells on a box whose state Ug (3, ny+2, nx+2) and
+    terrain Tg (2, ny+2, nx+2) carry one ghost cell; returns (ny, nx) int8 tags
+    (2 = TagBox::SET, else 0)."""
+    U = np.ascontiguousarray(Ug)
+    T = np.ascontiguousarray(Tg, dtype=U.dtype)
+    ny, nx = U.shape[1] - 2, U.shape[2] - 2
+    R = _real(U.dtype)
+    tags = np.zeros((ny, nx), dtype=np.int8)
+    lib_ = ref_level_lib(U.dtype, True)
+    _ref_call(getattr(lib_, "hxref_tag_cells_" + _suffix(U.dtype)), ctypes.c_int(method), ctypes.c_int(nx),
+              ctypes.c_int(ny), R(dx), R(dy), _ptr(U), _ptr(T), R(time), R(h_th), R(u_th), R(z_th), _ptr(tags))
+    return tags

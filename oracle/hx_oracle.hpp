@@ -67,14 +67,16 @@ enum LimiterAbs { LIMITER_FLOAT_ABS = 0, LIMITER_INT_ABS = 1 };
 template <class R> inline R limiter_abs(R r, int mode) {
     if (mode == LIMITER_INT_ABS) {
         // abs((int)r): truncation toward zero, then converted back in the
-        // expression.  Out-of-range values saturate (the C conversion is UB).
-        double t = (double)r;
-        int iv;
-        if (!(t == t)) iv = 0;
-        else if (t >= 2147483647.0) iv = 2147483647;
-        else if (t <= -2147483647.0) iv = -2147483647;
-        else iv = (int)t;
-        return (R)std::abs(iv);
+        // expression.  A value outside the int range (or NaN) has no defined
+        // conversion in C; this follows what the x86-64 build of the
+        // reference does (cvttsd2si / cvttss2si give INT_MIN, and abs(INT_MIN)
+        // wraps to INT_MIN), the machine the golden vectors come from.
+        const double t = (double)r;
+        long long v;
+        if (!(t == t) || t >= 2147483648.0 || t <= -2147483649.0) v = -2147483648ll;
+        else v = (long long)(int)t;
+        const long long a = (v == -2147483648ll) ? v : (v < 0 ? -v : v);
+        return (R)a;
     }
     return std::abs(r);
 }
@@ -297,13 +299,37 @@ inline void roe_classic(R hi, R hui, R hvi, R zi, R ni, R hj, R huj, R hvj, R zj
 // Ghost-extended single-box level.
 // ---------------------------------------------------------------------------
 
-// Physical boundary kinds of the inputs file (include/boundaries/BCFill.H:35-86):
-// code 0 is a reflective wall, any other code is transmissive (foextrap).
+// Physical boundary kinds of the inputs file (include/boundaries/BCFill.H:35-138):
+// code 0 is a reflective wall, any other code is transmissive (foextrap) --
+// except 2, a closed wall of this library (below), which the reference's
+// inputs do not have.
+//
+// Code 0, the reference's wall, as its time loop fills the ghosts: the state
+// ghosts come from FillPatch(lev, time, U_ext, UBCs, 1, 2) (HydrostaticRoe.cpp
+// :477, Roe.cpp:337), which reaches the BC functor through FillPatchFrom ->
+// FillPatchSingleLevel(..., fphysbc, 0) (include/utils/FillPatchUtils.H
+// :128-129); HydroPhysBC starts at BC record 0 for the first filled component
+// (BCFill.H:244-264), so hu (component 1) takes record 0 -- the scalar rule,
+// reflect_even on every wall -- and hv (component 2) takes record 1, the
+// x-momentum rules: reflect_odd across x walls, reflect_even across y walls.
+// Code 2 gives each momentum its own record: hu reflect_odd across x walls,
+// hv reflect_odd across y walls, even across the others.
 enum GhostRule { FOEXTRAP = 0, REFLECT_EVEN = 1, REFLECT_ODD = 2 };
+constexpr int BC_WALL = 0, BC_CLOSED_WALL = 2;
 
-inline int scalar_rule(int code) { return code == 0 ? REFLECT_EVEN : FOEXTRAP; }
-inline int normal_rule(int code) { return code == 0 ? REFLECT_ODD : FOEXTRAP; }
-inline int tangential_rule(int code) { return code == 0 ? REFLECT_EVEN : FOEXTRAP; }
+inline bool is_wall(int code) { return code == BC_WALL || code == BC_CLOSED_WALL; }
+inline int scalar_rule(int code) { return is_wall(code) ? REFLECT_EVEN : FOEXTRAP; }
+// hu at an x side (xdir) or a y side
+inline int hu_rule(int code, bool xdir) {
+    if (!is_wall(code)) return FOEXTRAP;
+    return (code == BC_CLOSED_WALL && xdir) ? REFLECT_ODD : REFLECT_EVEN;
+}
+// hv at an x side (xdir) or a y side
+inline int hv_rule(int code, bool xdir) {
+    if (!is_wall(code)) return FOEXTRAP;
+    if (code == BC_WALL) return xdir ? REFLECT_ODD : REFLECT_EVEN;
+    return xdir ? REFLECT_EVEN : REFLECT_ODD;
+}
 
 // A plane of (nx + 2G) x (ny + 2G) values, x fastest, cell (i, j) of the valid
 // box at offset (i + G) + (j + G) * (nx + 2G).
@@ -358,12 +384,12 @@ inline void rules_scalar(const int lo[2], const int hi[2], int out[4]) {
     out[2] = scalar_rule(lo[1]); out[3] = scalar_rule(hi[1]);
 }
 inline void rules_xmom(const int lo[2], const int hi[2], int out[4]) {
-    out[0] = normal_rule(lo[0]); out[1] = normal_rule(hi[0]);
-    out[2] = tangential_rule(lo[1]); out[3] = tangential_rule(hi[1]);
+    out[0] = hu_rule(lo[0], true); out[1] = hu_rule(hi[0], true);
+    out[2] = hu_rule(lo[1], false); out[3] = hu_rule(hi[1], false);
 }
 inline void rules_ymom(const int lo[2], const int hi[2], int out[4]) {
-    out[0] = tangential_rule(lo[0]); out[1] = tangential_rule(hi[0]);
-    out[2] = normal_rule(lo[1]); out[3] = normal_rule(hi[1]);
+    out[0] = hv_rule(lo[0], true); out[1] = hv_rule(hi[0], true);
+    out[2] = hv_rule(lo[1], false); out[3] = hv_rule(hi[1], false);
 }
 inline void rules_terrain(int out[4]) { out[0] = out[1] = out[2] = out[3] = FOEXTRAP; }
 

@@ -1,3 +1,3 @@
-// Host-only stand-in: the reference kernels need only the qualifier macros.
+// Host-only stand-in: every AMReX name the reference drivers use is in hx_amrex_shim.H.
 #pragma once
-#include <AMReX_REAL.H>
+#include "hx_amrex_shim.H"

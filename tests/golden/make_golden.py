@@ -1,7 +1,7 @@
 """Regenerate the golden vectors in this folder from the reference itself.
 
 Run from the repository root, in a checkout that has the reference source tree
-(default /root/reference, or $HX_REFERENCE_ROOT):
+(where oracle/build_ref.sh finds it, or $HX_REFERENCE_ROOT):
 
     python tests/golden/make_golden.py
 
@@ -16,6 +16,14 @@ What it writes (all seeded, all small):
   (include/utils/MaskedAverageDown.H:64-104) on fields with NaN and sentinels.
 * ``dambreak_exact.npz`` -- the exact dam-break-on-wet-bed profiles of the
   reference's tests/dambreak/analytical.py, imported from the reference tree.
+* ``drivers_{f64,f32}.npz`` -- the reference's per-box solver drivers
+  (src/solvers/HydrostaticRoe.cpp, src/solvers/Roe.cpp with SolverVariant and
+  the BCFill.H ghost filler) compiled verbatim and run at one level by
+  oracle/ref_level.cpp: for each case the inputs, the state, clock and status
+  after the reference's own time loop, with the limiter's abs() bound both
+  ways (``fabs``: the floating abs; ``iabs``: C's int abs), the first CFL
+  bound, and tag flags (``python tests/golden/make_golden.py drivers``
+  rewrites these two files alone).
 
 The families of inputs are chosen to drive every branch of the kernels: dry
 clamps, both sonic entropy fixes, both positivity guards, both thrust forms,
@@ -35,7 +43,7 @@ sys.path.insert(0, str(ROOT))
 import oracle  # noqa: E402
 
 OUT = Path(__file__).resolve().parent
-REF = Path(os.environ.get("HX_REFERENCE_ROOT", "/root/reference"))
+REF = oracle.reference_root()
 
 
 def hydro_states(rng, n):
@@ -88,9 +96,85 @@ def classic_states(rng, n):
     return states, aux
 
 
+def driver_cases():
+    """Small single-level cases that reach every branch of the drivers: walls
+    with flow against them (both momentum components), mixed and open
+    boundaries, NODATA walls, Manning friction, wet/dry fronts, the lake at
+    rest, and the classic solver's collapse next to NODATA."""
+    from hydroexa_gb300 import workloads
+    out = []
+    c = workloads.dam_break(40, 32, x_dam=0.25)
+    c.hv = 0.3 * c.h
+    out.append(("walls_flow", c, (1, 0), 30))
+    c = workloads.fractal_dam_break(40, 32, seed=5, amplitude=1.0, nodata_frac=0.15)
+    out.append(("fractal_nodata", c, (1,), 12))
+    c = workloads.fractal_dam_break(40, 32, seed=6, amplitude=1.0, nodata_frac=0.0)
+    c.n[:] = 0.03
+    c.geom.bc_lo, c.geom.bc_hi = (1, 0), (0, 1)
+    out.append(("friction_mixed_bc", c, (1, 0), 15))
+    c = workloads.fractal_dam_break(37, 23, seed=9, amplitude=0.5, nodata_frac=0.1)
+    c.geom.bc_lo, c.geom.bc_hi = (1, 1), (1, 1)
+    out.append(("open_ragged", c, (1,), 15))
+    c = workloads.fractal_dam_break(37, 23, seed=9, amplitude=0.5, nodata_frac=0.0)
+    c.geom.bc_lo, c.geom.bc_hi = (1, 1), (1, 1)
+    out.append(("open_ragged_classic", c, (0,), 15))
+    c = workloads.lake_at_rest(40, 40, seed=2, nodata_frac=0.1)
+    out.append(("lake_nodata", c, (1,), 25))
+    c = workloads.fractal_dam_break(40, 32, seed=12, amplitude=2.0, nodata_frac=0.2)
+    out.append(("classic_nodata_collapse", c, (0,), 60))
+    return out
+
+
+def driver_goldens():
+    """drivers_{f64,f32}.npz from the reference's own drivers (oracle/ref_level.cpp)."""
+    for dtype, sfx in ((np.float64, "f64"), (np.float32, "f32")):
+        rec = {}
+        for name, c, methods, nsteps in driver_cases():
+            g = c.geom
+            L = oracle.Level(g.nx, g.ny, g.dx, g.dy, g.bc_lo, g.bc_hi)
+            planes = [a.astype(dtype) for a in (c.h, c.hu, c.hv, c.z, c.n)]
+            for k, key in enumerate(("h", "hu", "hv", "z", "n")):
+                rec[f"{name}/{key}"] = planes[k]
+            rec[f"{name}/geom"] = np.array([g.nx, g.ny, g.bc_lo[0], g.bc_lo[1], g.bc_hi[0], g.bc_hi[1]], np.int32)
+            rec[f"{name}/dxdy_cfl"] = np.array([g.dx, g.dy, c.cfl], np.float64)
+            rec[f"{name}/nsteps"] = np.int32(nsteps)
+            rec[f"{name}/methods"] = np.array(methods, np.int32)
+            for m in methods:
+                rec[f"{name}/m{m}/dt0"] = np.float64(oracle.ref_compute_dt(L, m, *planes[:4], cfl=1.0))
+                for fa, tag in ((True, "fabs"), (False, "iabs")):
+                    h, hu, hv, t, dtl, st = oracle.ref_run(L, m, *planes, nsteps, c.cfl, float_abs=fa)
+                    rec[f"{name}/m{m}/{tag}/state"] = np.stack([h, hu, hv])
+                    rec[f"{name}/m{m}/{tag}/t_status"] = np.array([t, st], np.float64)
+        # tags: an evolved state with one ghost ring copied from the edge, two threshold sets, t = 0 and t > 0
+        c = workloads_fractal(48, 36)
+        g = c.geom
+        L = oracle.Level(g.nx, g.ny, g.dx, g.dy, g.bc_lo, g.bc_hi)
+        h, hu, hv, *_ = oracle.ref_run(L, 1, *[a.astype(dtype) for a in (c.h, c.hu, c.hv, c.z, c.n)], 8, c.cfl)
+        U = np.pad(np.stack([h, hu, hv]), ((0, 0), (1, 1), (1, 1)), mode="edge")
+        T = np.pad(np.stack([c.z, c.n]).astype(dtype), ((0, 0), (1, 1), (1, 1)), mode="edge")
+        rec["tags/U"], rec["tags/T"] = U, T
+        rec["tags/dxdy"] = np.array([g.dx, g.dy], np.float64)
+        for m in (0, 1):
+            for ti, time in enumerate((0.0, 0.5)):
+                for si, th in enumerate(((0.5, 0.5, 2.0), (5.0, 20.0, 50.0), (1e9, 1e9, 20.0))):
+                    rec[f"tags/m{m}/t{ti}/s{si}"] = oracle.ref_tag_cells(m, U, T, g.dx, g.dy, time, *th)
+        np.savez_compressed(OUT / f"drivers_{sfx}.npz", **rec)
+
+
+def workloads_fractal(nx, ny):
+    from hydroexa_gb300 import workloads
+    return workloads.fractal_dam_break(nx, ny, seed=31, amplitude=2.0, nodata_frac=0.15)
+
+
 def main():
+    if len(sys.argv) > 1 and sys.argv[1] == "drivers":
+        if oracle.build_ref() is None:
+            raise SystemExit("reference tree not found (oracle/build_ref.sh --root names none)")
+        driver_goldens()
+        print("driver golden vectors written to", OUT)
+        return
     if oracle.build_ref() is None:
-        raise SystemExit(f"reference tree not found at {REF}")
+        raise SystemExit("reference tree not found (oracle/build_ref.sh --root names none)")
     rng = np.random.default_rng(20261203)
 
     s, nr = hydro_states(rng, 4096)
@@ -129,6 +213,7 @@ def main():
             prof[f"h_t{t}"] = np.asarray(h, dtype=np.float64)
             prof[f"u_t{t}"] = np.asarray(u, dtype=np.float64)
     np.savez_compressed(OUT / "dambreak_exact.npz", x=x, hl=1.0, hr=0.1, x0=0.5, **prof)
+    driver_goldens()
     print("golden vectors written to", OUT)
 
 
