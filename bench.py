@@ -105,32 +105,47 @@ def make_case(nx, ny):
     return workloads.fractal_dam_break(nx, ny, seed=3)
 
 
-def cpu_sample(case, nsteps_max=50, budget_s=12.0, method=1):
-    """Oracle restatement (OpenMP, all host threads) on a bounded window of the
-    workload: a 1024 x 1024 crop with walls, stepped until ~budget_s."""
-    import numpy as np
-    import oracle
-    oracle.build()
-    w = 1024
-    j0 = (case.geom.ny - w) // 2
-    i0 = (case.geom.nx - w) // 2
-    sl = (slice(j0, j0 + w), slice(i0, i0 + w))
-    arrs = [np.ascontiguousarray(a[sl]) for a in (case.h, case.hu, case.hv, case.z, case.n)]
-    L = oracle.Level(w, w, case.geom.dx, case.geom.dy, (0, 0), (0, 0))
-    threads = oracle.max_threads()
-    h, hu, hv = arrs[0], arrs[1], arrs[2]
-    done = 0
+class CpuLevel:
+    """The oracle's OpenMP time loop (all host threads) on the whole level:
+    library, level descriptor and state copies are prepared here, outside any
+    timed region; ``steps(k)`` then advances the state in place (per step the
+    CFL reduction and one advance, as the reference's time loop does)."""
+
+    def __init__(self, case, method):
+        import numpy as np
+        import oracle
+        oracle.build()
+        self.oracle = oracle
+        self.case = case
+        self.method = method
+        g = case.geom
+        self.L = oracle.Level(g.nx, g.ny, g.dx, g.dy, g.bc_lo, g.bc_hi)
+        self.st = [np.array(a, dtype=np.float64, order="C", copy=True) for a in (case.h, case.hu, case.hv)]
+        self.z = np.ascontiguousarray(case.z, dtype=np.float64)
+        self.n = np.ascontiguousarray(case.n, dtype=np.float64)
+        self.threads = oracle.max_threads()
+        self.cells = g.nx * g.ny
+
+    def steps(self, k):
+        r = self.oracle.run(self.L, self.method, *self.st, self.z, self.n, k, self.case.cfl, copy=False)
+        assert r[5] == 0, "oracle time loop stopped (dt collapse)"
+
+
+def cpu_sample(case, method=1, budget_s=12.0):
+    """A bounded sample of the CPU time loop on the whole level: one untimed
+    step, then as many steps as fit in ~budget_s (2 to 20)."""
+    cpu = CpuLevel(case, method)
     t0 = time.perf_counter()
-    while done < nsteps_max:
-        mn, _ = oracle.compute_dt(L, h, hu, hv, arrs[3])
-        h, hu, hv = oracle.advance(L, method, h, hu, hv, arrs[3], arrs[4], mn * case.cfl)
-        done += 1
-        if time.perf_counter() - t0 > budget_s:
-            break
+    cpu.steps(1)
+    t1 = time.perf_counter() - t0
+    k = max(2, min(20, int(budget_s / max(t1, 1e-3))))
+    t0 = time.perf_counter()
+    cpu.steps(k)
     el = time.perf_counter() - t0
-    return {"value": w * w * done / el / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"oracle OpenMP restatement (not the reference binary), {done} steps of a {w}x{w} crop of the "
-                      f"{case.geom.nx}x{case.geom.ny} workload, {el:.1f} s"}
+    g = case.geom
+    return {"value": cpu.cells * k / el / 1e6, "unit": UNIT, "cores": cpu.threads, "kind": "port",
+            "sample": f"oracle OpenMP restatement (not the reference binary): {k} steps of the whole "
+                      f"{g.nx}x{g.ny} level, {el:.1f} s"}
 
 
 def run_reference(args):
@@ -138,28 +153,22 @@ def run_reference(args):
     if rank != 0:
         return 0
     case = make_case(NX, NY)
-    import numpy as np  # noqa: F401
-    import oracle
-    oracle.build()
-    # warm-up: W bounded steps; timed: K bounded steps (1024x1024 crop each)
-    w_budget = 2.0
-    for _ in range(args.warmup):
-        cpu_sample(case, nsteps_max=1, budget_s=w_budget)
-    vals = []
+    cpu = CpuLevel(case, 1)  # set-up (build, copies, level descriptor) outside the timed region
+    cpu.steps(args.warmup)
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        vals.append(cpu_sample(case, nsteps_max=1, budget_s=60.0))
+    cpu.steps(args.steps)
     el = time.perf_counter() - t0
-    value = 1024 * 1024 * args.steps / el / 1e6
+    value = cpu.cells * args.steps / el / 1e6
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": config_dict(),
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": vals[0]["cores"], "kind": "port",
-                         "sample": "one advance (hydrostatic-Roe, with its CFL reduction) of a 1024x1024 crop of the "
-                                   "8192x8192 workload per step; oracle OpenMP restatement of the reference's "
-                                   "per-box arithmetic (the reference needs AMReX/MPI/HDF5 and cannot be built here)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cpu.threads, "kind": "port",
+                         "sample": "%d steps (after %d untimed) of the whole %dx%d level: per step the CFL reduction "
+                                   "and one hydrostatic-Roe advance; oracle OpenMP restatement of the reference's "
+                                   "per-box arithmetic (the reference needs AMReX/MPI/HDF5 and cannot be built "
+                                   "here)" % (args.steps, args.warmup, NX, NY)},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -189,6 +198,8 @@ def main():
     ap.add_argument("--ensemble-count", type=int, default=256, help="ensemble members (default 256)")
     ap.add_argument("--adjoint-steps", type=int, default=2000, help="adjoint run length (default 2000)")
     ap.add_argument("--method", default="hydrostatic", choices=["hydrostatic", "roe"])
+    ap.add_argument("--details", default=str(ROOT / "_build" / "bench_details.json"),
+                    help="file for the full ensemble and adjoint tables (the JSON line carries their summaries)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     NX = NY = args.size
@@ -313,10 +324,19 @@ def main():
         cpu = cpu_sample(case, method=method)
 
     if rank == 0:
+        pipe = (fp64_pipe(profile, kms) if (args.precision, args.method, args.arith) == ("f64", "hydrostatic", "fast")
+                and cells >= 1 << 22 else None)
+        if ens is not None or adj is not None:
+            Path(args.details).parent.mkdir(parents=True, exist_ok=True)
+            Path(args.details).write_text(json.dumps({"ensemble": ens, "adjoint": adj}, indent=1))
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": args.precision, "data": "synthetic (seeded fractal terrain; no dataset)",
+            "fp64_pipe_frac": pipe["frac"] if pipe else None,
+            "ensemble": ensemble_summary(ens),
+            "adjoint": adjoint_summary(adj),
+            "details_file": args.details if (ens is not None or adj is not None) else None,
             "config": dict(config_dict(), arith=args.arith, nx=NX, ny=NY, precision=args.precision.upper(),
                            method={"hydrostatic": "HydrostaticRoe", "roe": "Roe (no NODATA)"}[args.method]),
             "e2e": e2e,
@@ -331,12 +351,8 @@ def main():
                     ",32,32" if (args.method, args.precision) == ("hydrostatic", "f64") and cells >= 1 << 22 else ""),
                 "kernel_ms": kms, "algorithmic_bytes_per_launch": BYTES_PER_CELL[args.precision] * cells,
                 "note": "FP64-issue bound on GB300: see fp64_pipe",
-                "fp64_pipe": (fp64_pipe(profile, kms)
-                              if (args.precision, args.method, args.arith) == ("f64", "hydrostatic", "fast")
-                              and cells >= 1 << 22 else None),
+                "fp64_pipe": pipe,
             },
-            "ensemble": ens,
-            "adjoint": adj,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
         }
@@ -555,6 +571,33 @@ def adjoint_measure(dev, nsteps=2000, every=45, fd_eps=1e-6):
             "fd_horizon_scan": {"workload": "same bed and gauges, free surface 1.0 + 0.05 m undulation + 0.2 m hump, "
                                             "smooth currents up to 0.2 m/s (no quiescent region)",
                                 "runs": scan}}
+
+
+def ensemble_summary(ens):
+    """The ensemble figures the JSON line carries (the full record goes to the details file)."""
+    if ens is None:
+        return None
+    return {"batched": ens["batched"], "member_loop": ens["member_loop"],
+            "host_dt_loop": ens["plain_loop_host_dt"], "ratio": ens["speedup_vs_plain_loop"],
+            "ratio_vs_member_loop": ens["speedup_vs_member_loop"], "unit": UNIT,
+            "tile_shape_per_class": ens["tile_shape_per_class"]}
+
+
+def adjoint_summary(adj):
+    """The adjoint figures the JSON line carries: cost against the forward run,
+    the gradient against the N-step tangent-linear model, and the central
+    differences with the configured step 1e-6 (configured run; kink-free state)."""
+    if adj is None:
+        return None
+    fd = adj["fd_check"]
+    kink_free = [v["best_rel_err"] for run in adj["fd_kink_free"]["runs"].values() for v in run.values()]
+    return {"cost_vs_forward": adj["cost_vs_forward"], "reverse_vs_forward": adj["reverse_vs_forward"],
+            "tangent_rel_err": adj["tangent_check"]["rel_err"],
+            "fd_configured_rel_err": {k: v["step_1e-06"]["rel_err"] for k, v in fd.items()},
+            "fd_kink_free_max_rel_err": max(kink_free) if kink_free else None,
+            "binomial_cost_vs_forward": adj["binomial"]["cost_vs_forward"],
+            "store_all_cost_vs_forward": adj["store_all"]["cost_vs_forward"],
+            "work_bytes_checkpointed": adj["work_bytes_checkpointed"]}
 
 
 def load_profile_summary():
