@@ -957,7 +957,12 @@ int hx_debug_roe_points_f32(int method, int arith, long n, const float* st, cons
 
 int hx_debug_rcp_f64(long n, const double* x, double* y, hx_stream_t s) {
     if (n < 0 || (n > 0 && (!x || !y))) return fail(HX_ERR_ARG, "bad reciprocal arrays");
-    return launched(launch_rcp<true>(n, x, y, (cudaStream_t)s), "hx_debug_rcp_f64");
+    return launched(launch_rcp<true>(n, x, y, 0, (cudaStream_t)s), "hx_debug_rcp_f64");
+}
+
+int hx_debug_sqrt_f64(long n, const double* x, double* y, hx_stream_t s) {
+    if (n < 0 || (n > 0 && (!x || !y))) return fail(HX_ERR_ARG, "bad square-root arrays");
+    return launched(launch_rcp<true>(n, x, y, 1, (cudaStream_t)s), "hx_debug_sqrt_f64");
 }
 
 }  // extern "C"

@@ -167,17 +167,45 @@ template <class R> __host__ __device__ __forceinline__ R smax_i(R a, R b) { retu
 // max of two non-negative values
 template <class R> __host__ __device__ __forceinline__ R nnmax_i(R a, R b) { return sbits(a) < sbits(b) ? b : a; }
 
-// Reciprocal of a finite normal x from the hardware estimate
-// rcp.approx.ftz.f64 by one third-order Newton step on f(y) = 1/y - x:
-// with e = 1 - x y, y <- y + y (e + e^2), which cubes the relative error
-// (Householder's method of order 3; see Markstein, IBM J. Res. Dev. 34, 1990,
-// for the FMA formulation of these iterations): three FMAs instead of a full
-// IEEE division.  Faithful (within an ulp), as the tests check against IEEE
-// division; callers pass finite normal arguments only.
+// The double holding a normal float exactly, built on the integer pipe.
+__host__ __device__ __forceinline__ double f64_widen(float f) {
+    const unsigned b = (unsigned)sbits(f);
+    const unsigned long long d = ((unsigned long long)(b & 0x80000000u) << 32) |
+                                 ((unsigned long long)(((b >> 23) & 0xFFu) + (1023u - 127u)) << 52) |
+                                 ((unsigned long long)(b & 0x7FFFFFu) << 29);
+    double y;
+    memcpy(&y, &d, sizeof y);
+    return y;
+}
+// True when |x| has an exponent well inside the normal float range, so that
+// f32_lead(x) is a normal float and its reciprocal / reciprocal square root
+// are normal too.
+__host__ __device__ __forceinline__ bool in_f32_range(double x) {
+    const int e = (int)(((unsigned long long)sbits(x) >> 52) & 0x7FFu) - 1023;
+    return e > -120 && e < 120;
+}
+
+// Reciprocal of a finite normal x by one third-order Newton step on
+// f(y) = 1/y - x from a seed y0 of relative error d: with e = 1 - x y0,
+// y0 + y0 (e + e^2) has error of order d^3 (Householder's method of order 3;
+// see Markstein, IBM J. Res. Dev. 34, 1990, for the FMA formulation of these
+// iterations): three FMAs instead of a full IEEE division.  The seed is the
+// float estimate rcp.approx.ftz.f32 of the leading bits of x, widened on the
+// integer pipe, so that only the three FMAs issue on the FP64 pipe (d < 2^-21,
+// error ~2^-63 before the last rounding); outside the float range the FP64
+// estimate rcp.approx.ftz.f64 seeds the same step.  Faithful (within an ulp),
+// as the tests check against IEEE division; callers pass finite normal
+// arguments only.
 __host__ __device__ __forceinline__ double rcp_nr(double x) {
 #ifdef __CUDA_ARCH__
     double y;
-    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    if (in_f32_range(x)) {
+        float yf;
+        asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(yf) : "f"(f32_lead(x)));
+        y = f64_widen(yf);
+    } else {
+        asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    }
     const double e = fma(-x, y, 1.0);
     return fma(y, fma(e, e, e), y);
 #else
@@ -197,10 +225,30 @@ __host__ __device__ __forceinline__ float rcp_nr(float x) {
 #endif
 }
 
-// Square root of the fast form: IEEE in FP64 (CUDA's sqrt already issues fewer
-// FP64 instructions than a Goldschmidt iteration from rsqrt.approx), the
-// hardware approximation sqrt.approx.ftz.f32 in float.
-__host__ __device__ __forceinline__ double fast_sqrt(double x) { return sqrt(x); }
+// Square root of the fast form.  FP64: from the float estimate r0 of 1/sqrt(x)
+// (rsqrt.approx.ftz.f32 of the leading bits, widened on the integer pipe), one
+// third-order correction of t = x r0: with d = 1 - t r0, sqrt(x) = t (1 - d)^(-1/2)
+// = t (1 + d/2 + 3 d^2/8 + ...), truncated after the d^2 term (Householder's
+// order-3 step for the reciprocal square root, published with the FMA
+// formulation by Markstein, IBM J. Res. Dev. 34, 1990).  Five FP64
+// instructions; the truncation error is ~2.5 delta^3 for a seed error delta
+// < 2^-21, so the result is within about an ulp (tests hold it to 2 ulps of
+// the IEEE square root).  Zero, negative, non-finite and out-of-float-range
+// arguments take the IEEE square root.  Float: sqrt.approx.ftz.f32.
+__host__ __device__ __forceinline__ double fast_sqrt(double x) {
+#ifdef __CUDA_ARCH__
+    if (!pos_i(x) || !in_f32_range(x)) return sqrt(x);
+    float rf;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(rf) : "f"(f32_lead(x)));
+    const double r0 = f64_widen(rf);
+    const double t = x * r0;
+    const double d = fma(-t, r0, 1.0);
+    const double p = fma(0.375, d, 0.5);
+    return fma(t, d * p, t);
+#else
+    return sqrt(x);
+#endif
+}
 __host__ __device__ __forceinline__ float fast_sqrt(float x) {
 #ifdef __CUDA_ARCH__
     float y;

@@ -41,7 +41,7 @@ template cudaError_t launch_adj_forward_rec<true>(const LevelSrc<double>&, const
 template cudaError_t launch_adj_forward_linear<true>(const LevelSrc<double>&, const Cells3<double>&,
                                                      const Plane<double>&, const Cells3W<double>&, const IBox&, double,
                                                      double, const double*, cudaStream_t);
-template cudaError_t launch_rcp<true>(long, const double*, double*, cudaStream_t);
+template cudaError_t launch_rcp<true>(long, const double*, double*, int, cudaStream_t);
 template cudaError_t launch_points<double, true>(int, long, const double*, const double*, double*, cudaStream_t);
 template cudaError_t launch_points<float, true>(int, long, const float*, const float*, float*, cudaStream_t);
 }  // namespace hx

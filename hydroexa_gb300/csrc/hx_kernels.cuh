@@ -11,6 +11,8 @@
 // written once per step.
 #pragma once
 
+#include <type_traits>
+
 #include "hx_device.cuh"
 #include "hx_internal.h"
 
@@ -136,9 +138,9 @@ template <class R> struct ScreenCell {
     bool nod = false, live = false;
 };
 
-template <class R, bool FAST, bool LINEAR>
+template <class R, bool FAST, bool LINEAR, class NP = Plane<R>>
 __device__ __forceinline__ void step_cell(R o0, R o1, R o2, R dx0, R dx1, R dx2, R dy0, R dy1, R dy2, R cx, R cy,
-                                          R dt, const Plane<R>& nplane, const Cells3W<R>& out, int gi, int gj,
+                                          R dt, const NP& nplane, const Cells3W<R>& out, int gi, int gj,
                                           bool nod, R dx, R dy, R idx, R idy, bool fold_dt, R& rate, R& mv,
                                           unsigned& flags, unsigned& pflags, ScreenCell<R>* sc = nullptr) {
     R un[3];
@@ -343,13 +345,29 @@ __device__ __forceinline__ void screened_fold(const ScreenCell<double>* c, doubl
     }
 }
 
+// A thread's share of the next CFL bound, kept across the tiles of a
+// persistent block and folded into the accumulator once at the end.
+template <class R> struct ThreadFold {
+    R rate = R(0), mv = R(0);
+    unsigned flags = 0;
+};
+// Points in the tile body where a persistent kernel does its own work: after
+// the grown tile is loaded (every thread, before the barrier that ends phase A)
+// and after the faces are computed (every thread, after the barrier that ends
+// phase C, when the grown-tile and slope arrays are dead).
+struct NoHooks {
+    __device__ __forceinline__ void after_load() const {}
+    __device__ __forceinline__ void after_faces() const {}
+};
+
 template <class R, bool FAST, int TXv, int TYv, int NTv, class Src, bool LINEAR = false, class Div = NoDiv,
-          class Rec = NoRec>
-__device__ __forceinline__ void hydro_tile_body(HydroSmem<R, TXv, TYv>& S, const Src& src, const Cells3<R>& uo,
-                                                const Plane<R>& nplane, const Cells3W<R>& out, const FaceOut<R>& fo,
+          class Rec = NoRec, class UO = Cells3<R>, class NP = Plane<R>, class Hooks = NoHooks>
+__device__ __forceinline__ void hydro_tile_body(HydroSmem<R, TXv, TYv>& S, const Src& src, const UO& uo,
+                                                const NP& nplane, const Cells3W<R>& out, const FaceOut<R>& fo,
                                                 const IBox& vb, int x0, int y0, R dt, R dx, R dy, DtAccum* dt_out,
                                                 unsigned* status, unsigned* post_flags = nullptr,
-                                                const Div& div = Div{}, const Rec& rec = Rec{}) {
+                                                const Div& div = Div{}, const Rec& rec = Rec{},
+                                                const Hooks& hooks = Hooks{}, ThreadFold<R>* defer = nullptr) {
     static_assert(!Rec::on || (FAST && sizeof(R) == 8), "face records are kept for the FP64 fast form");
     constexpr int GX = HydroSmem<R, TXv, TYv>::GX, GY = HydroSmem<R, TXv, TYv>::GY;
     constexpr int CELLS = TXv * TYv;
@@ -385,6 +403,7 @@ __device__ __forceinline__ void hydro_tile_body(HydroSmem<R, TXv, TYv>& S, const
         S.u[r][c] = uu;
         S.v[r][c] = vv;
     }
+    hooks.after_load();
     __syncthreads();
 
     // --- B: van Leer slopes, once per cell and direction ---------------------
@@ -493,6 +512,7 @@ __device__ __forceinline__ void hydro_tile_body(HydroSmem<R, TXv, TYv>& S, const
         }
     }
     __syncthreads();
+    hooks.after_faces();
 
     // --- D: update, Manning friction, dry clamp (HydrostaticRoe.cpp:551-604) --
     R rate = R(0), mv = R(0);
@@ -500,6 +520,7 @@ __device__ __forceinline__ void hydro_tile_body(HydroSmem<R, TXv, TYv>& S, const
     const R cx = S.kc[0], cy = S.kc[1], idx = S.kc[2], idy = S.kc[3];
     // the FP64 fast form folds the next CFL bound through the float screen
     constexpr bool SCREEN = FAST && sizeof(R) == 8 && CELLS == NTv && !LINEAR && !Div::on;
+    const bool fold = dt_out != nullptr || defer != nullptr;
     ScreenCell<R> sc;
     for (int k = t; k < CELLS; k += NTv) {
         const int tx = k % TXv, ty = k / TXv;
@@ -516,14 +537,25 @@ __device__ __forceinline__ void hydro_tile_body(HydroSmem<R, TXv, TYv>& S, const
             continue;
         }
         const R o0 = uo.ld(0, gi, gj), o1 = uo.ld(1, gi, gj), o2 = uo.ld(2, gi, gj);
-        step_cell<R, FAST, LINEAR>(o0, o1, o2, dx0, dx1, dx2, dy0, dy1, dy2, cx, cy, dt, nplane, out, gi, gj,
-                                   S.nod[ty + 2][tx + 2] != 0, dx, dy, idx, idy, dt_out != nullptr && !SCREEN, rate,
-                                   mv, flags, pflags, (SCREEN && dt_out) ? &sc : nullptr);
+        step_cell<R, FAST, LINEAR, NP>(o0, o1, o2, dx0, dx1, dx2, dy0, dy1, dy2, cx, cy, dt, nplane, out, gi, gj,
+                                   S.nod[ty + 2][tx + 2] != 0, dx, dy, idx, idy, fold && !SCREEN, rate, mv, flags,
+                                   pflags, (SCREEN && fold) ? &sc : nullptr);
     }
     if constexpr (SCREEN) {
-        if (dt_out) screened_fold<NTv>(&sc, dx, dy, idx, idy, rate, mv, flags);
+        if (fold) screened_fold<NTv>(&sc, dx, dy, idx, idy, rate, mv, flags);
     }
-    if (dt_out) block_fold_dt<R, NTv>(rate, mv, flags, dt_out);
+    if (defer) {
+        if constexpr (FAST) {
+            defer->rate = nnmax_i(defer->rate, rate);
+            defer->mv = nnmax_i(defer->mv, mv);
+        } else {
+            defer->rate = smax(defer->rate, rate);
+            defer->mv = smax(defer->mv, mv);
+        }
+        defer->flags |= flags;
+    } else if (dt_out) {
+        block_fold_dt<R, NTv>(rate, mv, flags, dt_out);
+    }
     if ((flags & DTF_NAN) && status) atomicOr(status, (unsigned)HX_STATUS_NAN);
     if (post_flags) {
         pflags = __reduce_or_sync(0xffffffffu, pflags);
@@ -567,6 +599,150 @@ __global__ void __launch_bounds__(TXH * TYH, min_ctas(TXH * TYH))
     hydro_tile_body<R, FAST, TXH, TYH, TXH * TYH>(S, src, uo, nplane, out, fo, vb, vb.lo0 + (int)blockIdx.x * TXH,
                                                   vb.lo1 + (int)blockIdx.y * TYH, dt, ctl.dx, ctl.dy, ctl.dt_out,
                                                   ctl.status);
+}
+
+// ---------------------------------------------------------------------------
+// The persistent FP64 level step on 32 x 32 tiles.  One block of 1024 threads
+// per SM walks its tiles (k = blockIdx.x, blockIdx.x + gridDim.x, ...; row-major
+// over the box, so the blocks in flight share halo rows in L2).  The grown tile
+// of the next tile -- h, hu, hv, z of its in-level cells and the roughness of
+// its own cells -- is copied into shared memory by cp.async while the current
+// tile is updated, so phase A reads shared memory and the global-load latency
+// is hidden under the update's FP64 work.  The staging buffer lies on the slope
+// arrays, which are dead from the end of phase C of one tile to phase B of the
+// next; the own cells' stored state and roughness, which the update reads, are
+// copied out of it during phase A.  Ghosts outside the level are resolved from
+// staged in-level cells by the rules of ghost_source (a tile touching a
+// boundary holds the cells its ghosts mirror or copy), so every value is the
+// one LevelSrc::fetch reads and the arithmetic is k_hydro_tile's, bit for bit.
+// The next CFL bound is folded per thread across the block's tiles and into
+// the accumulator once.
+// ---------------------------------------------------------------------------
+constexpr int kPT = 32;       // tile side
+constexpr int kPG = kPT + 4;  // grown tile side (2-cell MUSCL halo)
+struct PersistStaging {
+    double h[kPG][kPG], hu[kPG][kPG], hv[kPG][kPG], z[kPG][kPG];
+    double n[kPT][kPT];
+};
+struct PersistOwn {
+    double h[kPT * kPT], hu[kPT * kPT], hv[kPT * kPT], n[kPT * kPT];
+    ThreadFold<double> fold[kPT * kPT];  // each thread's share of the next CFL bound (kept out of registers)
+};
+static_assert(sizeof(PersistStaging) <= sizeof(double) * 6 * kPT * (kPT + 2),
+              "the staging buffer must fit in the slope arrays it lies on");
+constexpr size_t persist_smem_bytes() { return sizeof(HydroSmem<double, kPT, kPT>) + sizeof(PersistOwn); }
+
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// Issue the copies of tile (x0, y0) into st (every thread of the block).
+__device__ __forceinline__ void persist_stage(PersistStaging* st, const LevelSrc<double>& src, int x0, int y0) {
+    const int t = threadIdx.x;
+    for (int idx = t; idx < kPG * kPG; idx += kPT * kPT) {
+        const int r = idx / kPG, c = idx - r * kPG;
+        const int gi = x0 - 2 + c, gj = y0 - 2 + r;
+        if (gi < 0 || gi >= src.nx || gj < 0 || gj >= src.ny) continue;
+        const long long o = (long long)gi + (long long)gj * src.pitch;
+        cp_async8(&st->h[r][c], src.h + o);
+        cp_async8(&st->hu[r][c], src.hu + o);
+        cp_async8(&st->hv[r][c], src.hv + o);
+        cp_async8(&st->z[r][c], src.z + o);
+    }
+    const int r = t / kPT, c = t % kPT, gi = x0 + c, gj = y0 + r;
+    if (gi < src.nx && gj < src.ny) cp_async8(&st->n[r][c], src.n + (long long)gi + (long long)gj * src.pitch);
+    cp_async_commit();
+}
+
+// Phase A's source: the staged grown tile, ghosts resolved as LevelSrc does.
+struct StagedSrc {
+    const PersistStaging* st;
+    int x0, y0, nx, ny;
+    int bc_xlo, bc_xhi, bc_ylo, bc_yhi;
+    int glo0, glo1, ghi0, ghi1;
+    __device__ __forceinline__ bool inside(int i, int j) const {
+        return i >= glo0 && i <= ghi0 && j >= glo1 && j <= ghi1;
+    }
+    __device__ __forceinline__ void fetch(int i, int j, double& eta, double& zz, double& qx, double& qy,
+                                          double& nn) const {
+        int mi, mj, ei, ej;
+        bool neg_u, neg_v;
+        ghost_source(i, j, nx, ny, bc_xlo, bc_xhi, bc_ylo, bc_yhi, mi, mj, ei, ej, neg_u, neg_v);
+        const int mr = mj - y0 + 2, mc = mi - x0 + 2, er = ej - y0 + 2, ec = ei - x0 + 2;
+        eta = st->h[mr][mc] + st->z[mr][mc];
+        zz = st->z[er][ec];
+        nn = 0.0;
+        const double a = st->hu[mr][mc], b = st->hv[mr][mc];
+        qx = neg_u ? -a : a;
+        qy = neg_v ? -b : b;
+    }
+};
+// The update's stored state and roughness of the tile's own cells.
+struct OwnState {
+    const PersistOwn* o;
+    int x0, y0;
+    __device__ __forceinline__ double ld(int c, int i, int j) const {
+        const int k = (j - y0) * kPT + (i - x0);
+        return c == 0 ? o->h[k] : (c == 1 ? o->hu[k] : o->hv[k]);
+    }
+};
+struct OwnRough {
+    const PersistOwn* o;
+    int x0, y0;
+    __device__ __forceinline__ double ld(int i, int j) const { return o->n[(j - y0) * kPT + (i - x0)]; }
+};
+struct PersistHooks {
+    PersistStaging* st;
+    PersistOwn* own;
+    const LevelSrc<double>* src;
+    int nx0, ny0;  // origin of the next tile
+    bool next;
+    __device__ __forceinline__ void after_load() const {
+        const int t = threadIdx.x, r = t / kPT + 2, c = t % kPT + 2;
+        own->h[t] = st->h[r][c];
+        own->hu[t] = st->hu[r][c];
+        own->hv[t] = st->hv[r][c];
+        own->n[t] = st->n[r - 2][c - 2];
+    }
+    __device__ __forceinline__ void after_faces() const {
+        if (next) persist_stage(st, *src, nx0, ny0);
+    }
+};
+
+template <bool FAST>
+__global__ void __launch_bounds__(kPT * kPT, 1)
+    k_hydro_persist(LevelSrc<double> src, Cells3W<double> out, IBox vb, int tiles_x, int ntiles,
+                    StepCtl<double> ctl) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    HydroSmem<double, kPT, kPT>& S = *reinterpret_cast<HydroSmem<double, kPT, kPT>*>(smem_raw);
+    PersistOwn* own = reinterpret_cast<PersistOwn*>(smem_raw + sizeof(HydroSmem<double, kPT, kPT>));
+    PersistStaging* st = reinterpret_cast<PersistStaging*>(&S.sxe[0][0]);
+    double dt;
+    if (!resolve_dt(ctl, dt)) return;
+    step_bookkeeping(ctl, dt);
+    int k = (int)blockIdx.x;
+    if (k >= ntiles) return;
+    persist_stage(st, src, vb.lo0 + (k % tiles_x) * kPT, vb.lo1 + (k / tiles_x) * kPT);
+    ThreadFold<double>* tf = &own->fold[threadIdx.x];
+    *tf = ThreadFold<double>{};
+    const FaceOut<double> fo{};
+    for (; k < ntiles; k += (int)gridDim.x) {
+        const int x0 = vb.lo0 + (k % tiles_x) * kPT, y0 = vb.lo1 + (k / tiles_x) * kPT;
+        const int kn = k + (int)gridDim.x;
+        const PersistHooks hooks{st, own, &src, vb.lo0 + (kn % tiles_x) * kPT, vb.lo1 + (kn / tiles_x) * kPT,
+                                 kn < ntiles};
+        const StagedSrc ss{st, x0, y0, src.nx, src.ny, src.bc_xlo, src.bc_xhi, src.bc_ylo, src.bc_yhi,
+                           src.glo0, src.glo1, src.ghi0, src.ghi1};
+        cp_async_wait_all();  // this thread's copies of tile k; the body's first barrier publishes everyone's
+        hydro_tile_body<double, FAST, kPT, kPT, kPT * kPT, StagedSrc, false, NoDiv, NoRec, OwnState, OwnRough,
+                        PersistHooks>(S, ss, OwnState{own, x0, y0}, OwnRough{own, x0, y0}, out, fo, vb, x0, y0, dt,
+                                      ctl.dx, ctl.dy, nullptr, ctl.status, nullptr, NoDiv{}, NoRec{}, hooks,
+                                      ctl.dt_out ? tf : nullptr);
+    }
+    if (ctl.dt_out) block_fold_dt<double, kPT * kPT>(tf->rate, tf->mv, tf->flags, ctl.dt_out);
 }
 
 // ---------------------------------------------------------------------------
@@ -1155,6 +1331,26 @@ template <class K> inline cudaError_t ensure_smem(K kernel, size_t bytes) {
 template <class R, bool FAST, class Src>
 cudaError_t launch_hydro(const Src& src, const Cells3<R>& uo, const Plane<R>& np, const Cells3W<R>& out,
                          const FaceOut<R>& fo, const IBox& vb, const StepCtl<R>& ctl, cudaStream_t st) {
+    if constexpr (std::is_same_v<Src, LevelSrc<double>>) {
+        // a whole level (or a band of its rows) on the big tile: the persistent kernel, when the stored state
+        // and roughness are the level's own planes and no face arrays are asked for
+        if (big_tile<R>(vb) && !fo.on && !fo.mean && uo.p[0] == src.h && uo.p[1] == src.hu && uo.p[2] == src.hv &&
+            uo.js == src.pitch && uo.lo0 == 0 && uo.lo1 == 0 && np.p == src.n && np.js == src.pitch &&
+            np.lo0 == 0 && np.lo1 == 0) {
+            const dim3 tg = tile_grid(vb, kPT, kPT);
+            const int ntiles = (int)(tg.x * tg.y);
+            int dev = 0, sms = 0;
+            cudaError_t e = cudaGetDevice(&dev);
+            if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            if (e != cudaSuccess) return e;
+            auto k = k_hydro_persist<FAST>;
+            e = ensure_smem(k, persist_smem_bytes());
+            if (e != cudaSuccess) return e;
+            k<<<(unsigned)(ntiles < sms ? ntiles : sms), kPT * kPT, persist_smem_bytes(), st>>>(src, out, vb, (int)tg.x,
+                                                                                              ntiles, ctl);
+            return cudaGetLastError();
+        }
+    }
     if (big_tile<R>(vb)) {
         constexpr int BX = BigTile<R>::X, BY = BigTile<R>::Y;
         const size_t sm = sizeof(HydroSmem<R, BX, BY>);
@@ -1297,15 +1493,16 @@ cudaError_t launch_adj_forward_linear(const LevelSrc<double>& src, const Cells3<
     return big_tile<double>(vb) ? go(BigTile<double>{}) : go(SmallTile{});
 }
 
-// The fast form's reciprocal (rcp_nr) of n values, for checking it against IEEE division.
-template <bool FAST> __global__ void k_rcp_probe(long n, const double* x, double* y) {
+// The fast form's reciprocal (rcp_nr, which == 0) or square root (fast_sqrt,
+// which == 1) of n values, for checking them against IEEE division and sqrt.
+template <bool FAST> __global__ void k_rcp_probe(long n, const double* x, double* y, int which) {
     const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) y[i] = rcp_nr(x[i]);
+    if (i < n) y[i] = which ? fast_sqrt(x[i]) : rcp_nr(x[i]);
 }
-template <bool FAST> cudaError_t launch_rcp(long n, const double* x, double* y, cudaStream_t st) {
-    static_assert(FAST, "the reciprocal belongs to the fast form");
+template <bool FAST> cudaError_t launch_rcp(long n, const double* x, double* y, int which, cudaStream_t st) {
+    static_assert(FAST, "the reciprocal and square root belong to the fast form");
     if (n <= 0) return cudaSuccess;
-    k_rcp_probe<FAST><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, x, y);
+    k_rcp_probe<FAST><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, x, y, which);
     return cudaGetLastError();
 }
 

@@ -36,7 +36,7 @@ cudaError_t launch_dt_reduce(const Cells3<R>& U, const Plane<R>& Z, const IBox& 
 
 template <class R, bool FAST>
 cudaError_t launch_points(int method, long n, const R* st, const R* aux, R* out, cudaStream_t stream);
-template <bool FAST> cudaError_t launch_rcp(long n, const double* x, double* y, cudaStream_t st);
+template <bool FAST> cudaError_t launch_rcp(long n, const double* x, double* y, int which, cudaStream_t st);
 
 template <class R>
 cudaError_t launch_tag(int method, const V4<R>& U, const V4<R>& T, const V4<signed char>& tags, const IBox& vb, R dx,

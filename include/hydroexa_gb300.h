@@ -638,6 +638,8 @@ int hx_debug_roe_points_f32(int method, int arith, long n, const float* states, 
                             hx_stream_t stream);
 /* The fast form's FP64 reciprocal of n device values (to check it against IEEE division). */
 int hx_debug_rcp_f64(long n, const double* x, double* y, hx_stream_t stream);
+/* The fast form's FP64 square root of n device values (to check it against the IEEE square root). */
+int hx_debug_sqrt_f64(long n, const double* x, double* y, hx_stream_t stream);
 /* The row bands hx_level_run_host_f64 uses for ny rows (host only, no GPU):
  * writes band starts into starts[0..n] (starts[n] = ny) and returns n, at
  * most 10; max_bands must be at least 10. */

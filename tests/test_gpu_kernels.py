@@ -364,3 +364,41 @@ def test_fast_reciprocal_is_faithful(cuda, hxlib):
     ulps = np.abs(y.view(np.int64) - ref.view(np.int64))
     assert ulps.max() <= 1, ulps.max()
     assert (ulps == 0).mean() > 0.99
+
+
+@pytest.mark.parametrize("lo,hi", [(1e-30, 1e30), (1e-300, 1e300)])
+def test_fast_reciprocal_float_seed(cuda, hxlib, lo, hi):
+    """Inside the float exponent range the reciprocal is seeded from the float
+    estimate of the leading bits (widened on the integer pipe), outside it from
+    the FP64 estimate: within one ulp of IEEE division either way, mostly
+    correctly rounded."""
+    rng = np.random.default_rng(12)
+    n = 1 << 21
+    x = np.exp(rng.uniform(np.log(lo), np.log(hi), n)) * rng.choice([-1.0, 1.0], n)
+    xt = torch.from_numpy(x).to(cuda)
+    yt = torch.empty_like(xt)
+    hxlib.check(hxlib.lib().hx_debug_rcp_f64(n, dptr(xt), dptr(yt), None), "rcp")
+    ulps = np.abs(yt.cpu().numpy().view(np.int64) - (1.0 / x).view(np.int64))
+    assert ulps.max() <= 1, ulps.max()
+    assert (ulps == 0).mean() > 0.99
+
+
+def test_fast_sqrt_is_within_two_ulps(cuda, hxlib):
+    """The fast form's FP64 square root (float estimate of 1/sqrt, one
+    third-order correction) is within 2 ulps of the IEEE square root over 2^22
+    values from 1e-300 to 1e300, including the depths a face sees (1e-6 to 1e4),
+    exactly 0 at 0, and mostly correctly rounded."""
+    rng = np.random.default_rng(13)
+    n = 1 << 22
+    x = np.exp(rng.uniform(np.log(1e-300), np.log(1e300), n))
+    x[: n // 2] = np.exp(rng.uniform(np.log(1e-6), np.log(1e4), n // 2))
+    x[:8] = [0.0, 1.0, 4.0, 2.0, 1e-6, 9.81e-6, 2.0 ** -60, 2.0 ** 60]
+    xt = torch.from_numpy(x).to(cuda)
+    yt = torch.empty_like(xt)
+    hxlib.check(hxlib.lib().hx_debug_sqrt_f64(n, dptr(xt), dptr(yt), None), "sqrt")
+    y = yt.cpu().numpy()
+    ref = np.sqrt(x)
+    ulps = np.abs(y.view(np.int64) - ref.view(np.int64))
+    assert ulps.max() <= 2, ulps.max()
+    assert y[0] == 0.0 and y[1] == 1.0 and y[2] == 2.0
+    assert (ulps == 0).mean() > 0.9

@@ -395,3 +395,29 @@ def test_screened_dt_reduce_equals_the_fused_fold(cuda, oracle_lib, n, kind):
     assert torch.equal(got, ref), (got.tolist(), ref.tolist())
     flags = int(ref[16])
     assert (flags & 2) == (2 if kind == "varied" else 0) and (kind == "varied" or flags == 0)
+
+
+def test_host_buffer_run_on_two_devices(cuda, hxlib):
+    """hx_level_run_host_f64 keeps its device buffers, streams and events per
+    device: one thread calling it on device 0, then device 1, then device 0
+    again gets each device's own resources (the results equal the device
+    loop on each).  Needs two GPUs; skipped on one."""
+    import ctypes
+    if torch.cuda.device_count() < 2:
+        pytest.skip("needs two GPUs")
+    case = workloads.fractal_dam_break(64, 48, seed=7, amplitude=1.0, nodata_frac=0.1)
+    lo = (ctypes.c_int32 * 2)(*case.geom.bc_lo)
+    hi = (ctypes.c_int32 * 2)(*case.geom.bc_hi)
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    ref = to_level(case, case.h, case.hu, case.hv, cuda)
+    ref.run(1, 3, case.cfl, arith=EXACT)
+    want = ref.state.cpu().numpy()
+    for dev in (0, 1, 0):
+        with torch.cuda.device(dev):
+            h, hu, hv = case.h.copy(), case.hu.copy(), case.hv.copy()
+            t = ctypes.c_double()
+            rc = hxlib.lib().hx_level_run_host_f64(1, 64, 48, case.geom.dx, case.geom.dy, lo, hi, P(h), P(hu), P(hv),
+                                                   P(case.z), P(case.n), 3, case.cfl, EXACT, ctypes.byref(t), None)
+            assert rc == 0, hxlib.lib().hx_last_error()
+            assert np.array_equal(h, want[0]) and np.array_equal(hu, want[1]) and np.array_equal(hv, want[2])
+    hxlib.lib().hx_host_cache_release()
