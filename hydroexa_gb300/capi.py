@@ -89,6 +89,7 @@ class EnsembleMemberF64(Structure):
 HX_TILE_32x8 = 0
 HX_TILE_16x16 = 1
 HX_TILE_64x4 = 2
+HX_TILE_32x32 = 3
 
 _lib = None
 

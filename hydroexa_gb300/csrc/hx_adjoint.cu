@@ -255,7 +255,7 @@ __device__ __forceinline__ void roe_fwd_rec(double hi, double ui, double vi, dou
     F.hmb = (R.fl & RR_HM) != 0;
     const double den = 2.0 * cm + T12;
     const double sden = si + sj + T12;
-    F.rs = (cm * den) * R.q; F.rden = (sden * cm) * R.q; F.rcm = (sden * den) * R.q;
+    F.rs = den * R.q; F.rden = sden * R.q; F.rcm = rcp_nr(cm);  // the record's q is 1 / (sden den)
     F.rsi = 0.0; F.rsj = 0.0;
     if (wi && wj) {
         const double r = rcp_nr(si * sj);

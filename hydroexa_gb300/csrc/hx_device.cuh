@@ -212,6 +212,27 @@ __host__ __device__ __forceinline__ double rcp_nr(double x) {
     return 1.0 / x;
 #endif
 }
+// 2 / x, bit for bit 2 * rcp_nr(x): the doubled seed (exact) carried through
+// the same three FMAs, whose every rounding scales by 2 exactly.  Saves the
+// FP64 multiply or add that doubling the result would cost.
+__host__ __device__ __forceinline__ double rcp_nr_twice(double x) {
+#ifdef __CUDA_ARCH__
+    double y, y2;
+    if (in_f32_range(x)) {
+        float yf;
+        asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(yf) : "f"(f32_lead(x)));
+        y = f64_widen(yf);
+        y2 = f64_widen(yf * 2.0f);
+    } else {
+        asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+        y2 = y + y;
+    }
+    const double e = fma(-x, y, 1.0);
+    return fma(y2, fma(e, e, e), y2);
+#else
+    return 2.0 / x;
+#endif
+}
 // Float: the hardware approximation alone (rcp.approx.ftz.f32, within an ulp);
 // the FP32 fast form is held to 1e-5 of the oracle in float, and is bound by
 // instruction issue, where the IEEE reciprocal's correction steps cost.
@@ -249,6 +270,25 @@ __host__ __device__ __forceinline__ double fast_sqrt(double x) {
     return sqrt(x);
 #endif
 }
+// sqrt(x) as fast_sqrt (same bits) and, for one more FMA, 1/sqrt(x) from the
+// same correction: r0 (1 + d/2 + 3 d^2/8), within about an ulp.  x must be a
+// positive normal double inside the float exponent range (a depth above the
+// dry tolerance, times g).
+__device__ __forceinline__ double fast_sqrt_rsqrt(double x, double& rsq) {
+    if (!in_f32_range(x)) {
+        const double s = sqrt(x);
+        rsq = 1.0 / s;
+        return s;
+    }
+    float rf;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(rf) : "f"(f32_lead(x)));
+    const double r0 = f64_widen(rf);
+    const double t = x * r0;
+    const double d = fma(-t, r0, 1.0);
+    const double dp = d * fma(0.375, d, 0.5);
+    rsq = fma(r0, dp, r0);
+    return fma(t, dp, t);
+}
 __host__ __device__ __forceinline__ float fast_sqrt(float x) {
 #ifdef __CUDA_ARCH__
     float y;
@@ -276,7 +316,8 @@ template <class R, bool FAST> __host__ __device__ __forceinline__ R van_leer_slo
     } else {
         // phi(r) dp with r = dm/dp is 0 for r <= 0 and 2 dm dp / (dm + dp) otherwise.
         const R p = dm * dp;
-        return pos_i(p) ? (p + p) * rcp_nr(dm + dp) : R(0);
+        if constexpr (sizeof(R) == 8) return pos_i(p) ? p * rcp_nr_twice(dm + dp) : R(0);  // == (p + p) * rcp_nr
+        else return pos_i(p) ? (p + p) * rcp_nr(dm + dp) : R(0);
     }
 }
 
@@ -361,18 +402,19 @@ __host__ __device__ __forceinline__ void roe_hydrostatic_exact(R hi, R hui, R hv
 // half wave strengths, with the branch flags.  Recorded by the adjoint's
 // segment recompute so the reverse sweep does not evaluate them again.
 struct RoeRecVals {
-    double si, sj, cm, q, um, vm, l0, l2, a0h, a1h, a2h;
+    double si, sj, cm, q, um, vm, l0, l2, a0h, a1h, a2h;  // q = 1 / (sden den)
     unsigned fl;  // RR_WI | RR_WJ | RR_HM | RR_FIX0 | RR_FIX2
 };
 constexpr int NREC = 11;  // doubles of a RoeRecVals
 constexpr unsigned RR_WI = 1u, RR_WJ = 2u, RR_HM = 4u, RR_FIX0 = 8u, RR_FIX2 = 16u;
 
 // Fast form: inputs are the face depths and face velocities (the reference
-// rebuilds the velocity as (h u)/h, which equals u to an ulp).  One division
-// serves both Roe-average quotients and one serves the three wave strengths;
-// the wave speeds sqrt(g h) reuse sqrt(h).  With REC the intermediates go to
-// *rv (values only stored: the arithmetic is the same instruction for
-// instruction).
+// rebuilds the velocity as (h u)/h, which equals u to an ulp).  In FP64 one
+// reciprocal 1/(sden den) gives both 1/sden (the Roe averages) and 1/den (two
+// wave strengths), and 1/cm (the contact wave) comes from the correction step
+// of cm's own square root; the wave speeds sqrt(g h) reuse sqrt(h).  With REC
+// the intermediates go to *rv (values only stored: the arithmetic is the same
+// instruction for instruction).
 template <class R, int DIR, bool REC = false>
 __host__ __device__ __forceinline__ void roe_hydrostatic_fast(R hi, R ui, R vi, R hj, R uj, R vj, R& F0, R& F1,
                                                              R& F2, RoeRecVals* rv = nullptr) {
@@ -392,15 +434,27 @@ __host__ __device__ __forceinline__ void roe_hydrostatic_fast(R hi, R ui, R vi, 
     const R hh = R(0.5) * (hi + hj);
     const bool hmb = gt_bits(hh, C::toldry_bits);
     const R hm = hmb ? hh : C::toldry;
-    const R cm = fast_sqrt(C::g * hm);
+    R cm, rcm;
+    if constexpr (sizeof(R) == 8) {
+        cm = fast_sqrt_rsqrt(C::g * hm, rcm);  // 1/cm from the square root's own correction
+    } else {
+        cm = fast_sqrt(C::g * hm);
+    }
     const R den = R(2) * cm + C::tol12;
     const R sden = si + sj + C::tol12;
-    // one reciprocal for 1/sden, 1/den and 1/cm
-    const R cd = cm * den;
-    const R q = rcp_nr(sden * cd);
-    const R rs = cd * q;
-    const R rden = (sden * cm) * q;
-    const R rcm = (sden * den) * q;
+    // one reciprocal for 1/sden and 1/den (FP64; float shares it with 1/cm too)
+    R q, rs, rden;
+    if constexpr (sizeof(R) == 8) {
+        q = rcp_nr(sden * den);
+        rs = den * q;
+        rden = sden * q;
+    } else {
+        const R cd = cm * den;
+        q = rcp_nr(sden * cd);
+        rs = cd * q;
+        rden = (sden * cm) * q;
+        rcm = (sden * den) * q;
+    }
     const R um = (uni * si + unj * sj) * rs;
     const R vm = (uti * si + utj * sj) * rs;
     R l0 = um - cm;

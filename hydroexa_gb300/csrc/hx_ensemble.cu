@@ -33,7 +33,9 @@ Layout layout(int n) {
 }
 
 int tile_w(int shape) { return shape == HX_TILE_16x16 ? 16 : (shape == HX_TILE_64x4 ? 64 : 32); }
-int tile_h(int shape) { return shape == HX_TILE_16x16 ? 16 : (shape == HX_TILE_64x4 ? 4 : 8); }
+int tile_h(int shape) {
+    return shape == HX_TILE_16x16 ? 16 : (shape == HX_TILE_64x4 ? 4 : (shape == HX_TILE_32x32 ? 32 : 8));
+}
 
 int err(int code, const char* fmt, int a) {
     char buf[256];
@@ -57,8 +59,13 @@ extern "C" int hx_ensemble_run_f64(int n, const hx_ensemble_member_f64* members,
     DtAccum* slots = reinterpret_cast<DtAccum*>(base + Lw.slots);
     unsigned long long* queue = reinterpret_cast<unsigned long long*>(base + Lw.queue);
 
+    // the table holds the 256-thread members first, then the 32 x 32 ones; each group numbers its own tiles
     std::vector<EnsInstance<double>> host((size_t)n);
-    long long tiles = 0;
+    int nbig = 0;
+    for (int i = 0; i < n; ++i) nbig += members[i].tile_shape == HX_TILE_32x32 ? 1 : 0;
+    const int nsmall = n - nbig;
+    long long tiles = 0, tiles_big = 0;
+    int ks = 0, kb = nsmall;
     for (int i = 0; i < n; ++i) {
         const hx_ensemble_member_f64& m = members[i];
         const hx_level_f64& L = m.level;
@@ -66,9 +73,10 @@ extern "C" int hx_ensemble_run_f64(int n, const hx_ensemble_member_f64* members,
             return err(HX_ERR_ARG, "hx_ensemble_run_f64: member %d has a null plane", i);
         if (L.nx < 2 || L.ny < 2 || L.pitch < L.nx || !(L.dx > 0) || !(L.dy > 0))
             return err(HX_ERR_ARG, "hx_ensemble_run_f64: member %d has a bad geometry", i);
-        if (m.tile_shape < 0 || m.tile_shape > HX_TILE_64x4)
+        if (m.tile_shape < 0 || m.tile_shape > HX_TILE_32x32)
             return err(HX_ERR_ARG, "hx_ensemble_run_f64: member %d has an unknown tile shape", i);
-        EnsInstance<double>& I = host[(size_t)i];
+        const bool big = m.tile_shape == HX_TILE_32x32;
+        EnsInstance<double>& I = host[(size_t)(big ? kb++ : ks++)];
         I.st[0][0] = const_cast<double*>(L.h);
         I.st[0][1] = const_cast<double*>(L.hu);
         I.st[0][2] = const_cast<double*>(L.hv);
@@ -86,8 +94,9 @@ extern "C" int hx_ensemble_run_f64(int n, const hx_ensemble_member_f64* members,
         I.shape = m.tile_shape;
         const int tw = tile_w(m.tile_shape), th = tile_h(m.tile_shape);
         I.tiles_x = (L.nx + tw - 1) / tw;
-        I.tile_base = tiles;
-        tiles += (long long)I.tiles_x * ((L.ny + th - 1) / th);
+        long long& count = big ? tiles_big : tiles;
+        I.tile_base = count;
+        count += (long long)I.tiles_x * ((L.ny + th - 1) / th);
         I.slots = slots + 3 * (size_t)i;
         I.status = status + i;
         I.time = time_dev + i;
@@ -118,10 +127,26 @@ extern "C" int hx_ensemble_run_f64(int n, const hx_ensemble_member_f64* members,
     if (per_sm <= 0 || sms <= 0) return set_error(HX_ERR_LAUNCH, "hx_ensemble_run_f64: occupancy query failed");
     long long g = (long long)per_sm * sms;
     const int grid = (int)(g < tiles ? g : tiles);
+    const int grid_big = (int)(sms < tiles_big ? sms : tiles_big);
 
+    // one step: the 256-thread members, then the 32 x 32 ones (each group drains its own tile queue)
+    int per_step = 0;
     auto launch = [&](int step, cudaStream_t s) {
-        return arith == HX_ARITH_EXACT ? launch_ensemble<double, false>(desc, n, tiles, step, cfl, queue, grid, s)
-                                       : launch_ensemble<double, true>(desc, n, tiles, step, cfl, queue, grid, s);
+        cudaError_t r = cudaSuccess;
+        per_step = 0;
+        if (nsmall > 0) {
+            r = arith == HX_ARITH_EXACT ? launch_ensemble<double, false>(desc, nsmall, tiles, step, cfl, queue, grid, s)
+                                        : launch_ensemble<double, true>(desc, nsmall, tiles, step, cfl, queue, grid, s);
+            ++per_step;
+        }
+        if (r == cudaSuccess && nbig > 0) {
+            const EnsInstance<double>* db = desc + nsmall;
+            r = arith == HX_ARITH_EXACT
+                    ? launch_ensemble_big<double, false>(db, nbig, tiles_big, step, cfl, queue, grid_big, s)
+                    : launch_ensemble_big<double, true>(db, nbig, tiles_big, step, cfl, queue, grid_big, s);
+            ++per_step;
+        }
+        return r;
     };
 
     int done = 0;
@@ -144,12 +169,12 @@ extern "C" int hx_ensemble_run_f64(int n, const hx_ensemble_member_f64* members,
         if (cap) cudaStreamDestroy(cap);
         if (e != cudaSuccess) return set_error(HX_ERR_LAUNCH, cudaGetErrorString(e));
         done = reps * kPeriod;
-        note_launches(done);
+        note_launches(done * per_step);
     }
     for (int s = done; s < nsteps; ++s) {
         e = launch(s, st);
         if (e != cudaSuccess) return set_error(HX_ERR_LAUNCH, cudaGetErrorString(e));
-        note_launches(1);
+        note_launches(per_step);
     }
     if (final_in_alt) *final_in_alt = nsteps % 2;
     return HX_OK;

@@ -712,17 +712,23 @@ struct PersistHooks {
     }
 };
 
-template <bool FAST>
+// With Div = DivOut<double> the kernel writes the flux differences of every
+// cell instead of the update (the first step of the host-buffer call, whose
+// update waits for the level's dt): no dt, no CFL fold.
+template <bool FAST, class Div = NoDiv>
 __global__ void __launch_bounds__(kPT * kPT, 1)
     k_hydro_persist(LevelSrc<double> src, Cells3W<double> out, IBox vb, int tiles_x, int ntiles,
-                    StepCtl<double> ctl) {
+                    StepCtl<double> ctl, Div div = Div{}) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     HydroSmem<double, kPT, kPT>& S = *reinterpret_cast<HydroSmem<double, kPT, kPT>*>(smem_raw);
     PersistOwn* own = reinterpret_cast<PersistOwn*>(smem_raw + sizeof(HydroSmem<double, kPT, kPT>));
     PersistStaging* st = reinterpret_cast<PersistStaging*>(&S.sxe[0][0]);
-    double dt;
-    if (!resolve_dt(ctl, dt)) return;
-    step_bookkeeping(ctl, dt);
+    double dt = 0.0;
+    if constexpr (!Div::on) {
+        if (!resolve_dt(ctl, dt)) return;
+        step_bookkeeping(ctl, dt);
+    }
+    const bool fold = !Div::on && ctl.dt_out != nullptr;
     int k = (int)blockIdx.x;
     if (k >= ntiles) return;
     persist_stage(st, src, vb.lo0 + (k % tiles_x) * kPT, vb.lo1 + (k / tiles_x) * kPT);
@@ -737,12 +743,12 @@ __global__ void __launch_bounds__(kPT * kPT, 1)
         const StagedSrc ss{st, x0, y0, src.nx, src.ny, src.bc_xlo, src.bc_xhi, src.bc_ylo, src.bc_yhi,
                            src.glo0, src.glo1, src.ghi0, src.ghi1};
         cp_async_wait_all();  // this thread's copies of tile k; the body's first barrier publishes everyone's
-        hydro_tile_body<double, FAST, kPT, kPT, kPT * kPT, StagedSrc, false, NoDiv, NoRec, OwnState, OwnRough,
+        hydro_tile_body<double, FAST, kPT, kPT, kPT * kPT, StagedSrc, false, Div, NoRec, OwnState, OwnRough,
                         PersistHooks>(S, ss, OwnState{own, x0, y0}, OwnRough{own, x0, y0}, out, fo, vb, x0, y0, dt,
-                                      ctl.dx, ctl.dy, nullptr, ctl.status, nullptr, NoDiv{}, NoRec{}, hooks,
-                                      ctl.dt_out ? tf : nullptr);
+                                      ctl.dx, ctl.dy, nullptr, Div::on ? nullptr : ctl.status, nullptr, div,
+                                      NoRec{}, hooks, fold ? tf : nullptr);
     }
-    if (ctl.dt_out) block_fold_dt<double, kPT * kPT>(tf->rate, tf->mv, tf->flags, ctl.dt_out);
+    if (fold) block_fold_dt<double, kPT * kPT>(tf->rate, tf->mv, tf->flags, ctl.dt_out);
 }
 
 // ---------------------------------------------------------------------------
@@ -831,6 +837,57 @@ template <class R> constexpr size_t ens_smem_bytes() {
     return a > b ? (a > c ? a : c) : (b > c ? b : c);
 }
 
+// The member owning queue tile `tile` and that member's dt for this step; false
+// when the member's CFL chain has collapsed (block-uniform: the member's slot is
+// launch-constant).  Resets the slot of the step after next and advances the
+// member's clock on the member's first tile.
+template <class R>
+__device__ __forceinline__ bool ens_member(const EnsInstance<R>* __restrict__ inst, int ninst, long long tile, int step,
+                                           R cfl, const EnsInstance<R>*& Ip, long long& local, R& dt) {
+    int lo = 0, hi = ninst - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (inst[mid].tile_base <= tile) lo = mid;
+        else hi = mid - 1;
+    }
+    const EnsInstance<R>& I = inst[lo];
+    Ip = &I;
+    const DtAccum* din = &I.slots[step % 3];
+    const unsigned fl = din->flags;
+    const R m = accum_dt_min<R>(din->rate_bits, fl);
+    local = tile - I.tile_base;
+    if ((fl & DTF_COLLAPSED) || m < R(1.e-12)) {
+        if (local == 0 && threadIdx.x == 0) {
+            atomicOr(I.status, (unsigned)HX_STATUS_DT_COLLAPSE);
+            atomicOr(&I.slots[(step + 1) % 3].flags, (unsigned)DTF_COLLAPSED);
+        }
+        return false;
+    }
+    dt = m * cfl;
+    if (local == 0 && threadIdx.x == 0) {
+        DtAccum* r = &I.slots[(step + 2) % 3];
+        r->rate_bits = 0ull;
+        r->maxvel_bits = 0ull;
+        r->flags = 0u;
+        *I.time += dt;
+    }
+    return true;
+}
+
+template <class R>
+__device__ __forceinline__ void ens_views(const EnsInstance<R>& I, int par, LevelSrc<R>& src, Cells3<R>& uo,
+                                          Cells3W<R>& out) {
+    src.h = I.st[par][0]; src.hu = I.st[par][1]; src.hv = I.st[par][2]; src.z = I.z; src.n = I.n;
+    src.pitch = I.pitch;
+    src.nx = I.nx; src.ny = I.ny;
+    src.bc_xlo = I.bc[0]; src.bc_xhi = I.bc[1]; src.bc_ylo = I.bc[2]; src.bc_yhi = I.bc[3];
+    src.glo0 = -2; src.glo1 = -2; src.ghi0 = I.nx + 1; src.ghi1 = I.ny + 1;
+    uo.p[0] = I.st[par][0]; uo.p[1] = I.st[par][1]; uo.p[2] = I.st[par][2];
+    uo.js = I.pitch; uo.lo0 = 0; uo.lo1 = 0;
+    out.p[0] = I.st[par ^ 1][0]; out.p[1] = I.st[par ^ 1][1]; out.p[2] = I.st[par ^ 1][2];
+    out.js = I.pitch; out.lo0 = 0; out.lo1 = 0;
+}
+
 template <class R, bool FAST>
 __global__ void __launch_bounds__(NT) k_ensemble_hydro(const EnsInstance<R>* __restrict__ inst, int ninst,
                                                        long long total_tiles, int step, R cfl,
@@ -846,45 +903,16 @@ __global__ void __launch_bounds__(NT) k_ensemble_hydro(const EnsInstance<R>* __r
         const long long tile = s_tile;
         __syncthreads();
         if (tile >= total_tiles) break;
-        int lo = 0, hi = ninst - 1;  // the instance owning this tile
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (inst[mid].tile_base <= tile) lo = mid;
-            else hi = mid - 1;
-        }
-        const EnsInstance<R>& I = inst[lo];
-        const DtAccum* din = &I.slots[step % 3];
-        const unsigned fl = din->flags;
-        const R m = accum_dt_min<R>(din->rate_bits, fl);
-        const long long local = tile - I.tile_base;
-        if ((fl & DTF_COLLAPSED) || m < R(1.e-12)) {  // launch-constant: the whole block agrees
-            if (local == 0 && threadIdx.x == 0) {
-                atomicOr(I.status, (unsigned)HX_STATUS_DT_COLLAPSE);
-                atomicOr(&I.slots[(step + 1) % 3].flags, (unsigned)DTF_COLLAPSED);
-            }
-            continue;
-        }
-        const R dt = m * cfl;
-        if (local == 0 && threadIdx.x == 0) {
-            DtAccum* r = &I.slots[(step + 2) % 3];
-            r->rate_bits = 0ull;
-            r->maxvel_bits = 0ull;
-            r->flags = 0u;
-            *I.time += dt;
-        }
+        const EnsInstance<R>* Ip;
+        long long local;
+        R dt;
+        if (!ens_member(inst, ninst, tile, step, cfl, Ip, local, dt)) continue;
+        const EnsInstance<R>& I = *Ip;
         const int bx = (int)(local % I.tiles_x), by = (int)(local / I.tiles_x);
         LevelSrc<R> src;
-        src.h = I.st[par][0]; src.hu = I.st[par][1]; src.hv = I.st[par][2]; src.z = I.z; src.n = I.n;
-        src.pitch = I.pitch;
-        src.nx = I.nx; src.ny = I.ny;
-        src.bc_xlo = I.bc[0]; src.bc_xhi = I.bc[1]; src.bc_ylo = I.bc[2]; src.bc_yhi = I.bc[3];
-        src.glo0 = -2; src.glo1 = -2; src.ghi0 = I.nx + 1; src.ghi1 = I.ny + 1;
         Cells3<R> uo;
-        uo.p[0] = I.st[par][0]; uo.p[1] = I.st[par][1]; uo.p[2] = I.st[par][2];
-        uo.js = I.pitch; uo.lo0 = 0; uo.lo1 = 0;
         Cells3W<R> out;
-        out.p[0] = I.st[par ^ 1][0]; out.p[1] = I.st[par ^ 1][1]; out.p[2] = I.st[par ^ 1][2];
-        out.js = I.pitch; out.lo0 = 0; out.lo1 = 0;
+        ens_views(I, par, src, uo, out);
         const Plane<R> np{I.n, I.pitch, 0, 0};
         FaceOut<R> fo{};
         fo.on = 0;
@@ -903,6 +931,45 @@ __global__ void __launch_bounds__(NT) k_ensemble_hydro(const EnsInstance<R>* __r
                 hydro_tile_body<R, FAST, 32, 8, NT>(*reinterpret_cast<HydroSmem<R, 32, 8>*>(smem_raw), src, uo, np,
                                                     out, fo, vb, bx * 32, by * 8, dt, I.dx, I.dy, dout, I.status);
         }
+    }
+}
+
+// The ensemble's large members on 32 x 32 tiles: the same queue discipline
+// (counters queue[2 + parity]) with one CTA of 1024 threads per SM, so that
+// members of many tiles run with the level kernel's halo economy (1.27 loaded
+// cells, 6.4 slopes and 2.06 faces per cell against 1.56, 6.75 and 2.13 on
+// 16 x 16 tiles).
+template <class R, bool FAST>
+__global__ void __launch_bounds__(32 * 32, 1) k_ensemble_big(const EnsInstance<R>* __restrict__ inst, int ninst,
+                                                            long long total_tiles, int step, R cfl,
+                                                            unsigned long long* queue) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ long long s_tile;
+    if (blockIdx.x == 0 && threadIdx.x == 0) queue[2 + ((step + 1) & 1)] = 0ull;
+    const int par = step & 1;
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = (long long)atomicAdd(&queue[2 + par], 1ull);
+        __syncthreads();
+        const long long tile = s_tile;
+        __syncthreads();
+        if (tile >= total_tiles) break;
+        const EnsInstance<R>* Ip;
+        long long local;
+        R dt;
+        if (!ens_member(inst, ninst, tile, step, cfl, Ip, local, dt)) continue;
+        const EnsInstance<R>& I = *Ip;
+        const int bx = (int)(local % I.tiles_x), by = (int)(local / I.tiles_x);
+        LevelSrc<R> src;
+        Cells3<R> uo;
+        Cells3W<R> out;
+        ens_views(I, par, src, uo, out);
+        const Plane<R> np{I.n, I.pitch, 0, 0};
+        FaceOut<R> fo{};
+        fo.on = 0;
+        const IBox vb{0, 0, I.nx - 1, I.ny - 1};
+        hydro_tile_body<R, FAST, 32, 32, 32 * 32>(*reinterpret_cast<HydroSmem<R, 32, 32>*>(smem_raw), src, uo, np,
+                                                   out, fo, vb, bx * 32, by * 32, dt, I.dx, I.dy,
+                                                   &I.slots[(step + 1) % 3], I.status);
     }
 }
 
@@ -1347,7 +1414,7 @@ cudaError_t launch_hydro(const Src& src, const Cells3<R>& uo, const Plane<R>& np
             e = ensure_smem(k, persist_smem_bytes());
             if (e != cudaSuccess) return e;
             k<<<(unsigned)(ntiles < sms ? ntiles : sms), kPT * kPT, persist_smem_bytes(), st>>>(src, out, vb, (int)tg.x,
-                                                                                              ntiles, ctl);
+                                                                                              ntiles, ctl, NoDiv{});
             return cudaGetLastError();
         }
     }
@@ -1391,6 +1458,17 @@ cudaError_t launch_ensemble(const EnsInstance<R>* inst, int ninst, long long tot
 }
 
 template <class R, bool FAST>
+cudaError_t launch_ensemble_big(const EnsInstance<R>* inst, int ninst, long long total_tiles, int step, R cfl,
+                               unsigned long long* queue, int grid, cudaStream_t st) {
+    const size_t sm = sizeof(HydroSmem<R, 32, 32>);
+    auto k = k_ensemble_big<R, FAST>;
+    cudaError_t e = ensure_smem(k, sm);
+    if (e != cudaSuccess) return e;
+    k<<<grid, 32 * 32, sm, st>>>(inst, ninst, total_tiles, step, cfl, queue);
+    return cudaGetLastError();
+}
+
+template <class R, bool FAST>
 int ensemble_blocks_per_sm() {
     int n = 0;
     if (ensure_smem(k_ensemble_hydro<R, FAST>, ens_smem_bytes<R>()) != cudaSuccess) return 0;
@@ -1414,6 +1492,26 @@ cudaError_t launch_boxlevel(const BoxSetSrc& src, const int* tiles, int ntiles, 
 template <class R, bool FAST>
 cudaError_t launch_hydro_split(const LevelSrc<R>& src, const Cells3<R>& uo, const Plane<R>& np, const DivOut<R>& div,
                                const IBox& vb, R dx, R dy, cudaStream_t st) {
+    if constexpr (std::is_same_v<R, double>) {
+        if (big_tile<R>(vb) && uo.p[0] == src.h && uo.p[1] == src.hu && uo.p[2] == src.hv) {
+            const dim3 tg = tile_grid(vb, kPT, kPT);
+            const int ntiles = (int)(tg.x * tg.y);
+            int dev = 0, sms = 0;
+            cudaError_t e = cudaGetDevice(&dev);
+            if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            if (e != cudaSuccess) return e;
+            auto k = k_hydro_persist<FAST, DivOut<double>>;
+            e = ensure_smem(k, persist_smem_bytes());
+            if (e != cudaSuccess) return e;
+            StepCtl<double> ctl{};
+            ctl.dx = dx;
+            ctl.dy = dy;
+            (void)np;
+            k<<<(unsigned)(ntiles < sms ? ntiles : sms), kPT * kPT, persist_smem_bytes(), st>>>(
+                src, Cells3W<double>{}, vb, (int)tg.x, ntiles, ctl, div);
+            return cudaGetLastError();
+        }
+    }
     if (big_tile<R>(vb)) {
         constexpr int BX = BigTile<R>::X, BY = BigTile<R>::Y;
         const size_t sm = sizeof(HydroSmem<R, BX, BY>);

@@ -62,6 +62,10 @@ cudaError_t launch_ensemble(const EnsInstance<R>* inst, int ninst, long long tot
                            unsigned long long* queue, int grid, cudaStream_t st);
 
 template <class R, bool FAST> int ensemble_blocks_per_sm();
+// The large members on 32 x 32 tiles (queue counters queue[2], queue[3]), one CTA per SM.
+template <class R, bool FAST>
+cudaError_t launch_ensemble_big(const EnsInstance<R>* inst, int ninst, long long total_tiles, int step, R cfl,
+                               unsigned long long* queue, int grid, cudaStream_t st);
 
 // Forward step of the adjoint's sweeps: the tile body with dt from the device
 // chain (dt_fixed == nullptr; the step's dt is resolved from ctl) or from

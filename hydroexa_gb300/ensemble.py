@@ -6,7 +6,9 @@ queue spanning every member, each member with its own dt chain, steps replayed
 from a CUDA graph.  ``plain_loop`` is the comparison: the same members advanced
 one after another by the per-level path, with the host reading each member's
 CFL bound every step (the reference's ``compute_dt`` + ``compute_fluxes``
-pattern).  ``autotune`` picks the tile shape per size class by timing.
+pattern).  ``autotune`` picks the tile shape per size class by timing (256-cell tiles on
+256-thread blocks, or 32 x 32 tiles on 1024-thread blocks, which the large
+members run in a second launch of the step).
 """
 from __future__ import annotations
 
@@ -20,8 +22,9 @@ import torch
 from . import capi
 from .level import Level
 
-SHAPES = (capi.HX_TILE_32x8, capi.HX_TILE_16x16, capi.HX_TILE_64x4)
-SHAPE_NAMES = {capi.HX_TILE_32x8: "32x8", capi.HX_TILE_16x16: "16x16", capi.HX_TILE_64x4: "64x4"}
+SHAPES = (capi.HX_TILE_32x8, capi.HX_TILE_16x16, capi.HX_TILE_64x4, capi.HX_TILE_32x32)
+SHAPE_NAMES = {capi.HX_TILE_32x8: "32x8", capi.HX_TILE_16x16: "16x16", capi.HX_TILE_64x4: "64x4",
+               capi.HX_TILE_32x32: "32x32"}
 # size classes by level side: small, medium, large
 CLASS_EDGES = (128, 384)
 
@@ -113,7 +116,8 @@ def autotune(cases, device="cuda", steps=6, cfl=0.45, use_cache=True, verbose=Fa
     ensemble kernel on the members of each class with every candidate shape.
     Results are cached per GPU name."""
     dev = torch.device(device)
-    key = torch.cuda.get_device_name(dev)
+    # the candidate set is part of the key: a cache written for other shapes is not reused
+    key = "%s|%s" % (torch.cuda.get_device_name(dev), ",".join(SHAPE_NAMES[x] for x in SHAPES))
     path = _cache_path()
     if use_cache and path.exists():
         try:

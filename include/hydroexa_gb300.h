@@ -416,7 +416,10 @@ void hx_host_cache_release(void);
  * (which advances one hierarchy per process); per member the arithmetic is
  * exactly that of hx_level_run_f64.
  */
-enum { HX_TILE_32x8 = 0, HX_TILE_16x16 = 1, HX_TILE_64x4 = 2 };
+/* Tile shapes: 256-cell tiles on 256-thread blocks, several per SM, for small
+ * and medium members; HX_TILE_32x32 on 1024-thread blocks, one per SM, for
+ * large members (fewer halo cells, slopes and faces per cell). */
+enum { HX_TILE_32x8 = 0, HX_TILE_16x16 = 1, HX_TILE_64x4 = 2, HX_TILE_32x32 = 3 };
 
 typedef struct hx_ensemble_member_f64 {
     hx_level_f64 level; /* state (advanced in place, see final_in_alt), terrain, geometry, BC codes */

@@ -23,7 +23,7 @@ def members():
 
 
 @pytest.mark.parametrize("arith", [capi.HX_ARITH_EXACT, capi.HX_ARITH_FAST])
-@pytest.mark.parametrize("shape", [capi.HX_TILE_32x8, capi.HX_TILE_16x16, capi.HX_TILE_64x4])
+@pytest.mark.parametrize("shape", [capi.HX_TILE_32x8, capi.HX_TILE_16x16, capi.HX_TILE_64x4, capi.HX_TILE_32x32])
 def test_ensemble_equals_member_runs(cuda, hxlib, arith, shape):
     cases = members()
     nsteps = 13  # two graph periods of six steps plus one direct launch
@@ -38,12 +38,22 @@ def test_ensemble_equals_member_runs(cuda, hxlib, arith, shape):
 
 
 def test_ensemble_without_graph_and_mixed_shapes(cuda, hxlib):
+    """Mixed shapes, the 32 x 32 members in the step's second launch among them,
+    with and without graphs: the same states."""
     cases = members()
     a = Ensemble(cases, device=cuda, shapes=[0, 1, 2, 1, 0])
     b = Ensemble(cases, device=cuda, shapes=[2, 2, 0, 0, 1])
+    c = Ensemble(cases, device=cuda, shapes=[3, 1, 3, 0, 3])
     assert a.run(8, 0.45, use_graph=False) == [0] * 5
     assert b.run(8, 0.45, use_graph=True) == [0] * 5
-    for x, y in zip(a.states(), b.states()):
+    assert c.run(8, 0.45, use_graph=False) == [0] * 5
+    for x, y, z in zip(a.states(), b.states(), c.states()):
+        assert torch.equal(x, y) and torch.equal(x, z)
+    d = Ensemble(cases, device=cuda, shapes=[3, 3, 0, 3, 2])
+    assert d.run(13, 0.45, use_graph=True) == [0] * 5
+    e = Ensemble(cases, device=cuda, shapes=[0] * 5)
+    assert e.run(13, 0.45, use_graph=True) == [0] * 5
+    for x, y in zip(d.states(), e.states()):
         assert torch.equal(x, y)
 
 
@@ -64,7 +74,7 @@ def test_autotune_picks_a_shape_per_class(cuda, hxlib, tmp_path, monkeypatch):
     monkeypatch.setenv("HX_CACHE_DIR", str(tmp_path))
     cases = workloads.ensemble(count=12, seed=9, smax=512)
     per_class, report = autotune(cases, device=cuda, steps=6)
-    assert len(per_class) == 3 and all(s in (0, 1, 2) for s in per_class)
+    assert len(per_class) == 3 and all(s in (0, 1, 2, 3) for s in per_class)
     again, _ = autotune(cases, device=cuda, steps=6)  # served from the cache
     assert again == per_class
     assert np.isfinite(list(report["timings_ms"].values())).all()

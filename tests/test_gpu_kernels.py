@@ -163,13 +163,14 @@ def test_box_form_matches_level_form(cuda, hxlib, oracle_lib):
     mn, _ = oracle_lib.compute_dt(L, h, hu, hv, case.z)
     dt = mn * case.cfl
     (rh, rhu, rhv), F = oracle_lib.advance(L, 1, h, hu, hv, case.z, case.n, dt, faces=True)
-    # ghost-filled arrays (2 ghosts) exactly as FillPatch + HydroPhysBC leave them
+    # ghost-filled arrays (2 ghosts) exactly as FillPatch + HydroPhysBC leave them: the momenta are filled with
+    # BC-record offset 0 (include/utils/FillPatchUtils.H:128-129), hu with the depth's record, hv with hu's
     G = 2
     eta = h + case.z
     ext = lambda a, mode_x, mode_y: _bc_ext(a, G, mode_x, mode_y)
     eta_e = ext(eta, "even", "even")
-    hu_e = ext(hu, "odd", "even")
-    hv_e = ext(hv, "even", "odd")
+    hu_e = ext(hu, "even", "even")
+    hv_e = ext(hv, "odd", "even")
     z_e = ext(case.z, "edge", "edge")
     n_e = ext(case.n, "edge", "edge")
     dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(cuda)
@@ -260,8 +261,8 @@ def test_hydrostatic_reflux_flux_from_the_advance(cuda, hxlib, oracle_lib):
     G = 2
     dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(cuda)
     Eta = dev(_bc_ext(h + case.z, G, "even", "even")[None])
-    Uext = dev(np.stack([np.zeros((g.ny + 2 * G, g.nx + 2 * G)), _bc_ext(hu, G, "odd", "even"),
-                         _bc_ext(hv, G, "even", "odd")]))
+    Uext = dev(np.stack([np.zeros((g.ny + 2 * G, g.nx + 2 * G)), _bc_ext(hu, G, "even", "even"),
+                         _bc_ext(hv, G, "odd", "even")]))  # the reference FillPatch's records (offset 0)
     Text = dev(np.stack([_bc_ext(case.z, G, "edge", "edge"), _bc_ext(case.n, G, "edge", "edge")]))
     Uold = dev(np.stack([h, hu, hv]))
     Unew = torch.zeros_like(Uold)
@@ -292,8 +293,8 @@ def test_classic_box_form_and_reflux_selection(cuda, hxlib, oracle_lib):
 
     def inputs():
         Eta = dev(_bc_ext(h + case.z, G, "even", "even")[None])
-        Uold = dev(np.stack([np.zeros((g.ny + 2 * G, g.nx + 2 * G)), _bc_ext(hu, G, "odd", "even"),
-                             _bc_ext(hv, G, "even", "odd")]))
+        Uold = dev(np.stack([np.zeros((g.ny + 2 * G, g.nx + 2 * G)), _bc_ext(hu, G, "even", "even"),
+                             _bc_ext(hv, G, "odd", "even")]))  # the reference FillPatch's records (offset 0)
         T = dev(np.stack([_bc_ext(case.z, G, "edge", "edge"), _bc_ext(case.n, G, "edge", "edge")]))
         return Eta, Uold, T
 
