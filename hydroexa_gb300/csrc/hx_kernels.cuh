@@ -274,13 +274,35 @@ struct FaceRec {
 // regions of uniform state (a lake at rest, the still water ahead of a wave)
 // is all warps but one.  Cell k of thread t is candidate number k * NTv + t.
 // Every thread of the block must call it.
-template <int NTv, int K = 1>
+// The threads that run one tile body together.  BlockSync: the whole block,
+// barrier 0.  HalfSync: one of the two 512-thread halves of a 1024-thread
+// block (warps 0-15 or 16-31), with its own named barrier 1 + g, so that the
+// halves step through their tiles' phases independently; slot() picks the
+// half's copy of the body's shared reduction scratch.
+struct BlockSync {
+    __device__ __forceinline__ int tid() const { return threadIdx.x; }
+    __device__ __forceinline__ void bar() const { __syncthreads(); }
+    __device__ __forceinline__ int slot() const { return 0; }
+};
+struct HalfSync {
+    int g;  // 0 or 1
+    __device__ __forceinline__ int tid() const { return threadIdx.x & 511; }
+    __device__ __forceinline__ void bar() const { asm volatile("bar.sync %0, 512;" ::"r"(1 + g) : "memory"); }
+    __device__ __forceinline__ int slot() const { return g; }
+};
+
+template <int NTv, int K = 1, class Sync = BlockSync>
 __device__ __forceinline__ void screened_fold(const ScreenCell<double>* c, double dx, double dy, double idx,
-                                              double idy, double& rate, double& mv, unsigned& flags) {
-    __shared__ float s_r[NTv / 32], s_m[NTv / 32];
-    __shared__ int s_rep;
-    __shared__ long long s_bits[3];
-    const int t = threadIdx.x;
+                                              double idy, double& rate, double& mv, unsigned& flags,
+                                              const Sync& sy = Sync{}) {
+    __shared__ float s_r_all[2][NTv / 32], s_m_all[2][NTv / 32];
+    __shared__ int s_rep_all[2];
+    __shared__ long long s_bits_all[2][3];
+    float* s_r = s_r_all[sy.slot()];
+    float* s_m = s_m_all[sy.slot()];
+    int& s_rep = s_rep_all[sy.slot()];
+    long long* s_bits = s_bits_all[sy.slot()];
+    const int t = sy.tid();
     bool wet[K], bad[K];
     float r32[K], m32[K], wr = 0.f, wm = 0.f;
 #pragma unroll
@@ -313,7 +335,7 @@ __device__ __forceinline__ void screened_fold(const ScreenCell<double>* c, doubl
     }
     if (t == 0) s_rep = K * NTv;
     if ((t & 31) == 0) { s_r[t >> 5] = wr; s_m[t >> 5] = wm; }
-    __syncthreads();
+    sy.bar();
     float br = 0.f, bm = 0.f;
 #pragma unroll
     for (int k = 0; k < NTv / 32; ++k) { br = fmaxf(br, s_r[k]); bm = fmaxf(bm, s_m[k]); }
@@ -324,12 +346,12 @@ __device__ __forceinline__ void screened_fold(const ScreenCell<double>* c, doubl
         cand[k] = bad[k] || (wet[k] && (r32[k] >= kr || m32[k] >= km));
         if (cand[k]) atomicMin(&s_rep, k * NTv + t);
     }
-    __syncthreads();
+    sy.bar();
     const int rep = s_rep;
 #pragma unroll
     for (int k = 0; k < K; ++k)
         if (k * NTv + t == rep) { s_bits[0] = sbits(c[k].h); s_bits[1] = sbits(c[k].hu); s_bits[2] = sbits(c[k].hv); }
-    __syncthreads();
+    sy.bar();
 #pragma unroll
     for (int k = 0; k < K; ++k) {
         const bool same = k * NTv + t != rep && sbits(c[k].h) == s_bits[0] && sbits(c[k].hu) == s_bits[1] &&
@@ -361,18 +383,19 @@ struct NoHooks {
 };
 
 template <class R, bool FAST, int TXv, int TYv, int NTv, class Src, bool LINEAR = false, class Div = NoDiv,
-          class Rec = NoRec, class UO = Cells3<R>, class NP = Plane<R>, class Hooks = NoHooks>
+          class Rec = NoRec, class UO = Cells3<R>, class NP = Plane<R>, class Hooks = NoHooks, class Sync = BlockSync>
 __device__ __forceinline__ void hydro_tile_body(HydroSmem<R, TXv, TYv>& S, const Src& src, const UO& uo,
                                                 const NP& nplane, const Cells3W<R>& out, const FaceOut<R>& fo,
                                                 const IBox& vb, int x0, int y0, R dt, R dx, R dy, DtAccum* dt_out,
                                                 unsigned* status, unsigned* post_flags = nullptr,
                                                 const Div& div = Div{}, const Rec& rec = Rec{},
-                                                const Hooks& hooks = Hooks{}, ThreadFold<R>* defer = nullptr) {
+                                                const Hooks& hooks = Hooks{}, ThreadFold<R>* defer = nullptr,
+                                                const Sync& sy = Sync{}) {
     static_assert(!Rec::on || (FAST && sizeof(R) == 8), "face records are kept for the FP64 fast form");
     constexpr int GX = HydroSmem<R, TXv, TYv>::GX, GY = HydroSmem<R, TXv, TYv>::GY;
     constexpr int CELLS = TXv * TYv;
-    const int t = threadIdx.x;
-    __syncthreads();  // the previous tile of this block is done with S
+    const int t = sy.tid();
+    sy.bar();  // the previous tile of this block is done with S
     if (t == 0) {     // read after the barriers below
         S.kc[0] = dt / dx;
         S.kc[1] = dt / dy;
@@ -404,7 +427,7 @@ __device__ __forceinline__ void hydro_tile_body(HydroSmem<R, TXv, TYv>& S, const
         S.v[r][c] = vv;
     }
     hooks.after_load();
-    __syncthreads();
+    sy.bar();
 
     // --- B: van Leer slopes, once per cell and direction ---------------------
     auto xslopes = [&](int row, int col) {  // tile cell (col, row), col in -1..TXv
@@ -454,7 +477,7 @@ __device__ __forceinline__ void hydro_tile_body(HydroSmem<R, TXv, TYv>& S, const
             yslopes((m < TXv) ? -1 : TYv, m % TXv);                // rows -1 and TY
         }
     }
-    __syncthreads();
+    sy.bar();
 
     // --- C: faces.  The x face at the left of each cell and the y face below
     // it, then the right column and the top row. ------------------------------
@@ -503,15 +526,26 @@ __device__ __forceinline__ void hydro_tile_body(HydroSmem<R, TXv, TYv>& S, const
         if (gi <= vb.hi0 + 1 && gj <= vb.hi1) xface(tx, ty);
         if (gi <= vb.hi0 && gj <= vb.hi1 + 1) yface(tx, ty);
     }
-    for (int k = t; k < TYv + TXv; k += NTv) {
-        if (k < TYv) {
-            if (x0 + TXv <= vb.hi0 + 1 && y0 + k <= vb.hi1) xface(TXv, k);
-        } else {
-            const int m = k - TYv;
-            if (x0 + m <= vb.hi0 && y0 + TYv <= vb.hi1 + 1) yface(m, TYv);
+    // the right column and the top row: where the tile leaves enough threads without a cell, those take them
+    // (two faces at most, as every other thread), so that no thread computes a third face while the rest wait
+    constexpr int SPARE = NTv - CELLS;
+    if constexpr (SPARE >= TXv && SPARE >= TYv) {
+        const int e = t - CELLS;
+        if (e >= 0) {
+            if (e < TYv && x0 + TXv <= vb.hi0 + 1 && y0 + e <= vb.hi1) xface(TXv, e);
+            if (e < TXv && x0 + e <= vb.hi0 && y0 + TYv <= vb.hi1 + 1) yface(e, TYv);
+        }
+    } else {
+        for (int k = t; k < TYv + TXv; k += NTv) {
+            if (k < TYv) {
+                if (x0 + TXv <= vb.hi0 + 1 && y0 + k <= vb.hi1) xface(TXv, k);
+            } else {
+                const int m = k - TYv;
+                if (x0 + m <= vb.hi0 && y0 + TYv <= vb.hi1 + 1) yface(m, TYv);
+            }
         }
     }
-    __syncthreads();
+    sy.bar();
     hooks.after_faces();
 
     // --- D: update, Manning friction, dry clamp (HydrostaticRoe.cpp:551-604) --
@@ -519,7 +553,7 @@ __device__ __forceinline__ void hydro_tile_body(HydroSmem<R, TXv, TYv>& S, const
     unsigned flags = 0, pflags = 0;
     const R cx = S.kc[0], cy = S.kc[1], idx = S.kc[2], idy = S.kc[3];
     // the FP64 fast form folds the next CFL bound through the float screen
-    constexpr bool SCREEN = FAST && sizeof(R) == 8 && CELLS == NTv && !LINEAR && !Div::on;
+    constexpr bool SCREEN = FAST && sizeof(R) == 8 && CELLS <= NTv && !LINEAR && !Div::on;  // at most a cell a thread
     const bool fold = dt_out != nullptr || defer != nullptr;
     ScreenCell<R> sc;
     for (int k = t; k < CELLS; k += NTv) {
@@ -542,7 +576,7 @@ __device__ __forceinline__ void hydro_tile_body(HydroSmem<R, TXv, TYv>& S, const
                                    pflags, (SCREEN && fold) ? &sc : nullptr);
     }
     if constexpr (SCREEN) {
-        if (fold) screened_fold<NTv>(&sc, dx, dy, idx, idy, rate, mv, flags);
+        if (fold) screened_fold<NTv, 1, Sync>(&sc, dx, dy, idx, idy, rate, mv, flags, sy);
     }
     if (defer) {
         if constexpr (FAST) {
@@ -618,19 +652,21 @@ __global__ void __launch_bounds__(TXH * TYH, min_ctas(TXH * TYH))
 // The next CFL bound is folded per thread across the block's tiles and into
 // the accumulator once.
 // ---------------------------------------------------------------------------
-constexpr int kPT = 32;       // tile side
-constexpr int kPG = kPT + 4;  // grown tile side (2-cell MUSCL halo)
+constexpr int kPX = 32, kPY = 32;              // tile
+constexpr int kPGX = kPX + 4, kPGY = kPY + 4;  // grown tile (2-cell MUSCL halo)
+constexpr int kPN = 1024;                      // threads of the block, one cell each at most
 struct PersistStaging {
-    double h[kPG][kPG], hu[kPG][kPG], hv[kPG][kPG], z[kPG][kPG];
-    double n[kPT][kPT];
+    double h[kPGY][kPGX], hu[kPGY][kPGX], hv[kPGY][kPGX], z[kPGY][kPGX];
+    double n[kPY][kPX];
 };
 struct PersistOwn {
-    double h[kPT * kPT], hu[kPT * kPT], hv[kPT * kPT], n[kPT * kPT];
-    ThreadFold<double> fold[kPT * kPT];  // each thread's share of the next CFL bound (kept out of registers)
+    double h[kPX * kPY], hu[kPX * kPY], hv[kPX * kPY], n[kPX * kPY];
+    ThreadFold<double> fold[kPN];  // each thread's share of the next CFL bound (kept out of registers)
 };
-static_assert(sizeof(PersistStaging) <= sizeof(double) * 6 * kPT * (kPT + 2),
+static_assert(kPX * kPY <= kPN, "one cell per thread at most");
+static_assert(sizeof(PersistStaging) <= sizeof(double) * 3 * (kPY * (kPX + 2) + (kPY + 2) * kPX),
               "the staging buffer must fit in the slope arrays it lies on");
-constexpr size_t persist_smem_bytes() { return sizeof(HydroSmem<double, kPT, kPT>) + sizeof(PersistOwn); }
+constexpr size_t persist_smem_bytes() { return sizeof(HydroSmem<double, kPX, kPY>) + sizeof(PersistOwn); }
 
 __device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
     const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
@@ -642,8 +678,8 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // Issue the copies of tile (x0, y0) into st (every thread of the block).
 __device__ __forceinline__ void persist_stage(PersistStaging* st, const LevelSrc<double>& src, int x0, int y0) {
     const int t = threadIdx.x;
-    for (int idx = t; idx < kPG * kPG; idx += kPT * kPT) {
-        const int r = idx / kPG, c = idx - r * kPG;
+    for (int idx = t; idx < kPGX * kPGY; idx += kPN) {
+        const int r = idx / kPGX, c = idx - r * kPGX;
         const int gi = x0 - 2 + c, gj = y0 - 2 + r;
         if (gi < 0 || gi >= src.nx || gj < 0 || gj >= src.ny) continue;
         const long long o = (long long)gi + (long long)gj * src.pitch;
@@ -652,8 +688,9 @@ __device__ __forceinline__ void persist_stage(PersistStaging* st, const LevelSrc
         cp_async8(&st->hv[r][c], src.hv + o);
         cp_async8(&st->z[r][c], src.z + o);
     }
-    const int r = t / kPT, c = t % kPT, gi = x0 + c, gj = y0 + r;
-    if (gi < src.nx && gj < src.ny) cp_async8(&st->n[r][c], src.n + (long long)gi + (long long)gj * src.pitch);
+    const int r = t / kPX, c = t % kPX, gi = x0 + c, gj = y0 + r;
+    if (t < kPX * kPY && gi < src.nx && gj < src.ny)
+        cp_async8(&st->n[r][c], src.n + (long long)gi + (long long)gj * src.pitch);
     cp_async_commit();
 }
 
@@ -685,14 +722,14 @@ struct OwnState {
     const PersistOwn* o;
     int x0, y0;
     __device__ __forceinline__ double ld(int c, int i, int j) const {
-        const int k = (j - y0) * kPT + (i - x0);
+        const int k = (j - y0) * kPX + (i - x0);
         return c == 0 ? o->h[k] : (c == 1 ? o->hu[k] : o->hv[k]);
     }
 };
 struct OwnRough {
     const PersistOwn* o;
     int x0, y0;
-    __device__ __forceinline__ double ld(int i, int j) const { return o->n[(j - y0) * kPT + (i - x0)]; }
+    __device__ __forceinline__ double ld(int i, int j) const { return o->n[(j - y0) * kPX + (i - x0)]; }
 };
 struct PersistHooks {
     PersistStaging* st;
@@ -701,7 +738,8 @@ struct PersistHooks {
     int nx0, ny0;  // origin of the next tile
     bool next;
     __device__ __forceinline__ void after_load() const {
-        const int t = threadIdx.x, r = t / kPT + 2, c = t % kPT + 2;
+        const int t = threadIdx.x, r = t / kPX + 2, c = t % kPX + 2;
+        if (t >= kPX * kPY) return;
         own->h[t] = st->h[r][c];
         own->hu[t] = st->hu[r][c];
         own->hv[t] = st->hv[r][c];
@@ -716,12 +754,12 @@ struct PersistHooks {
 // cell instead of the update (the first step of the host-buffer call, whose
 // update waits for the level's dt): no dt, no CFL fold.
 template <bool FAST, class Div = NoDiv>
-__global__ void __launch_bounds__(kPT * kPT, 1)
+__global__ void __launch_bounds__(kPN, 1)
     k_hydro_persist(LevelSrc<double> src, Cells3W<double> out, IBox vb, int tiles_x, int ntiles,
                     StepCtl<double> ctl, Div div = Div{}) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    HydroSmem<double, kPT, kPT>& S = *reinterpret_cast<HydroSmem<double, kPT, kPT>*>(smem_raw);
-    PersistOwn* own = reinterpret_cast<PersistOwn*>(smem_raw + sizeof(HydroSmem<double, kPT, kPT>));
+    HydroSmem<double, kPX, kPY>& S = *reinterpret_cast<HydroSmem<double, kPX, kPY>*>(smem_raw);
+    PersistOwn* own = reinterpret_cast<PersistOwn*>(smem_raw + sizeof(HydroSmem<double, kPX, kPY>));
     PersistStaging* st = reinterpret_cast<PersistStaging*>(&S.sxe[0][0]);
     double dt = 0.0;
     if constexpr (!Div::on) {
@@ -731,24 +769,66 @@ __global__ void __launch_bounds__(kPT * kPT, 1)
     const bool fold = !Div::on && ctl.dt_out != nullptr;
     int k = (int)blockIdx.x;
     if (k >= ntiles) return;
-    persist_stage(st, src, vb.lo0 + (k % tiles_x) * kPT, vb.lo1 + (k / tiles_x) * kPT);
+    persist_stage(st, src, vb.lo0 + (k % tiles_x) * kPX, vb.lo1 + (k / tiles_x) * kPY);
     ThreadFold<double>* tf = &own->fold[threadIdx.x];
     *tf = ThreadFold<double>{};
     const FaceOut<double> fo{};
     for (; k < ntiles; k += (int)gridDim.x) {
-        const int x0 = vb.lo0 + (k % tiles_x) * kPT, y0 = vb.lo1 + (k / tiles_x) * kPT;
+        const int x0 = vb.lo0 + (k % tiles_x) * kPX, y0 = vb.lo1 + (k / tiles_x) * kPY;
         const int kn = k + (int)gridDim.x;
-        const PersistHooks hooks{st, own, &src, vb.lo0 + (kn % tiles_x) * kPT, vb.lo1 + (kn / tiles_x) * kPT,
+        const PersistHooks hooks{st, own, &src, vb.lo0 + (kn % tiles_x) * kPX, vb.lo1 + (kn / tiles_x) * kPY,
                                  kn < ntiles};
         const StagedSrc ss{st, x0, y0, src.nx, src.ny, src.bc_xlo, src.bc_xhi, src.bc_ylo, src.bc_yhi,
                            src.glo0, src.glo1, src.ghi0, src.ghi1};
         cp_async_wait_all();  // this thread's copies of tile k; the body's first barrier publishes everyone's
-        hydro_tile_body<double, FAST, kPT, kPT, kPT * kPT, StagedSrc, false, Div, NoRec, OwnState, OwnRough,
+        hydro_tile_body<double, FAST, kPX, kPY, kPN, StagedSrc, false, Div, NoRec, OwnState, OwnRough,
                         PersistHooks>(S, ss, OwnState{own, x0, y0}, OwnRough{own, x0, y0}, out, fo, vb, x0, y0, dt,
                                       ctl.dx, ctl.dy, nullptr, Div::on ? nullptr : ctl.status, nullptr, div,
                                       NoRec{}, hooks, fold ? tf : nullptr);
     }
-    if (fold) block_fold_dt<double, kPT * kPT>(tf->rate, tf->mv, tf->flags, ctl.dt_out);
+    if (fold) block_fold_dt<double, kPN>(tf->rate, tf->mv, tf->flags, ctl.dt_out);
+}
+
+// ---------------------------------------------------------------------------
+// The FP64 level step with two tiles in flight per SM: a 1024-thread block of
+// two independent 512-thread halves, each walking its own 32 x 16 tiles
+// (tile 2 b + g, then + 2 gridDim.x) with its own named barrier, so that one
+// half's FP64 work fills the pipe while the other waits at a barrier, on its
+// loads, or in the unbalanced tail of a phase.  Same arithmetic per cell as
+// k_hydro_tile; the CFL bound is folded per thread across tiles and into the
+// accumulator once per block.
+// ---------------------------------------------------------------------------
+constexpr int kHX = 32, kHY = 16;
+constexpr size_t persist2_smem_bytes() {
+    return 2 * sizeof(HydroSmem<double, kHX, kHY>) + 1024 * sizeof(ThreadFold<double>);
+}
+
+template <bool FAST>
+__global__ void __launch_bounds__(1024, 1)
+    k_hydro_persist2(LevelSrc<double> src, Cells3<double> uo, Plane<double> np, Cells3W<double> out, IBox vb,
+                     int tiles_x, int ntiles, StepCtl<double> ctl) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int g = (int)(threadIdx.x >> 9);
+    HydroSmem<double, kHX, kHY>& S =
+        *reinterpret_cast<HydroSmem<double, kHX, kHY>*>(smem_raw + g * sizeof(HydroSmem<double, kHX, kHY>));
+    ThreadFold<double>* tf =
+        reinterpret_cast<ThreadFold<double>*>(smem_raw + 2 * sizeof(HydroSmem<double, kHX, kHY>)) + threadIdx.x;
+    double dt;
+    if (!resolve_dt(ctl, dt)) return;
+    step_bookkeeping(ctl, dt);
+    *tf = ThreadFold<double>{};
+    const bool fold = ctl.dt_out != nullptr;
+    const FaceOut<double> fo{};
+    const HalfSync sy{g};
+    for (int k = 2 * (int)blockIdx.x + g; k < ntiles; k += 2 * (int)gridDim.x) {
+        const int x0 = vb.lo0 + (k % tiles_x) * kHX, y0 = vb.lo1 + (k / tiles_x) * kHY;
+        hydro_tile_body<double, FAST, kHX, kHY, kHX * kHY, LevelSrc<double>, false, NoDiv, NoRec, Cells3<double>,
+                        Plane<double>, NoHooks, HalfSync>(S, src, uo, np, out, fo, vb, x0, y0, dt, ctl.dx, ctl.dy,
+                                                          nullptr, ctl.status, nullptr, NoDiv{}, NoRec{}, NoHooks{},
+                                                          fold ? tf : nullptr, sy);
+    }
+    __syncthreads();
+    if (fold) block_fold_dt<double, 1024>(tf->rate, tf->mv, tf->flags, ctl.dt_out);
 }
 
 // ---------------------------------------------------------------------------
@@ -1404,7 +1484,7 @@ cudaError_t launch_hydro(const Src& src, const Cells3<R>& uo, const Plane<R>& np
         if (big_tile<R>(vb) && !fo.on && !fo.mean && uo.p[0] == src.h && uo.p[1] == src.hu && uo.p[2] == src.hv &&
             uo.js == src.pitch && uo.lo0 == 0 && uo.lo1 == 0 && np.p == src.n && np.js == src.pitch &&
             np.lo0 == 0 && np.lo1 == 0) {
-            const dim3 tg = tile_grid(vb, kPT, kPT);
+            const dim3 tg = tile_grid(vb, kPX, kPY);
             const int ntiles = (int)(tg.x * tg.y);
             int dev = 0, sms = 0;
             cudaError_t e = cudaGetDevice(&dev);
@@ -1413,8 +1493,8 @@ cudaError_t launch_hydro(const Src& src, const Cells3<R>& uo, const Plane<R>& np
             auto k = k_hydro_persist<FAST>;
             e = ensure_smem(k, persist_smem_bytes());
             if (e != cudaSuccess) return e;
-            k<<<(unsigned)(ntiles < sms ? ntiles : sms), kPT * kPT, persist_smem_bytes(), st>>>(src, out, vb, (int)tg.x,
-                                                                                              ntiles, ctl, NoDiv{});
+            k<<<(unsigned)(ntiles < sms ? ntiles : sms), kPN, persist_smem_bytes(), st>>>(src, out, vb, (int)tg.x,
+                                                                                        ntiles, ctl, NoDiv{});
             return cudaGetLastError();
         }
     }
@@ -1494,7 +1574,7 @@ cudaError_t launch_hydro_split(const LevelSrc<R>& src, const Cells3<R>& uo, cons
                                const IBox& vb, R dx, R dy, cudaStream_t st) {
     if constexpr (std::is_same_v<R, double>) {
         if (big_tile<R>(vb) && uo.p[0] == src.h && uo.p[1] == src.hu && uo.p[2] == src.hv) {
-            const dim3 tg = tile_grid(vb, kPT, kPT);
+            const dim3 tg = tile_grid(vb, kPX, kPY);
             const int ntiles = (int)(tg.x * tg.y);
             int dev = 0, sms = 0;
             cudaError_t e = cudaGetDevice(&dev);
@@ -1507,7 +1587,7 @@ cudaError_t launch_hydro_split(const LevelSrc<R>& src, const Cells3<R>& uo, cons
             ctl.dx = dx;
             ctl.dy = dy;
             (void)np;
-            k<<<(unsigned)(ntiles < sms ? ntiles : sms), kPT * kPT, persist_smem_bytes(), st>>>(
+            k<<<(unsigned)(ntiles < sms ? ntiles : sms), kPN, persist_smem_bytes(), st>>>(
                 src, Cells3W<double>{}, vb, (int)tg.x, ntiles, ctl, div);
             return cudaGetLastError();
         }
