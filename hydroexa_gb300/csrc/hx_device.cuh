@@ -270,23 +270,23 @@ __host__ __device__ __forceinline__ double fast_sqrt(double x) {
     return sqrt(x);
 #endif
 }
-// sqrt(x) as fast_sqrt (same bits) and, for one more FMA, 1/sqrt(x) from the
-// same correction: r0 (1 + d/2 + 3 d^2/8), within about an ulp.  x must be a
-// positive normal double inside the float exponent range (a depth above the
-// dry tolerance, times g).
-__device__ __forceinline__ double fast_sqrt_rsqrt(double x, double& rsq) {
+// sqrt(x) as fast_sqrt (same bits) and, for one more FMA, half the reciprocal
+// square root 1/(2 sqrt(x)) from the same correction: (r0/2) (1 + d/2 +
+// 3 d^2/8), the halved seed being exact, within about an ulp.  x must be a
+// positive normal double (a depth above the dry tolerance, times g).
+__device__ __forceinline__ double fast_sqrt_hrsqrt(double x, double& hrsq) {
     if (!in_f32_range(x)) {
         const double s = sqrt(x);
-        rsq = 1.0 / s;
+        hrsq = 0.5 / s;
         return s;
     }
     float rf;
     asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(rf) : "f"(f32_lead(x)));
-    const double r0 = f64_widen(rf);
+    const double r0 = f64_widen(rf), r0h = f64_widen(rf * 0.5f);
     const double t = x * r0;
     const double d = fma(-t, r0, 1.0);
     const double dp = d * fma(0.375, d, 0.5);
-    rsq = fma(r0, dp, r0);
+    hrsq = fma(r0h, dp, r0h);
     return fma(t, dp, t);
 }
 __host__ __device__ __forceinline__ float fast_sqrt(float x) {
@@ -434,26 +434,27 @@ __host__ __device__ __forceinline__ void roe_hydrostatic_fast(R hi, R ui, R vi, 
     const R hh = R(0.5) * (hi + hj);
     const bool hmb = gt_bits(hh, C::toldry_bits);
     const R hm = hmb ? hh : C::toldry;
-    R cm, rcm;
+    R cm, hrcm;  // hrcm = 1 / (2 cm)
+    const R sden = si + sj + C::tol12;
+    // FP64: one reciprocal 1 / (2 sden den) = q/2 for 1/sden and 1/(2 den), 1/(2 cm) from cm's square root
+    // (den = 2 cm + tol12 and 2 den = 4 cm + 2 tol12 exactly, so every value is that of q = 1/(sden den));
+    // float: one reciprocal for all three
+    R q, rs, hrden;
     if constexpr (sizeof(R) == 8) {
-        cm = fast_sqrt_rsqrt(C::g * hm, rcm);  // 1/cm from the square root's own correction
+        cm = fast_sqrt_hrsqrt(C::g * hm, hrcm);
+        const R den2 = R(4) * cm + R(2) * C::tol12;
+        const R hq = rcp_nr(sden * den2);
+        rs = den2 * hq;
+        hrden = sden * hq;
+        q = hq + hq;
     } else {
         cm = fast_sqrt(C::g * hm);
-    }
-    const R den = R(2) * cm + C::tol12;
-    const R sden = si + sj + C::tol12;
-    // one reciprocal for 1/sden and 1/den (FP64; float shares it with 1/cm too)
-    R q, rs, rden;
-    if constexpr (sizeof(R) == 8) {
-        q = rcp_nr(sden * den);
-        rs = den * q;
-        rden = sden * q;
-    } else {
+        const R den = R(2) * cm + C::tol12;
         const R cd = cm * den;
         q = rcp_nr(sden * cd);
         rs = cd * q;
-        rden = (sden * cm) * q;
-        rcm = (sden * den) * q;
+        hrden = R(0.5) * ((sden * cm) * q);
+        hrcm = R(0.5) * ((sden * den) * q);
     }
     const R um = (uni * si + unj * sj) * rs;
     const R vm = (uti * si + utj * sj) * rs;
@@ -488,9 +489,8 @@ __host__ __device__ __forceinline__ void roe_hydrostatic_fast(R hi, R ui, R vi, 
     const R qi = hi * uni, qj = hj * unj;
     const R dhu = qj - qi;
     const R dhv = hj * utj - hi * uti;
-    const R hrden = R(0.5) * rden;
     const R a0h = (l2 * dh - dhu) * hrden;  // alpha0 / 2
-    const R a1h = (dhv - vm * dh) * (R(0.5) * rcm);
+    const R a1h = (dhv - vm * dh) * hrcm;
     const R a2h = (dhu - l0 * dh) * hrden;
     const R w0 = fabs(l0) * a0h;
     const R w1 = fabs(l1) * a1h;

@@ -53,11 +53,23 @@ __device__ __forceinline__ void hydro_face(bool wall, R zL, R zR, R eL, R eR, R 
     const R vLf = vL + R(0.5) * svL;
     const R vRf = vR - R(0.5) * svR;
     R hLu, hRu, hLs, hRs;
+    R pW = R(0);       // fast form: the pressure correction of the lower-bed side (the other side's is 0)
+    bool lhigh = false;  // fast form: the left bed is the face bed
     if constexpr (FAST) {
-        hLu = max0_i(etaLf - zL);
-        hRu = max0_i(etaRf - zR);
-        hLs = max0_i(etaLf - zf);
-        hRs = max0_i(etaRf - zf);
+        // The side whose bed is the face bed zf has its capped depth equal to its own (uncapped) one, so its
+        // pressure correction is exactly +0: only the lower side's depths and correction are computed, and
+        // the results are those of computing both (bit for bit).
+        lhigh = !(okey(zL) < okey(zR));  // zf == zL
+        const R eH = lhigh ? etaLf : etaRf, zH = lhigh ? zL : zR;
+        const R eW = lhigh ? etaRf : etaLf, zW = lhigh ? zR : zL;
+        const R hH = max0_i(eH - zH);
+        const R hWu = max0_i(eW - zW), hWs = max0_i(eW - zf);
+        // (a^2 - b^2) = (a - b)(a + b) is exactly zero whenever a == b (lake at rest)
+        pW = Cst<R>::half_g * ((hWu - hWs) * (hWu + hWs));
+        hLu = lhigh ? hH : hWu;
+        hLs = lhigh ? hH : hWs;
+        hRu = lhigh ? hWu : hH;
+        hRs = lhigh ? hWs : hH;
     } else {
         hLu = max0(etaLf - zL);
         hRu = max0(etaRf - zR);
@@ -80,9 +92,10 @@ __device__ __forceinline__ void hydro_face(bool wall, R zL, R zR, R eL, R eR, R 
         pL = Cst<R>::half_g * (hLu * hLu - hLs * hLs);
         pR = Cst<R>::half_g * (hRu * hRu - hRs * hRs);
     } else {
-        // (a^2 - b^2) = (a - b)(a + b) is exactly zero whenever a == b (lake at rest)
-        pL = Cst<R>::half_g * ((hLu - hLs) * (hLu + hLs));
-        pR = Cst<R>::half_g * ((hRu - hRs) * (hRu + hRs));
+        pL = lhigh ? R(0) : pW;
+        pR = lhigh ? pW : R(0);
+        (void)hLu;
+        (void)hRu;
     }
     F0 = f0;
     if (DIR == 0) { Fa = f1 + pL; Fb = f1 + pR; Fc = f2; }
