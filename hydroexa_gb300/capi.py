@@ -29,6 +29,11 @@ HX_METHOD_HYDROSTATIC_ROE = 1
 HX_BC_REFLECTIVE = 0
 HX_BC_TRANSMISSIVE = 1
 HX_BC_CLOSED_WALL = 2
+HX_FAST_OP_RCP = 0
+HX_FAST_OP_SQRT = 1
+HX_FAST_OP_SLOPE = 2
+HX_FAST_OP_RCP_FAITHFUL = 3
+HX_FAST_OP_SQRT_FAITHFUL = 4
 
 
 class HxError(RuntimeError):
@@ -140,6 +145,7 @@ def _declare(L):
                                                             c_void_p]
     L.hx_debug_rcp_f64.argtypes = [c_long, c_void_p, c_void_p, c_void_p]
     L.hx_debug_sqrt_f64.argtypes = [c_long, c_void_p, c_void_p, c_void_p]
+    L.hx_debug_fast_op_f64.argtypes = [c_int, c_long, c_void_p, c_void_p, c_void_p]
     L.hx_debug_host_bands.argtypes = [c_int, c_void_p, c_int]
     L.hx_status_clear.argtypes = [c_void_p, c_void_p]
     L.hx_status_read.argtypes = [c_void_p, c_void_p]
@@ -223,7 +229,8 @@ EXPORTED = [
     "hx_level_advance_f64",
     "hx_level_advance_f32", "hx_level_dt_reduce_f64", "hx_level_dt_reduce_f32", "hx_level_run_work_bytes",
     "hx_level_run_f64", "hx_level_run_f32", "hx_level_run_host_f64", "hx_host_cache_release",
-    "hx_debug_roe_points_f64", "hx_debug_roe_points_f32", "hx_debug_rcp_f64", "hx_debug_sqrt_f64", "hx_debug_host_bands",
+    "hx_debug_roe_points_f64", "hx_debug_roe_points_f32", "hx_debug_rcp_f64", "hx_debug_sqrt_f64", "hx_debug_fast_op_f64",
+    "hx_debug_host_bands",
     "hx_level_run_static_f64",
     "hx_ensemble_work_bytes", "hx_ensemble_tiles", "hx_ensemble_run_f64",
     "hx_adjoint_work_bytes_f64", "hx_adjoint_recompute_steps", "hx_adjoint_forward_f64", "hx_adjoint_reverse_f64", "hx_adjoint_step_f64",

@@ -32,6 +32,8 @@ template <> struct Cst<double> {
     // IEEE bit patterns of the positive tolerances (for integer comparisons)
     static constexpr long long toldry_bits = 0x3eb0c6f7a0b5ed8dll;
     static constexpr long long tol12_bits = 0x3d719799812dea11ll;
+    static constexpr long long toldry2_bits = 0x3ec0c6f7a0b5ed8dll;  // 2 toldry
+    static constexpr double g_toldry = 9.81 * 1e-6;                  // g toldry, rounded once
     static constexpr double max_value = 1.7976931348623157e308;  // std::numeric_limits<double>::max()
 };
 template <> struct Cst<float> {
@@ -43,6 +45,8 @@ template <> struct Cst<float> {
     static constexpr float tol10 = 1e-10f;
     static constexpr int toldry_bits = 0x358637bd;
     static constexpr int tol12_bits = 0x2b8cbccc;
+    static constexpr int toldry2_bits = 0x360637bd;
+    static constexpr float g_toldry = 9.81f * 1e-6f;
     static constexpr float max_value = 3.40282347e38f;  // std::numeric_limits<float>::max()
 };
 
@@ -185,52 +189,61 @@ __host__ __device__ __forceinline__ bool in_f32_range(double x) {
     return e > -120 && e < 120;
 }
 
-// Reciprocal of a finite normal x by one third-order Newton step on
-// f(y) = 1/y - x from a seed y0 of relative error d: with e = 1 - x y0,
-// y0 + y0 (e + e^2) has error of order d^3 (Householder's method of order 3;
-// see Markstein, IBM J. Res. Dev. 34, 1990, for the FMA formulation of these
-// iterations): three FMAs instead of a full IEEE division.  The seed is the
-// float estimate rcp.approx.ftz.f32 of the leading bits of x, widened on the
-// integer pipe, so that only the three FMAs issue on the FP64 pipe (d < 2^-21,
-// error ~2^-63 before the last rounding); outside the float range the FP64
-// estimate rcp.approx.ftz.f64 seeds the same step.  Faithful (within an ulp),
-// as the tests check against IEEE division; callers pass finite normal
-// arguments only.
+// FP64 reciprocal and square root of the fast form.  Each starts from a float
+// estimate (rcp.approx.ftz.f32 / rsqrt.approx.ftz.f32) of the leading 24
+// significand bits, widened to a double on the integer pipe, so only the
+// correction steps issue on the FP64 pipe (GB300 issues FP64 at 1/64 of its
+// FP32 rate).  The seeds carry a relative error delta below 2^-21.5.
+//
+// The flux arithmetic takes ONE Newton step, whose error is of order delta^2
+// (below 2^-42 relative, typically ~2^-46): two FMAs for 1/x, three FP64
+// instructions for sqrt(x).  A face flux built from them differs from the
+// IEEE-rounded one by a few parts in 1e14 of its terms, inside the fast form's
+// 1e-12-per-step bound with two orders of magnitude to spare, and the rounding
+// of the exact form is not what the fast form reproduces anyway.
+//
+// The CFL rate takes the third-order step (Householder's method of order 3;
+// Markstein, IBM J. Res. Dev. 34, 1990, gives the FMA formulation), within an
+// ulp: the time step stays that of the exact form to the last few ulps.  It
+// runs once per candidate cell of the screened fold, not per face.
+
+// The double of a positive normal float f times 2^k with the sign bit sg, assembled on the integer pipe (the
+// exponent field must stay within 1..2046: the callers select another value where it would not).
+__device__ __forceinline__ double f64_of_f32_scaled(float f, int k, unsigned sg) {
+    const unsigned fb = (unsigned)__float_as_int(f);
+    const unsigned hi = sg | ((fb >> 3) + ((unsigned)(896 + k) << 20));
+    return __hiloint2double((int)hi, (int)(fb << 29));
+}
+// Float seed of 1/x for any normal double x below 2^1021 in magnitude: the
+// reciprocal of the significand's leading bits (a float in [1, 2)), with the
+// exponent and sign put back on the integer pipe.  No branch on the range.
+__device__ __forceinline__ double rcp_seed(double x) {
+    const unsigned hx = (unsigned)__double2hiint(x), lx = (unsigned)__double2loint(x);
+    const int ex = (int)((hx >> 20) & 0x7FFu);
+    float rf;
+    asm("rcp.approx.ftz.f32 %0, %1;"
+        : "=f"(rf)
+        : "f"(__int_as_float((int)(0x3F800000u | ((hx & 0xFFFFFu) << 3) | (lx >> 29)))));
+    return f64_of_f32_scaled(rf, 1023 - ex, hx & 0x80000000u);  // rf in (0.5, 1]
+}
+// 1/x, one Newton step: y0 (1 + e) with e = 1 - x y0.  Callers pass finite
+// normal arguments below 2^1021 in magnitude (depths, wave-speed sums).
 __host__ __device__ __forceinline__ double rcp_nr(double x) {
 #ifdef __CUDA_ARCH__
-    double y;
-    if (in_f32_range(x)) {
-        float yf;
-        asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(yf) : "f"(f32_lead(x)));
-        y = f64_widen(yf);
-    } else {
-        asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
-    }
-    const double e = fma(-x, y, 1.0);
-    return fma(y, fma(e, e, e), y);
+    const double y = rcp_seed(x);
+    return fma(y, fma(-x, y, 1.0), y);
 #else
     return 1.0 / x;
 #endif
 }
-// 2 / x, bit for bit 2 * rcp_nr(x): the doubled seed (exact) carried through
-// the same three FMAs, whose every rounding scales by 2 exactly.  Saves the
-// FP64 multiply or add that doubling the result would cost.
-__host__ __device__ __forceinline__ double rcp_nr_twice(double x) {
+// 1/x within an ulp (the CFL rate): y0 + y0 (e + e^2).
+__host__ __device__ __forceinline__ double rcp_fa(double x) {
 #ifdef __CUDA_ARCH__
-    double y, y2;
-    if (in_f32_range(x)) {
-        float yf;
-        asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(yf) : "f"(f32_lead(x)));
-        y = f64_widen(yf);
-        y2 = f64_widen(yf * 2.0f);
-    } else {
-        asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
-        y2 = y + y;
-    }
+    const double y = rcp_seed(x);
     const double e = fma(-x, y, 1.0);
-    return fma(y2, fma(e, e, e), y2);
+    return fma(y, fma(e, e, e), y);
 #else
-    return 2.0 / x;
+    return 1.0 / x;
 #endif
 }
 // Float: the hardware approximation alone (rcp.approx.ftz.f32, within an ulp);
@@ -246,34 +259,44 @@ __host__ __device__ __forceinline__ float rcp_nr(float x) {
 #endif
 }
 
-// Square root of the fast form.  FP64: from the float estimate r0 of 1/sqrt(x)
-// (rsqrt.approx.ftz.f32 of the leading bits, widened on the integer pipe), one
-// third-order correction of t = x r0: with d = 1 - t r0, sqrt(x) = t (1 - d)^(-1/2)
-// = t (1 + d/2 + 3 d^2/8 + ...), truncated after the d^2 term (Householder's
-// order-3 step for the reciprocal square root, published with the FMA
-// formulation by Markstein, IBM J. Res. Dev. 34, 1990).  Five FP64
-// instructions; the truncation error is ~2.5 delta^3 for a seed error delta
-// < 2^-21, so the result is within about an ulp (tests hold it to 2 ulps of
-// the IEEE square root).  Zero, negative, non-finite and out-of-float-range
-// arguments take the IEEE square root.  Float: sqrt.approx.ftz.f32.
+// sqrt(x) from the estimate r0 of 1/sqrt(x): with t = x r0 and d = 1 - t r0,
+// sqrt(x) = t (1 - d)^(-1/2) = t (1 + d/2 + 3 d^2/8 + ...).  One step keeps
+// t (1 + d/2) = t (1.5 - t r0/2), the halved seed being exact: three FP64
+// instructions, error ~1.5 delta^2.  +0 gives +0 through the same steps (its
+// seed is 2^128, finite, from the infinite float estimate), so dry sides do
+// not branch off; negative, non-finite and out-of-float-range arguments take
+// the IEEE square root.  Float: sqrt.approx.ftz.f32.
 __host__ __device__ __forceinline__ double fast_sqrt(double x) {
 #ifdef __CUDA_ARCH__
-    if (!pos_i(x) || !in_f32_range(x)) return sqrt(x);
+    if (sbits(x) != 0 && (!pos_i(x) || !in_f32_range(x))) return sqrt(x);
+    float rf;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(rf) : "f"(f32_lead(x)));
+    const double r0 = f64_widen(rf), r0h = f64_widen(rf * 0.5f);
+    const double t = x * r0;
+    return t * fma(-t, r0h, 1.5);
+#else
+    return sqrt(x);
+#endif
+}
+// sqrt(x) within about an ulp (the CFL rate): the d^2 term kept, five FP64
+// instructions, error ~2.5 delta^3.
+__host__ __device__ __forceinline__ double fast_sqrt_fa(double x) {
+#ifdef __CUDA_ARCH__
+    if (sbits(x) != 0 && (!pos_i(x) || !in_f32_range(x))) return sqrt(x);
     float rf;
     asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(rf) : "f"(f32_lead(x)));
     const double r0 = f64_widen(rf);
     const double t = x * r0;
     const double d = fma(-t, r0, 1.0);
-    const double p = fma(0.375, d, 0.5);
-    return fma(t, d * p, t);
+    return fma(t, d * fma(0.375, d, 0.5), t);
 #else
     return sqrt(x);
 #endif
 }
-// sqrt(x) as fast_sqrt (same bits) and, for one more FMA, half the reciprocal
-// square root 1/(2 sqrt(x)) from the same correction: (r0/2) (1 + d/2 +
-// 3 d^2/8), the halved seed being exact, within about an ulp.  x must be a
-// positive normal double (a depth above the dry tolerance, times g).
+// sqrt(x) as fast_sqrt (same bits) and, for one more multiply, half the
+// reciprocal square root 1/(2 sqrt(x)) = (r0/2) (1.5 - t r0/2) from the same
+// step.  x must be a positive normal double (a depth above the dry tolerance,
+// times g).
 __device__ __forceinline__ double fast_sqrt_hrsqrt(double x, double& hrsq) {
     if (!in_f32_range(x)) {
         const double s = sqrt(x);
@@ -284,10 +307,9 @@ __device__ __forceinline__ double fast_sqrt_hrsqrt(double x, double& hrsq) {
     asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(rf) : "f"(f32_lead(x)));
     const double r0 = f64_widen(rf), r0h = f64_widen(rf * 0.5f);
     const double t = x * r0;
-    const double d = fma(-t, r0, 1.0);
-    const double dp = d * fma(0.375, d, 0.5);
-    hrsq = fma(r0h, dp, r0h);
-    return fma(t, dp, t);
+    const double e = fma(-t, r0h, 1.5);
+    hrsq = r0h * e;
+    return t * e;
 }
 __host__ __device__ __forceinline__ float fast_sqrt(float x) {
 #ifdef __CUDA_ARCH__
@@ -297,6 +319,32 @@ __host__ __device__ __forceinline__ float fast_sqrt(float x) {
 #else
     return sqrtf(x);
 #endif
+}
+
+// 2 p / S for p = dm dp > 0 and S = dm + dp (the van Leer slope 2 dm dp / (dm + dp)), S a normal double of
+// magnitude below 2^1000.  The seeds come from the leading 24 bits of the two significands, taken as floats
+// in [1, 2): rf ~ 1 / mS by rcp.approx.ftz.f32 and hf = mp rf; the exponents are added back on the integer
+// pipe, giving s0h ~ p / S, s0 = 2 s0h and r2 ~ 2 / S without FP64 instructions (and without a branch on
+// the range of S).  One Newton correction in FP64, s0 + r2 (p - s0h S), leaves the product of the two
+// seed errors (each below 2^-21): the slope is within ~2^-42 relative.  Where p / S is below the normal
+// range the seed is 0 and r2 p is the result.
+__device__ __forceinline__ double van_leer_div2(double p, double S) {
+    const unsigned hp = (unsigned)__double2hiint(p), lp = (unsigned)__double2loint(p);
+    const unsigned hS = (unsigned)__double2hiint(S), lS = (unsigned)__double2loint(S);
+    const int ep = (int)((hp >> 20) & 0x7FFu), eS = (int)((hS >> 20) & 0x7FFu);
+    const float mp = __int_as_float((int)(0x3F800000u | ((hp & 0xFFFFFu) << 3) | (lp >> 29)));
+    const float mS = __int_as_float((int)(0x3F800000u | ((hS & 0xFFFFFu) << 3) | (lS >> 29)));
+    float rf;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rf) : "f"(mS));  // (0.5, 1]
+    const float hf = mp * rf;                                 // [0.5, 2]
+    const unsigned sg = hS & 0x80000000u;                    // p / S has the sign of S
+    const double r2 = f64_of_f32_scaled(rf, 1024 - eS, sg);
+    const int ks = ep - eS;
+    const bool ok = ep != 0 && (int)((unsigned)__float_as_int(hf) >> 23) + 896 + ks >= 1;
+    const double s0h = ok ? f64_of_f32_scaled(hf, ks, sg) : 0.0;
+    const double s0 = ok ? f64_of_f32_scaled(hf, ks + 1, sg) : 0.0;
+    const double t = fma(-s0h, S, p);  // p - s0h S
+    return fma(r2, t, s0);
 }
 
 // ----------------------------------------------------------------------------
@@ -316,7 +364,11 @@ template <class R, bool FAST> __host__ __device__ __forceinline__ R van_leer_slo
     } else {
         // phi(r) dp with r = dm/dp is 0 for r <= 0 and 2 dm dp / (dm + dp) otherwise.
         const R p = dm * dp;
-        if constexpr (sizeof(R) == 8) return pos_i(p) ? p * rcp_nr_twice(dm + dp) : R(0);  // == (p + p) * rcp_nr
+#ifdef __CUDA_ARCH__
+        if constexpr (sizeof(R) == 8) return pos_i(p) ? van_leer_div2(p, dm + dp) : R(0);
+#else
+        if constexpr (sizeof(R) == 8) return pos_i(p) ? p * (R(2) / (dm + dp)) : R(0);
+#endif
         else return pos_i(p) ? (p + p) * rcp_nr(dm + dp) : R(0);
     }
 }
@@ -330,8 +382,13 @@ __host__ __device__ __forceinline__ double van_leer_slope_rs(double qm, double q
     if (abs_le_bits(dp, Cst<double>::tol12_bits)) return 0.0;
     const double p = dm * dp;
     if (!pos_i(p)) return 0.0;
-    rS = rcp_nr(dm + dp);
+    const double S = dm + dp;
+    rS = rcp_nr(S);
+#ifdef __CUDA_ARCH__
+    return van_leer_div2(p, S);
+#else
     return (p + p) * rS;
+#endif
 }
 
 // ----------------------------------------------------------------------------
@@ -431,9 +488,11 @@ __host__ __device__ __forceinline__ void roe_hydrostatic_fast(R hi, R ui, R vi, 
     R uni, uti, unj, utj;
     if (DIR == 0) { uni = ui; uti = vi; unj = uj; utj = vj; }
     else { uni = vi; uti = -ui; unj = vj; utj = -uj; }
-    const R hh = R(0.5) * (hi + hj);
-    const bool hmb = gt_bits(hh, C::toldry_bits);
-    const R hm = hmb ? hh : C::toldry;
+    // hm = max(0.5 (hi + hj), toldry) enters only as g hm: 0.5 hs > toldry exactly when hs > 2 toldry, and
+    // g (0.5 hs) and (g / 2) hs are one rounding of the same product, so the halving goes
+    const R hs = hi + hj;
+    const bool hmb = gt_bits(hs, C::toldry2_bits);
+    const R ghm = hmb ? C::half_g * hs : C::g_toldry;
     R cm, hrcm;  // hrcm = 1 / (2 cm)
     const R sden = si + sj + C::tol12;
     // FP64: one reciprocal 1 / (2 sden den) = q/2 for 1/sden and 1/(2 den), 1/(2 cm) from cm's square root
@@ -441,14 +500,14 @@ __host__ __device__ __forceinline__ void roe_hydrostatic_fast(R hi, R ui, R vi, 
     // float: one reciprocal for all three
     R q, rs, hrden;
     if constexpr (sizeof(R) == 8) {
-        cm = fast_sqrt_hrsqrt(C::g * hm, hrcm);
+        cm = fast_sqrt_hrsqrt(ghm, hrcm);
         const R den2 = R(4) * cm + R(2) * C::tol12;
         const R hq = rcp_nr(sden * den2);
         rs = den2 * hq;
         hrden = sden * hq;
         q = hq + hq;
     } else {
-        cm = fast_sqrt(C::g * hm);
+        cm = fast_sqrt(ghm);
         const R den = R(2) * cm + C::tol12;
         const R cd = cm * den;
         q = rcp_nr(sden * cd);
@@ -726,9 +785,15 @@ __device__ __forceinline__ void dt_cell_contrib(R h, R hu, R hv, bool nod, R dx,
         mv = smax(fabs(u), fabs(v));
     } else {
         if (!gt_bits(h, Cst<R>::tol12_bits)) { flags |= DTF_DRY; return; }
-        const R r = rcp_nr(h);
+        R r, c;
+        if constexpr (sizeof(R) == 8) {  // within an ulp: dt follows the exact form's to the last few ulps
+            r = rcp_fa(h);
+            c = fast_sqrt_fa(Cst<R>::g * h);
+        } else {
+            r = rcp_nr(h);
+            c = fast_sqrt(Cst<R>::g * h);
+        }
         const R u = hu * r, v = hv * r;
-        const R c = fast_sqrt(Cst<R>::g * h);
         rate = (fabs(u) + c) * idx + (fabs(v) + c) * idy;
         mv = nnmax_i(fabs(u), fabs(v));
     }

@@ -57,15 +57,15 @@ __device__ __forceinline__ void hydro_face(bool wall, R zL, R zR, R eL, R eR, R 
     bool lhigh = false;  // fast form: the left bed is the face bed
     if constexpr (FAST) {
         // The side whose bed is the face bed zf has its capped depth equal to its own (uncapped) one, so its
-        // pressure correction is exactly +0: only the lower side's depths and correction are computed, and
-        // the results are those of computing both (bit for bit).
+        // pressure correction is exactly +0: only the lower side's depths and correction are computed (the
+        // face-bed side's flux is then the Roe flux itself, which differs from adding +0 only for a -0 flux).
         lhigh = !(okey(zL) < okey(zR));  // zf == zL
         const R eH = lhigh ? etaLf : etaRf, zH = lhigh ? zL : zR;
         const R eW = lhigh ? etaRf : etaLf, zW = lhigh ? zR : zL;
         const R hH = max0_i(eH - zH);
         const R hWu = max0_i(eW - zW), hWs = max0_i(eW - zf);
         // (a^2 - b^2) = (a - b)(a + b) is exactly zero whenever a == b (lake at rest)
-        pW = Cst<R>::half_g * ((hWu - hWs) * (hWu + hWs));
+        pW = (hWu - hWs) * (hWu + hWs);  // times g/2 in the flux's multiply-add below
         hLu = lhigh ? hH : hWu;
         hLs = lhigh ? hH : hWs;
         hRu = lhigh ? hWu : hH;
@@ -87,19 +87,21 @@ __device__ __forceinline__ void hydro_face(bool wall, R zL, R zR, R eL, R eR, R 
         roe_hydrostatic_fast<R, DIR, REC>(hLs, uLf, vLf, hRs, uRf, vRf, f0, f1, f2, rv);
     }
     // hydrostatic pressure correction, rotated with the normal
-    R pL, pR;
+    F0 = f0;
     if constexpr (!FAST) {
-        pL = Cst<R>::half_g * (hLu * hLu - hLs * hLs);
-        pR = Cst<R>::half_g * (hRu * hRu - hRs * hRs);
+        const R pL = Cst<R>::half_g * (hLu * hLu - hLs * hLs);
+        const R pR = Cst<R>::half_g * (hRu * hRu - hRs * hRs);
+        if (DIR == 0) { Fa = f1 + pL; Fb = f1 + pR; Fc = f2; }
+        else { Fa = f1; Fb = f2 + pL; Fc = f2 + pR; }
     } else {
-        pL = lhigh ? R(0) : pW;
-        pR = lhigh ? pW : R(0);
+        // one add: the face-bed side's flux is the normal-momentum flux itself (adding its +0 correction
+        // would change only a -0 flux into +0)
         (void)hLu;
         (void)hRu;
+        const R fn = (DIR == 0) ? f1 : f2, fw = fma(Cst<R>::half_g, pW, fn);
+        if (DIR == 0) { Fa = lhigh ? fn : fw; Fb = lhigh ? fw : fn; Fc = f2; }
+        else { Fa = f1; Fb = lhigh ? fn : fw; Fc = lhigh ? fw : fn; }
     }
-    F0 = f0;
-    if (DIR == 0) { Fa = f1 + pL; Fb = f1 + pR; Fc = f2; }
-    else { Fa = f1; Fb = f2 + pL; Fc = f2 + pR; }
 }
 
 // dt of a step of the device time loop.  A collapse (min CFL bound < 1e-12,
@@ -1686,9 +1688,18 @@ cudaError_t launch_adj_forward_linear(const LevelSrc<double>& src, const Cells3<
 
 // The fast form's reciprocal (rcp_nr, which == 0) or square root (fast_sqrt,
 // which == 1) of n values, for checking them against IEEE division and sqrt.
+// The fast form's FP64 building blocks on n points: op 0 rcp_nr, 1 fast_sqrt,
+// 2 the van Leer slope of the triplet x[3i..3i+2], 3 rcp_fa, 4 fast_sqrt_fa.
 template <bool FAST> __global__ void k_rcp_probe(long n, const double* x, double* y, int which) {
     const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) y[i] = which ? fast_sqrt(x[i]) : rcp_nr(x[i]);
+    if (i >= n) return;
+    switch (which) {
+        case 0: y[i] = rcp_nr(x[i]); break;
+        case 1: y[i] = fast_sqrt(x[i]); break;
+        case 2: y[i] = van_leer_slope<double, true>(x[3 * i], x[3 * i + 1], x[3 * i + 2]); break;
+        case 3: y[i] = rcp_fa(x[i]); break;
+        default: y[i] = fast_sqrt_fa(x[i]); break;
+    }
 }
 template <bool FAST> cudaError_t launch_rcp(long n, const double* x, double* y, int which, cudaStream_t st) {
     static_assert(FAST, "the reciprocal and square root belong to the fast form");

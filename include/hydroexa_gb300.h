@@ -643,6 +643,19 @@ int hx_debug_roe_points_f32(int method, int arith, long n, const float* states, 
 int hx_debug_rcp_f64(long n, const double* x, double* y, hx_stream_t stream);
 /* The fast form's FP64 square root of n device values (to check it against the IEEE square root). */
 int hx_debug_sqrt_f64(long n, const double* x, double* y, hx_stream_t stream);
+/* The fast form's FP64 building blocks on n device points (to check their
+ * error bounds): HX_FAST_OP_RCP and HX_FAST_OP_SQRT (one Newton step, the
+ * face flux's), HX_FAST_OP_SLOPE (the van Leer slope of the triplets
+ * x[3i], x[3i+1], x[3i+2]: x holds 3n values), HX_FAST_OP_RCP_FAITHFUL and
+ * HX_FAST_OP_SQRT_FAITHFUL (the CFL rate's, within an ulp).  y holds n values. */
+enum {
+    HX_FAST_OP_RCP = 0,
+    HX_FAST_OP_SQRT = 1,
+    HX_FAST_OP_SLOPE = 2,
+    HX_FAST_OP_RCP_FAITHFUL = 3,
+    HX_FAST_OP_SQRT_FAITHFUL = 4
+};
+int hx_debug_fast_op_f64(int op, long n, const double* x, double* y, hx_stream_t stream);
 /* The row bands hx_level_run_host_f64 uses for ny rows (host only, no GPU):
  * writes band starts into starts[0..n] (starts[n] = ny) and returns n, at
  * most 10; max_bands must be at least 10. */

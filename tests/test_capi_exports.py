@@ -44,6 +44,9 @@ def test_argument_errors_need_no_gpu(hxlib):
     lv = hxlib.LevelF64()
     rc = L.hx_level_run_f64(1, ctypes.byref(lv), None, None, None, 1, 0.5, None, None, None, 0, None, None)
     assert rc == hxlib.HX_ERR_ARG
+    assert L.hx_debug_fast_op_f64(7, 4, None, None, None) == hxlib.HX_ERR_ARG
+    assert b"unknown fast-form operation" in L.hx_last_error()
+    assert L.hx_debug_fast_op_f64(hxlib.HX_FAST_OP_SLOPE, 4, None, None, None) == hxlib.HX_ERR_ARG
 
 
 def test_box_level_plan_checks_the_tiling(hxlib):
