@@ -34,8 +34,10 @@
  * an _f32 form (SINGLE build).  Arithmetic: HX_ARITH_EXACT repeats the
  * reference's operation order with no multiply-add contraction (bit-for-bit
  * the reference's host arithmetic up to cbrt); HX_ARITH_FAST shares
- * reciprocals and square roots between terms and contracts multiply-adds,
- * agreeing with the exact form to ~1e-15 relative per step.
+ * reciprocals and square roots between terms, takes them from float seeds
+ * with one FP64 Newton step (within 2^-42) and contracts multiply-adds,
+ * agreeing with the exact form to a few 1e-15 relative per step (bound:
+ * 1e-12 per step); its time step follows the exact form's to a few ulps.
  */
 #ifndef HYDROEXA_GB300_H
 #define HYDROEXA_GB300_H
