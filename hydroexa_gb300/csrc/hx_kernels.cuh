@@ -289,21 +289,12 @@ struct FaceRec {
 // regions of uniform state (a lake at rest, the still water ahead of a wave)
 // is all warps but one.  Cell k of thread t is candidate number k * NTv + t.
 // Every thread of the block must call it.
-// The threads that run one tile body together.  BlockSync: the whole block,
-// barrier 0.  HalfSync: one of the two 512-thread halves of a 1024-thread
-// block (warps 0-15 or 16-31), with its own named barrier 1 + g, so that the
-// halves step through their tiles' phases independently; slot() picks the
-// half's copy of the body's shared reduction scratch.
+// The threads that run one tile body together (a policy of the body and the
+// fold: the whole block, barrier 0).
 struct BlockSync {
     __device__ __forceinline__ int tid() const { return threadIdx.x; }
     __device__ __forceinline__ void bar() const { __syncthreads(); }
     __device__ __forceinline__ int slot() const { return 0; }
-};
-struct HalfSync {
-    int g;  // 0 or 1
-    __device__ __forceinline__ int tid() const { return threadIdx.x & 511; }
-    __device__ __forceinline__ void bar() const { asm volatile("bar.sync %0, 512;" ::"r"(1 + g) : "memory"); }
-    __device__ __forceinline__ int slot() const { return g; }
 };
 
 template <int NTv, int K = 1, class Sync = BlockSync>
@@ -802,48 +793,6 @@ __global__ void __launch_bounds__(kPN, 1)
                                       NoRec{}, hooks, fold ? tf : nullptr);
     }
     if (fold) block_fold_dt<double, kPN>(tf->rate, tf->mv, tf->flags, ctl.dt_out);
-}
-
-// ---------------------------------------------------------------------------
-// The FP64 level step with two tiles in flight per SM: a 1024-thread block of
-// two independent 512-thread halves, each walking its own 32 x 16 tiles
-// (tile 2 b + g, then + 2 gridDim.x) with its own named barrier, so that one
-// half's FP64 work fills the pipe while the other waits at a barrier, on its
-// loads, or in the unbalanced tail of a phase.  Same arithmetic per cell as
-// k_hydro_tile; the CFL bound is folded per thread across tiles and into the
-// accumulator once per block.
-// ---------------------------------------------------------------------------
-constexpr int kHX = 32, kHY = 16;
-constexpr size_t persist2_smem_bytes() {
-    return 2 * sizeof(HydroSmem<double, kHX, kHY>) + 1024 * sizeof(ThreadFold<double>);
-}
-
-template <bool FAST>
-__global__ void __launch_bounds__(1024, 1)
-    k_hydro_persist2(LevelSrc<double> src, Cells3<double> uo, Plane<double> np, Cells3W<double> out, IBox vb,
-                     int tiles_x, int ntiles, StepCtl<double> ctl) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int g = (int)(threadIdx.x >> 9);
-    HydroSmem<double, kHX, kHY>& S =
-        *reinterpret_cast<HydroSmem<double, kHX, kHY>*>(smem_raw + g * sizeof(HydroSmem<double, kHX, kHY>));
-    ThreadFold<double>* tf =
-        reinterpret_cast<ThreadFold<double>*>(smem_raw + 2 * sizeof(HydroSmem<double, kHX, kHY>)) + threadIdx.x;
-    double dt;
-    if (!resolve_dt(ctl, dt)) return;
-    step_bookkeeping(ctl, dt);
-    *tf = ThreadFold<double>{};
-    const bool fold = ctl.dt_out != nullptr;
-    const FaceOut<double> fo{};
-    const HalfSync sy{g};
-    for (int k = 2 * (int)blockIdx.x + g; k < ntiles; k += 2 * (int)gridDim.x) {
-        const int x0 = vb.lo0 + (k % tiles_x) * kHX, y0 = vb.lo1 + (k / tiles_x) * kHY;
-        hydro_tile_body<double, FAST, kHX, kHY, kHX * kHY, LevelSrc<double>, false, NoDiv, NoRec, Cells3<double>,
-                        Plane<double>, NoHooks, HalfSync>(S, src, uo, np, out, fo, vb, x0, y0, dt, ctl.dx, ctl.dy,
-                                                          nullptr, ctl.status, nullptr, NoDiv{}, NoRec{}, NoHooks{},
-                                                          fold ? tf : nullptr, sy);
-    }
-    __syncthreads();
-    if (fold) block_fold_dt<double, 1024>(tf->rate, tf->mv, tf->flags, ctl.dt_out);
 }
 
 // ---------------------------------------------------------------------------
