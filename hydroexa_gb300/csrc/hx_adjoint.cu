@@ -65,6 +65,11 @@ constexpr int H3 = 3;  // forward halo of the reverse tile
 
 // sign with sgn(+-0) = 0, decided on the integer pipe
 __device__ __forceinline__ double sgn(double x) { return pos_i(x) ? 1.0 : (neg_i(x) ? -1.0 : 0.0); }
+// sgn(x) a, all on the integer pipe (a sign flip or a zero instead of a multiply)
+__device__ __forceinline__ double sgn_mul(double x, double a) {
+    const double na = __longlong_as_double(__double_as_longlong(a) ^ (long long)0x8000000000000000ull);
+    return pos_i(x) ? a : (neg_i(x) ? na : 0.0);
+}
 
 // ---------------------------------------------------------------------------
 // Reverse of the homogeneous Roe flux in the face-normal frame.  (hi, ui, vi)
@@ -180,7 +185,7 @@ __device__ void roe_rev(double hi, double ui, double vi, double hj, double uj, d
 // entropy-fixed speeds and wave strengths as the forward step computed them;
 // only 1/si and 1/sj are formed).  roe_rev_core then runs the reverse.
 struct RoeFwd {
-    double Hi, Hj, Ui, Uj, Vi, Vj, si, sj, rsi, rsj, cm, rs, rden, rcm, um, vm, l0, l2, dh;
+    double Hi, Hj, Ui, Uj, Vi, Vj, si, sj, hrsi, hrsj, cm, rs, rden, rcm, um, vm, l0, l2, dh;  // hrs = 1/(2 s)
     double a0h, a1h, a2h, w0, w1, w2, hrden, hrcm;  // half wave strengths, w = |l| ah, halves of 1/den, 1/cm
     double e0i, e0j, e2i, e2j, l0a, l2a, rD0, rD2;
     bool wi, wj, hmb, fix0, fix2;
@@ -195,28 +200,30 @@ __device__ __forceinline__ void roe_fwd_fast(double hi, double ui, double vi, do
     const double Hi = wi ? hi : 0.0, Hj = wj ? hj : 0.0;
     const double Ui = wi ? ui : 0.0, Vi = wi ? vi : 0.0, Uj = wj ? uj : 0.0, Vj = wj ? vj : 0.0;
     F.Hi = Hi; F.Hj = Hj; F.Ui = Ui; F.Uj = Uj; F.Vi = Vi; F.Vj = Vj;
-    const double si = sqrt(Hi), sj = sqrt(Hj);
+    // the forward's own square roots (fast_sqrt, fast_sqrt_hrsqrt of g hm = (g/2)(Hi + Hj)), bit for bit
+    const double si = fast_sqrt(Hi), sj = fast_sqrt(Hj);
     F.si = si; F.sj = sj;
     const double hh = 0.5 * (Hi + Hj);
     F.hmb = gt_bits(hh, C::toldry_bits);
     const double hm = F.hmb ? hh : TD;
-    const double cm = sqrt(G * hm);
+    double hrcm_unused;
+    const double cm = fast_sqrt_hrsqrt(G * hm, hrcm_unused);
     F.cm = cm;
     const double den = 2.0 * cm + T12;
     const double sden = si + sj + T12;
     const double cd = cm * den, S3 = sden * cd;
     double q3;
-    F.rsi = 0.0; F.rsj = 0.0;
+    F.hrsi = 0.0; F.hrsj = 0.0;
     if (wi && wj) {
         const double pij = si * sj;
         const double q = rcp_nr(S3 * pij);
         q3 = pij * q;
-        F.rsi = (sj * S3) * q;
-        F.rsj = (si * S3) * q;
+        F.hrsi = (sj * (0.5 * S3)) * q;
+        F.hrsj = (si * (0.5 * S3)) * q;
     } else {
         q3 = rcp_nr(S3);
-        if (wi) F.rsi = rcp_nr(si);
-        if (wj) F.rsj = rcp_nr(sj);
+        if (wi) F.hrsi = rcp_nr(si + si);
+        if (wj) F.hrsj = rcp_nr(sj + sj);
     }
     F.rs = cd * q3; F.rden = (sden * cm) * q3; F.rcm = (sden * den) * q3;
     const double um = (Ui * si + Uj * sj) * F.rs;
@@ -253,17 +260,15 @@ __device__ __forceinline__ void roe_fwd_rec(double hi, double ui, double vi, dou
     const double si = R.si, sj = R.sj, cm = R.cm;
     F.si = si; F.sj = sj; F.cm = cm;
     F.hmb = (R.fl & RR_HM) != 0;
-    const double den = 2.0 * cm + T12;
-    const double sden = si + sj + T12;
-    F.rs = den * R.q; F.rden = sden * R.q; F.rcm = rcp_nr(cm);  // the record's q is 1 / (sden den)
-    F.rsi = 0.0; F.rsj = 0.0;
+    F.rs = R.rs; F.hrden = R.hrden; F.hrcm = R.hrcm;  // as the forward computed them
+    F.hrsi = 0.0; F.hrsj = 0.0;
     if (wi && wj) {
-        const double r = rcp_nr(si * sj);
-        F.rsi = sj * r;
-        F.rsj = si * r;
+        const double r = rcp_nr((si + si) * sj);
+        F.hrsi = sj * r;
+        F.hrsj = si * r;
     } else {
-        if (wi) F.rsi = rcp_nr(si);
-        if (wj) F.rsj = rcp_nr(sj);
+        if (wi) F.hrsi = rcp_nr(si + si);
+        if (wj) F.hrsj = rcp_nr(sj + sj);
     }
     F.um = R.um; F.vm = R.vm; F.l0 = R.l0; F.l2 = R.l2;
     F.fix0 = (R.fl & RR_FIX0) != 0;
@@ -278,7 +283,6 @@ __device__ __forceinline__ void roe_fwd_rec(double hi, double ui, double vi, dou
     F.dh = Hj - Hi;
     F.a0h = R.a0h; F.a1h = R.a1h; F.a2h = R.a2h;
     F.w0 = fabs(R.l0) * R.a0h; F.w1 = fabs(R.um) * R.a1h; F.w2 = fabs(R.l2) * R.a2h;
-    F.hrden = 0.5 * F.rden; F.hrcm = 0.5 * F.rcm;
 }
 
 __device__ __forceinline__ void roe_rev_core(const RoeFwd& F, double b0, double b1, double b2, double& ghi,
@@ -299,10 +303,10 @@ __device__ __forceinline__ void roe_rev_core(const RoeFwd& F, double b0, double 
     const double gw1 = -b2 * cm;
     const double gw2 = -b0 - b1 * l2 - b2 * vm;
     // w_k = |l_k| ah_k, ah_k = alpha_k / 2
-    double gl0 = fma(gw0, sgn(l0) * F.a0h, -b1 * w0);
-    double gl2 = fma(gw2, sgn(l2) * F.a2h, -b1 * w2);
+    double gl0 = fma(gw0, sgn_mul(l0, F.a0h), -b1 * w0);
+    double gl2 = fma(gw2, sgn_mul(l2, F.a2h), -b1 * w2);
     double gvm = -b2 * (w0 + w2), gcm = -b2 * w1;
-    const double gl1 = gw1 * (sgn(l1) * F.a1h);
+    const double gl1 = gw1 * sgn_mul(l1, F.a1h);
     const double ga0 = gw0 * fabs(l0) * F.hrden;  // d/d alpha0, already divided by den
     const double ga1 = gw1 * fabs(l1) * F.hrcm;   // d/d alpha1, already divided by cm
     const double ga2 = gw2 * fabs(l2) * F.hrden;
@@ -344,13 +348,14 @@ __device__ __forceinline__ void roe_rev_core(const RoeFwd& F, double b0, double 
     const double gsi = gnu * Ui + gnv * Vi + gsden + C::sqrt_g * gci;
     const double gsj = gnu * Uj + gnv * Vj + gsden + C::sqrt_g * gcj;
     if (F.hmb) {
-        const double hghm = gcm * (0.25 * G) * F.rcm;
+        const double hghm = gcm * (0.5 * G) * F.hrcm;
         gHi += hghm; gHj += hghm;
     }
-    gHi = fma(0.5 * gsi, F.rsi, gHi);
-    gHj = fma(0.5 * gsj, F.rsj, gHj);
-    if (F.wi) { ghi += gHi; gui += gUi; gvi += gVi; }
-    if (F.wj) { ghj += gHj; guj += gUj; gvj += gVj; }
+    gHi = fma(gsi, F.hrsi, gHi);
+    gHj = fma(gsj, F.hrsj, gHj);
+    // written, not added: the caller's outputs hold nothing before (a dry side's are 0)
+    ghi = F.wi ? gHi : 0.0; gui = F.wi ? gUi : 0.0; gvi = F.wi ? gVi : 0.0;
+    ghj = F.wj ? gHj : 0.0; guj = F.wj ? gUj : 0.0; gvj = F.wj ? gVj : 0.0;
 }
 
 // Inputs and adjoints of one hydrostatic face: eta, z, u, v of the two cells
@@ -360,7 +365,7 @@ struct FaceVals {
 };
 
 // Reverse of the hydrostatic face (HydrostaticRoe.cpp:247-396) for direction
-// DIR, given the adjoints of FL and FR (global frame).  Adds to g.
+// DIR, given the adjoints of FL and FR (global frame).  Writes g.
 template <int DIR, bool FAST, bool REC = false>
 __device__ void face_rev(const FaceVals& f, const double gFL[3], const double gFR[3], FaceVals& g,
                          const RoeRecVals* rec = nullptr) {
@@ -390,26 +395,50 @@ __device__ void face_rev(const FaceVals& f, const double gFL[3], const double gF
         roe_rev(hLs, unL, utL, hRs, unR, utR, gf0, b1, b2, ghLs, gunL, gutL, ghRs, gunR, gutR);
     }
     // pressure correction p = HG (hu^2 - hs^2)
-    const double ghLu = gpL * (G * hLu), ghRu = gpR * (G * hRu);
-    ghLs = fma(-gpL, G * hLs, ghLs);
-    ghRs = fma(-gpR, G * hRs, ghRs);
-    double getaL = 0, getaR = 0, gzL = 0, gzR = 0, gzf = 0;
-    if (pos_i(dLu)) { getaL += ghLu; gzL -= ghLu; }
-    if (pos_i(dRu)) { getaR += ghRu; gzR -= ghRu; }
-    if (pos_i(dLs)) { getaL += ghLs; gzf -= ghLs; }
-    if (pos_i(dRs)) { getaR += ghRs; gzf -= ghRs; }
-    if (zLmax) gzL += gzf; else gzR += gzf;
+    double getaL, getaR, gzL, gzR;
+    if constexpr (FAST) {
+        // the face-bed side's capped and uncapped depths are one value, so its two pressure terms cancel:
+        // only the lower side's are formed (as in the fast forward); the depth caps max(0, .) pass the
+        // adjoints where their argument is positive
+        if (zLmax) {  // left: the face-bed side
+            ghRs = fma(-gpR, G * hRs, ghRs);
+            const double ghRu = gpR * (G * hRu);
+            const double sL = pos_i(dLs) ? ghLs : 0.0, sR = pos_i(dRs) ? ghRs : 0.0;
+            const double uR = pos_i(dRu) ? ghRu : 0.0;
+            getaL = sL; getaR = sR + uR;
+            gzL = -(sL + sR); gzR = -uR;
+        } else {
+            ghLs = fma(-gpL, G * hLs, ghLs);
+            const double ghLu = gpL * (G * hLu);
+            const double sL = pos_i(dLs) ? ghLs : 0.0, sR = pos_i(dRs) ? ghRs : 0.0;
+            const double uL = pos_i(dLu) ? ghLu : 0.0;
+            getaL = sL + uL; getaR = sR;
+            gzL = -uL; gzR = -(sL + sR);
+        }
+    } else {
+        getaL = 0; getaR = 0; gzL = 0; gzR = 0;
+        double gzf = 0;
+        const double ghLu = gpL * (G * hLu), ghRu = gpR * (G * hRu);
+        ghLs = fma(-gpL, G * hLs, ghLs);
+        ghRs = fma(-gpR, G * hRs, ghRs);
+        if (pos_i(dLu)) { getaL += ghLu; gzL -= ghLu; }
+        if (pos_i(dRu)) { getaR += ghRu; gzR -= ghRu; }
+        if (pos_i(dLs)) { getaL += ghLs; gzf -= ghLs; }
+        if (pos_i(dRs)) { getaR += ghRs; gzf -= ghRs; }
+        if (zLmax) gzL += gzf; else gzR += gzf;
+    }
     double guL, gvL, guR, gvR;
     if (DIR == 0) { guL = gunL; gvL = gutL; guR = gunR; gvR = gutR; }
     else { gvL = gunL; guL = -gutL; gvR = gunR; guR = -gutR; }
-    g.eL += getaL; g.seL += 0.5 * getaL;
-    g.eR += getaR; g.seR -= 0.5 * getaR;
-    g.uL += guL; g.suL += 0.5 * guL;
-    g.uR += guR; g.suR -= 0.5 * guR;
-    g.vL += gvL; g.svL += 0.5 * gvL;
-    g.vR += gvR; g.svR -= 0.5 * gvR;
-    g.zL += gzL;
-    g.zR += gzR;
+    // every field written (the caller's g holds nothing else): no FP64 adds onto zeros
+    g.eL = getaL; g.seL = 0.5 * getaL;
+    g.eR = getaR; g.seR = -0.5 * getaR;
+    g.uL = guL; g.suL = 0.5 * guL;
+    g.uR = guR; g.suR = -0.5 * guR;
+    g.vL = gvL; g.svL = 0.5 * gvL;
+    g.vR = gvR; g.svR = -0.5 * gvR;
+    g.zL = gzL;
+    g.zR = gzR;
 }
 
 // Reverse of van_leer_slope(qm, q, qp) (HydrostaticRoe.cpp:179-195).
@@ -493,6 +522,13 @@ struct AdjArgs {
     long long* p_idx;
     unsigned* p_fl;
     FaceRec rec;  // the step's face records (k_adj_faces<true, true>)
+    // the step's finish, run by the last block to finish (done != null): block counter (zero between
+    // launches), CFL number, gauges and the reference series of step n
+    unsigned* done = nullptr;
+    double cfl = 0.0, seed = 0.0;
+    int ngauges = 0;
+    const long long* gauges = nullptr;
+    const double* href = nullptr;
 };
 
 // The record of x face (f, j) (d = 0) or y face (i, f) (d = 1).
@@ -500,13 +536,87 @@ __device__ __forceinline__ RoeRecVals load_rec(const FaceRec& R, int d, long lon
     const double* b = R.f[d] + o;
     const long long ps = R.plane[d];
     RoeRecVals r;
-    r.si = b[0]; r.sj = b[ps]; r.cm = b[2 * ps]; r.q = b[3 * ps]; r.um = b[4 * ps]; r.vm = b[5 * ps];
-    r.l0 = b[6 * ps]; r.l2 = b[7 * ps]; r.a0h = b[8 * ps]; r.a1h = b[9 * ps]; r.a2h = b[10 * ps];
+    r.si = b[0]; r.sj = b[ps]; r.cm = b[2 * ps]; r.rs = b[3 * ps]; r.hrden = b[4 * ps]; r.hrcm = b[5 * ps];
+    r.um = b[6 * ps]; r.vm = b[7 * ps]; r.l0 = b[8 * ps]; r.l2 = b[9 * ps]; r.a0h = b[10 * ps];
+    r.a1h = b[11 * ps]; r.a2h = b[12 * ps];
     r.fl = R.fl[d][o];
     return r;
 }
 
 __device__ __forceinline__ double fget(const FaceVals& f, int k) { return (&f.eL)[k]; }
+
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5;
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) sh[w] = v;
+    __syncthreads();
+    double s = 0;
+    if (threadIdx.x == 0)
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += sh[k];
+    return s;
+}
+
+// The end of a reverse step: the CFL arg max and dt adjoint over the blocks' partials, the dt term
+// folded into lambda at the arg-max cell, and the gauge misfit of step n.  One block.
+__device__ __forceinline__ void adj_finish_body(int nblocks, const double* dtbar_p, const double* prate,
+                                                     const long long* pidx, const unsigned* pflags, double cfl,
+                                                     double dx, double dy, const double* h, const double* hu,
+                                                     const double* hv, double* lam_h, double* lam_hu, double* lam_hv,
+                                                     int with_dt, int ngauges, const long long* gauges,
+                                                     const double* href, double seed) {
+    __shared__ double sh[ANT / 32];
+    __shared__ double s_rate[ANT / 32];
+    __shared__ long long s_idx[ANT / 32];
+    __shared__ unsigned s_fl[ANT / 32];
+    double d = 0, rate = 0;
+    long long idx = 0x7fffffffffffffffll;
+    unsigned fl = 0;
+    if (with_dt) {
+        for (int k = threadIdx.x; k < nblocks; k += ANT) {
+            d += __ldcg(dtbar_p + k);
+            const double pr = __ldcg(prate + k);
+            const long long pi = __ldcg(pidx + k);
+            if (pr > rate || (pr == rate && pi < idx)) { rate = pr; idx = pi; }
+            fl |= __ldcg(pflags + k);
+        }
+    }
+    const double dtbar = block_sum(d, sh);
+    for (int o = 16; o > 0; o >>= 1) {  // arg max: the larger rate, then the lower cell offset
+        const double r2 = __shfl_xor_sync(0xffffffffu, rate, o);
+        const long long i2 = __shfl_xor_sync(0xffffffffu, idx, o);
+        if (r2 > rate || (r2 == rate && i2 < idx)) { rate = r2; idx = i2; }
+    }
+    fl = __reduce_or_sync(0xffffffffu, fl);
+    if ((threadIdx.x & 31) == 0) {
+        s_rate[threadIdx.x >> 5] = rate;
+        s_idx[threadIdx.x >> 5] = idx;
+        s_fl[threadIdx.x >> 5] = fl;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && with_dt) {
+        for (int k = 1; k < ANT / 32; ++k) {
+            if (s_rate[k] > rate || (s_rate[k] == rate && s_idx[k] < idx)) { rate = s_rate[k]; idx = s_idx[k]; }
+            fl |= s_fl[k];
+        }
+        // dt = cfl * min(1/rate, 1e6 if a dry cell, 1e30 if NODATA): differentiable through the rate only
+        const double m = accum_dt_min<double>(to_bits<double>(rate), fl);
+        if (rate > 0 && m == 1.0 / rate) {
+            const double hh = h[idx], u = hu[idx] / hh, v = hv[idx] / hh, c = sqrt(G * hh);
+            const double gr = dtbar * (-cfl / (rate * rate));  // d dt / d rate
+            const double su = sgn(u), sv = sgn(v), dc = G / (2.0 * c);
+            lam_h[idx] = __ldcg(lam_h + idx) + gr * ((su * (-u / hh) + dc) / dx + (sv * (-v / hh) + dc) / dy);
+            lam_hu[idx] = __ldcg(lam_hu + idx) + gr * su / (hh * dx);
+            lam_hv[idx] = __ldcg(lam_hv + idx) + gr * sv / (hh * dy);
+        }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < ngauges; k += ANT) {  // atomic: a cell may be listed twice
+        const long long gcell = gauges[k];
+        atomicAdd(&lam_h[gcell], seed * 2.0 * (h[gcell] - href[k]));
+    }
+}
+
 
 template <bool FAST, bool REC = false>
 __global__ void __launch_bounds__(ANT) k_adj_faces(AdjArgs A) {
@@ -584,11 +694,12 @@ __global__ void __launch_bounds__(ANT) k_adj_faces(AdjArgs A) {
                 fv.seL = P.s[0][row][fcol - 1 + 2]; fv.seR = P.s[0][row][fcol + 2];
                 fv.suL = P.s[1][row][fcol - 1 + 2]; fv.suR = P.s[1][row][fcol + 2];
                 fv.svL = P.s[2][row][fcol - 1 + 2]; fv.svR = P.s[2][row][fcol + 2];
-                // FL(f) enters cell f-1 with -cx, FR(f) enters cell f with +cx
+                // FL(f) enters cell f-1 with -cx, FR(f) enters cell f with +cx; the face reverse is linear in
+                // these, so it runs on -lambda, +lambda and the gathers below apply cx once per cell
                 double gFL[3], gFR[3];
                 for (int c = 0; c < 3; ++c) {
-                    gFL[c] = -A.cx * S.lam[c][r][cl];
-                    gFR[c] = A.cx * S.lam[c][r][cr];
+                    gFL[c] = -S.lam[c][r][cl];
+                    gFR[c] = S.lam[c][r][cr];
                 }
                 if constexpr (REC) {
                     const RoeRecVals rv = load_rec(A.rec, 0, (long long)f + (long long)gj * (nx + 1));
@@ -620,16 +731,12 @@ __global__ void __launch_bounds__(ANT) k_adj_faces(AdjArgs A) {
         auto gather_x = [&](int row, int col, double& ge, double& gu, double& gv, double& gz) {
             auto F = [&](int q, int fcol) { return (fcol >= -1 && fcol <= ATX + 1) ? P.fa[q][row][fcol + 1] : 0.0; };
             auto SP = [&](int q, int scol) { return (scol >= -1 && scol <= ATX) ? P.sp[q][row][scol + 1] : 0.0; };
-            ge = F(1, col) + F(0, col + 1) + SP(2, col - 1) + SP(1, col) + SP(0, col + 1);
-            gu = F(5, col) + F(4, col + 1) + SP(5, col - 1) + SP(4, col) + SP(3, col + 1);
-            gv = F(7, col) + F(6, col + 1) + SP(8, col - 1) + SP(7, col) + SP(6, col + 1);
-            gz = F(3, col) + F(2, col + 1);
+            ge = A.cx * (F(1, col) + F(0, col + 1) + SP(2, col - 1) + SP(1, col) + SP(0, col + 1));
+            gu = A.cx * (F(5, col) + F(4, col + 1) + SP(5, col - 1) + SP(4, col) + SP(3, col + 1));
+            gv = A.cx * (F(7, col) + F(6, col + 1) + SP(8, col - 1) + SP(7, col) + SP(6, col + 1));
+            gz = A.cx * (F(3, col) + F(2, col + 1));
         };
-        {
-            double ge, gu, gv, gz;
-            gather_x(ty, tx, ge, gu, gv, gz);
-            ae += ge; au += gu; av += gv; az += gz;
-        }
+        gather_x(ty, tx, ae, au, av, az);  // the x pass starts the cell's sums
         // x-boundary ghosts: one thread per row folds both sides
         if (t < ATY && y0 + t < ny) {
             const int row = t, gj = y0 + row, r = row + H3;
@@ -708,10 +815,10 @@ __global__ void __launch_bounds__(ANT) k_adj_faces(AdjArgs A) {
                 fv.seL = P.s[0][frow - 1 + 2][col]; fv.seR = P.s[0][frow + 2][col];
                 fv.suL = P.s[1][frow - 1 + 2][col]; fv.suR = P.s[1][frow + 2][col];
                 fv.svL = P.s[2][frow - 1 + 2][col]; fv.svR = P.s[2][frow + 2][col];
-                double gFL[3], gFR[3];
+                double gFL[3], gFR[3];  // unscaled, as in the x pass; cy in the gathers
                 for (int q = 0; q < 3; ++q) {
-                    gFL[q] = -A.cy * S.lam[q][rl][c];
-                    gFR[q] = A.cy * S.lam[q][rr][c];
+                    gFL[q] = -S.lam[q][rl][c];
+                    gFR[q] = S.lam[q][rr][c];
                 }
                 if constexpr (REC) {
                     const RoeRecVals rv = load_rec(A.rec, 1, (long long)gi + (long long)f * nx);
@@ -741,10 +848,10 @@ __global__ void __launch_bounds__(ANT) k_adj_faces(AdjArgs A) {
         auto gather_y = [&](int row, int col, double& ge, double& gu, double& gv, double& gz) {
             auto F = [&](int q, int frow) { return (frow >= -1 && frow <= ATY + 1) ? P.fa[q][frow + 1][col] : 0.0; };
             auto SP = [&](int q, int srow) { return (srow >= -1 && srow <= ATY) ? P.sp[q][srow + 1][col] : 0.0; };
-            ge = F(1, row) + F(0, row + 1) + SP(2, row - 1) + SP(1, row) + SP(0, row + 1);
-            gu = F(5, row) + F(4, row + 1) + SP(5, row - 1) + SP(4, row) + SP(3, row + 1);
-            gv = F(7, row) + F(6, row + 1) + SP(8, row - 1) + SP(7, row) + SP(6, row + 1);
-            gz = F(3, row) + F(2, row + 1);
+            ge = A.cy * (F(1, row) + F(0, row + 1) + SP(2, row - 1) + SP(1, row) + SP(0, row + 1));
+            gu = A.cy * (F(5, row) + F(4, row + 1) + SP(5, row - 1) + SP(4, row) + SP(3, row + 1));
+            gv = A.cy * (F(7, row) + F(6, row + 1) + SP(8, row - 1) + SP(7, row) + SP(6, row + 1));
+            gz = A.cy * (F(3, row) + F(2, row + 1));
         };
         {
             double ge, gu, gv, gz;
@@ -814,18 +921,55 @@ __global__ void __launch_bounds__(ANT) k_adj_faces(AdjArgs A) {
         A.out[1][o] = S.lam[1][r][c] + ghu + S.fold[1][ty][tx];
         A.out[2][o] = S.lam[2][r][c] + ghv + S.fold[2][ty][tx];
         A.zbar[o] += gz + S.fold[3][ty][tx];
-        const double h = A.src.h[o], hu = A.src.hu[o], hv = A.src.hv[o];
-        double mv;
-        dt_cell_contrib<double, FAST>(h, hu, hv, S.nod[r][c] != 0, A.dx, A.dy, A.idx, A.idy, rate, mv, rfl);
-        if (pos_i(rate)) ridx = o;
         if (A.un1[0])
-            dtb = (S.lam[0][r][c] * (A.un1[0][o] - h) + S.lam[1][r][c] * (A.un1[1][o] - hu) +
-                   S.lam[2][r][c] * (A.un1[2][o] - hv)) * A.idt;
+            dtb = (S.lam[0][r][c] * (A.un1[0][o] - A.src.h[o]) + S.lam[1][r][c] * (A.un1[1][o] - A.src.hu[o]) +
+                   S.lam[2][r][c] * (A.un1[2][o] - A.src.hv[o])) * A.idt;
     }
-    // block reductions (every thread takes part)
+    // The block's CFL arg max.  The fast form screens it in float first (as the forward's fold does): only
+    // the cells within 2^-12 of the block's largest float estimate, or with a non-finite one, take the FP64
+    // rate; the cell holding the true maximum is always among them, ties included.
     __shared__ double s_sum[ANT / 32], s_rate[ANT / 32];
     __shared__ long long s_idx[ANT / 32];
     __shared__ unsigned s_fl[ANT / 32];
+    __shared__ float s_r32[ANT / 32];
+    {
+        const int r = ty + H3, c = tx + H3;
+        const long long o = (long long)gi + (long long)gj * A.pitch;
+        double h = 0.0, hu = 0.0, hv = 0.0;
+        bool wet = false, bad = false;
+        float r32 = 0.f;
+        if (own) {
+            h = A.src.h[o]; hu = A.src.hu[o]; hv = A.src.hv[o];
+            if (S.nod[r][c]) rfl |= DTF_NODATA;
+            else if (!gt_bits(h, Cst<double>::tol12_bits)) rfl |= DTF_DRY;
+            else wet = true;
+        }
+        if constexpr (FAST) {
+            if (wet) {
+                const float hf = f32_lead(h), qx = fabsf(f32_lead(hu)), qy = fabsf(f32_lead(hv));
+                const float rh = rcp_nr(hf);
+                const float u = qx * rh, v = qy * rh;
+                const float cc = fast_sqrt(9.81f * hf);
+                r32 = (u + cc) * f32_lead(A.idx) + (v + cc) * f32_lead(A.idy);
+                bad = !(r32 <= 3.0e38f);
+            }
+            float wr = (wet && !bad) ? r32 : 0.f;
+            for (int off = 16; off > 0; off >>= 1) wr = fmaxf(wr, __shfl_xor_sync(0xffffffffu, wr, off));
+            if ((t & 31) == 0) s_r32[t >> 5] = wr;
+            __syncthreads();
+            float br = 0.f;
+#pragma unroll
+            for (int k = 0; k < ANT / 32; ++k) br = fmaxf(br, s_r32[k]);
+            wet = bad || (wet && r32 >= br * (1.f - 0x1p-12f));
+        }
+        if (wet) {
+            double mv;
+            unsigned f = 0;
+            dt_cell_contrib<double, FAST>(h, hu, hv, false, A.dx, A.dy, A.idx, A.idy, rate, mv, f);
+            rfl |= f;
+            if (pos_i(rate)) ridx = o;
+        }
+    }
     for (int off = 16; off > 0; off >>= 1) {
         dtb += __shfl_xor_sync(0xffffffffu, dtb, off);
         const double r2 = __shfl_xor_sync(0xffffffffu, rate, off);
@@ -849,6 +993,21 @@ __global__ void __launch_bounds__(ANT) k_adj_faces(AdjArgs A) {
         A.p_fl[b] = rfl;
         if (A.un1[0]) A.p_dt[b] = sum;
     }
+    if (A.done) {  // the last block to get here runs the step's finish (k_adj_finish's work, no launch)
+        __shared__ bool s_last;
+        const unsigned nb = gridDim.x * gridDim.y;
+        if (t == 0) {
+            __threadfence();  // this block's partials and lambda before its count
+            s_last = atomicAdd(A.done, 1u) == nb - 1u;
+        }
+        __syncthreads();
+        if (s_last) {
+            __threadfence();
+            adj_finish_body((int)nb, A.p_dt, A.p_rate, A.p_idx, A.p_fl, A.cfl, A.dx, A.dy, A.src.h, A.src.hu,
+                            A.src.hv, A.out[0], A.out[1], A.out[2], 1, A.ngauges, A.gauges, A.href, A.seed);
+            if (t == 0) *A.done = 0u;  // for the next step's launch (stream-ordered)
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -867,17 +1026,6 @@ struct PostArgs {
     double dt;
 };
 
-__device__ __forceinline__ double block_sum(double v, double* sh) {
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    const int w = threadIdx.x >> 5;
-    __syncthreads();
-    if ((threadIdx.x & 31) == 0) sh[w] = v;
-    __syncthreads();
-    double s = 0;
-    if (threadIdx.x == 0)
-        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += sh[k];
-    return s;
-}
 
 __global__ void __launch_bounds__(ANT) k_adj_post(PostArgs P) {
     __shared__ double sh[ANT / 32];
@@ -937,54 +1085,8 @@ __global__ void __launch_bounds__(ANT) k_adj_finish(int nblocks, const double* d
                                                      const double* hv, double* lam_h, double* lam_hu, double* lam_hv,
                                                      int with_dt, int ngauges, const long long* gauges,
                                                      const double* href, double seed) {
-    __shared__ double sh[ANT / 32];
-    __shared__ double s_rate[ANT / 32];
-    __shared__ long long s_idx[ANT / 32];
-    __shared__ unsigned s_fl[ANT / 32];
-    double d = 0, rate = 0;
-    long long idx = 0x7fffffffffffffffll;
-    unsigned fl = 0;
-    if (with_dt) {
-        for (int k = threadIdx.x; k < nblocks; k += ANT) {
-            d += dtbar_p[k];
-            if (prate[k] > rate || (prate[k] == rate && pidx[k] < idx)) { rate = prate[k]; idx = pidx[k]; }
-            fl |= pflags[k];
-        }
-    }
-    const double dtbar = block_sum(d, sh);
-    for (int o = 16; o > 0; o >>= 1) {  // arg max: the larger rate, then the lower cell offset
-        const double r2 = __shfl_xor_sync(0xffffffffu, rate, o);
-        const long long i2 = __shfl_xor_sync(0xffffffffu, idx, o);
-        if (r2 > rate || (r2 == rate && i2 < idx)) { rate = r2; idx = i2; }
-    }
-    fl = __reduce_or_sync(0xffffffffu, fl);
-    if ((threadIdx.x & 31) == 0) {
-        s_rate[threadIdx.x >> 5] = rate;
-        s_idx[threadIdx.x >> 5] = idx;
-        s_fl[threadIdx.x >> 5] = fl;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0 && with_dt) {
-        for (int k = 1; k < ANT / 32; ++k) {
-            if (s_rate[k] > rate || (s_rate[k] == rate && s_idx[k] < idx)) { rate = s_rate[k]; idx = s_idx[k]; }
-            fl |= s_fl[k];
-        }
-        // dt = cfl * min(1/rate, 1e6 if a dry cell, 1e30 if NODATA): differentiable through the rate only
-        const double m = accum_dt_min<double>(to_bits<double>(rate), fl);
-        if (rate > 0 && m == 1.0 / rate) {
-            const double hh = h[idx], u = hu[idx] / hh, v = hv[idx] / hh, c = sqrt(G * hh);
-            const double gr = dtbar * (-cfl / (rate * rate));  // d dt / d rate
-            const double su = sgn(u), sv = sgn(v), dc = G / (2.0 * c);
-            lam_h[idx] += gr * ((su * (-u / hh) + dc) / dx + (sv * (-v / hh) + dc) / dy);
-            lam_hu[idx] += gr * su / (hh * dx);
-            lam_hv[idx] += gr * sv / (hh * dy);
-        }
-    }
-    __syncthreads();
-    for (int k = threadIdx.x; k < ngauges; k += ANT) {  // atomic: a cell may be listed twice
-        const long long gcell = gauges[k];
-        atomicAdd(&lam_h[gcell], seed * 2.0 * (h[gcell] - href[k]));
-    }
+    adj_finish_body(nblocks, dtbar_p, prate, pidx, pflags, cfl, dx, dy, h, hu, hv, lam_h, lam_hu, lam_hv,
+                    with_dt, ngauges, gauges, href, seed);
 }
 
 // h of the final state at the gauge cells.
@@ -1003,7 +1105,8 @@ namespace {
 struct AdjLayout {
     size_t plane;                 // doubles per plane (ny * pitch)
     int nslots, seg, binom;       // stored states; segment length (uniform); snapshot slots (binomial)
-    size_t states, segbuf, segbuf_stride, lam, lamlin, lin, tmp, nxt, dthist, pflags, slots, status, part, total;
+    size_t states, segbuf, segbuf_stride, lam, lamlin, lin, tmp, nxt, dthist, pflags, slots, status, done, part,
+        total;
     int nblocks;
     // face records (uniform checkpoints, fast form, on request): one set per step of the two segments in
     // flight, after everything else so the layout is otherwise the same with and without them
@@ -1103,6 +1206,7 @@ AdjLayout adj_layout(int nx, int ny, long long pitch, int nsteps, int every, boo
     L.pflags = o; o += al256((size_t)nsteps * sizeof(unsigned));
     L.slots = o; o += 256;
     L.status = o; o += 256;
+    L.done = o; o += 256;  // the reverse kernel's block counter (its fused finish)
     L.nblocks = ((nx + ATX - 1) / ATX) * ((ny + ATY - 1) / ATY);
     L.part = o; o += al256((size_t)L.nblocks * (2 * sizeof(double) + sizeof(long long) + sizeof(unsigned)));
     if (records && L.seg) {
@@ -1364,6 +1468,7 @@ int adjoint_reverse_binomial(const hx_level_f64* L, int nsteps, double cfl, int 
     if (e == cudaSuccess) e = cudaMemcpyAsync(pf_host.data(), pfl, nsteps * sizeof(unsigned), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e == cudaSuccess) e = cudaMemsetAsync(grad_z, 0, pb, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(base + A.done, 0, sizeof(unsigned), st);
     double* lamb[2] = {V.state(A.lam, 0), V.state(A.lam, 1)};
     if (e == cudaSuccess) e = cudaMemsetAsync(lamb[0], 0, 3 * pb, st);
     if (e == cudaSuccess)
@@ -1382,6 +1487,14 @@ int adjoint_reverse_binomial(const hx_level_f64* L, int nsteps, double cfl, int 
                                         n >= 1 ? ngauges : 0, gcells, series_ref, seed);
         ++launches;
         return cudaGetLastError();
+    };
+    // the reverse kernel's own finish of step n (with the dt term)
+    auto fused_finish = [&](AdjArgs& B, int n) {
+        B.done = reinterpret_cast<unsigned*>(base + A.done);
+        B.cfl = cfl; B.seed = seed;
+        B.ngauges = n >= 1 ? ngauges : 0;
+        B.gauges = gcells;
+        B.href = n >= 1 ? href + (size_t)(n - 1) * ngauges : nullptr;
     };
     // forward from state a (in src) to state m into dst, with the recorded dt
     auto advance = [&](long long a, const double* src, long long m, double* dst) -> cudaError_t {
@@ -1425,11 +1538,11 @@ int adjoint_reverse_binomial(const hx_level_f64* L, int nsteps, double cfl, int 
             lam_for_faces = ll;
             un1 = nullptr;
         }
-        const AdjArgs B = faces_args(L, A, base, Uj, un1, lam_for_faces, lam0, grad_z, dt);
+        AdjArgs B = faces_args(L, A, base, Uj, un1, lam_for_faces, lam0, grad_z, dt);
+        fused_finish(B, (int)j);
         k_adj_faces<FAST><<<grid, ANT, sizeof(AdjSmem), st>>>(B);
         ++launches;
         if (r == cudaSuccess) r = cudaGetLastError();
-        if (r == cudaSuccess) r = finish((int)j, Uj, lam0, 1);
         if (r == cudaSuccess && j > 0) r = cudaMemcpyAsync(nxt, Uj, 3 * pb, cudaMemcpyDeviceToDevice, st);
         cur ^= 1;
         return r;
@@ -1498,6 +1611,7 @@ int adjoint_reverse(const hx_level_f64* L, int nsteps, double cfl, int ngauges, 
     if (e == cudaSuccess) e = cudaMemcpyAsync(pf_host.data(), pfl, nsteps * sizeof(unsigned), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e == cudaSuccess) e = cudaMemsetAsync(grad_z, 0, pb, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(base + A.done, 0, sizeof(unsigned), st);
     double* lamb[2] = {V.state(A.lam, 0), V.state(A.lam, 1)};
     if (e == cudaSuccess) e = cudaMemsetAsync(lamb[0], 0, 3 * pb, st);
     if (e == cudaSuccess)
@@ -1524,6 +1638,14 @@ int adjoint_reverse(const hx_level_f64* L, int nsteps, double cfl, int ngauges, 
                                         n >= 1 ? ngauges : 0, gcells, series_ref, seed);
         ++launches;
         return cudaGetLastError();
+    };
+    // the reverse kernel's own finish of step n (with the dt term)
+    auto fused_finish = [&](AdjArgs& B, int n) {
+        B.done = reinterpret_cast<unsigned*>(base + A.done);
+        B.cfl = cfl; B.seed = seed;
+        B.ngauges = n >= 1 ? ngauges : 0;
+        B.gauges = gcells;
+        B.href = n >= 1 ? href + (size_t)(n - 1) * ngauges : nullptr;
     };
     const int L_seg = A.seg ? A.seg : nsteps;
     const int nseg = (nsteps + L_seg - 1) / L_seg;
@@ -1596,6 +1718,7 @@ int adjoint_reverse(const hx_level_f64* L, int nsteps, double cfl, int ngauges, 
                 un1 = nullptr;  // the post kernel wrote the dt partials
             }
             AdjArgs B = faces_args(L, A, base, Un, un1, lam_for_faces, lam0, grad_z, dt);
+            fused_finish(B, n);
             if constexpr (FAST) {
                 if (use_rec) {
                     B.rec = rec_at(A, base, (sg & 1) * L_seg + (n - n0), L->nx, L->ny);
@@ -1608,7 +1731,6 @@ int adjoint_reverse(const hx_level_f64* L, int nsteps, double cfl, int ngauges, 
             }
             ++launches;
             if (e == cudaSuccess) e = cudaGetLastError();
-            if (e == cudaSuccess) e = finish(n, Un, lam0, 1);
             cur ^= 1;
         }
         if (A.seg && e == cudaSuccess) e = cudaEventRecord(side.freed[sg & 1], st);

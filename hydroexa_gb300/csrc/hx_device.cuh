@@ -459,10 +459,10 @@ __host__ __device__ __forceinline__ void roe_hydrostatic_exact(R hi, R hui, R hv
 // half wave strengths, with the branch flags.  Recorded by the adjoint's
 // segment recompute so the reverse sweep does not evaluate them again.
 struct RoeRecVals {
-    double si, sj, cm, q, um, vm, l0, l2, a0h, a1h, a2h;  // q = 1 / (sden den)
+    double si, sj, cm, rs, hrden, hrcm, um, vm, l0, l2, a0h, a1h, a2h;  // 1/sden, 1/(2 den), 1/(2 cm)
     unsigned fl;  // RR_WI | RR_WJ | RR_HM | RR_FIX0 | RR_FIX2
 };
-constexpr int NREC = 11;  // doubles of a RoeRecVals
+constexpr int NREC = 13;  // doubles of a RoeRecVals
 constexpr unsigned RR_WI = 1u, RR_WJ = 2u, RR_HM = 4u, RR_FIX0 = 8u, RR_FIX2 = 16u;
 
 // Fast form: inputs are the face depths and face velocities (the reference
@@ -498,19 +498,18 @@ __host__ __device__ __forceinline__ void roe_hydrostatic_fast(R hi, R ui, R vi, 
     // FP64: one reciprocal 1 / (2 sden den) = q/2 for 1/sden and 1/(2 den), 1/(2 cm) from cm's square root
     // (den = 2 cm + tol12 and 2 den = 4 cm + 2 tol12 exactly, so every value is that of q = 1/(sden den));
     // float: one reciprocal for all three
-    R q, rs, hrden;
+    R rs, hrden;
     if constexpr (sizeof(R) == 8) {
         cm = fast_sqrt_hrsqrt(ghm, hrcm);
         const R den2 = R(4) * cm + R(2) * C::tol12;
         const R hq = rcp_nr(sden * den2);
         rs = den2 * hq;
         hrden = sden * hq;
-        q = hq + hq;
     } else {
         cm = fast_sqrt(ghm);
         const R den = R(2) * cm + C::tol12;
         const R cd = cm * den;
-        q = rcp_nr(sden * cd);
+        const R q = rcp_nr(sden * cd);
         rs = cd * q;
         hrden = R(0.5) * ((sden * cm) * q);
         hrcm = R(0.5) * ((sden * den) * q);
@@ -561,7 +560,8 @@ __host__ __device__ __forceinline__ void roe_hydrostatic_fast(R hi, R ui, R vi, 
     if (DIR == 0) { F1 = f1; F2 = f2; }
     else { F1 = -f2; F2 = f1; }
     if constexpr (REC) {
-        rv->si = si; rv->sj = sj; rv->cm = cm; rv->q = q; rv->um = um; rv->vm = vm; rv->l0 = l0; rv->l2 = l2;
+        rv->si = si; rv->sj = sj; rv->cm = cm; rv->rs = rs; rv->hrden = hrden; rv->hrcm = hrcm;
+        rv->um = um; rv->vm = vm; rv->l0 = l0; rv->l2 = l2;
         rv->a0h = a0h; rv->a1h = a1h; rv->a2h = a2h;
         rv->fl = (wi ? RR_WI : 0u) | (wj ? RR_WJ : 0u) | (hmb ? RR_HM : 0u) | (fix0 ? RR_FIX0 : 0u) |
                  (fix2 ? RR_FIX2 : 0u);

@@ -261,8 +261,9 @@ struct FaceRec {
     __device__ __forceinline__ void put(int d, long long o, const RoeRecVals& r) const {
         double* b = f[d] + o;
         const long long ps = plane[d];
-        b[0] = r.si; b[ps] = r.sj; b[2 * ps] = r.cm; b[3 * ps] = r.q; b[4 * ps] = r.um; b[5 * ps] = r.vm;
-        b[6 * ps] = r.l0; b[7 * ps] = r.l2; b[8 * ps] = r.a0h; b[9 * ps] = r.a1h; b[10 * ps] = r.a2h;
+        b[0] = r.si; b[ps] = r.sj; b[2 * ps] = r.cm; b[3 * ps] = r.rs; b[4 * ps] = r.hrden; b[5 * ps] = r.hrcm;
+        b[6 * ps] = r.um; b[7 * ps] = r.vm; b[8 * ps] = r.l0; b[9 * ps] = r.l2; b[10 * ps] = r.a0h;
+        b[11 * ps] = r.a1h; b[12 * ps] = r.a2h;
         fl[d][o] = (unsigned char)r.fl;
     }
     __device__ __forceinline__ void put_x(int gi, int gj, const RoeRecVals& r, bool extra) const {
