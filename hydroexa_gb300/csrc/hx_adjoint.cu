@@ -430,15 +430,12 @@ __device__ void face_rev(const FaceVals& f, const double gFL[3], const double gF
     double guL, gvL, guR, gvR;
     if (DIR == 0) { guL = gunL; gvL = gutL; guR = gunR; gvR = gutR; }
     else { gvL = gunL; guL = -gutL; gvR = gunR; guR = -gutR; }
-    // every field written (the caller's g holds nothing else): no FP64 adds onto zeros
-    g.eL = getaL; g.seL = 0.5 * getaL;
-    g.eR = getaR; g.seR = -0.5 * getaR;
-    g.uL = guL; g.suL = 0.5 * guL;
-    g.uR = guR; g.suR = -0.5 * guR;
-    g.vL = gvL; g.svL = 0.5 * gvL;
-    g.vR = gvR; g.svR = -0.5 * gvR;
-    g.zL = gzL;
-    g.zR = gzR;
+    // the adjoints of the face states (written: the caller's g holds nothing else).  Those of the cells'
+    // slopes follow from them (+1/2 on the left, -1/2 on the right), and the slope reverse forms them there.
+    g.eL = getaL; g.eR = getaR;
+    g.uL = guL; g.uR = guR;
+    g.vL = gvL; g.vR = gvR;
+    g.zL = gzL; g.zR = gzR;
 }
 
 // Reverse of van_leer_slope(qm, q, qp) (HydrostaticRoe.cpp:179-195).
@@ -461,20 +458,21 @@ __device__ __forceinline__ void slope_rev(double qm, double q, double qp, double
     gqp = gdp;
 }
 
-// slope_rev with the reciprocal from van_leer_slope_rs (rS == 0: the slope was 0 by a branch).
-__device__ __forceinline__ void slope_rev_rs(double qm, double q, double qp, double rS, double gs, double& gqm,
+// slope_rev with the reciprocal from van_leer_slope_rs (rS == 0: the slope was 0 by a branch), given
+// gs2 = twice the slope's adjoint (what the faces hand over: the slope enters each face state with 1/2).
+__device__ __forceinline__ void slope_rev_rs(double qm, double q, double qp, double rS, double gs2, double& gqm,
                                              double& gq, double& gqp) {
     gqm = gq = gqp = 0.0;
-    if ((sbits(gs) << 1) == 0) return;
+    if ((sbits(gs2) << 1) == 0) return;
     const double dm = q - qm, dp = qp - q;
     if ((sbits(rS) << 1) == 0) {
         if (!abs_le_bits(dp, Cst<double>::tol12_bits) && (sbits(dm) << 1) == 0) {  // r = 0: d s / d dm = 1
-            gq = gs;
-            gqm = -gs;
+            gq = 0.5 * gs2;
+            gqm = -gq;
         }
         return;
     }
-    const double t = 2.0 * gs * rS * rS;
+    const double t = gs2 * rS * rS;  // 2 gs / S^2
     const double gdm = t * dp * dp, gdp = t * dm * dm;
     gq = gdm - gdp;
     gqm = -gdm;
@@ -492,13 +490,13 @@ struct AdjSmem {
         struct {  // x pass
             double s[3][ATY][ATX + 4];      // slopes of columns x0-2 .. x0+TX+1
             double rs[3][ATY][ATX + 4];     // their 1 / (dm + dp) (fast form; 0 where the slope is 0 by a branch)
-            double fa[14][ATY][ATX + 3];    // face adjoints, faces x0-1 .. x0+TX+1
+            double fa[8][ATY][ATX + 3];     // face adjoints of eta, z, u, v on either side, faces x0-1 .. x0+TX+1
             double sp[9][ATY][ATX + 2];     // slope-reverse partials, columns x0-1 .. x0+TX
         } x;
         struct {  // y pass
             double s[3][ATY + 4][ATX];
             double rs[3][ATY + 4][ATX];
-            double fa[14][ATY + 3][ATX];
+            double fa[8][ATY + 3][ATX];
             double sp[9][ATY + 2][ATX];
         } y;
     } p;
@@ -708,19 +706,22 @@ __global__ void __launch_bounds__(ANT) k_adj_faces(AdjArgs A) {
                     face_rev<0, FAST>(fv, gFL, gFR, g);
                 }
             }
-            for (int q = 0; q < 14; ++q) P.fa[q][row][fcol + 1] = fget(g, q);
+            for (int q = 0; q < 8; ++q) P.fa[q][row][fcol + 1] = fget(g, q);
         }
         __syncthreads();
         for (int k = t; k < ATY * (ATX + 2); k += ANT) {  // slope reverse, columns x0-1 .. x0+TX
             const int row = k / (ATX + 2), col = k % (ATX + 2) - 1;
             const int r = row + H3, c = col + H3;
-            // slope of this column: read as the R slope by face col (index col+1) and as the L slope by face col+1
+            // slope of this column: read as the R slope by face col (index col+1), where the face state is
+            // q - s/2, and as the L slope by face col+1, where it is q + s/2; twice its adjoint is the
+            // difference of the two face states' adjoints
             for (int qi = 0; qi < 3; ++qi) {
-                const double gs = P.fa[9 + 2 * qi][row][col + 1] + P.fa[8 + 2 * qi][row][col + 2];
+                const int qL = qi == 0 ? 0 : 2 + 2 * qi, qR = qL + 1;  // eta: 0, 1; u: 4, 5; v: 6, 7
+                const double gs2 = P.fa[qL][row][col + 2] - P.fa[qR][row][col + 1];
                 const double(*Q)[GX] = qi == 0 ? S.eta : (qi == 1 ? S.u : S.v);
                 double gm, g0, gp;
-                if constexpr (FAST) slope_rev_rs(Q[r][c - 1], Q[r][c], Q[r][c + 1], P.rs[qi][row][col + 2], gs, gm, g0, gp);
-                else slope_rev(Q[r][c - 1], Q[r][c], Q[r][c + 1], gs, gm, g0, gp);
+                if constexpr (FAST) slope_rev_rs(Q[r][c - 1], Q[r][c], Q[r][c + 1], P.rs[qi][row][col + 2], gs2, gm, g0, gp);
+                else slope_rev(Q[r][c - 1], Q[r][c], Q[r][c + 1], 0.5 * gs2, gm, g0, gp);
                 P.sp[3 * qi + 0][row][col + 1] = gm;  // to column col-1
                 P.sp[3 * qi + 1][row][col + 1] = g0;  // to column col
                 P.sp[3 * qi + 2][row][col + 1] = gp;  // to column col+1
@@ -827,18 +828,19 @@ __global__ void __launch_bounds__(ANT) k_adj_faces(AdjArgs A) {
                     face_rev<1, FAST>(fv, gFL, gFR, g);
                 }
             }
-            for (int q = 0; q < 14; ++q) P.fa[q][frow + 1][col] = fget(g, q);
+            for (int q = 0; q < 8; ++q) P.fa[q][frow + 1][col] = fget(g, q);
         }
         __syncthreads();
         for (int k = t; k < (ATY + 2) * ATX; k += ANT) {  // slope reverse, rows y0-1 .. y0+TY
             const int row = k / ATX - 1, col = k % ATX;
             const int r = row + H3, c = col + H3;
-            for (int qi = 0; qi < 3; ++qi) {
-                const double gs = P.fa[9 + 2 * qi][row + 1][col] + P.fa[8 + 2 * qi][row + 2][col];
+            for (int qi = 0; qi < 3; ++qi) {  // as in the x pass: faces row (R side) and row+1 (L side)
+                const int qL = qi == 0 ? 0 : 2 + 2 * qi, qR = qL + 1;
+                const double gs2 = P.fa[qL][row + 2][col] - P.fa[qR][row + 1][col];
                 const double(*Q)[GX] = qi == 0 ? S.eta : (qi == 1 ? S.u : S.v);
                 double gm, g0, gp;
-                if constexpr (FAST) slope_rev_rs(Q[r - 1][c], Q[r][c], Q[r + 1][c], P.rs[qi][row + 2][col], gs, gm, g0, gp);
-                else slope_rev(Q[r - 1][c], Q[r][c], Q[r + 1][c], gs, gm, g0, gp);
+                if constexpr (FAST) slope_rev_rs(Q[r - 1][c], Q[r][c], Q[r + 1][c], P.rs[qi][row + 2][col], gs2, gm, g0, gp);
+                else slope_rev(Q[r - 1][c], Q[r][c], Q[r + 1][c], 0.5 * gs2, gm, g0, gp);
                 P.sp[3 * qi + 0][row + 1][col] = gm;
                 P.sp[3 * qi + 1][row + 1][col] = g0;
                 P.sp[3 * qi + 2][row + 1][col] = gp;
