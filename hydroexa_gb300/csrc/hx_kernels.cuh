@@ -21,6 +21,11 @@ namespace hx {
 // ---------------------------------------------------------------------------
 // Hydrostatic-Roe tile kernel.
 // ---------------------------------------------------------------------------
+// Sources with an interior fetch (kInterior): the fast form's phase A reads the stored depth directly on
+// tiles whose grown region lies in the level.
+template <class T, class = void> struct InteriorFetch : std::false_type {};
+template <class T> struct InteriorFetch<T, std::void_t<decltype(T::kInterior)>> : std::bool_constant<T::kInterior> {};
+
 template <class R, int TXv = TX, int TYv = TY> struct HydroSmem {
     static constexpr int GX = TXv + 4, GY = TYv + 4;
     R z[GY][GX], eta[GY][GX], u[GY][GX], v[GY][GX];
@@ -411,7 +416,28 @@ __device__ __forceinline__ void hydro_tile_body(HydroSmem<R, TXv, TYv>& S, const
     }
 
     // --- A: grown tile -> h rebuilt, eta = h + z, velocities -----------------
-    for (int idx = t; idx < GX * GY; idx += NTv) {
+    // The fast form on a grown tile inside the level (no ghost rule applies) takes the stored depth as it
+    // is: the reference's rebuild max(0, (h + z) - z) differs from it by rounding only.
+    bool interior = false;
+    if constexpr (FAST && InteriorFetch<Src>::value)
+        interior = src.interior(x0 - 2, y0 - 2, x0 + TXv + 1, y0 + TYv + 1);
+    if constexpr (FAST && InteriorFetch<Src>::value) {
+        if (interior) {
+            for (int idx = t; idx < GX * GY; idx += NTv) {
+                const int r = idx / GX, c = idx - r * GX;
+                R hh, zz, qx, qy;
+                src.fetch_in(x0 + c - 2, y0 + r - 2, hh, zz, qx, qy);
+                const R hp = max0_i(hh);
+                const R rh = gt_bits(hp, Cst<R>::tol12_bits) ? rcp_nr(hp) : R(0);
+                S.nod[r][c] = is_nodata(zz) ? 1 : 0;
+                S.z[r][c] = zz;
+                S.eta[r][c] = hp + zz;
+                S.u[r][c] = qx * rh;
+                S.v[r][c] = qy * rh;
+            }
+        }
+    }
+    for (int idx = interior ? GX * GY : t; idx < GX * GY; idx += NTv) {
         const int r = idx / GX, c = idx - r * GX;
         const int gi = x0 + c - 2, gj = y0 + r - 2;
         R e = R(0), zz = R(0), qx = R(0), qy = R(0), nn = R(0);
@@ -703,12 +729,25 @@ __device__ __forceinline__ void persist_stage(PersistStaging* st, const LevelSrc
 
 // Phase A's source: the staged grown tile, ghosts resolved as LevelSrc does.
 struct StagedSrc {
+    static constexpr bool kInterior = true;  // has interior() / fetch_in()
     const PersistStaging* st;
     int x0, y0, nx, ny;
     int bc_xlo, bc_xhi, bc_ylo, bc_yhi;
     int glo0, glo1, ghi0, ghi1;
     __device__ __forceinline__ bool inside(int i, int j) const {
         return i >= glo0 && i <= ghi0 && j >= glo1 && j <= ghi1;
+    }
+    // true when cells (i0, j0) .. (i1, j1) all lie in the level
+    __device__ __forceinline__ bool interior(int i0, int j0, int i1, int j1) const {
+        return i0 >= 0 && j0 >= 0 && i1 < nx && j1 < ny;
+    }
+    // (h, z, hu, hv) of a cell of the level, as stored
+    __device__ __forceinline__ void fetch_in(int i, int j, double& h, double& zz, double& qx, double& qy) const {
+        const int r = j - y0 + 2, c = i - x0 + 2;
+        h = st->h[r][c];
+        zz = st->z[r][c];
+        qx = st->hu[r][c];
+        qy = st->hv[r][c];
     }
     __device__ __forceinline__ void fetch(int i, int j, double& eta, double& zz, double& qx, double& qy,
                                           double& nn) const {
