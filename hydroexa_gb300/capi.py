@@ -20,6 +20,7 @@ HX_ERR_LAUNCH = -2
 HX_ERR_CUDA = -3
 HX_STATUS_DT_COLLAPSE = 1
 HX_STATUS_NAN = 2
+HX_STATUS_STAGING_TIMEOUT = 4
 HX_ARITH_EXACT = 0
 HX_ARITH_FAST = 1
 HX_ADJ_FACE_RECORDS = 0x100

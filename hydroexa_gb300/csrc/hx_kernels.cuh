@@ -11,6 +11,10 @@
 // written once per step.
 #pragma once
 
+#include <cuda.h>  // CUtensorMap (the type only; its encoder is reached through the runtime)
+
+#include <cstdint>
+#include <cstring>
 #include <type_traits>
 
 #include "hx_device.cuh"
@@ -391,6 +395,7 @@ template <class R> struct ThreadFold {
 // phase C, when the grown-tile and slope arrays are dead).
 struct NoHooks {
     __device__ __forceinline__ void after_load() const {}
+    __device__ __forceinline__ void faces_done() const {}
     __device__ __forceinline__ void after_faces() const {}
 };
 
@@ -402,12 +407,12 @@ __device__ __forceinline__ void hydro_tile_body(HydroSmem<R, TXv, TYv>& S, const
                                                 unsigned* status, unsigned* post_flags = nullptr,
                                                 const Div& div = Div{}, const Rec& rec = Rec{},
                                                 const Hooks& hooks = Hooks{}, ThreadFold<R>* defer = nullptr,
-                                                const Sync& sy = Sync{}) {
+                                                const Sync& sy = Sync{}, bool start_barrier = true) {
     static_assert(!Rec::on || (FAST && sizeof(R) == 8), "face records are kept for the FP64 fast form");
     constexpr int GX = HydroSmem<R, TXv, TYv>::GX, GY = HydroSmem<R, TXv, TYv>::GY;
     constexpr int CELLS = TXv * TYv;
     const int t = sy.tid();
-    sy.bar();  // the previous tile of this block is done with S
+    if (start_barrier) sy.bar();  // the previous tile of this block is done with S (else the caller synced)
     if (t == 0) {     // read after the barriers below
         S.kc[0] = dt / dx;
         S.kc[1] = dt / dy;
@@ -578,6 +583,7 @@ __device__ __forceinline__ void hydro_tile_body(HydroSmem<R, TXv, TYv>& S, const
             }
         }
     }
+    hooks.faces_done();
     sy.bar();
     hooks.after_faces();
 
@@ -695,11 +701,67 @@ struct PersistStaging {
 struct PersistOwn {
     double h[kPX * kPY], hu[kPX * kPY], hv[kPX * kPY], n[kPX * kPY];
     ThreadFold<double> fold[kPN];  // each thread's share of the next CFL bound (kept out of registers)
+    unsigned long long mbar;       // completion barrier of the TMA staging
 };
 static_assert(kPX * kPY <= kPN, "one cell per thread at most");
 static_assert(sizeof(PersistStaging) <= sizeof(double) * 3 * (kPY * (kPX + 2) + (kPY + 2) * kPX),
               "the staging buffer must fit in the slope arrays it lies on");
-constexpr size_t persist_smem_bytes() { return sizeof(HydroSmem<double, kPX, kPY>) + sizeof(PersistOwn); }
+// (+128: the staging arrays start on a 128-byte boundary, which the kernel rounds its shared base up to)
+constexpr size_t persist_smem_bytes() { return sizeof(HydroSmem<double, kPX, kPY>) + sizeof(PersistOwn) + 128; }
+static_assert(sizeof(double) * 4 * kPGX * kPGY % 128 == 0, "the staging buffer starts 128-byte aligned");
+static_assert(sizeof(double) * kPGX * kPGY % 128 == 0 && sizeof(double) * kPGX % 16 == 0,
+              "each staged plane starts 128-byte aligned; a staged row is a whole number of 16-byte units");
+
+// Tensor maps of the level's planes for the TMA staging: h, hu, hv, z in 36 x 36 boxes (the grown tile),
+// n in 32 x 32 boxes (the own cells).  valid = 0: the planes do not meet TMA's alignment (16-byte base
+// and row pitch); the kernel stages by cp.async instead.
+struct PersistMaps {
+    CUtensorMap h, hu, hv, z, n;
+    int valid;
+};
+constexpr unsigned kStageBytes = (unsigned)(sizeof(double) * (4 * kPGX * kPGY + kPX * kPY));
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long* bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Waits for the phase of the given parity to complete, for about a second at most (each try_wait suspends
+// for a bounded, hardware-chosen time); false when it did not.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity) {
+    for (int k = 0; k < (1 << 21); ++k)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+// One 2D tile of a tensor map into shared memory; its bytes complete the barrier's transaction count.
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, unsigned long long* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+        ::"r"(smem_u32(dst)), "l"(map), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+// Thread 0: the five planes of tile (x0, y0).  x0 is a multiple of 32, so the grown box's x = x0 - 2 is
+// even: 16-byte aligned in doubles, as TMA requires of the innermost coordinate.  Boxes reaching past the
+// level are filled with zeros there; nothing reads those cells (ghosts are resolved to level cells).
+__device__ __forceinline__ void persist_stage_tma(PersistStaging* st, const PersistMaps& m, int x0, int y0,
+                                                  unsigned long long* bar) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(kStageBytes)
+                 : "memory");
+    tma_load_2d(&st->h[0][0], &m.h, x0 - 2, y0 - 2, bar);
+    tma_load_2d(&st->hu[0][0], &m.hu, x0 - 2, y0 - 2, bar);
+    tma_load_2d(&st->hv[0][0], &m.hv, x0 - 2, y0 - 2, bar);
+    tma_load_2d(&st->z[0][0], &m.z, x0 - 2, y0 - 2, bar);
+    tma_load_2d(&st->n[0][0], &m.n, x0, y0, bar);
+}
 
 __device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
     const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
@@ -781,6 +843,7 @@ struct PersistHooks {
     PersistStaging* st;
     PersistOwn* own;
     const LevelSrc<double>* src;
+    const PersistMaps* maps;  // null: cp.async staging
     int nx0, ny0;  // origin of the next tile
     bool next;
     __device__ __forceinline__ void after_load() const {
@@ -791,21 +854,36 @@ struct PersistHooks {
         own->hv[t] = st->hv[r][c];
         own->n[t] = st->n[r - 2][c - 2];
     }
+    // the staging buffer lies on the slope arrays: order this thread's accesses to them (generic proxy)
+    // before the TMA writes (async proxy) that the next tile's staging issues after the barrier
+    __device__ __forceinline__ void faces_done() const {
+        if (maps) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
     __device__ __forceinline__ void after_faces() const {
-        if (next) persist_stage(st, *src, nx0, ny0);
+        if (!next) return;
+        if (maps) {
+            if (threadIdx.x == 0) persist_stage_tma(st, *maps, nx0, ny0, &own->mbar);
+        } else {
+            persist_stage(st, *src, nx0, ny0);
+        }
     }
 };
 
 // With Div = DivOut<double> the kernel writes the flux differences of every
 // cell instead of the update (the first step of the host-buffer call, whose
 // update waits for the level's dt): no dt, no CFL fold.
+// The next tile is staged by TMA (five 2D tensor-map loads issued by one thread, completing on an mbarrier)
+// when the planes allow it (maps.valid), else by cp.async from every thread.  A TMA wait that runs out
+// (about a second) sets HX_STATUS_STAGING_TIMEOUT and ends the block's work after a second bounded wait for
+// the copies in flight.
 template <bool FAST, class Div = NoDiv>
 __global__ void __launch_bounds__(kPN, 1)
     k_hydro_persist(LevelSrc<double> src, Cells3W<double> out, IBox vb, int tiles_x, int ntiles,
-                    StepCtl<double> ctl, Div div = Div{}) {
+                    StepCtl<double> ctl, Div div, const __grid_constant__ PersistMaps maps, unsigned* err) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    HydroSmem<double, kPX, kPY>& S = *reinterpret_cast<HydroSmem<double, kPX, kPY>*>(smem_raw);
-    PersistOwn* own = reinterpret_cast<PersistOwn*>(smem_raw + sizeof(HydroSmem<double, kPX, kPY>));
+    unsigned char* base = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);  // 128-byte aligned
+    HydroSmem<double, kPX, kPY>& S = *reinterpret_cast<HydroSmem<double, kPX, kPY>*>(base);
+    PersistOwn* own = reinterpret_cast<PersistOwn*>(base + sizeof(HydroSmem<double, kPX, kPY>));
     PersistStaging* st = reinterpret_cast<PersistStaging*>(&S.sxe[0][0]);
     double dt = 0.0;
     if constexpr (!Div::on) {
@@ -815,24 +893,87 @@ __global__ void __launch_bounds__(kPN, 1)
     const bool fold = !Div::on && ctl.dt_out != nullptr;
     int k = (int)blockIdx.x;
     if (k >= ntiles) return;
-    persist_stage(st, src, vb.lo0 + (k % tiles_x) * kPX, vb.lo1 + (k / tiles_x) * kPY);
+    const bool tma = maps.valid != 0;
+    if (tma) {
+        if (threadIdx.x == 0) {
+            mbar_init(&own->mbar);
+            persist_stage_tma(st, maps, vb.lo0 + (k % tiles_x) * kPX, vb.lo1 + (k / tiles_x) * kPY, &own->mbar);
+        }
+        __syncthreads();  // the barrier is initialised before any thread waits on it
+    } else {
+        persist_stage(st, src, vb.lo0 + (k % tiles_x) * kPX, vb.lo1 + (k / tiles_x) * kPY);
+    }
     ThreadFold<double>* tf = &own->fold[threadIdx.x];
     *tf = ThreadFold<double>{};
     const FaceOut<double> fo{};
+    unsigned parity = 0;
     for (; k < ntiles; k += (int)gridDim.x) {
         const int x0 = vb.lo0 + (k % tiles_x) * kPX, y0 = vb.lo1 + (k / tiles_x) * kPY;
         const int kn = k + (int)gridDim.x;
-        const PersistHooks hooks{st, own, &src, vb.lo0 + (kn % tiles_x) * kPX, vb.lo1 + (kn / tiles_x) * kPY,
-                                 kn < ntiles};
+        const PersistHooks hooks{st, own, &src, tma ? &maps : nullptr, vb.lo0 + (kn % tiles_x) * kPX,
+                                 vb.lo1 + (kn / tiles_x) * kPY, kn < ntiles};
         const StagedSrc ss{st, x0, y0, src.nx, src.ny, src.bc_xlo, src.bc_xhi, src.bc_ylo, src.bc_yhi,
                            src.glo0, src.glo1, src.ghi0, src.ghi1};
-        cp_async_wait_all();  // this thread's copies of tile k; the body's first barrier publishes everyone's
+        if (tma) {
+            // tile k's planes have landed (the barrier below also ends the previous tile's use of S)
+            const bool late = !mbar_wait_bounded(&own->mbar, parity);
+            parity ^= 1u;
+            if (__syncthreads_or(late)) {
+                if (threadIdx.x == 0) {
+                    if (err) atomicOr(err, (unsigned)HX_STATUS_STAGING_TIMEOUT);
+                    mbar_wait_bounded(&own->mbar, parity ^ 1u);  // the copies in flight, once more
+                }
+                __syncthreads();
+                return;
+            }
+        } else {
+            cp_async_wait_all();  // this thread's copies of tile k; the body's first barrier publishes everyone's
+        }
         hydro_tile_body<double, FAST, kPX, kPY, kPN, StagedSrc, false, Div, NoRec, OwnState, OwnRough,
                         PersistHooks>(S, ss, OwnState{own, x0, y0}, OwnRough{own, x0, y0}, out, fo, vb, x0, y0, dt,
                                       ctl.dx, ctl.dy, nullptr, Div::on ? nullptr : ctl.status, nullptr, div,
-                                      NoRec{}, hooks, fold ? tf : nullptr);
+                                      NoRec{}, hooks, fold ? tf : nullptr, BlockSync{}, !tma);
     }
     if (fold) block_fold_dt<double, kPN>(tf->rate, tf->mv, tf->flags, ctl.dt_out);
+}
+
+// Tensor maps of the level's planes for k_hydro_persist's TMA staging (host side; valid = 0 where the
+// planes do not meet TMA's alignment, or the encoder is unavailable).
+inline PersistMaps persist_maps(const LevelSrc<double>& src) {
+    PersistMaps m;
+    std::memset(&m, 0, sizeof m);
+    using Encode = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+    static const Encode enc = [] {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            fn = nullptr;
+        return reinterpret_cast<Encode>(fn);
+    }();
+    const unsigned long long row = (unsigned long long)src.pitch * sizeof(double);
+    const double* planes[5] = {src.h, src.hu, src.hv, src.z, src.n};
+    if (!enc || row % 16 != 0) return m;
+    for (const double* p : planes)
+        if (reinterpret_cast<uintptr_t>(p) % 16 != 0) return m;
+    const cuuint64_t dims[2] = {(cuuint64_t)src.nx, (cuuint64_t)src.ny};
+    const cuuint64_t strides[1] = {(cuuint64_t)row};
+    const cuuint32_t grown[2] = {(cuuint32_t)kPGX, (cuuint32_t)kPGY}, own[2] = {(cuuint32_t)kPX, (cuuint32_t)kPY};
+    const cuuint32_t unit[2] = {1, 1};
+    CUtensorMap* maps[5] = {&m.h, &m.hu, &m.hv, &m.z, &m.n};
+    for (int k = 0; k < 5; ++k) {
+        if (enc(maps[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, const_cast<double*>(planes[k]), dims, strides,
+                k < 4 ? grown : own, unit, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS) {
+            std::memset(&m, 0, sizeof m);
+            return m;
+        }
+    }
+    m.valid = 1;
+    return m;
 }
 
 // ---------------------------------------------------------------------------
@@ -1497,8 +1638,9 @@ cudaError_t launch_hydro(const Src& src, const Cells3<R>& uo, const Plane<R>& np
             auto k = k_hydro_persist<FAST>;
             e = ensure_smem(k, persist_smem_bytes());
             if (e != cudaSuccess) return e;
-            k<<<(unsigned)(ntiles < sms ? ntiles : sms), kPN, persist_smem_bytes(), st>>>(src, out, vb, (int)tg.x,
-                                                                                        ntiles, ctl, NoDiv{});
+            const PersistMaps maps = persist_maps(src);
+            k<<<(unsigned)(ntiles < sms ? ntiles : sms), kPN, persist_smem_bytes(), st>>>(
+                src, out, vb, (int)tg.x, ntiles, ctl, NoDiv{}, maps, ctl.status);
             return cudaGetLastError();
         }
     }
@@ -1591,8 +1733,9 @@ cudaError_t launch_hydro_split(const LevelSrc<R>& src, const Cells3<R>& uo, cons
             ctl.dx = dx;
             ctl.dy = dy;
             (void)np;
+            const PersistMaps maps = persist_maps(src);
             k<<<(unsigned)(ntiles < sms ? ntiles : sms), kPN, persist_smem_bytes(), st>>>(
-                src, Cells3W<double>{}, vb, (int)tg.x, ntiles, ctl, div);
+                src, Cells3W<double>{}, vb, (int)tg.x, ntiles, ctl, div, maps, nullptr);
             return cudaGetLastError();
         }
     }

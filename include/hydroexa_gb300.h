@@ -61,6 +61,8 @@ enum {
 enum {
     HX_STATUS_DT_COLLAPSE = 1, /* min CFL bound < 1e-12 (HydrostaticRoe.cpp:77, Roe.cpp:88) */
     HX_STATUS_NAN = 2,         /* a NaN or Inf appeared in an updated state */
+    HX_STATUS_STAGING_TIMEOUT = 4, /* the level kernel's TMA staging wait ran out (about a second); the step
+                                      is incomplete (not expected: a fault of the copy hardware or driver) */
 };
 
 enum { HX_ARITH_EXACT = 0, HX_ARITH_FAST = 1 };

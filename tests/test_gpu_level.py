@@ -421,3 +421,25 @@ def test_host_buffer_run_on_two_devices(cuda, hxlib):
             assert rc == 0, hxlib.lib().hx_last_error()
             assert np.array_equal(h, want[0]) and np.array_equal(hu, want[1]) and np.array_equal(hv, want[2])
     hxlib.lib().hx_host_cache_release()
+
+
+@pytest.mark.parametrize("arith", [EXACT, FAST])
+def test_persistent_staging_tma_equals_cp_async(cuda, arith):
+    """The persistent level kernel stages each tile by TMA when the planes' rows
+    are whole 16-byte units, else by cp.async: a 2048^2 level stored with row
+    pitch 2048 and 2050 (TMA) and 2049 (cp.async) gives the same state, bit for
+    bit, after three steps of the device loop, with a clean status."""
+    case = workloads.fractal_dam_break(2048, 2048, seed=5)
+    out = []
+    for pitch in (2048, 2049, 2050):
+        st = torch.zeros((3, 2048, pitch), dtype=torch.float64)
+        tr = torch.zeros((2, 2048, pitch), dtype=torch.float64)
+        for k, a in enumerate((case.h, case.hu, case.hv)):
+            st[k, :, :2048] = torch.from_numpy(a)
+        tr[0, :, :2048] = torch.from_numpy(case.z)
+        tr[1, :, :2048] = torch.from_numpy(case.n)
+        lev = Level(case.geom, st.to(cuda), tr.to(cuda))
+        assert lev.run(1, 3, case.cfl, arith=arith) == 0
+        out.append((lev.state[:, :, :2048].cpu().numpy(), lev.time.item()))
+    for s, t in out[1:]:
+        assert np.array_equal(s, out[0][0]) and t == out[0][1]
