@@ -503,6 +503,11 @@ namespace hx {
 // thread's last error text.
 void note_launches(int n) { g_launches.fetch_add((unsigned long long)n, std::memory_order_relaxed); }
 int set_error(int code, const char* msg) { return fail(code, "%s", msg); }
+// The persistent level kernel's extra expected staging bytes (hx_debug_staging_extra_bytes).
+unsigned& staging_test_extra_bytes() {
+    static unsigned extra = 0;
+    return extra;
+}
 }  // namespace hx
 
 // ============================================================================
@@ -982,6 +987,12 @@ int hx_debug_rcp_f64(long n, const double* x, double* y, hx_stream_t s) {
 int hx_debug_sqrt_f64(long n, const double* x, double* y, hx_stream_t s) {
     if (n < 0 || (n > 0 && (!x || !y))) return fail(HX_ERR_ARG, "bad square-root arrays");
     return launched(launch_rcp<true>(n, x, y, 1, (cudaStream_t)s), "hx_debug_sqrt_f64");
+}
+
+int hx_debug_staging_extra_bytes(unsigned bytes) {
+    const unsigned old = staging_test_extra_bytes();
+    staging_test_extra_bytes() = bytes;
+    return (int)old;
 }
 
 int hx_debug_fast_op_f64(int op, long n, const double* x, double* y, hx_stream_t s) {

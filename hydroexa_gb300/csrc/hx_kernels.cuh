@@ -718,6 +718,7 @@ static_assert(sizeof(double) * kPGX * kPGY % 128 == 0 && sizeof(double) * kPGX %
 struct PersistMaps {
     CUtensorMap h, hu, hv, z, n;
     int valid;
+    unsigned extra_tx;  // added to the expected bytes: nonzero only to test the bounded wait (it then runs out)
 };
 constexpr unsigned kStageBytes = (unsigned)(sizeof(double) * (4 * kPGX * kPGY + kPX * kPY));
 
@@ -735,11 +736,20 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned 
         : "memory");
     return ok != 0;
 }
-// Waits for the phase of the given parity to complete, for about a second at most (each try_wait suspends
-// for a bounded, hardware-chosen time); false when it did not.
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+// Waits for the phase of the given parity to complete, for one second at most by the global timer (each
+// try_wait suspends for a bounded, hardware-chosen time, and at most 2^24 of them are tried); false when
+// it did not.
 __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity) {
-    for (int k = 0; k < (1 << 21); ++k)
+    const unsigned long long t0 = global_ns();
+    for (int k = 0; k < (1 << 24); ++k) {
         if (mbar_try_wait(bar, parity)) return true;
+        if (global_ns() - t0 > 1000000000ull) break;
+    }
     return false;
 }
 // One 2D tile of a tensor map into shared memory; its bytes complete the barrier's transaction count.
@@ -754,7 +764,8 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
 // level are filled with zeros there; nothing reads those cells (ghosts are resolved to level cells).
 __device__ __forceinline__ void persist_stage_tma(PersistStaging* st, const PersistMaps& m, int x0, int y0,
                                                   unsigned long long* bar) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(kStageBytes)
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(kStageBytes + m.extra_tx)
                  : "memory");
     tma_load_2d(&st->h[0][0], &m.h, x0 - 2, y0 - 2, bar);
     tma_load_2d(&st->hu[0][0], &m.hu, x0 - 2, y0 - 2, bar);
@@ -937,6 +948,9 @@ __global__ void __launch_bounds__(kPN, 1)
     if (fold) block_fold_dt<double, kPN>(tf->rate, tf->mv, tf->flags, ctl.dt_out);
 }
 
+// Extra bytes the next launches' staging waits for (a test setting; 0 in use).
+unsigned& staging_test_extra_bytes();
+
 // Tensor maps of the level's planes for k_hydro_persist's TMA staging (host side; valid = 0 where the
 // planes do not meet TMA's alignment, or the encoder is unavailable).
 inline PersistMaps persist_maps(const LevelSrc<double>& src) {
@@ -973,6 +987,7 @@ inline PersistMaps persist_maps(const LevelSrc<double>& src) {
         }
     }
     m.valid = 1;
+    m.extra_tx = staging_test_extra_bytes();
     return m;
 }
 

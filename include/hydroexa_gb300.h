@@ -660,6 +660,10 @@ enum {
     HX_FAST_OP_SQRT_FAITHFUL = 4
 };
 int hx_debug_fast_op_f64(int op, long n, const double* x, double* y, hx_stream_t stream);
+/* Test setting of the persistent level kernel's TMA staging: the next launches wait for this many bytes
+ * more than the tiles bring, so the bounded wait runs out (about a second per block) and the step ends with
+ * HX_STATUS_STAGING_TIMEOUT; 0 (the default) restores normal operation.  Returns the previous value. */
+int hx_debug_staging_extra_bytes(unsigned bytes);
 /* The row bands hx_level_run_host_f64 uses for ny rows (host only, no GPU):
  * writes band starts into starts[0..n] (starts[n] = ny) and returns n, at
  * most 10; max_bands must be at least 10. */

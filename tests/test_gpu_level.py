@@ -443,3 +443,22 @@ def test_persistent_staging_tma_equals_cp_async(cuda, arith):
         out.append((lev.state[:, :, :2048].cpu().numpy(), lev.time.item()))
     for s, t in out[1:]:
         assert np.array_equal(s, out[0][0]) and t == out[0][1]
+
+
+def test_persistent_staging_wait_is_bounded(cuda, hxlib):
+    """The persistent kernel's TMA staging wait is bounded: with the test
+    setting that makes every tile wait for 16 bytes more than it brings, the
+    wait runs out after about a second, the step ends with
+    HX_STATUS_STAGING_TIMEOUT instead of hanging, and the context stays usable:
+    the same step with the normal setting runs clean afterwards."""
+    case = workloads.fractal_dam_break(2048, 2048, seed=5)
+    L = hxlib.lib()
+    lev = Level.from_numpy(case.geom, case.h, case.hu, case.hv, case.z, case.n, device=cuda)
+    assert L.hx_debug_staging_extra_bytes(16) == 0
+    try:
+        st = lev.run(1, 1, case.cfl, arith=FAST)
+    finally:
+        L.hx_debug_staging_extra_bytes(0)
+    assert st & capi.HX_STATUS_STAGING_TIMEOUT
+    lev = Level.from_numpy(case.geom, case.h, case.hu, case.hv, case.z, case.n, device=cuda)
+    assert lev.run(1, 1, case.cfl, arith=FAST) == 0
