@@ -406,12 +406,14 @@ template <class R> int accum_read(const hx_dt_accum* acc, R* dtmin, R* maxvel, c
 }
 
 // ---------------------------------------------------------------- host form
-// Device buffers of the host-buffer entry, kept between calls, and four
+// Device buffers of the host-buffer entry, kept between calls, and three
 // streams: uploads and downloads (one each: a copy engine does not interleave
-// two streams' queues, so bands go in order on one), the CFL reduction of the
-// uploaded level and the first step's per-band updates.  The last two run at
-// the highest priority, so that their few blocks are scheduled ahead of the
-// flux work queued on the caller's stream and the bands go down early.
+// two streams' queues, so bands go in order on one) and the CFL reduction of
+// the uploaded level, at the highest priority, so that its few blocks are
+// scheduled ahead of the flux work queued on the caller's stream.  (The
+// split bands' updates run on the caller's stream once dt is known: on a
+// stream of their own they only got the GPU between two of the persistent
+// flux kernels, which hold every SM, and their bands went down late.)
 constexpr int kHostBands = 10;  // at most: a short first and last band, up to eight between
 constexpr int kHeadRows = 2;  // rows of the next band the flux differences of a band read (the MUSCL reach)
 // One cache per device and thread: the buffers, streams and events are created
@@ -420,15 +422,16 @@ struct HostCache {
     int device = -1;  // ordinal the resources belong to
     void* base = nullptr;
     size_t bytes = 0;
-    cudaStream_t cs[4] = {nullptr, nullptr, nullptr, nullptr};  // uploads, downloads, CFL reduction, updates
-    // start, dt known, updates done, four joins; per band: landed, head landed, flux differences, computed
+    static constexpr int kStreams = 3;
+    cudaStream_t cs[kStreams] = {nullptr, nullptr, nullptr};  // uploads, downloads, CFL reduction
+    // start, dt known, (spare), four joins; per band: landed, head landed, (spare), computed
     cudaEvent_t ev[7 + 4 * kHostBands] = {};
     bool streams_ok = false;
     bool ensure_streams() {
         if (streams_ok) return true;
         int least = 0, greatest = 0;
         if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) return false;
-        for (int k = 0; k < 4; ++k)
+        for (int k = 0; k < kStreams; ++k)
             if (cudaStreamCreateWithPriority(&cs[k], cudaStreamNonBlocking, k >= 2 ? greatest : least) != cudaSuccess)
                 return false;
         for (auto& e : ev)
@@ -731,7 +734,7 @@ int hx_level_run_host_f64(int method, int nx, int ny, double dx, double dy, cons
     cudaEvent_t* ev = hc->ev;
     // an error after work was queued returns once the queued copies have finished with the caller's buffers
     auto drain = [&](int r) -> int {
-        for (int k = 0; k < 4; ++k) cudaStreamSynchronize(cs[k]);
+        for (int k = 0; k < HostCache::kStreams; ++k) cudaStreamSynchronize(cs[k]);
         cudaStreamSynchronize(st);
         return r;
     };
@@ -764,20 +767,19 @@ int hx_level_run_host_f64(int method, int nx, int ny, double dx, double dy, cons
     };
     // Upload in row bands (stream up), after the caller's earlier work; from the second band on, a band's
     // first kHeadRows rows go up ahead of the rest.  The CFL reduction of each band runs as soon as its rows
-    // have landed.  Split: the reduction on its own stream (dts), while st runs each band's flux differences
-    // once the head of the band after it has landed; the updates (stream upd) start when dt is known, each
-    // after its band's flux differences, and each band's rows go down (stream down) under the flux work of
-    // later bands.
-    cudaStream_t up = cs[0], down = cs[1], dts = cs[2], upd = cs[3];
-    cudaEvent_t ev_start = ev[0], ev_dt = ev[1], ev_upd = ev[2];
+    // have landed.  Split: the reduction on its own high-priority stream (dts), while st runs each split
+    // band's flux differences once the head of the band after it has landed, then (dt known) the split
+    // bands' updates and the later bands' fused steps; each band's rows go down (stream down) as soon as
+    // they are final, under the rest of the step.
+    cudaStream_t up = cs[0], down = cs[1], dts = cs[2];
+    cudaEvent_t ev_start = ev[0], ev_dt = ev[1];
     cudaEvent_t* ev_join = ev + 3;
     cudaEvent_t* ev_up = ev + 7;
     cudaEvent_t* ev_head = ev + 7 + kHostBands;
-    cudaEvent_t* ev_flux = ev + 7 + 2 * kHostBands;
     cudaEvent_t* ev_k = ev + 7 + 3 * kHostBands;
     cudaError_t e = cudaMemsetAsync(tail, 0, 128 + 3 * sizeof(DtAccum), st);
     if (e == cudaSuccess) e = cudaEventRecord(ev_start, st);
-    for (int k = 0; k < 4 && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(cs[k], ev_start, 0);
+    for (int k = 0; k < HostCache::kStreams && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(cs[k], ev_start, 0);
     int rc = HX_OK;
     cudaStream_t dstream = split ? dts : st;
     auto upload = [&](int r0, int r1) -> cudaError_t {  // rows r0..r1 of the five planes
@@ -836,14 +838,16 @@ int hx_level_run_host_f64(int method, int nx, int ny, double dx, double dy, cons
         Cells3W<double> ow;
         ow.p[0] = o[0]; ow.p[1] = o[1]; ow.p[2] = o[2];
         ow.js = nx; ow.lo0 = 0; ow.lo1 = 0;
-        // Bands from kf on start once dt is known, when the whole level has landed: the fused kernel advances
-        // them in one pass, without the flux-difference planes and the separate update (the same arithmetic).
-        // kf is the first band starting past 55% of the rows.  The upload (40 B per cell at ~210 GB/s on
-        // GB300) takes under half as long as the flux work (~3.3 us per row of 8192 cells), so dt is known
-        // before the flux work of the bands ahead of kf runs out.
+        // The bands ahead of kf are split: their flux differences run as their rows land.  kf is the first
+        // band starting past 45% of the rows: on GB300 the upload (40 B per cell at ~210 GB/s) takes about as
+        // long as the flux work of that share (~3.2 us per row of 8192 cells), so dt -- whose reduction runs
+        // on its own stream as the rows land, in the gaps between the flux kernels -- is known when that work
+        // ends.  Then, on the caller's stream, the split bands' updates (short: their rows start going down at
+        // once, under the rest of the step) and the later bands through the fused kernel in one pass, without
+        // the flux-difference planes and the separate update (the same arithmetic).
         int kf = nbands;
         for (int b = 1; b < nbands; ++b)
-            if ((long long)starts[b] * 20 >= (long long)ny * 11) {
+            if ((long long)starts[b] * 20 >= (long long)ny * 9) {
                 kf = b;
                 break;
             }
@@ -857,32 +861,23 @@ int hx_level_run_host_f64(int method, int nx, int ny, double dx, double dy, cons
             const int c = band_of(r, nbands, starts);
             e = cudaStreamWaitEvent(st, (c > b && r < starts[c] + kHeadRows) ? ev_head[c] : ev_up[c], 0);
             if (e == cudaSuccess) rc = flux_band(b);
-            if (rc == HX_OK && e == cudaSuccess) e = cudaEventRecord(ev_flux[b], st);
         }
-        if (e == cudaSuccess) e = cudaStreamWaitEvent(upd, ev_dt, 0);  // dt of the whole level
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ev_dt, 0);  // dt of the whole level
         for (int b = 0; b < kf && rc == HX_OK && e == cudaSuccess; ++b) {
             int j0, j1;
             rows(b, j0, j1);
             const IBox vb{0, j0, nx - 1, j1};
-            const StepCtl<double> cb = step_ctl(0, b);
-            e = cudaStreamWaitEvent(upd, ev_flux[b], 0);
-            if (e != cudaSuccess) break;
-            rc = launched(fast ? launch_hydro_update<double, true>(uo, div, np, zp, ow, vb, cb, upd)
-                               : launch_hydro_update<double, false>(uo, div, np, zp, ow, vb, cb, upd),
+            rc = launched(fast ? launch_hydro_update<double, true>(uo, div, np, zp, ow, vb, step_ctl(0, b), st)
+                               : launch_hydro_update<double, false>(uo, div, np, zp, ow, vb, step_ctl(0, b), st),
                           "hx_level_run_host_f64 (update)");
-            if (rc == HX_OK && nsteps == 1) e = download(b, o, upd);
+            if (rc == HX_OK && nsteps == 1) e = download(b, o, st);
         }
-        // (queued after the split bands' downloads: the copy stream runs its copies in queue order)
-        if (e == cudaSuccess && kf < nbands) e = cudaStreamWaitEvent(st, ev_dt, 0);
         for (int b = kf; b < nbands && rc == HX_OK && e == cudaSuccess; ++b) {
             int j0, j1;
             rows(b, j0, j1);
             rc = level_advance<double>(method, &L, step_ctl(0, b), o[0], o[1], o[2], arith, st, j0, j1);
             if (rc == HX_OK && nsteps == 1) e = download(b, o, st);
         }
-        // the later steps read every band's update
-        if (rc == HX_OK && e == cudaSuccess) e = cudaEventRecord(ev_upd, upd);
-        if (rc == HX_OK && e == cudaSuccess) e = cudaStreamWaitEvent(st, ev_upd, 0);
         if (e != cudaSuccess) return drain(fail(HX_ERR_CUDA, "split step: %s", cudaGetErrorString(e)));
         if (rc) return drain(rc);
         res[0] = o[0]; res[1] = o[1]; res[2] = o[2];
@@ -914,8 +909,8 @@ int hx_level_run_host_f64(int method, int nx, int ny, double dx, double dy, cons
         for (int k = 0; k < 3 && e == cudaSuccess; ++k)
             e = cudaMemcpyAsync(dst[k], res[k], pb, cudaMemcpyDeviceToHost, down);
     }
-    for (int k = 0; k < 4 && e == cudaSuccess; ++k) e = cudaEventRecord(ev_join[k], cs[k]);  // join all four
-    for (int k = 0; k < 4 && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(st, ev_join[k], 0);
+    for (int k = 0; k < HostCache::kStreams && e == cudaSuccess; ++k) e = cudaEventRecord(ev_join[k], cs[k]);
+    for (int k = 0; k < HostCache::kStreams && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(st, ev_join[k], 0);
     uint32_t sv = 0;
     double tv = 0;
     if (e == cudaSuccess) e = cudaMemcpyAsync(&sv, status, 4, cudaMemcpyDeviceToHost, st);
