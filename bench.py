@@ -295,18 +295,20 @@ def main():
             e2e_step()
         ke = max(3, min(args.steps, 10))
         barrier()
-        f0 = torch.cuda.Event(enable_timing=True)
-        f1 = torch.cuda.Event(enable_timing=True)
-        f0.record(stream)
-        for _ in range(ke):
+        marks = [torch.cuda.Event(enable_timing=True) for _ in range(ke + 1)]
+        marks[0].record(stream)
+        for k in range(ke):
             e2e_step()
-        f1.record(stream)
-        f1.synchronize()
-        ems = ranks.reduce_real_max([f0.elapsed_time(f1)])[0]
+            marks[k + 1].record(stream)
+        marks[-1].synchronize()
+        ems = ranks.reduce_real_max([marks[0].elapsed_time(marks[-1])])[0]
+        calls = sorted(marks[k].elapsed_time(marks[k + 1]) for k in range(ke))
         L.hx_host_cache_release()
         e2e = {"value": ws * cells * ke / (ems * 1e-3) / 1e6, "unit": UNIT, "h2d_bytes_per_step": 40 * cells,
                "d2h_bytes_per_step": 24 * cells + 12, "steps": ke,
-               "call": "hx_level_run_host_f64 (host buffers in/out, one step per call)"}
+               "call": "hx_level_run_host_f64 (host buffers in/out, one step per call)",
+               # the spread of the calls (each includes its host copies, whose rate varies with the host)
+               "ms_per_call": {"min": calls[0], "median": calls[len(calls) // 2], "max": calls[-1]}}
 
     ens = None
     if args.precision == "f64" and args.method == "hydrostatic" and not args.no_ensemble:
