@@ -275,6 +275,9 @@ def main():
     kms = statistics.mean(ev[2 * k].elapsed_time(ev[2 * k + 1]) for k in range(5))
     achieved_gbs = BYTES_PER_CELL[args.precision] * cells / (kms * 1e-3) / 1e9
     profile = load_profile_summary()
+    epi = None
+    if args.method == "hydrostatic":
+        epi = epilogue_measure(lev, dt, acc_out, arith, stream)
 
     # ---- end to end through the host-buffer C-ABI call (pinned host memory)
     e2e = None
@@ -338,6 +341,7 @@ def main():
             "fp64_pipe_frac": pipe["frac"] if pipe else None,
             "ensemble": ensemble_summary(ens),
             "adjoint": adjoint_summary(adj),
+            "epilogue": epi,
             "details_file": args.details if (ens is not None or adj is not None) else None,
             "config": dict(config_dict(), arith=args.arith, nx=NX, ny=NY, precision=args.precision.upper(),
                            method={"hydrostatic": "HydrostaticRoe", "roe": "Roe (no NODATA)"}[args.method]),
@@ -360,6 +364,62 @@ def main():
         dist.barrier()
         dist.destroy_process_group()
     return 0
+
+
+def epilogue_measure(lev, dt, out, arith, stream, reps=5):
+    """The step with its epilogue (eta = h + z and the conservation diagnostics
+    written by the update) against the plain step followed by the separate eta
+    and diagnostics passes, one launch sequence at a time with events on the
+    launching stream.  Inputs larger than L2 (8192^2 x 5 planes)."""
+    import ctypes
+
+    import torch
+
+    from hydroexa_gb300 import capi
+    from hydroexa_gb300.level import array4, box
+    L = capi.lib()
+    g = lev.geom
+    b = box((0, 0), (g.nx - 1, g.ny - 1))
+    eta = torch.empty_like(lev.state[0])
+    diag = torch.empty(5, dtype=torch.float64, device=lev.state.device)
+    work = torch.empty(int(L.hx_diagnostics_work_bytes(b)), dtype=torch.uint8, device=lev.state.device)
+    vp = lambda t: ctypes.c_void_p(t.data_ptr())
+    sfx = lev.sfx
+    d_out = lev._desc(out)
+    T, O, E = array4(lev.terrain), array4(out), array4(eta)
+    sh = ctypes.c_void_p(stream.cuda_stream)
+
+    def fused():
+        lev.advance_epilogue(dt, out=out, arith=arith, stream=stream)
+
+    def separate():
+        lev.advance(capi.HX_METHOD_HYDROSTATIC_ROE, dt, out=out, arith=arith, stream=stream)
+        capi.check(getattr(L, "hx_derive_eta_box_" + sfx)(ctypes.byref(O), ctypes.byref(T), ctypes.byref(E), b, sh))
+        if sfx == "f64":
+            capi.check(L.hx_level_diagnostics_f64(ctypes.byref(d_out), vp(diag), vp(work), sh))
+        else:
+            Rt = ctypes.c_float
+            capi.check(L.hx_diagnostics_box_f32(ctypes.byref(O), ctypes.byref(T), b, Rt(g.dx), Rt(g.dy), vp(diag),
+                                                vp(work), sh))
+
+    def timed(fn):
+        fn()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * reps)]
+        for k in range(reps):
+            ev[2 * k].record(stream)
+            fn()
+            ev[2 * k + 1].record(stream)
+        torch.cuda.synchronize(lev.state.device)
+        return statistics.mean(ev[2 * k].elapsed_time(ev[2 * k + 1]) for k in range(reps))
+
+    def plain():
+        lev.advance(capi.HX_METHOD_HYDROSTATIC_ROE, dt, out=out, arith=arith, stream=stream)
+
+    p_ms, f_ms, s_ms = timed(plain), timed(fused), timed(separate)
+    return {"fused_ms": f_ms, "separate_ms": s_ms, "plain_step_ms": p_ms,
+            "fused_over_plain": f_ms / p_ms - 1.0, "separate_over_plain": s_ms / p_ms - 1.0,
+            "what": "step + eta (DeriveEtaFrom) + mass/momentum/KE/min-h diagnostics: fused into the update "
+                    "(hx_level_advance_epilogue) vs the plain step then the two separate passes"}
 
 
 def ensemble_measure(dev, steps=24, warmup=6, plain_steps=6, count=256):

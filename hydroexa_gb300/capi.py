@@ -138,6 +138,12 @@ def _declare(L):
                                                              c_void_p]
         getattr(L, f"hx_level_advance_{sfx}").argtypes = [c_int, POINTER(Lv), real, c_void_p, c_void_p, c_void_p,
                                                          c_void_p, c_void_p, c_int, c_void_p]
+        getattr(L, f"hx_advance_box_hydrostatic_epilogue_{sfx}").argtypes = [P4, P4, P4, P4, P4, Box, real, real,
+                                                                            real, c_void_p, c_void_p, c_int, P4,
+                                                                            c_void_p, c_void_p, c_void_p]
+        getattr(L, f"hx_level_advance_epilogue_{sfx}").argtypes = [POINTER(Lv), real, c_void_p, c_void_p, c_void_p,
+                                                                  c_void_p, c_void_p, c_int, c_void_p, c_void_p,
+                                                                  c_void_p, c_void_p]
         getattr(L, f"hx_level_dt_reduce_{sfx}").argtypes = [POINTER(Lv), c_void_p, c_void_p]
         getattr(L, f"hx_level_run_{sfx}").argtypes = [c_int, POINTER(Lv), c_void_p, c_void_p, c_void_p, c_int, real,
                                                      c_void_p, c_void_p, c_void_p, c_int, POINTER(c_int), c_void_p]
@@ -227,7 +233,8 @@ EXPORTED = [
     "hx_masked_average_down_box_f64", "hx_masked_average_down_box_f32", "hx_average_down_box_f64",
     "hx_average_down_box_f32", "hx_derive_eta_box_f64",
     "hx_derive_eta_box_f32", "hx_diagnostics_work_bytes", "hx_diagnostics_box_f64", "hx_diagnostics_box_f32",
-    "hx_level_diagnostics_f64", "hx_measure_fp64_rate", "hx_boxlevel_work_bytes", "hx_boxlevel_run_f64", "hx_write_plotfile_f64",
+    "hx_level_diagnostics_f64", "hx_advance_box_hydrostatic_epilogue_f64", "hx_advance_box_hydrostatic_epilogue_f32",
+    "hx_level_advance_epilogue_f64", "hx_level_advance_epilogue_f32", "hx_measure_fp64_rate", "hx_boxlevel_work_bytes", "hx_boxlevel_run_f64", "hx_write_plotfile_f64",
     "hx_level_advance_f64",
     "hx_level_advance_f32", "hx_level_dt_reduce_f64", "hx_level_dt_reduce_f32", "hx_level_run_work_bytes",
     "hx_level_run_f64", "hx_level_run_f32", "hx_level_run_host_f64", "hx_host_cache_release",

@@ -115,7 +115,7 @@ template <class R> StepCtl<R> host_ctl(R dt, R dx, R dy, hx_dt_accum* next_dt, u
 template <class R, class A>
 int advance_box_hydro(const A* eta, const A* Ue, const A* Te, const A* Uo, A* Un, hx_box vb, R dt, R dx, R dy,
                       const A* FL, const A* FR, hx_dt_accum* nd, uint32_t* status, int arith, cudaStream_t st,
-                      const A* Fm = nullptr) {
+                      const A* Fm = nullptr, const EpiOut<R>* epi = nullptr) {
     if (!box_ok(vb)) return HX_ERR_ARG;
     if (!covers(eta, vb, 2, 1, "eta_ext") || !covers(Ue, vb, 2, 3, "U_ext") || !covers(Te, vb, 2, 2, "T_ext") ||
         !covers(Uo, vb, 0, 3, "U_old") || !covers(Un, vb, 0, 3, "U_new"))
@@ -147,9 +147,43 @@ int advance_box_hydro(const A* eta, const A* Ue, const A* Te, const A* Uo, A* Un
     src.glo0 = vb.lo[0] - 2; src.glo1 = vb.lo[1] - 2; src.ghi0 = vb.hi[0] + 2; src.ghi1 = vb.hi[1] + 2;
     const StepCtl<R> ctl = host_ctl<R>(dt, dx, dy, nd, status);
     cudaError_t e = (arith == HX_ARITH_EXACT)
-                        ? launch_hydro<R, false, BoxSrc<R>>(src, cells3(*Uo), plane(*Te, 1), cells3w(*Un), fo, ibox(vb), ctl, st)
-                        : launch_hydro<R, true, BoxSrc<R>>(src, cells3(*Uo), plane(*Te, 1), cells3w(*Un), fo, ibox(vb), ctl, st);
+                        ? launch_hydro<R, false, BoxSrc<R>>(src, cells3(*Uo), plane(*Te, 1), cells3w(*Un), fo, ibox(vb), ctl, st, epi)
+                        : launch_hydro<R, true, BoxSrc<R>>(src, cells3(*Uo), plane(*Te, 1), cells3w(*Un), fo, ibox(vb), ctl, st, epi);
     return launched(e, "hx_advance_box_hydrostatic");
+}
+
+// The epilogue's outputs over the valid box vb: eta (one component covering vb)
+// and the diagnostics with their work buffer; false (error set) when a given
+// output is malformed or neither is given.
+template <class R, class A>
+bool epi_out(A* eta, double* diag, void* work, hx_box vb, R dA, EpiOut<R>& e, const char* who) {
+    e = EpiOut<R>{};
+    if (!eta && !diag) { fail(HX_ERR_ARG, "%s: neither eta nor diagnostics asked for", who); return false; }
+    if (eta) {
+        if (!covers(eta, vb, 0, 1, "eta_new")) return false;
+        e.eta = eta->p;
+        e.ejs = eta->jstride;
+        e.elo0 = eta->lo[0];
+        e.elo1 = eta->lo[1];
+    }
+    if (diag) {
+        if (!work) { fail(HX_ERR_ARG, "%s: diagnostics need a work buffer", who); return false; }
+        e.part = static_cast<double*>(work);
+        e.out = diag;
+    }
+    e.dA = dA;
+    return true;
+}
+
+template <class R, class A>
+int advance_box_hydro_epi(const A* eta, const A* Ue, const A* Te, const A* Uo, A* Un, hx_box vb, R dt, R dx, R dy,
+                          hx_dt_accum* nd, uint32_t* status, int arith, A* eta_new, double* diag, void* work,
+                          cudaStream_t st) {
+    if (!box_ok(vb)) return HX_ERR_ARG;
+    EpiOut<R> e;
+    if (!epi_out<R>(eta_new, diag, work, vb, dx * dy, e, "hx_advance_box_hydrostatic_epilogue")) return HX_ERR_ARG;
+    return advance_box_hydro<R, A>(eta, Ue, Te, Uo, Un, vb, dt, dx, dy, nullptr, nullptr, nd, status, arith, st,
+                                   nullptr, &e);
 }
 
 template <class R, class A>
@@ -307,7 +341,7 @@ template <class R, class L> LevelSrc<R> level_src(const L* lv, int g) {
 // as halo, nothing outside the rows is written).
 template <class R, class L>
 int level_advance(int method, const L* lv, const StepCtl<R>& ctl, R* ho, R* huo, R* hvo, int arith, cudaStream_t st,
-                  int j0 = 0, int j1 = -1) {
+                  int j0 = 0, int j1 = -1, const EpiOut<R>* epi = nullptr) {
     const IBox vb{0, j0, lv->nx - 1, j1 < 0 ? lv->ny - 1 : j1};
     Cells3W<R> out;
     out.p[0] = ho; out.p[1] = huo; out.p[2] = hvo;
@@ -321,8 +355,8 @@ int level_advance(int method, const L* lv, const StepCtl<R>& ctl, R* ho, R* huo,
         FaceOut<R> fo{};
         fo.on = 0;
         const LevelSrc<R> src = level_src<R>(lv, 2);
-        e = (arith == HX_ARITH_EXACT) ? launch_hydro<R, false, LevelSrc<R>>(src, uo, np, out, fo, vb, ctl, st)
-                                      : launch_hydro<R, true, LevelSrc<R>>(src, uo, np, out, fo, vb, ctl, st);
+        e = (arith == HX_ARITH_EXACT) ? launch_hydro<R, false, LevelSrc<R>>(src, uo, np, out, fo, vb, ctl, st, epi)
+                                      : launch_hydro<R, true, LevelSrc<R>>(src, uo, np, out, fo, vb, ctl, st, epi);
     } else {
         FaceOut9<R> fo{};
         fo.on = 0;
@@ -333,6 +367,23 @@ int level_advance(int method, const L* lv, const StepCtl<R>& ctl, R* ho, R* huo,
                                       : launch_classic<R, true, LevelSrc<R>>(src, out, fo, hb, vb, ctl, st);
     }
     return launched(e, "hx_level_advance");
+}
+
+template <class R, class L>
+int level_advance_epi(const L* lv, R dt, R* ho, R* huo, R* hvo, hx_dt_accum* nd, uint32_t* status, int arith,
+                      R* eta_out, double* diag, void* work, cudaStream_t st) {
+    if (!level_ok(lv)) return HX_ERR_ARG;
+    if (!ho || !huo || !hvo) return fail(HX_ERR_ARG, "null output planes");
+    EpiOut<R> e{};
+    if (!eta_out && !diag) return fail(HX_ERR_ARG, "hx_level_advance_epilogue: neither eta nor diagnostics asked for");
+    if (diag && !work) return fail(HX_ERR_ARG, "hx_level_advance_epilogue: diagnostics need a work buffer");
+    e.eta = eta_out;
+    e.ejs = lv->pitch;
+    e.part = diag ? static_cast<double*>(work) : nullptr;
+    e.out = diag;
+    e.dA = lv->dx * lv->dy;
+    return level_advance<R>(HX_METHOD_HYDROSTATIC_ROE, lv, host_ctl<R>(dt, lv->dx, lv->dy, nd, status), ho, huo, hvo,
+                            arith, st, 0, -1, &e);
 }
 
 template <class R, class L>
@@ -561,6 +612,22 @@ int hx_advance_box_hydrostatic_f32(const hx_array4_f32* eta, const hx_array4_f32
                                    uint32_t* status, int arith, hx_stream_t st) {
     return advance_box_hydro<float>(eta, Ue, Te, Uo, Un, vb, dt, dx, dy, FL, FR, nd, status, arith, (cudaStream_t)st);
 }
+int hx_advance_box_hydrostatic_epilogue_f64(const hx_array4_f64* eta, const hx_array4_f64* Ue,
+                                            const hx_array4_f64* Te, const hx_array4_f64* Uo, hx_array4_f64* Un,
+                                            hx_box vb, double dt, double dx, double dy, hx_dt_accum* nd,
+                                            uint32_t* status, int arith, hx_array4_f64* eta_new, double* diag,
+                                            void* work, hx_stream_t st) {
+    return advance_box_hydro_epi<double>(eta, Ue, Te, Uo, Un, vb, dt, dx, dy, nd, status, arith, eta_new, diag, work,
+                                         (cudaStream_t)st);
+}
+int hx_advance_box_hydrostatic_epilogue_f32(const hx_array4_f32* eta, const hx_array4_f32* Ue,
+                                            const hx_array4_f32* Te, const hx_array4_f32* Uo, hx_array4_f32* Un,
+                                            hx_box vb, float dt, float dx, float dy, hx_dt_accum* nd,
+                                            uint32_t* status, int arith, hx_array4_f32* eta_new, double* diag,
+                                            void* work, hx_stream_t st) {
+    return advance_box_hydro_epi<float>(eta, Ue, Te, Uo, Un, vb, dt, dx, dy, nd, status, arith, eta_new, diag, work,
+                                        (cudaStream_t)st);
+}
 int hx_advance_box_roe_f64(const hx_array4_f64* eta, hx_array4_f64* Uo, const hx_array4_f64* T, hx_array4_f64* Un,
                            hx_box vb, double dt, double dx, double dy, const hx_array4_f64* F,
                            const hx_array4_f64* Sm, const hx_array4_f64* Sp, hx_dt_accum* nd, uint32_t* status,
@@ -685,6 +752,16 @@ int hx_level_advance_f32(int method, const hx_level_f32* L, float dt, float* ho,
     if (method != HX_METHOD_ROE && method != HX_METHOD_HYDROSTATIC_ROE) return fail(HX_ERR_ARG, "unknown method");
     return level_advance<float>(method, L, host_ctl<float>(dt, L->dx, L->dy, nd, status), ho, huo, hvo, arith,
                                 (cudaStream_t)st);
+}
+int hx_level_advance_epilogue_f64(const hx_level_f64* L, double dt, double* ho, double* huo, double* hvo,
+                                  hx_dt_accum* nd, uint32_t* status, int arith, double* eta_out, double* diag,
+                                  void* work, hx_stream_t st) {
+    return level_advance_epi<double>(L, dt, ho, huo, hvo, nd, status, arith, eta_out, diag, work, (cudaStream_t)st);
+}
+int hx_level_advance_epilogue_f32(const hx_level_f32* L, float dt, float* ho, float* huo, float* hvo,
+                                  hx_dt_accum* nd, uint32_t* status, int arith, float* eta_out, double* diag,
+                                  void* work, hx_stream_t st) {
+    return level_advance_epi<float>(L, dt, ho, huo, hvo, nd, status, arith, eta_out, diag, work, (cudaStream_t)st);
 }
 int hx_level_dt_reduce_f64(const hx_level_f64* L, hx_dt_accum* acc, hx_stream_t st) {
     return level_dt<double>(L, acc, (cudaStream_t)st);

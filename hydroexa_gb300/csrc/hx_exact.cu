@@ -5,13 +5,12 @@
 
 namespace hx {
 #define HX_INST(R)                                                                                             \
-    template cudaError_t launch_hydro<R, false, LevelSrc<R>>(const LevelSrc<R>&, const Cells3<R>&,            \
-                                                             const Plane<R>&, const Cells3W<R>&,               \
-                                                             const FaceOut<R>&, const IBox&, const StepCtl<R>&, \
-                                                             cudaStream_t);                                    \
-    template cudaError_t launch_hydro<R, false, BoxSrc<R>>(const BoxSrc<R>&, const Cells3<R>&, const Plane<R>&, \
-                                                           const Cells3W<R>&, const FaceOut<R>&, const IBox&,  \
-                                                           const StepCtl<R>&, cudaStream_t);                   \
+    template cudaError_t launch_hydro<R, false, LevelSrc<R>>(                                                  \
+        const LevelSrc<R>&, const Cells3<R>&, const Plane<R>&, const Cells3W<R>&, const FaceOut<R>&,           \
+        const IBox&, const StepCtl<R>&, cudaStream_t, const EpiOut<R>*);                                       \
+    template cudaError_t launch_hydro<R, false, BoxSrc<R>>(                                                    \
+        const BoxSrc<R>&, const Cells3<R>&, const Plane<R>&, const Cells3W<R>&, const FaceOut<R>&,             \
+        const IBox&, const StepCtl<R>&, cudaStream_t, const EpiOut<R>*);                                       \
     template cudaError_t launch_classic<R, false, LevelSrc<R>>(const LevelSrc<R>&, const Cells3W<R>&,         \
                                                                const FaceOut9<R>&, const RebuildOut<R>&,       \
                                                                const IBox&, const StepCtl<R>&, cudaStream_t);  \

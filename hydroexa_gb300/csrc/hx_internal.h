@@ -74,6 +74,27 @@ template <class R> struct Cells3W {
     }
 };
 
+// The advance epilogue: what the update of a step writes beside the state.
+// eta (null: none) receives eta = h + z of every updated cell, the kernel of
+// AmrMeshState::DeriveEtaFrom (src/state/AmrMeshState_AMR.cpp:203-224); part
+// (null: none) receives 5 doubles per block of the conservation diagnostics
+// of the updated state (AmrMeshState::ComputeMassDiagnostics,
+// src/state/AmrMeshState_Utils.cpp:213-300), folded into out[5] after the step.
+template <class R> struct EpiOut {
+    R* eta;
+    long long ejs;
+    int elo0, elo1;
+    double* part;
+    double* out;
+    R dA;
+};
+// A thread's running diagnostics: the four sums and min h as the bits of a
+// positive double (whose order as integers is the order of the values).
+struct DiagAcc {
+    double m = 0.0, px = 0.0, py = 0.0, ke = 0.0;
+    unsigned long long mn = 0x7fefffffffffffffull;  // DBL_MAX
+};
+
 // No flux-difference output (the fused step).
 struct NoDiv {
     static constexpr bool on = false;

@@ -389,6 +389,84 @@ template <class R> struct ThreadFold {
     R rate = R(0), mv = R(0);
     unsigned flags = 0;
 };
+// ---------------------------------------------------------------------------
+// The advance epilogue (EpiOut): eta and the conservation diagnostics of the
+// updated state, taken from the values the update stores, so neither needs
+// another pass over the level.
+// ---------------------------------------------------------------------------
+constexpr long long kNodataRoughBits = (long long)0xC0C3878000000000ull;  // -9999.0, the NODATA roughness
+
+// One updated cell.  eta = h + z (AmrMeshState_AMR.cpp:219).  The cell counts
+// when its roughness is not NODATA (== -9999) and h > 0
+// (AmrMeshState_Utils.cpp:270-283).  Exact form: the reference's terms,
+// s_mass = h dA, s_mx = hu dA, s_my = hv dA, s_ke = 0.5 (hu^2 + hv^2) / h dA
+// in its types and order (the 0.5 literal is double), as k_diag_partial takes
+// them.  FP64 fast form: h, hu, hv and (hu^2 + hv^2) / h through the
+// float-seeded reciprocal (2^-44 relative) summed unscaled, dA and 0.5 dA
+// applied once per block; the predicates on the integer pipe (a NaN h is not
+// counted, as h > 0 is false for it).
+template <class R, bool FAST>
+__device__ __forceinline__ void epi_cell(const EpiOut<R>& e, int i, int j, R h, R a, R c, R z, R n, DiagAcc& acc) {
+    if (e.eta) e.eta[(long long)(i - e.elo0) + (long long)(j - e.elo1) * e.ejs] = h + z;
+    if (!e.part) return;
+    if constexpr (FAST && sizeof(R) == 8) {
+        const long long hb = sbits(h);
+        if (sbits(n) != kNodataRoughBits && hb > 0 && hb <= 0x7ff0000000000000ll) {
+            acc.m += h;
+            acc.px += a;
+            acc.py += c;
+            acc.ke += fma(a, a, c * c) * rcp_nr(h);
+            if ((unsigned long long)hb < acc.mn) acc.mn = (unsigned long long)hb;
+        }
+    } else {
+        if (!(n == R(-9999.0)) && h > R(0)) {
+            const R s_mass = h * e.dA, s_mx = a * e.dA, s_my = c * e.dA;
+            const R s_ke = 0.5 * (a * a + c * c) / h * e.dA;
+            acc.m += s_mass;
+            acc.px += s_mx;
+            acc.py += s_my;
+            acc.ke += s_ke;
+            const unsigned long long hb = (unsigned long long)sbits((double)h);
+            if (hb < acc.mn) acc.mn = hb;
+        }
+    }
+}
+
+// The block's sums and min of the diagnostics into q[0..4] by a fixed tree
+// (shuffles within each warp, then thread 0 over the warps in order); the sums
+// are scaled by sm (mass, momenta) and sk (kinetic energy) at the end.  Every
+// thread of the block calls it.
+template <int NTv>
+__device__ __forceinline__ void diag_block_store(double m, double px, double py, double ke, double mn, double* q,
+                                                 double sm = 1.0, double sk = 1.0) {
+    __shared__ double sh[5][NTv / 32];
+    for (int o = 16; o > 0; o >>= 1) {
+        m += __shfl_xor_sync(0xffffffffu, m, o);
+        px += __shfl_xor_sync(0xffffffffu, px, o);
+        py += __shfl_xor_sync(0xffffffffu, py, o);
+        ke += __shfl_xor_sync(0xffffffffu, ke, o);
+        mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+    }
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) { sh[0][w] = m; sh[1][w] = px; sh[2][w] = py; sh[3][w] = ke; sh[4][w] = mn; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < NTv / 32; ++k) {
+            m += sh[0][k]; px += sh[1][k]; py += sh[2][k]; ke += sh[3][k]; mn = fmin(mn, sh[4][k]);
+        }
+        q[0] = m * sm; q[1] = px * sm; q[2] = py * sm; q[3] = ke * sk; q[4] = mn;
+    }
+}
+template <class R, bool FAST, int NTv>
+__device__ __forceinline__ void epi_block_store(const EpiOut<R>& e, const DiagAcc& acc, long long slot) {
+    constexpr bool SCALED = FAST && sizeof(R) == 8;
+    const double dA = (double)e.dA;
+    // no cell counted: the reference's initial min, std::numeric_limits<R>::max()
+    const double mn = acc.mn == DiagAcc{}.mn ? (double)Cst<R>::max_value : __longlong_as_double((long long)acc.mn);
+    diag_block_store<NTv>(acc.m, acc.px, acc.py, acc.ke, mn, e.part + 5 * slot, SCALED ? dA : 1.0,
+                          SCALED ? 0.5 * dA : 1.0);
+}
+
 // Points in the tile body where a persistent kernel does its own work: after
 // the grown tile is loaded (every thread, before the barrier that ends phase A)
 // and after the faces are computed (every thread, after the barrier that ends
@@ -400,15 +478,18 @@ struct NoHooks {
 };
 
 template <class R, bool FAST, int TXv, int TYv, int NTv, class Src, bool LINEAR = false, class Div = NoDiv,
-          class Rec = NoRec, class UO = Cells3<R>, class NP = Plane<R>, class Hooks = NoHooks, class Sync = BlockSync>
+          class Rec = NoRec, class UO = Cells3<R>, class NP = Plane<R>, class Hooks = NoHooks, class Sync = BlockSync,
+          bool EPI = false>
 __device__ __forceinline__ void hydro_tile_body(HydroSmem<R, TXv, TYv>& S, const Src& src, const UO& uo,
                                                 const NP& nplane, const Cells3W<R>& out, const FaceOut<R>& fo,
                                                 const IBox& vb, int x0, int y0, R dt, R dx, R dy, DtAccum* dt_out,
                                                 unsigned* status, unsigned* post_flags = nullptr,
                                                 const Div& div = Div{}, const Rec& rec = Rec{},
                                                 const Hooks& hooks = Hooks{}, ThreadFold<R>* defer = nullptr,
-                                                const Sync& sy = Sync{}, bool start_barrier = true) {
+                                                const Sync& sy = Sync{}, bool start_barrier = true,
+                                                const EpiOut<R>* epi = nullptr, DiagAcc* eacc = nullptr) {
     static_assert(!Rec::on || (FAST && sizeof(R) == 8), "face records are kept for the FP64 fast form");
+    static_assert(!EPI || (!LINEAR && !Div::on), "the epilogue follows a whole update");
     constexpr int GX = HydroSmem<R, TXv, TYv>::GX, GY = HydroSmem<R, TXv, TYv>::GY;
     constexpr int CELLS = TXv * TYv;
     const int t = sy.tid();
@@ -612,7 +693,8 @@ __device__ __forceinline__ void hydro_tile_body(HydroSmem<R, TXv, TYv>& S, const
         const R o0 = uo.ld(0, gi, gj), o1 = uo.ld(1, gi, gj), o2 = uo.ld(2, gi, gj);
         step_cell<R, FAST, LINEAR, NP>(o0, o1, o2, dx0, dx1, dx2, dy0, dy1, dy2, cx, cy, dt, nplane, out, gi, gj,
                                    S.nod[ty + 2][tx + 2] != 0, dx, dy, idx, idy, fold && !SCREEN, rate, mv, flags,
-                                   pflags, (SCREEN && fold) ? &sc : nullptr);
+                                   pflags, ((SCREEN && fold) || EPI) ? &sc : nullptr);
+        if constexpr (EPI) epi_cell<R, FAST>(*epi, gi, gj, sc.h, sc.hu, sc.hv, S.z[ty + 2][tx + 2], nplane.ld(gi, gj), *eacc);
     }
     if constexpr (SCREEN) {
         if (fold) screened_fold<NTv, 1, Sync>(&sc, dx, dy, idx, idy, rate, mv, flags, sy);
@@ -661,17 +743,25 @@ template <class R> inline bool big_tile(const IBox& vb) {
            (long long)(vb.hi0 - vb.lo0 + 1) * (long long)(vb.hi1 - vb.lo1 + 1) >= kBigTileCells;
 }
 
-template <class R, bool FAST, class Src, int TXH = TX, int TYH = TY>
+// EPI: the advance epilogue (eta and this tile's diagnostics partial, slot =
+// the block's linear index).
+template <class R, bool FAST, class Src, int TXH = TX, int TYH = TY, bool EPI = false>
 __global__ void __launch_bounds__(TXH * TYH, min_ctas(TXH * TYH))
-    k_hydro_tile(Src src, Cells3<R> uo, Plane<R> nplane, Cells3W<R> out, FaceOut<R> fo, IBox vb, StepCtl<R> ctl) {
+    k_hydro_tile(Src src, Cells3<R> uo, Plane<R> nplane, Cells3W<R> out, FaceOut<R> fo, IBox vb, StepCtl<R> ctl,
+                 EpiOut<R> epi) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     HydroSmem<R, TXH, TYH>& S = *reinterpret_cast<HydroSmem<R, TXH, TYH>*>(smem_raw);
     R dt;
     if (!resolve_dt(ctl, dt)) return;
     step_bookkeeping(ctl, dt);
-    hydro_tile_body<R, FAST, TXH, TYH, TXH * TYH>(S, src, uo, nplane, out, fo, vb, vb.lo0 + (int)blockIdx.x * TXH,
-                                                  vb.lo1 + (int)blockIdx.y * TYH, dt, ctl.dx, ctl.dy, ctl.dt_out,
-                                                  ctl.status);
+    DiagAcc acc;
+    hydro_tile_body<R, FAST, TXH, TYH, TXH * TYH, Src, false, NoDiv, NoRec, Cells3<R>, Plane<R>, NoHooks, BlockSync,
+                    EPI>(S, src, uo, nplane, out, fo, vb, vb.lo0 + (int)blockIdx.x * TXH,
+                         vb.lo1 + (int)blockIdx.y * TYH, dt, ctl.dx, ctl.dy, ctl.dt_out, ctl.status, nullptr,
+                         NoDiv{}, NoRec{}, NoHooks{}, nullptr, BlockSync{}, true, &epi, &acc);
+    if constexpr (EPI) {
+        if (epi.part) epi_block_store<R, FAST, TXH * TYH>(epi, acc, blockIdx.x + (long long)blockIdx.y * gridDim.x);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -887,10 +977,14 @@ struct PersistHooks {
 // when the planes allow it (maps.valid), else by cp.async from every thread.  A TMA wait that runs out
 // (about a second) sets HX_STATUS_STAGING_TIMEOUT and ends the block's work after a second bounded wait for
 // the copies in flight.
-template <bool FAST, class Div = NoDiv>
+// EPI: the advance epilogue, each thread's diagnostics summed over its cells of
+// every tile of the block and the block's partial stored at slot blockIdx.x
+// (NaN when the block gave up on a staging wait).
+template <bool FAST, class Div = NoDiv, bool EPI = false>
 __global__ void __launch_bounds__(kPN, 1)
     k_hydro_persist(LevelSrc<double> src, Cells3W<double> out, IBox vb, int tiles_x, int ntiles,
-                    StepCtl<double> ctl, Div div, const __grid_constant__ PersistMaps maps, unsigned* err) {
+                    StepCtl<double> ctl, Div div, const __grid_constant__ PersistMaps maps, unsigned* err,
+                    EpiOut<double> epi) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     unsigned char* base = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);  // 128-byte aligned
     HydroSmem<double, kPX, kPY>& S = *reinterpret_cast<HydroSmem<double, kPX, kPY>*>(base);
@@ -918,6 +1012,7 @@ __global__ void __launch_bounds__(kPN, 1)
     *tf = ThreadFold<double>{};
     const FaceOut<double> fo{};
     unsigned parity = 0;
+    DiagAcc acc;
     for (; k < ntiles; k += (int)gridDim.x) {
         const int x0 = vb.lo0 + (k % tiles_x) * kPX, y0 = vb.lo1 + (k / tiles_x) * kPY;
         const int kn = k + (int)gridDim.x;
@@ -933,6 +1028,10 @@ __global__ void __launch_bounds__(kPN, 1)
                 if (threadIdx.x == 0) {
                     if (err) atomicOr(err, (unsigned)HX_STATUS_STAGING_TIMEOUT);
                     mbar_wait_bounded(&own->mbar, parity ^ 1u);  // the copies in flight, once more
+                    if constexpr (EPI) {
+                        if (epi.part)
+                            for (int c = 0; c < 5; ++c) epi.part[5ll * blockIdx.x + c] = __longlong_as_double(-1ll);
+                    }
                 }
                 __syncthreads();
                 return;
@@ -941,11 +1040,15 @@ __global__ void __launch_bounds__(kPN, 1)
             cp_async_wait_all();  // this thread's copies of tile k; the body's first barrier publishes everyone's
         }
         hydro_tile_body<double, FAST, kPX, kPY, kPN, StagedSrc, false, Div, NoRec, OwnState, OwnRough,
-                        PersistHooks>(S, ss, OwnState{own, x0, y0}, OwnRough{own, x0, y0}, out, fo, vb, x0, y0, dt,
-                                      ctl.dx, ctl.dy, nullptr, Div::on ? nullptr : ctl.status, nullptr, div,
-                                      NoRec{}, hooks, fold ? tf : nullptr, BlockSync{}, !tma);
+                        PersistHooks, BlockSync, EPI>(S, ss, OwnState{own, x0, y0}, OwnRough{own, x0, y0}, out, fo,
+                                                      vb, x0, y0, dt, ctl.dx, ctl.dy, nullptr,
+                                                      Div::on ? nullptr : ctl.status, nullptr, div, NoRec{}, hooks,
+                                                      fold ? tf : nullptr, BlockSync{}, !tma, &epi, &acc);
     }
     if (fold) block_fold_dt<double, kPN>(tf->rate, tf->mv, tf->flags, ctl.dt_out);
+    if constexpr (EPI) {
+        if (epi.part) epi_block_store<double, FAST, kPN>(epi, acc, blockIdx.x);
+    }
 }
 
 // Extra bytes the next launches' staging waits for (a test setting; 0 in use).
@@ -1468,7 +1571,6 @@ __global__ void __launch_bounds__(NT) k_derive_eta(V4<R> U, V4<R> T, V4<R> eta, 
 template <class R>
 __global__ void __launch_bounds__(NT) k_diag_partial(Plane<R> h, Plane<R> hu, Plane<R> hv, Plane<R> nr, IBox b, R dA,
                                                      double* part) {
-    __shared__ double sh[5][NT / 32];
     const int i = b.lo0 + blockIdx.x * TX + (threadIdx.x & (TX - 1));
     const int j = b.lo1 + blockIdx.y * TY + threadIdx.x / TX;
     double m = 0.0, px = 0.0, py = 0.0, ke = 0.0, mn = (double)Cst<R>::max_value;
@@ -1481,23 +1583,7 @@ __global__ void __launch_bounds__(NT) k_diag_partial(Plane<R> h, Plane<R> hu, Pl
             m = s_mass; px = s_mx; py = s_my; ke = s_ke; mn = hh;
         }
     }
-    for (int o = 16; o > 0; o >>= 1) {
-        m += __shfl_xor_sync(0xffffffffu, m, o);
-        px += __shfl_xor_sync(0xffffffffu, px, o);
-        py += __shfl_xor_sync(0xffffffffu, py, o);
-        ke += __shfl_xor_sync(0xffffffffu, ke, o);
-        mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
-    }
-    const int w = threadIdx.x >> 5;
-    if ((threadIdx.x & 31) == 0) { sh[0][w] = m; sh[1][w] = px; sh[2][w] = py; sh[3][w] = ke; sh[4][w] = mn; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int k = 1; k < NT / 32; ++k) {
-            m += sh[0][k]; px += sh[1][k]; py += sh[2][k]; ke += sh[3][k]; mn = fmin(mn, sh[4][k]);
-        }
-        double* q = part + 5 * (blockIdx.x + (long long)blockIdx.y * gridDim.x);
-        q[0] = m; q[1] = px; q[2] = py; q[3] = ke; q[4] = mn;
-    }
+    diag_block_store<NT>(m, px, py, ke, mn, part + 5 * (blockIdx.x + (long long)blockIdx.y * gridDim.x));
 }
 
 // The block partials folded in a fixed order into out[5] (one block; R only
@@ -1635,9 +1721,11 @@ template <class K> inline cudaError_t ensure_smem(K kernel, size_t bytes) {
     return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
-template <class R, bool FAST, class Src>
-cudaError_t launch_hydro(const Src& src, const Cells3<R>& uo, const Plane<R>& np, const Cells3W<R>& out,
-                         const FaceOut<R>& fo, const IBox& vb, const StepCtl<R>& ctl, cudaStream_t st) {
+// The step's kernel; nblocks receives its block count (the epilogue's partials).
+template <class R, bool FAST, class Src, bool EPI>
+cudaError_t launch_hydro_k(const Src& src, const Cells3<R>& uo, const Plane<R>& np, const Cells3W<R>& out,
+                           const FaceOut<R>& fo, const IBox& vb, const StepCtl<R>& ctl, cudaStream_t st,
+                           const EpiOut<R>& epi, long long& nblocks) {
     if constexpr (std::is_same_v<Src, LevelSrc<double>>) {
         // a whole level (or a band of its rows) on the big tile: the persistent kernel, when the stored state
         // and roughness are the level's own planes and no face arrays are asked for
@@ -1650,29 +1738,50 @@ cudaError_t launch_hydro(const Src& src, const Cells3<R>& uo, const Plane<R>& np
             cudaError_t e = cudaGetDevice(&dev);
             if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
             if (e != cudaSuccess) return e;
-            auto k = k_hydro_persist<FAST>;
+            auto k = k_hydro_persist<FAST, NoDiv, EPI>;
             e = ensure_smem(k, persist_smem_bytes());
             if (e != cudaSuccess) return e;
             const PersistMaps maps = persist_maps(src);
-            k<<<(unsigned)(ntiles < sms ? ntiles : sms), kPN, persist_smem_bytes(), st>>>(
-                src, out, vb, (int)tg.x, ntiles, ctl, NoDiv{}, maps, ctl.status);
+            const int grid = ntiles < sms ? ntiles : sms;
+            k<<<(unsigned)grid, kPN, persist_smem_bytes(), st>>>(src, out, vb, (int)tg.x, ntiles, ctl, NoDiv{}, maps,
+                                                                 ctl.status, epi);
+            nblocks = grid;
             return cudaGetLastError();
         }
     }
     if (big_tile<R>(vb)) {
         constexpr int BX = BigTile<R>::X, BY = BigTile<R>::Y;
         const size_t sm = sizeof(HydroSmem<R, BX, BY>);
-        auto k = k_hydro_tile<R, FAST, Src, BX, BY>;
+        auto k = k_hydro_tile<R, FAST, Src, BX, BY, EPI>;
         cudaError_t e = ensure_smem(k, sm);
         if (e != cudaSuccess) return e;
-        k<<<tile_grid(vb, BX, BY), BX * BY, sm, st>>>(src, uo, np, out, fo, vb, ctl);
+        const dim3 g = tile_grid(vb, BX, BY);
+        k<<<g, BX * BY, sm, st>>>(src, uo, np, out, fo, vb, ctl, epi);
+        nblocks = (long long)g.x * g.y;
         return cudaGetLastError();
     }
     const size_t sm = sizeof(HydroSmem<R>);
-    auto k = k_hydro_tile<R, FAST, Src>;
+    auto k = k_hydro_tile<R, FAST, Src, TX, TY, EPI>;
     cudaError_t e = ensure_smem(k, sm);
     if (e != cudaSuccess) return e;
-    k<<<tile_grid(vb, TX, TY), NT, sm, st>>>(src, uo, np, out, fo, vb, ctl);
+    const dim3 g = tile_grid(vb, TX, TY);
+    k<<<g, NT, sm, st>>>(src, uo, np, out, fo, vb, ctl, epi);
+    nblocks = (long long)g.x * g.y;
+    return cudaGetLastError();
+}
+
+// The hydrostatic step; with an epilogue (epi not null) the update also writes
+// eta and the diagnostics' block partials, which k_diag_final then folds into
+// epi->out.  The partials are at most one per TX x TY tile of vb.
+template <class R, bool FAST, class Src>
+cudaError_t launch_hydro(const Src& src, const Cells3<R>& uo, const Plane<R>& np, const Cells3W<R>& out,
+                         const FaceOut<R>& fo, const IBox& vb, const StepCtl<R>& ctl, cudaStream_t st,
+                         const EpiOut<R>* epi) {
+    long long nblocks = 0;
+    if (!epi) return launch_hydro_k<R, FAST, Src, false>(src, uo, np, out, fo, vb, ctl, st, EpiOut<R>{}, nblocks);
+    cudaError_t e = launch_hydro_k<R, FAST, Src, true>(src, uo, np, out, fo, vb, ctl, st, *epi, nblocks);
+    if (e != cudaSuccess || !epi->part) return e;
+    k_diag_final<R><<<1, NT, 0, st>>>(epi->part, nblocks, epi->out);
     return cudaGetLastError();
 }
 
@@ -1750,7 +1859,7 @@ cudaError_t launch_hydro_split(const LevelSrc<R>& src, const Cells3<R>& uo, cons
             (void)np;
             const PersistMaps maps = persist_maps(src);
             k<<<(unsigned)(ntiles < sms ? ntiles : sms), kPN, persist_smem_bytes(), st>>>(
-                src, Cells3W<double>{}, vb, (int)tg.x, ntiles, ctl, div, maps, nullptr);
+                src, Cells3W<double>{}, vb, (int)tg.x, ntiles, ctl, div, maps, nullptr, EpiOut<double>{});
             return cudaGetLastError();
         }
     }

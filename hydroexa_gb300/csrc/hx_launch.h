@@ -8,9 +8,12 @@
 
 namespace hx {
 
+// One hydrostatic step; epi (not null): with the advance epilogue (eta and the
+// conservation diagnostics of the updated state, folded into epi->out).
 template <class R, bool FAST, class Src>
 cudaError_t launch_hydro(const Src& src, const Cells3<R>& uo, const Plane<R>& np, const Cells3W<R>& out,
-                         const FaceOut<R>& fo, const IBox& vb, const StepCtl<R>& ctl, cudaStream_t st);
+                         const FaceOut<R>& fo, const IBox& vb, const StepCtl<R>& ctl, cudaStream_t st,
+                         const EpiOut<R>* epi = nullptr);
 
 template <class R, bool FAST, class Src>
 cudaError_t launch_classic(const Src& src, const Cells3W<R>& out, const FaceOut9<R>& fo, const RebuildOut<R>& hb,

@@ -164,6 +164,29 @@ class Level:
         del real
         return out
 
+    def advance_epilogue(self, dt: float, out: torch.Tensor | None = None, eta: bool = True, diag: bool = True,
+                         next_dt: DtAccum | None = None, arith: int = capi.HX_ARITH_EXACT, stream=None):
+        """One hydrostatic advance whose update also writes eta = h + z of the
+        new state (DeriveEtaFrom) and its conservation diagnostics (mass,
+        x- and y-momentum, kinetic energy, min h; ComputeMassDiagnostics).
+        Returns (new state, eta plane or None, 5 diagnostics on the device or None)."""
+        out = torch.empty_like(self.state) if out is None else out
+        e = torch.empty_like(self.state[0]) if eta else None
+        dg = torch.empty(5, dtype=torch.float64, device=self.state.device) if diag else None
+        work = getattr(self, "_diag_work", None)  # kept: the kernel may still use it when this returns
+        if diag and work is None:
+            b = box((0, 0), (self.geom.nx - 1, self.geom.ny - 1))
+            work = self._diag_work = torch.empty(int(capi.lib().hx_diagnostics_work_bytes(b)), dtype=torch.uint8,
+                                                 device=self.state.device)
+        d = self._desc(self.state)
+        vp = lambda t: ctypes.c_void_p(t.data_ptr()) if t is not None else None
+        capi.check(getattr(capi.lib(), f"hx_level_advance_epilogue_{self.sfx}")(
+            ctypes.byref(d), dt, *(ctypes.c_void_p(out[k].data_ptr()) for k in range(3)),
+            next_dt.ptr if next_dt is not None else None, self.status.ptr, arith, vp(e), vp(dg),
+            vp(work) if diag else None,
+            _stream_handle(stream)), "hx_level_advance_epilogue")
+        return out, e, dg
+
     def compute_dt(self, stream=None):
         """(min per-cell CFL bound, max |vel|) of the current state, before the CFL factor."""
         acc = getattr(self, "_acc", None)

@@ -325,6 +325,37 @@ int hx_diagnostics_box_f64(const hx_array4_f64* U, const hx_array4_f64* terrain,
 int hx_diagnostics_box_f32(const hx_array4_f32* U, const hx_array4_f32* terrain, hx_box b, float dx, float dy,
                            double* out, void* work, hx_stream_t stream);
 
+/*
+ * The hydrostatic step with its epilogue: hx_advance_box_hydrostatic_* (no face
+ * arrays) whose update also writes, from the values it stores in U_new,
+ *  - eta_new (not NULL; one component covering the valid box): eta = h + z of
+ *    every valid cell, the kernel of DeriveEtaFrom (AmrMeshState_AMR.cpp:219)
+ *    on the valid box.  The reference derives eta on the grown box and then
+ *    fills the ghost ring (FillBoundary); that ring is the caller's fill here.
+ *  - diag_out (not NULL; device, 5 doubles): the diagnostics of the updated
+ *    state on the valid box, as hx_diagnostics_box_* defines them, with work of
+ *    hx_diagnostics_work_bytes(valid) bytes.
+ * Neither output needs another pass over the box.  HX_ARITH_EXACT: every
+ * cell's terms are hx_diagnostics_box_*'s; on boxes below 2048 x 2048 cells
+ * the blocks are its blocks too and the result is identical to it, on larger
+ * ones only the sums' order differs.  HX_ARITH_FAST (double): h, hu, hv and
+ * (hu^2 + hv^2) / h are summed unscaled (the reciprocal within 2^-44) and
+ * scaled by dA and 0.5 dA once per block: within 1e-12 relative of the exact
+ * sums, min h identical.  At least one of eta_new and diag_out is given.
+ */
+int hx_advance_box_hydrostatic_epilogue_f64(const hx_array4_f64* eta_ext, const hx_array4_f64* U_ext,
+                                            const hx_array4_f64* T_ext, const hx_array4_f64* U_old,
+                                            hx_array4_f64* U_new, hx_box valid, double dt, double dx, double dy,
+                                            hx_dt_accum* next_dt, uint32_t* status, int arith,
+                                            hx_array4_f64* eta_new, double* diag_out, void* work,
+                                            hx_stream_t stream);
+int hx_advance_box_hydrostatic_epilogue_f32(const hx_array4_f32* eta_ext, const hx_array4_f32* U_ext,
+                                            const hx_array4_f32* T_ext, const hx_array4_f32* U_old,
+                                            hx_array4_f32* U_new, hx_box valid, float dt, float dx, float dy,
+                                            hx_dt_accum* next_dt, uint32_t* status, int arith,
+                                            hx_array4_f32* eta_new, double* diag_out, void* work,
+                                            hx_stream_t stream);
+
 /* ---- single-box level with the physical boundary fused into the loader --- */
 
 /*
@@ -366,6 +397,21 @@ int hx_level_advance_f64(int method, const hx_level_f64* L, double dt, double* h
                          double* hv_out, hx_dt_accum* next_dt, uint32_t* status, int arith, hx_stream_t stream);
 int hx_level_advance_f32(int method, const hx_level_f32* L, float dt, float* h_out, float* hu_out, float* hv_out,
                          hx_dt_accum* next_dt, uint32_t* status, int arith, hx_stream_t stream);
+
+/*
+ * One hydrostatic advance of the level with the epilogue of
+ * hx_advance_box_hydrostatic_epilogue_*: eta_out (not NULL; same pitch) = h + z
+ * of the updated state, diag_out (not NULL; device, 5 doubles) = its
+ * diagnostics as hx_level_diagnostics_f64 defines them, work of
+ * hx_diagnostics_work_bytes of the box (0,0)-(nx-1,ny-1) bytes.  Levels from
+ * 2048 x 2048 cells run the persistent kernel with the epilogue in it.
+ */
+int hx_level_advance_epilogue_f64(const hx_level_f64* L, double dt, double* h_out, double* hu_out, double* hv_out,
+                                  hx_dt_accum* next_dt, uint32_t* status, int arith, double* eta_out,
+                                  double* diag_out, void* work, hx_stream_t stream);
+int hx_level_advance_epilogue_f32(const hx_level_f32* L, float dt, float* h_out, float* hu_out, float* hv_out,
+                                  hx_dt_accum* next_dt, uint32_t* status, int arith, float* eta_out,
+                                  double* diag_out, void* work, hx_stream_t stream);
 
 /* compute_dt_Impl over the level (no ghosts needed). */
 int hx_level_dt_reduce_f64(const hx_level_f64* L, hx_dt_accum* acc, hx_stream_t stream);

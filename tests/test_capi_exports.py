@@ -49,6 +49,35 @@ def test_argument_errors_need_no_gpu(hxlib):
     assert L.hx_debug_fast_op_f64(hxlib.HX_FAST_OP_SLOPE, 4, None, None, None) == hxlib.HX_ERR_ARG
 
 
+def test_epilogue_arguments_checked_on_the_host(hxlib):
+    """The advance epilogue needs an output, and a work buffer for the
+    diagnostics; a malformed eta view is named.  Checked before any CUDA call
+    (the pointers below are never dereferenced)."""
+    L = hxlib.lib()
+    fake = ctypes.c_void_p(0x1000)
+    lv = hxlib.LevelF64()
+    for f in ("h", "hu", "hv", "z", "n"):
+        setattr(lv, f, ctypes.cast(fake, ctypes.POINTER(ctypes.c_double)))
+    lv.pitch, lv.nx, lv.ny, lv.dx, lv.dy = 64, 64, 32, 1.0, 1.0
+    out = [fake, fake, fake]
+    rc = L.hx_level_advance_epilogue_f64(ctypes.byref(lv), 1e-3, *out, None, None, 0, None, None, None, None)
+    assert rc == hxlib.HX_ERR_ARG and b"neither eta nor diagnostics" in L.hx_last_error()
+    rc = L.hx_level_advance_epilogue_f64(ctypes.byref(lv), 1e-3, *out, None, None, 0, None, fake, None, None)
+    assert rc == hxlib.HX_ERR_ARG and b"work buffer" in L.hx_last_error()
+    A = hxlib.Array4F64()
+    A.p = ctypes.cast(fake, ctypes.POINTER(ctypes.c_double))
+    A.jstride, A.nstride, A.ncomp = 64, 64 * 32, 3
+    A.lo[0], A.lo[1], A.hi[0], A.hi[1] = -2, -2, 61, 29
+    vb = hxlib.Box()
+    vb.lo[0], vb.lo[1], vb.hi[0], vb.hi[1] = 0, 0, 59, 27
+    small = hxlib.Array4F64()
+    small.p, small.jstride, small.nstride, small.ncomp = A.p, 10, 100, 1
+    small.lo[0], small.lo[1], small.hi[0], small.hi[1] = 0, 0, 9, 9
+    rc = L.hx_advance_box_hydrostatic_epilogue_f64(*(ctypes.byref(A),) * 5, vb, 1e-3, 1.0, 1.0, None, None, 0,
+                                                   ctypes.byref(small), None, None, None)
+    assert rc == hxlib.HX_ERR_ARG and b"eta_new" in L.hx_last_error()
+
+
 def test_box_level_plan_checks_the_tiling(hxlib):
     """The multi-box planner (host code) accepts boxes that tile the domain and
     rejects overlaps, gaps and boxes outside it, with a message."""
