@@ -35,6 +35,7 @@ HX_FAST_OP_SQRT = 1
 HX_FAST_OP_SLOPE = 2
 HX_FAST_OP_RCP_FAITHFUL = 3
 HX_FAST_OP_SQRT_FAITHFUL = 4
+HX_FAST_OP_RCBRT = 5
 
 
 class HxError(RuntimeError):

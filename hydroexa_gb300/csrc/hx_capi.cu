@@ -1068,7 +1068,7 @@ int hx_debug_staging_extra_bytes(unsigned bytes) {
 }
 
 int hx_debug_fast_op_f64(int op, long n, const double* x, double* y, hx_stream_t s) {
-    if (op < HX_FAST_OP_RCP || op > HX_FAST_OP_SQRT_FAITHFUL) return fail(HX_ERR_ARG, "unknown fast-form operation");
+    if (op < HX_FAST_OP_RCP || op > HX_FAST_OP_RCBRT) return fail(HX_ERR_ARG, "unknown fast-form operation");
     if (n < 0 || (n > 0 && (!x || !y))) return fail(HX_ERR_ARG, "bad operand arrays");
     return launched(launch_rcp<true>(n, x, y, op, (cudaStream_t)s), "hx_debug_fast_op_f64");
 }

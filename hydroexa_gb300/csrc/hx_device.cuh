@@ -321,6 +321,28 @@ __host__ __device__ __forceinline__ float fast_sqrt(float x) {
 #endif
 }
 
+// h^(-1/3) for a wet depth (a positive normal double within the float range) in the fast form's Manning
+// factor: the float seed rcbrtf of its leading 24 bits (within ~2^-22.5 with the truncation), widened on the
+// integer pipe, then one Newton step for f(r) = r^-3 - h, r + r (1 - h r^3) / 3, whose error is twice the
+// seed's squared (~2^-44): five FP64 instructions where cbrt and a division take several times that.
+// Float: rcbrtf alone.
+__host__ __device__ __forceinline__ double rcbrt_nr(double h) {
+#ifdef __CUDA_ARCH__
+    const double r = f64_widen(rcbrtf(f32_lead(h)));
+    const double e = fma(-h, r * r * r, 1.0);
+    return fma(r * e, 1.0 / 3.0, r);
+#else
+    return 1.0 / cbrt(h);
+#endif
+}
+__host__ __device__ __forceinline__ float rcbrt_nr(float h) {
+#ifdef __CUDA_ARCH__
+    return rcbrtf(h);
+#else
+    return 1.0f / cbrtf(h);
+#endif
+}
+
 // 2 p / S for p = dm dp > 0 and S = dm + dp (the van Leer slope 2 dm dp / (dm + dp)), S a normal double of
 // magnitude below 2^1000.  The seeds come from the leading 24 bits of the two significands, taken as floats
 // in [1, 2): rf ~ 1 / mS by rcp.approx.ftz.f32 and hf = mp rf; the exponents are added back on the integer

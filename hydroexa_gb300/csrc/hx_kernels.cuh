@@ -186,22 +186,32 @@ __device__ __forceinline__ void step_cell(R o0, R o1, R o2, R dx0, R dx1, R dx2,
         else rough = nsq > Cst<R>::tol12;
         if (rough) {  // the friction factor needs a rough bed
             const R qx = un[1], qy = un[2];
-            R modM;
             if constexpr (!FAST) {
                 const R inv_h = R(1.0) / hh;
                 const R uu = qx * inv_h, vv = qy * inv_h;
-                modM = sqrt(uu * uu + vv * vv);
+                const R modM = sqrt(uu * uu + vv * vv);
+                if (modM > Cst<R>::tol12) {
+                    pflags |= 1u;
+                    const R h43 = hh * cbrt(hh);
+                    const R tt = dt * Cst<R>::g * nsq * modM / h43;
+                    const R ff = sqrt(R(1.0) + R(4.0) * tt);
+                    const R fac = R(2.0) / (R(1.0) + ff);
+                    un[1] = qx * fac;
+                    un[2] = qy * fac;
+                }
             } else {
-                modM = fast_sqrt(qx * qx + qy * qy) * rcp_nr(hh);
-            }
-            if (modM > Cst<R>::tol12) {
-                pflags |= 1u;
-                const R h43 = hh * cbrt(hh);
-                const R tt = dt * Cst<R>::g * nsq * modM / h43;
-                const R ff = sqrt(R(1.0) + R(4.0) * tt);
-                const R fac = R(2.0) / (R(1.0) + ff);
-                un[1] = qx * fac;
-                un[2] = qy * fac;
+                // the same factor with h^(4/3) as h / h^(-1/3) sharing 1/h with |u|, and the square root and
+                // reciprocals of the fast form: 2 / (1 + ff) = 1 / (0.5 + 0.5 ff)
+                const R rh = rcp_nr(hh);
+                const R modM = fast_sqrt(qx * qx + qy * qy) * rh;
+                if (gt_bits(modM, Cst<R>::tol12_bits)) {
+                    pflags |= 1u;
+                    const R tt = dt * Cst<R>::g * nsq * modM * (rcbrt_nr(hh) * rh);
+                    const R ff = fast_sqrt(fma(R(4.0), tt, R(1.0)));
+                    const R fac = rcp_nr(fma(R(0.5), ff, R(0.5)));
+                    un[1] = qx * fac;
+                    un[2] = qy * fac;
+                }
             }
         }
     } else {
@@ -1954,7 +1964,8 @@ template <bool FAST> __global__ void k_rcp_probe(long n, const double* x, double
         case 1: y[i] = fast_sqrt(x[i]); break;
         case 2: y[i] = van_leer_slope<double, true>(x[3 * i], x[3 * i + 1], x[3 * i + 2]); break;
         case 3: y[i] = rcp_fa(x[i]); break;
-        default: y[i] = fast_sqrt_fa(x[i]); break;
+        case 4: y[i] = fast_sqrt_fa(x[i]); break;
+        default: y[i] = rcbrt_nr(x[i]); break;
     }
 }
 template <bool FAST> cudaError_t launch_rcp(long n, const double* x, double* y, int which, cudaStream_t st) {

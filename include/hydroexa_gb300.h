@@ -34,8 +34,9 @@
  * an _f32 form (SINGLE build).  Arithmetic: HX_ARITH_EXACT repeats the
  * reference's operation order with no multiply-add contraction (bit-for-bit
  * the reference's host arithmetic up to cbrt); HX_ARITH_FAST shares
- * reciprocals and square roots between terms, takes them from float seeds
- * with one FP64 Newton step (within 2^-42) and contracts multiply-adds,
+ * reciprocals and square roots between terms, takes them (and the Manning
+ * factor's h^(-1/3)) from float seeds with one FP64 Newton step (within
+ * 2^-42) and contracts multiply-adds,
  * agreeing with the exact form to a few 1e-15 relative per step (bound:
  * 1e-12 per step); its time step follows the exact form's to a few ulps.
  */
@@ -697,13 +698,16 @@ int hx_debug_sqrt_f64(long n, const double* x, double* y, hx_stream_t stream);
  * error bounds): HX_FAST_OP_RCP and HX_FAST_OP_SQRT (one Newton step, the
  * face flux's), HX_FAST_OP_SLOPE (the van Leer slope of the triplets
  * x[3i], x[3i+1], x[3i+2]: x holds 3n values), HX_FAST_OP_RCP_FAITHFUL and
- * HX_FAST_OP_SQRT_FAITHFUL (the CFL rate's, within an ulp).  y holds n values. */
+ * HX_FAST_OP_SQRT_FAITHFUL (the CFL rate's, within an ulp), HX_FAST_OP_RCBRT
+ * (h^(-1/3) of the Manning factor, for depths within the float range).  y holds
+ * n values. */
 enum {
     HX_FAST_OP_RCP = 0,
     HX_FAST_OP_SQRT = 1,
     HX_FAST_OP_SLOPE = 2,
     HX_FAST_OP_RCP_FAITHFUL = 3,
-    HX_FAST_OP_SQRT_FAITHFUL = 4
+    HX_FAST_OP_SQRT_FAITHFUL = 4,
+    HX_FAST_OP_RCBRT = 5
 };
 int hx_debug_fast_op_f64(int op, long n, const double* x, double* y, hx_stream_t stream);
 /* Test setting of the persistent level kernel's TMA staging: the next launches wait for this many bytes

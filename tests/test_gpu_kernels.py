@@ -427,6 +427,22 @@ def test_faithful_sqrt(cuda, hxlib):
     assert (u == 0).mean() > 0.9
 
 
+def test_fast_reciprocal_cube_root(cuda, hxlib):
+    """The Manning factor's h^(-1/3) in the fast form (the float rcbrtf of the
+    leading bits widened, one Newton step) is within 2^-42 relative of
+    1/cbrt(h) over depths from the dry tolerance to 1e4 m, and well inside it
+    for the bulk."""
+    rng = np.random.default_rng(15)
+    n = 1 << 22
+    x = wide_range(rng, n, 1e-6, 1e4, signed=False)
+    x[:6] = [1e-6, 1.0, 8.0, 0.125, 27.0, 1e4]
+    y = fast_op(hxlib, cuda, capi.HX_FAST_OP_RCBRT, x, n)
+    ref = 1.0 / np.cbrt(x)
+    rel = np.abs(y - ref) / ref
+    assert rel.max() <= 2.0 ** -42, rel.max()
+    assert np.median(rel) <= 2.0 ** -46
+
+
 def test_fast_van_leer_slope(cuda, hxlib):
     """The fast form's van Leer slope 2 dm dp / (dm + dp) (seeds of the quotient
     and of 2/S from float estimates, one Newton correction in FP64) against the
