@@ -442,38 +442,63 @@ __device__ __forceinline__ void epi_cell(const EpiOut<R>& e, int i, int j, R h, 
     }
 }
 
-// The block's sums and min of the diagnostics into q[0..4] by a fixed tree
-// (shuffles within each warp, then thread 0 over the warps in order); the sums
+// The block's sums and min of the diagnostics into q[0..4] by a fixed tree.
+// The four sums go through scr (4 NTv doubles of shared memory, free when
+// called): halved in place, row n + k into row k, while more than a warp's
+// worth is left, then one warp's shuffles; each level is full-width warp
+// instructions on the FP64 pipe, about 4 NTv / 32 of them in all instead of
+// five shuffle levels in every warp.  min h is taken on the bits (the values
+// are positive doubles, ordered as integers) on the integer pipe.  The sums
 // are scaled by sm (mass, momenta) and sk (kinetic energy) at the end.  Every
 // thread of the block calls it.
 template <int NTv>
 __device__ __forceinline__ void diag_block_store(double m, double px, double py, double ke, double mn, double* q,
-                                                 double sm = 1.0, double sk = 1.0) {
-    __shared__ double sh[5][NTv / 32];
+                                                 double* scr, double sm = 1.0, double sk = 1.0) {
+    static_assert(NTv % 32 == 0 && (NTv & (NTv - 1)) == 0, "a power-of-two block of whole warps");
+    __shared__ long long s_mn[NTv / 32];
+    const int t = threadIdx.x;
+    scr[t] = m;
+    scr[NTv + t] = px;
+    scr[2 * NTv + t] = py;
+    scr[3 * NTv + t] = ke;
+    long long mb = sbits(mn);
     for (int o = 16; o > 0; o >>= 1) {
-        m += __shfl_xor_sync(0xffffffffu, m, o);
-        px += __shfl_xor_sync(0xffffffffu, px, o);
-        py += __shfl_xor_sync(0xffffffffu, py, o);
-        ke += __shfl_xor_sync(0xffffffffu, ke, o);
-        mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+        const long long x = __shfl_xor_sync(0xffffffffu, mb, o);
+        mb = x < mb ? x : mb;
     }
-    const int w = threadIdx.x >> 5;
-    if ((threadIdx.x & 31) == 0) { sh[0][w] = m; sh[1][w] = px; sh[2][w] = py; sh[3][w] = ke; sh[4][w] = mn; }
+    if ((t & 31) == 0) s_mn[t >> 5] = mb;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int k = 1; k < NTv / 32; ++k) {
-            m += sh[0][k]; px += sh[1][k]; py += sh[2][k]; ke += sh[3][k]; mn = fmin(mn, sh[4][k]);
+#pragma unroll
+    for (int n = NTv / 2; n >= 32; n >>= 1) {
+        if (t < n)
+            for (int c = 0; c < 4; ++c) scr[c * NTv + t] += scr[c * NTv + t + n];
+        __syncthreads();
+    }
+    if (t < 32) {
+        double v[4];
+        for (int c = 0; c < 4; ++c) v[c] = scr[c * NTv + t];
+        long long mm = t < NTv / 32 ? s_mn[t] : 0x7fffffffffffffffll;
+        for (int o = 16; o > 0; o >>= 1) {
+            for (int c = 0; c < 4; ++c) v[c] += __shfl_xor_sync(0xffffffffu, v[c], o);
+            const long long x = __shfl_xor_sync(0xffffffffu, mm, o);
+            mm = x < mm ? x : mm;
         }
-        q[0] = m * sm; q[1] = px * sm; q[2] = py * sm; q[3] = ke * sk; q[4] = mn;
+        if (t == 0) {
+            q[0] = v[0] * sm; q[1] = v[1] * sm; q[2] = v[2] * sm; q[3] = v[3] * sk;
+            q[4] = __longlong_as_double(mm);
+        }
     }
 }
+// scr: shared memory the caller no longer reads (the tile kernels pass their
+// tile arrays; the call starts with a barrier so no thread still reads them).
 template <class R, bool FAST, int NTv>
-__device__ __forceinline__ void epi_block_store(const EpiOut<R>& e, const DiagAcc& acc, long long slot) {
+__device__ __forceinline__ void epi_block_store(const EpiOut<R>& e, const DiagAcc& acc, long long slot, double* scr) {
     constexpr bool SCALED = FAST && sizeof(R) == 8;
     const double dA = (double)e.dA;
     // no cell counted: the reference's initial min, std::numeric_limits<R>::max()
     const double mn = acc.mn == DiagAcc{}.mn ? (double)Cst<R>::max_value : __longlong_as_double((long long)acc.mn);
-    diag_block_store<NTv>(acc.m, acc.px, acc.py, acc.ke, mn, e.part + 5 * slot, SCALED ? dA : 1.0,
+    __syncthreads();
+    diag_block_store<NTv>(acc.m, acc.px, acc.py, acc.ke, mn, e.part + 5 * slot, scr, SCALED ? dA : 1.0,
                           SCALED ? 0.5 * dA : 1.0);
 }
 
@@ -759,6 +784,8 @@ template <class R, bool FAST, class Src, int TXH = TX, int TYH = TY, bool EPI = 
 __global__ void __launch_bounds__(TXH * TYH, min_ctas(TXH * TYH))
     k_hydro_tile(Src src, Cells3<R> uo, Plane<R> nplane, Cells3W<R> out, FaceOut<R> fo, IBox vb, StepCtl<R> ctl,
                  EpiOut<R> epi) {
+    static_assert(!EPI || sizeof(HydroSmem<R, TXH, TYH>) >= 4 * TXH * TYH * sizeof(double),
+                  "the epilogue's block sums reuse the tile arrays");
     extern __shared__ __align__(16) unsigned char smem_raw[];
     HydroSmem<R, TXH, TYH>& S = *reinterpret_cast<HydroSmem<R, TXH, TYH>*>(smem_raw);
     R dt;
@@ -770,7 +797,9 @@ __global__ void __launch_bounds__(TXH * TYH, min_ctas(TXH * TYH))
                          vb.lo1 + (int)blockIdx.y * TYH, dt, ctl.dx, ctl.dy, ctl.dt_out, ctl.status, nullptr,
                          NoDiv{}, NoRec{}, NoHooks{}, nullptr, BlockSync{}, true, &epi, &acc);
     if constexpr (EPI) {
-        if (epi.part) epi_block_store<R, FAST, TXH * TYH>(epi, acc, blockIdx.x + (long long)blockIdx.y * gridDim.x);
+        if (epi.part)
+            epi_block_store<R, FAST, TXH * TYH>(epi, acc, blockIdx.x + (long long)blockIdx.y * gridDim.x,
+                                                reinterpret_cast<double*>(smem_raw));
     }
 }
 
@@ -804,6 +833,8 @@ struct PersistOwn {
     unsigned long long mbar;       // completion barrier of the TMA staging
 };
 static_assert(kPX * kPY <= kPN, "one cell per thread at most");
+static_assert(sizeof(HydroSmem<double, kPX, kPY>) >= 4 * kPN * sizeof(double),
+              "the epilogue's block sums reuse the tile arrays");
 static_assert(sizeof(PersistStaging) <= sizeof(double) * 3 * (kPY * (kPX + 2) + (kPY + 2) * kPX),
               "the staging buffer must fit in the slope arrays it lies on");
 // (+128: the staging arrays start on a 128-byte boundary, which the kernel rounds its shared base up to)
@@ -1057,7 +1088,7 @@ __global__ void __launch_bounds__(kPN, 1)
     }
     if (fold) block_fold_dt<double, kPN>(tf->rate, tf->mv, tf->flags, ctl.dt_out);
     if constexpr (EPI) {
-        if (epi.part) epi_block_store<double, FAST, kPN>(epi, acc, blockIdx.x);
+        if (epi.part) epi_block_store<double, FAST, kPN>(epi, acc, blockIdx.x, reinterpret_cast<double*>(base));
     }
 }
 
@@ -1593,7 +1624,8 @@ __global__ void __launch_bounds__(NT) k_diag_partial(Plane<R> h, Plane<R> hu, Pl
             m = s_mass; px = s_mx; py = s_my; ke = s_ke; mn = hh;
         }
     }
-    diag_block_store<NT>(m, px, py, ke, mn, part + 5 * (blockIdx.x + (long long)blockIdx.y * gridDim.x));
+    __shared__ double scr[4 * NT];
+    diag_block_store<NT>(m, px, py, ke, mn, part + 5 * (blockIdx.x + (long long)blockIdx.y * gridDim.x), scr);
 }
 
 // The block partials folded in a fixed order into out[5] (one block; R only
