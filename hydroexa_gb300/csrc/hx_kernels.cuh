@@ -522,14 +522,15 @@ __device__ __forceinline__ void hydro_tile_body(HydroSmem<R, TXv, TYv>& S, const
                                                 const Div& div = Div{}, const Rec& rec = Rec{},
                                                 const Hooks& hooks = Hooks{}, ThreadFold<R>* defer = nullptr,
                                                 const Sync& sy = Sync{}, bool start_barrier = true,
-                                                const EpiOut<R>* epi = nullptr, DiagAcc* eacc = nullptr) {
+                                                const EpiOut<R>* epi = nullptr, DiagAcc* eacc = nullptr,
+                                                bool set_kc = true) {
     static_assert(!Rec::on || (FAST && sizeof(R) == 8), "face records are kept for the FP64 fast form");
     static_assert(!EPI || (!LINEAR && !Div::on), "the epilogue follows a whole update");
     constexpr int GX = HydroSmem<R, TXv, TYv>::GX, GY = HydroSmem<R, TXv, TYv>::GY;
     constexpr int CELLS = TXv * TYv;
     const int t = sy.tid();
     if (start_barrier) sy.bar();  // the previous tile of this block is done with S (else the caller synced)
-    if (t == 0) {     // read after the barriers below
+    if (set_kc && t == 0) {  // read after the barriers below (a persistent caller sets them once)
         S.kc[0] = dt / dx;
         S.kc[1] = dt / dy;
         S.kc[2] = R(1) / dx;
@@ -1051,6 +1052,12 @@ __global__ void __launch_bounds__(kPN, 1)
     }
     ThreadFold<double>* tf = &own->fold[threadIdx.x];
     *tf = ThreadFold<double>{};
+    if (threadIdx.x == 0) {  // the tile body's per-tile constants, the same for every tile of the launch
+        S.kc[0] = dt / ctl.dx;
+        S.kc[1] = dt / ctl.dy;
+        S.kc[2] = 1.0 / ctl.dx;
+        S.kc[3] = 1.0 / ctl.dy;
+    }
     const FaceOut<double> fo{};
     unsigned parity = 0;
     DiagAcc acc;
@@ -1084,7 +1091,7 @@ __global__ void __launch_bounds__(kPN, 1)
                         PersistHooks, BlockSync, EPI>(S, ss, OwnState{own, x0, y0}, OwnRough{own, x0, y0}, out, fo,
                                                       vb, x0, y0, dt, ctl.dx, ctl.dy, nullptr,
                                                       Div::on ? nullptr : ctl.status, nullptr, div, NoRec{}, hooks,
-                                                      fold ? tf : nullptr, BlockSync{}, !tma, &epi, &acc);
+                                                      fold ? tf : nullptr, BlockSync{}, !tma, &epi, &acc, false);
     }
     if (fold) block_fold_dt<double, kPN>(tf->rate, tf->mv, tf->flags, ctl.dt_out);
     if constexpr (EPI) {
