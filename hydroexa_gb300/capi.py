@@ -156,6 +156,8 @@ def _declare(L):
     L.hx_debug_fast_op_f64.argtypes = [c_int, c_long, c_void_p, c_void_p, c_void_p]
     L.hx_debug_staging_extra_bytes.argtypes = [ctypes.c_uint]
     L.hx_debug_host_bands.argtypes = [c_int, c_void_p, c_int]
+    L.hx_debug_host_split_frac.restype = c_double
+    L.hx_debug_host_split_frac.argtypes = []
     L.hx_status_clear.argtypes = [c_void_p, c_void_p]
     L.hx_status_read.argtypes = [c_void_p, c_void_p]
     L.hx_dt_accum_reset.argtypes = [c_void_p, c_void_p]
@@ -240,7 +242,7 @@ EXPORTED = [
     "hx_level_advance_f32", "hx_level_dt_reduce_f64", "hx_level_dt_reduce_f32", "hx_level_run_work_bytes",
     "hx_level_run_f64", "hx_level_run_f32", "hx_level_run_host_f64", "hx_host_cache_release",
     "hx_debug_roe_points_f64", "hx_debug_roe_points_f32", "hx_debug_rcp_f64", "hx_debug_sqrt_f64", "hx_debug_fast_op_f64", "hx_debug_staging_extra_bytes",
-    "hx_debug_host_bands",
+    "hx_debug_host_bands", "hx_debug_host_split_frac",
     "hx_level_run_static_f64",
     "hx_ensemble_work_bytes", "hx_ensemble_tiles", "hx_ensemble_run_f64",
     "hx_adjoint_work_bytes_f64", "hx_adjoint_recompute_steps", "hx_adjoint_forward_f64", "hx_adjoint_reverse_f64", "hx_adjoint_step_f64",

@@ -467,6 +467,19 @@ template <class R> int accum_read(const hx_dt_accum* acc, R* dtmin, R* maxvel, c
 // flux kernels, which hold every SM, and their bands went down late.)
 constexpr int kHostBands = 10;  // at most: a short first and last band, up to eight between
 constexpr int kHeadRows = 2;  // rows of the next band the flux differences of a band read (the MUSCL reach)
+// Share of the rows whose first step is split (flux differences as the rows land, the update once dt is
+// known), before a call has measured this host: on GB300 the upload of the level (40 B per cell at
+// ~210 GB/s) takes about as long as the flux work of 45% of the rows (~3.1 us per row of 8192 cells).
+constexpr double kSplitFrac = 0.45;
+// The split share for the next call from this call's upload time and the fused bands' time per row: the
+// split flux work should last as long as the upload (dt is known when the last rows have landed), less a
+// tenth for the split bands' flux-difference planes; halfway from the current share, within [0.15, 0.85].
+double next_split_frac(double cur, double up_ms, double fused_ms, int fused_rows, int ny) {
+    if (!(up_ms > 0) || !(fused_ms > 0) || fused_rows <= 0 || ny <= 0) return cur;
+    double f = 0.9 * up_ms / (fused_ms / fused_rows * ny);
+    f = f < 0.15 ? 0.15 : (f > 0.85 ? 0.85 : f);
+    return 0.5 * (cur + f);
+}
 // One cache per device and thread: the buffers, streams and events are created
 // with their device current and used only while it is current.
 struct HostCache {
@@ -477,6 +490,10 @@ struct HostCache {
     cudaStream_t cs[kStreams] = {nullptr, nullptr, nullptr};  // uploads, downloads, CFL reduction
     // start, dt known, (spare), four joins; per band: landed, head landed, (spare), computed
     cudaEvent_t ev[7 + 4 * kHostBands] = {};
+    // timing marks of the split first step (start, uploads done, split updates done, fused bands done) and
+    // the share of the rows it splits, adjusted after each call to the host's own copy rate
+    cudaEvent_t tev[4] = {};
+    double split_frac = kSplitFrac;
     bool streams_ok = false;
     bool ensure_streams() {
         if (streams_ok) return true;
@@ -487,6 +504,8 @@ struct HostCache {
                 return false;
         for (auto& e : ev)
             if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return false;
+        for (auto& e : tev)
+            if (cudaEventCreate(&e) != cudaSuccess) return false;
         streams_ok = true;
         return true;
     }
@@ -503,6 +522,7 @@ struct HostCache {
         bytes = 0;
         if (streams_ok) {
             for (auto& e : ev) cudaEventDestroy(e);
+            for (auto& e : tev) cudaEventDestroy(e);
             for (auto& c : cs) cudaStreamDestroy(c);
         }
         streams_ok = false;
@@ -856,6 +876,7 @@ int hx_level_run_host_f64(int method, int nx, int ny, double dx, double dy, cons
     cudaEvent_t* ev_k = ev + 7 + 3 * kHostBands;
     cudaError_t e = cudaMemsetAsync(tail, 0, 128 + 3 * sizeof(DtAccum), st);
     if (e == cudaSuccess) e = cudaEventRecord(ev_start, st);
+    if (e == cudaSuccess && split) e = cudaEventRecord(hc->tev[0], st);
     for (int k = 0; k < HostCache::kStreams && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(cs[k], ev_start, 0);
     int rc = HX_OK;
     cudaStream_t dstream = split ? dts : st;
@@ -882,6 +903,7 @@ int hx_level_run_host_f64(int method, int nx, int ny, double dx, double dy, cons
             rc = level_dt<double>(&L, reinterpret_cast<hx_dt_accum*>(&slot[0]), dstream, arith, j0, j1);
     }
     if (e == cudaSuccess && split) e = cudaEventRecord(ev_dt, dts);
+    if (e == cudaSuccess && split) e = cudaEventRecord(hc->tev[1], up);
     if (e != cudaSuccess) return drain(fail(HX_ERR_CUDA, "upload: %s", cudaGetErrorString(e)));
     if (rc) return drain(rc);
     const double* A[3] = {P[0], P[1], P[2]};
@@ -909,22 +931,22 @@ int hx_level_run_host_f64(int method, int nx, int ny, double dx, double dy, cons
                                 (size_t)(j1 - j0 + 1) * nx * sizeof(double), cudaMemcpyDeviceToHost, down);
         return r;
     };
-    int s0 = 0;
+    int s0 = 0, split_rows = 0;  // split_rows: the rows of the fused bands of the split step
     if (split) {
         double* o[3] = {B[0], B[1], B[2]};
         Cells3W<double> ow;
         ow.p[0] = o[0]; ow.p[1] = o[1]; ow.p[2] = o[2];
         ow.js = nx; ow.lo0 = 0; ow.lo1 = 0;
         // The bands ahead of kf are split: their flux differences run as their rows land.  kf is the first
-        // band starting past 45% of the rows: on GB300 the upload (40 B per cell at ~210 GB/s) takes about as
-        // long as the flux work of that share (~3.2 us per row of 8192 cells), so dt -- whose reduction runs
-        // on its own stream as the rows land, in the gaps between the flux kernels -- is known when that work
-        // ends.  Then, on the caller's stream, the split bands' updates (short: their rows start going down at
-        // once, under the rest of the step) and the later bands through the fused kernel in one pass, without
-        // the flux-difference planes and the separate update (the same arithmetic).
+        // band starting past the split share of the rows (kSplitFrac until a call has measured this host,
+        // then next_split_frac), so that dt -- whose reduction runs on its own stream as the rows land, in
+        // the gaps between the flux kernels -- is known when that work ends.  Then, on the caller's stream,
+        // the split bands' updates (short: their rows start going down at once, under the rest of the step)
+        // and the later bands through the fused kernel in one pass, without the flux-difference planes and
+        // the separate update (the same arithmetic, so the share changes the timing only).
         int kf = nbands;
         for (int b = 1; b < nbands; ++b)
-            if ((long long)starts[b] * 20 >= (long long)ny * 9) {
+            if ((double)starts[b] >= hc->split_frac * ny) {
                 kf = b;
                 break;
             }
@@ -949,16 +971,19 @@ int hx_level_run_host_f64(int method, int nx, int ny, double dx, double dy, cons
                           "hx_level_run_host_f64 (update)");
             if (rc == HX_OK && nsteps == 1) e = download(b, o, st);
         }
+        if (e == cudaSuccess && rc == HX_OK) e = cudaEventRecord(hc->tev[2], st);
         for (int b = kf; b < nbands && rc == HX_OK && e == cudaSuccess; ++b) {
             int j0, j1;
             rows(b, j0, j1);
             rc = level_advance<double>(method, &L, step_ctl(0, b), o[0], o[1], o[2], arith, st, j0, j1);
             if (rc == HX_OK && nsteps == 1) e = download(b, o, st);
         }
+        if (e == cudaSuccess && rc == HX_OK) e = cudaEventRecord(hc->tev[3], st);
         if (e != cudaSuccess) return drain(fail(HX_ERR_CUDA, "split step: %s", cudaGetErrorString(e)));
         if (rc) return drain(rc);
         res[0] = o[0]; res[1] = o[1]; res[2] = o[2];
         s0 = 1;
+        split_rows = kf < nbands ? ny - starts[kf] : 0;
     }
     // the other steps; the last one in row bands, each band's rows going down while the next computes
     for (int s = s0; s < nsteps; ++s) {
@@ -994,12 +1019,25 @@ int hx_level_run_host_f64(int method, int nx, int ny, double dx, double dy, cons
     if (e == cudaSuccess) e = cudaMemcpyAsync(&tv, tdev, 8, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return drain(fail(HX_ERR_CUDA, "download: %s", cudaGetErrorString(e)));
+    if (split && split_rows > 0) {  // the marks are complete: st has joined every stream
+        float up_ms = 0.f, fused_ms = 0.f;
+        if (cudaEventElapsedTime(&up_ms, hc->tev[0], hc->tev[1]) == cudaSuccess &&
+            cudaEventElapsedTime(&fused_ms, hc->tev[2], hc->tev[3]) == cudaSuccess)
+            hc->split_frac = next_split_frac(hc->split_frac, up_ms, fused_ms, split_rows, ny);
+        else
+            cudaGetLastError();  // a mark that was not recorded: keep the share, clear the error
+    }
     if (time_out) *time_out = tv;
     return (int)sv;
 }
 
 void hx_host_cache_release(void) {
     for (auto& c : g_host) c.release();
+}
+
+double hx_debug_host_split_frac(void) {
+    HostCache* hc = host_cache();
+    return hc ? hc->split_frac : -1.0;
 }
 
 int hx_debug_host_bands(int ny, int* starts, int max_bands) {

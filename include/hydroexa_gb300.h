@@ -718,6 +718,11 @@ int hx_debug_staging_extra_bytes(unsigned bytes);
  * writes band starts into starts[0..n] (starts[n] = ny) and returns n, at
  * most 10; max_bands must be at least 10. */
 int hx_debug_host_bands(int ny, int* starts, int max_bands);
+/* The share of the rows whose first step hx_level_run_host_f64 splits on the
+ * calling thread's current device (0.45 before a call; afterwards the value
+ * each call sets from its measured upload and compute times, within
+ * [0.15, 0.85]); -1 without a usable device. */
+double hx_debug_host_split_frac(void);
 
 #ifdef __cplusplus
 }
