@@ -1,8 +1,10 @@
 // C-ABI of the multi-box level: a same-level BoxArray advanced without
 // FillPatch.  The host checks that the boxes tile the domain, builds the map
 // from g x g blocks of the domain to boxes (g: the greatest common divisor of
-// the box corners) and the table of 32 x 8 tiles of all boxes; each step is
-// one launch over that table, with one dt chain for the level.
+// the box corners) and the table of the tiles of all boxes -- 32 x 8, or on
+// levels of 2048^2 cells and more 32 x 32 for the persistent kernel, as the
+// single-box level takes them; each step is one launch over that table, with
+// one dt chain for the level.
 #include <cstring>
 #include <numeric>
 #include <vector>
@@ -26,6 +28,7 @@ size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 struct Plan {
     int g = 0, mnx = 0, mny = 0;
+    bool big = false;  // 32 x 32 tiles and the persistent kernel
     std::vector<int> map, tiles;
     size_t off_boxes = 0, off_map = 0, off_tiles = 0, total = 0;
 };
@@ -43,6 +46,8 @@ int make_plan(int nb, const hx_levelbox_f64* boxes, int nx, int ny, Plan& P) {
         g = std::gcd(g, std::gcd(std::gcd(b.lo[0], b.lo[1]), std::gcd(b.hi[0] + 1, b.hi[1] + 1)));
     }
     P.g = g;
+    P.big = (long long)nx * (long long)ny >= kBigTileCells;
+    const int tx = P.big ? 32 : TX, ty = P.big ? 32 : TY;
     P.mnx = nx / g;
     P.mny = ny / g;
     P.map.assign((size_t)P.mnx * P.mny, -1);
@@ -54,8 +59,8 @@ int make_plan(int nb, const hx_levelbox_f64* boxes, int nx, int ny, Plan& P) {
                 if (m != -1) return set_error(HX_ERR_ARG, "boxlevel: boxes overlap");
                 m = k;
             }
-        for (int y0 = b.lo[1]; y0 <= b.hi[1]; y0 += TY)
-            for (int x0 = b.lo[0]; x0 <= b.hi[0]; x0 += TX) {
+        for (int y0 = b.lo[1]; y0 <= b.hi[1]; y0 += ty)
+            for (int x0 = b.lo[0]; x0 <= b.hi[0]; x0 += tx) {
                 P.tiles.push_back(k);
                 P.tiles.push_back(x0);
                 P.tiles.push_back(y0);
@@ -143,8 +148,8 @@ extern "C" int hx_boxlevel_run_f64(int nboxes, const hx_levelbox_f64* boxes, int
         ctl.dt_reset = &slot[(s + 2) % 3];
         ctl.status = status; ctl.time = time_dev; ctl.dx = dx; ctl.dy = dy;
         src.phase = s % 2;
-        e = arith == HX_ARITH_EXACT ? launch_boxlevel<false>(src, tiles, ntiles, ctl, st)
-                                    : launch_boxlevel<true>(src, tiles, ntiles, ctl, st);
+        e = arith == HX_ARITH_EXACT ? launch_boxlevel<false>(src, tiles, ntiles, ctl, st, P.big)
+                                    : launch_boxlevel<true>(src, tiles, ntiles, ctl, st, P.big);
         ++launches;
     }
     note_launches(launches);

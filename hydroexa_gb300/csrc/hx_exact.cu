@@ -35,7 +35,8 @@ HX_INST(float)
 template cudaError_t launch_ensemble<double, false>(const EnsInstance<double>*, int, long long, int, double, unsigned long long*, int, cudaStream_t);
 template cudaError_t launch_ensemble_big<double, false>(const EnsInstance<double>*, int, long long, int, double, unsigned long long*, int, cudaStream_t);
 template int ensemble_blocks_per_sm<double, false>();
-template cudaError_t launch_boxlevel<false>(const BoxSetSrc&, const int*, int, const StepCtl<double>&, cudaStream_t);
+template cudaError_t launch_boxlevel<false>(const BoxSetSrc&, const int*, int, const StepCtl<double>&, cudaStream_t,
+                                            bool);
 template cudaError_t launch_hydro_split<double, false>(const LevelSrc<double>&, const Cells3<double>&,
                                                       const Plane<double>&, const DivOut<double>&, const IBox&,
                                                       double, double, cudaStream_t);

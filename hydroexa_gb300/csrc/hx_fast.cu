@@ -24,7 +24,8 @@ HX_INST(float)
 template cudaError_t launch_ensemble<double, true>(const EnsInstance<double>*, int, long long, int, double, unsigned long long*, int, cudaStream_t);
 template cudaError_t launch_ensemble_big<double, true>(const EnsInstance<double>*, int, long long, int, double, unsigned long long*, int, cudaStream_t);
 template int ensemble_blocks_per_sm<double, true>();
-template cudaError_t launch_boxlevel<true>(const BoxSetSrc&, const int*, int, const StepCtl<double>&, cudaStream_t);
+template cudaError_t launch_boxlevel<true>(const BoxSetSrc&, const int*, int, const StepCtl<double>&, cudaStream_t,
+                                            bool);
 template cudaError_t launch_hydro_split<double, true>(const LevelSrc<double>&, const Cells3<double>&,
                                                       const Plane<double>&, const DivOut<double>&, const IBox&,
                                                       double, double, cudaStream_t);

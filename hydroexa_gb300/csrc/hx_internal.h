@@ -28,6 +28,10 @@ struct IBox {
     int lo0, lo1, hi0, hi1;
 };
 
+// Boxes (and levels) from 2048 x 2048 cells take the big FP64 tile (32 x 32, one block of 1024 threads per
+// SM): the persistent kernels on whole levels, the 32 x 32 tile kernel on boxes.
+constexpr long long kBigTileCells = 1ll << 22;
+
 // Array4-like strided view: element (i, j, c) at p[(i-lo0) + (j-lo1)*js + c*ns].
 template <class T> struct V4 {
     T* p;

@@ -538,8 +538,9 @@ __device__ __forceinline__ void hydro_tile_body(HydroSmem<R, TXv, TYv>& S, const
     }
 
     // --- A: grown tile -> h rebuilt, eta = h + z, velocities -----------------
-    // The fast form on a grown tile inside the level (no ghost rule applies) takes the stored depth as it
-    // is: the reference's rebuild max(0, (h + z) - z) differs from it by rounding only.
+    // The fast form takes the stored depth of a cell of the level as it is (sources with an interior fetch):
+    // the reference's rebuild max(0, (h + z) - z) differs from it by rounding only.  Tiles whose grown region
+    // lies inside the level skip the ghost rules altogether.
     bool interior = false;
     if constexpr (FAST && InteriorFetch<Src>::value)
         interior = src.interior(x0 - 2, y0 - 2, x0 + TXv + 1, y0 + TYv + 1);
@@ -563,14 +564,22 @@ __device__ __forceinline__ void hydro_tile_body(HydroSmem<R, TXv, TYv>& S, const
         const int r = idx / GX, c = idx - r * GX;
         const int gi = x0 + c - 2, gj = y0 + r - 2;
         R e = R(0), zz = R(0), qx = R(0), qy = R(0), nn = R(0);
-        if (src.inside(gi, gj)) src.fetch(gi, gj, e, zz, qx, qy, nn);
+        // the same rule per cell on tiles at the level's edge: a cell of the level takes its stored depth, so
+        // the result does not depend on where the tiles lie (a multi-box level tiles each box from its corner)
+        bool stored = false;
+        if constexpr (FAST && InteriorFetch<Src>::value) stored = src.interior(gi, gj, gi, gj);
+        if (stored) {
+            if constexpr (FAST && InteriorFetch<Src>::value) src.fetch_in(gi, gj, e, zz, qx, qy);  // e: h
+        } else if (src.inside(gi, gj)) {
+            src.fetch(gi, gj, e, zz, qx, qy, nn);
+        }
         R hp, uu, vv;
         if constexpr (!FAST) {
             hp = max0(e - zz);  // HydrostaticRoe.cpp:498
             uu = (hp > Cst<R>::tol12) ? qx / hp : R(0);
             vv = (hp > Cst<R>::tol12) ? qy / hp : R(0);
         } else {
-            hp = max0_i(e - zz);
+            hp = stored ? max0_i(e) : max0_i(e - zz);
             const R rh = gt_bits(hp, Cst<R>::tol12_bits) ? rcp_nr(hp) : R(0);
             uu = qx * rh;
             vv = qy * rh;
@@ -773,7 +782,6 @@ constexpr int min_ctas(int threads) { return threads >= 1024 ? 1 : (threads >= 5
 struct SmallTile {
     static constexpr int X = TX, Y = TY;
 };
-constexpr long long kBigTileCells = 1ll << 22;  // boxes from 2048 x 2048 cells take the big tile
 template <class R> inline bool big_tile(const IBox& vb) {
     return BigTile<R>::Y != TY &&
            (long long)(vb.hi0 - vb.lo0 + 1) * (long long)(vb.hi1 - vb.lo1 + 1) >= kBigTileCells;
@@ -982,6 +990,15 @@ struct OwnRough {
     int x0, y0;
     __device__ __forceinline__ double ld(int i, int j) const { return o->n[(j - y0) * kPX + (i - x0)]; }
 };
+// The own cells' stored state and roughness, out of the staging buffer (phase A, each thread its own cell).
+__device__ __forceinline__ void persist_own_copy(const PersistStaging* st, PersistOwn* own) {
+    const int t = threadIdx.x, r = t / kPX + 2, c = t % kPX + 2;
+    if (t >= kPX * kPY) return;
+    own->h[t] = st->h[r][c];
+    own->hu[t] = st->hu[r][c];
+    own->hv[t] = st->hv[r][c];
+    own->n[t] = st->n[r - 2][c - 2];
+}
 struct PersistHooks {
     PersistStaging* st;
     PersistOwn* own;
@@ -989,14 +1006,7 @@ struct PersistHooks {
     const PersistMaps* maps;  // null: cp.async staging
     int nx0, ny0;  // origin of the next tile
     bool next;
-    __device__ __forceinline__ void after_load() const {
-        const int t = threadIdx.x, r = t / kPX + 2, c = t % kPX + 2;
-        if (t >= kPX * kPY) return;
-        own->h[t] = st->h[r][c];
-        own->hu[t] = st->hu[r][c];
-        own->hv[t] = st->hv[r][c];
-        own->n[t] = st->n[r - 2][c - 2];
-    }
+    __device__ __forceinline__ void after_load() const { persist_own_copy(st, own); }
     // the staging buffer lies on the slope arrays: order this thread's accesses to them (generic proxy)
     // before the TMA writes (async proxy) that the next tile's staging issues after the barrier
     __device__ __forceinline__ void faces_done() const {
@@ -1097,6 +1107,99 @@ __global__ void __launch_bounds__(kPN, 1)
     if constexpr (EPI) {
         if (epi.part) epi_block_store<double, FAST, kPN>(epi, acc, blockIdx.x, reinterpret_cast<double*>(base));
     }
+}
+
+// ---------------------------------------------------------------------------
+// The persistent step of a multi-box level of 2048^2 cells and more: the tile
+// loop of k_hydro_persist over a table of the 32 x 32 tiles of every box.  A
+// tile's grown region is staged by cp.async from the boxes that own its cells
+// (the map of the domain), its ghosts outside the level are resolved from the
+// staged cells, and its update goes to its own box.  The staged values are
+// the ones the single-box level stages, and the tile arithmetic is the same,
+// so the two give the same state bit for bit.
+// ---------------------------------------------------------------------------
+// Issue the copies of tile (x0, y0) of box b into st (every thread of the block).
+__device__ __forceinline__ void boxset_stage(PersistStaging* st, const BoxSetSrc& s, int b, int x0, int y0) {
+    const int t = threadIdx.x;
+    const DevBox& B = s.boxes[b];
+    for (int idx = t; idx < kPGX * kPGY; idx += kPN) {
+        const int r = idx / kPGX, c = idx - r * kPGX;
+        const int gi = x0 - 2 + c, gj = y0 - 2 + r;
+        if (gi < 0 || gi >= s.nx || gj < 0 || gj >= s.ny) continue;  // a ghost: resolved from staged cells
+        const bool mine = gi >= B.lo0 && gi <= B.hi0 && gj >= B.lo1 && gj <= B.hi1;
+        const DevBox& O = mine ? B : s.boxes[ld_ro(s.map + (long long)(gj / s.g) * s.mnx + gi / s.g)];
+        const long long o = (long long)(gi - O.lo0) + (long long)(gj - O.lo1) * O.pitch;
+        cp_async8(&st->h[r][c], O.h[s.phase] + o);
+        cp_async8(&st->hu[r][c], O.hu[s.phase] + o);
+        cp_async8(&st->hv[r][c], O.hv[s.phase] + o);
+        cp_async8(&st->z[r][c], O.z + o);
+    }
+    const int r = t / kPX, c = t % kPX, gi = x0 + c, gj = y0 + r;
+    if (t < kPX * kPY && gi <= B.hi0 && gj <= B.hi1)
+        cp_async8(&st->n[r][c], B.n + (long long)(gi - B.lo0) + (long long)(gj - B.lo1) * B.pitch);
+    cp_async_commit();
+}
+struct BoxPersistHooks {
+    PersistStaging* st;
+    PersistOwn* own;
+    const BoxSetSrc* src;
+    int nb, nx0, ny0;  // the next tile: its box and origin
+    bool next;
+    __device__ __forceinline__ void after_load() const { persist_own_copy(st, own); }
+    __device__ __forceinline__ void faces_done() const {}
+    __device__ __forceinline__ void after_faces() const {
+        if (next) boxset_stage(st, *src, nb, nx0, ny0);
+    }
+};
+template <bool FAST>
+__global__ void __launch_bounds__(kPN, 1)
+    k_boxlevel_persist(BoxSetSrc src, const int* __restrict__ tiles, int ntiles, StepCtl<double> ctl) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    unsigned char* base = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);  // 128-byte aligned
+    HydroSmem<double, kPX, kPY>& S = *reinterpret_cast<HydroSmem<double, kPX, kPY>*>(base);
+    PersistOwn* own = reinterpret_cast<PersistOwn*>(base + sizeof(HydroSmem<double, kPX, kPY>));
+    PersistStaging* st = reinterpret_cast<PersistStaging*>(&S.sxe[0][0]);
+    double dt;
+    if (!resolve_dt(ctl, dt)) return;
+    step_bookkeeping(ctl, dt);
+    const bool fold = ctl.dt_out != nullptr;
+    int k = (int)blockIdx.x;
+    if (k >= ntiles) return;
+    boxset_stage(st, src, tiles[3 * k], tiles[3 * k + 1], tiles[3 * k + 2]);
+    ThreadFold<double>* tf = &own->fold[threadIdx.x];
+    *tf = ThreadFold<double>{};
+    if (threadIdx.x == 0) {  // the tile body's per-tile constants, the same for every tile of the launch
+        S.kc[0] = dt / ctl.dx;
+        S.kc[1] = dt / ctl.dy;
+        S.kc[2] = 1.0 / ctl.dx;
+        S.kc[3] = 1.0 / ctl.dy;
+    }
+    const FaceOut<double> fo{};
+    const int nxt = 1 - src.phase;
+    for (; k < ntiles; k += (int)gridDim.x) {
+        const int b = tiles[3 * k], x0 = tiles[3 * k + 1], y0 = tiles[3 * k + 2];
+        const int kn = k + (int)gridDim.x;
+        const bool next = kn < ntiles;
+        const BoxPersistHooks hooks{st, own, &src, next ? tiles[3 * kn] : 0, next ? tiles[3 * kn + 1] : 0,
+                                    next ? tiles[3 * kn + 2] : 0, next};
+        const StagedSrc ss{st, x0, y0, src.nx, src.ny, src.bc_xlo, src.bc_xhi, src.bc_ylo, src.bc_yhi,
+                           src.glo0, src.glo1, src.ghi0, src.ghi1};
+        const DevBox& B = src.boxes[b];
+        Cells3W<double> out;
+        out.p[0] = const_cast<double*>(B.h[nxt]);
+        out.p[1] = const_cast<double*>(B.hu[nxt]);
+        out.p[2] = const_cast<double*>(B.hv[nxt]);
+        out.js = B.pitch;
+        out.lo0 = B.lo0;
+        out.lo1 = B.lo1;
+        const IBox vb{B.lo0, B.lo1, B.hi0, B.hi1};
+        cp_async_wait_all();  // this thread's copies of tile k; the body's first barrier publishes everyone's
+        hydro_tile_body<double, FAST, kPX, kPY, kPN, StagedSrc, false, NoDiv, NoRec, OwnState, OwnRough,
+                        BoxPersistHooks>(S, ss, OwnState{own, x0, y0}, OwnRough{own, x0, y0}, out, fo, vb, x0, y0,
+                                         dt, ctl.dx, ctl.dy, nullptr, ctl.status, nullptr, NoDiv{}, NoRec{}, hooks,
+                                         fold ? tf : nullptr, BlockSync{}, true, nullptr, nullptr, false);
+    }
+    if (fold) block_fold_dt<double, kPN>(tf->rate, tf->mv, tf->flags, ctl.dt_out);
 }
 
 // Extra bytes the next launches' staging waits for (a test setting; 0 in use).
@@ -1879,8 +1982,19 @@ int ensemble_blocks_per_sm() {
 
 template <bool FAST>
 cudaError_t launch_boxlevel(const BoxSetSrc& src, const int* tiles, int ntiles, const StepCtl<double>& ctl,
-                            cudaStream_t st) {
+                            cudaStream_t st, bool big) {
     if (ntiles <= 0) return cudaSuccess;
+    if (big) {  // 32 x 32 tiles: the persistent kernel, one block per SM
+        int dev = 0, sms = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess) return e;
+        auto k = k_boxlevel_persist<FAST>;
+        e = ensure_smem(k, persist_smem_bytes());
+        if (e != cudaSuccess) return e;
+        k<<<(unsigned)(ntiles < sms ? ntiles : sms), kPN, persist_smem_bytes(), st>>>(src, tiles, ntiles, ctl);
+        return cudaGetLastError();
+    }
     const size_t sm = sizeof(HydroSmem<double>);
     cudaError_t e = ensure_smem(k_boxlevel_hydro<FAST>, sm);
     if (e != cudaSuccess) return e;

@@ -19,10 +19,11 @@ template <class R, bool FAST, class Src>
 cudaError_t launch_classic(const Src& src, const Cells3W<R>& out, const FaceOut9<R>& fo, const RebuildOut<R>& hb,
                            const IBox& vb, const StepCtl<R>& ctl, cudaStream_t st);
 
-// One hydrostatic step of a multi-box level (one block per tile of the tile table).
+// One hydrostatic step of a multi-box level over its tile table: 32 x 8 tiles one block each, or (big)
+// 32 x 32 tiles walked by the persistent kernel.
 template <bool FAST>
 cudaError_t launch_boxlevel(const BoxSetSrc& src, const int* tiles, int ntiles, const StepCtl<double>& ctl,
-                            cudaStream_t st);
+                            cudaStream_t st, bool big);
 
 // The hydrostatic step in two launches: flux differences (no dt), then the
 // update once dt is known (same arithmetic as launch_hydro).

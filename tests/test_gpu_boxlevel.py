@@ -34,6 +34,32 @@ def test_boxlevel_equals_single_box(cuda, hxlib, arith, name, bc):
     assert bl.time.item() == lev.time.item()
 
 
+BIG_DECOMPOSITIONS = {
+    "quarters": [((0, 0), (1023, 1023)), ((1024, 0), (2047, 1023)), ((0, 1024), (1023, 2047)),
+                 ((1024, 1024), (2047, 2047))],
+    "ragged": [((0, 0), (999, 2047)), ((1000, 0), (2047, 1039)), ((1000, 1040), (1599, 2047)),
+               ((1600, 1040), (2047, 2047))],
+}
+
+
+@pytest.mark.parametrize("arith", [capi.HX_ARITH_EXACT, capi.HX_ARITH_FAST])
+@pytest.mark.parametrize("name", list(BIG_DECOMPOSITIONS))
+def test_big_boxlevel_equals_single_box(cuda, hxlib, arith, name):
+    """A 2048^2 level (the persistent kernels on 32 x 32 tiles, for the boxes
+    and for the single box): tiles straddling box edges are staged from the
+    boxes that own their cells, partial tiles at box ends included; equal bit
+    for bit."""
+    c = workloads.fractal_dam_break(2048, 2048, seed=78, amplitude=1.5, nodata_frac=0.15)
+    c.geom.bc_lo, c.geom.bc_hi = (0, 1), (1, 0)
+    nsteps = 3
+    bl = BoxLevel(c.geom, BIG_DECOMPOSITIONS[name], c.h, c.hu, c.hv, c.z, c.n, device=cuda)
+    assert bl.run(nsteps, c.cfl, arith) == 0
+    lev = Level.from_numpy(c.geom, c.h, c.hu, c.hv, c.z, c.n, device=cuda)
+    assert lev.run(capi.HX_METHOD_HYDROSTATIC_ROE, nsteps, c.cfl, arith=arith) == 0
+    assert np.array_equal(bl.gather(), lev.state.cpu().numpy())
+    assert bl.time.item() == lev.time.item()
+
+
 def test_boxlevel_rejects_gaps_and_overlaps(cuda, hxlib):
     c = workloads.dam_break(64, 48)
     with pytest.raises(capi.HxError):
