@@ -278,6 +278,7 @@ __host__ __device__ __forceinline__ void ghost_source(int i, int j, int nx, int 
 // rules of ghost_source (walls mirror, open sides copy the edge; momentum
 // signs by the wall's BC records; terrain always copies the edge).
 template <class R> struct LevelSrc {
+    static constexpr bool kInterior = true;  // has interior() / fetch_in()
     const R* h; const R* hu; const R* hv; const R* z; const R* n;
     long long pitch;
     int nx, ny;
@@ -286,6 +287,18 @@ template <class R> struct LevelSrc {
 
     __device__ __forceinline__ bool inside(int i, int j) const {
         return i >= glo0 && i <= ghi0 && j >= glo1 && j <= ghi1;
+    }
+    // true when cells (i0, j0) .. (i1, j1) all lie in the level
+    __device__ __forceinline__ bool interior(int i0, int j0, int i1, int j1) const {
+        return i0 >= 0 && j0 >= 0 && i1 < nx && j1 < ny;
+    }
+    // (h, z, hu, hv) of a cell of the level, as stored
+    __device__ __forceinline__ void fetch_in(int i, int j, R& hh, R& zz, R& qx, R& qy) const {
+        const long long p = (long long)i + (long long)j * pitch;
+        hh = ld_ro(h + p);
+        zz = ld_ro(z + p);
+        qx = ld_ro(hu + p);
+        qy = ld_ro(hv + p);
     }
     // (eta, z, hu, hv, n) of any cell in the grown region.
     __device__ __forceinline__ void fetch(int i, int j, R& eta, R& zz, R& qx, R& qy, R& nn) const {
@@ -316,6 +329,7 @@ struct DevBox {
     int lo0, lo1, hi0, hi1;
 };
 struct BoxSetSrc {
+    static constexpr bool kInterior = true;  // has interior() / fetch_in()
     const DevBox* boxes;
     const int* map;   // box index of each g x g block of the domain
     int g, mnx;       // granularity, map row length
@@ -330,6 +344,19 @@ struct BoxSetSrc {
         const DevBox& b = boxes[self];
         if (i >= b.lo0 && i <= b.hi0 && j >= b.lo1 && j <= b.hi1) return self;
         return ld_ro(map + (long long)(j / g) * mnx + i / g);
+    }
+    // true when cells (i0, j0) .. (i1, j1) all lie in the domain
+    __device__ __forceinline__ bool interior(int i0, int j0, int i1, int j1) const {
+        return i0 >= 0 && j0 >= 0 && i1 < nx && j1 < ny;
+    }
+    // (h, z, hu, hv) of a cell of the domain, as the box that owns it stores them
+    __device__ __forceinline__ void fetch_in(int i, int j, double& hh, double& zz, double& qx, double& qy) const {
+        const DevBox& b = boxes[owner(i, j)];
+        const long long p = (long long)(i - b.lo0) + (long long)(j - b.lo1) * b.pitch;
+        hh = ld_ro(b.h[phase] + p);
+        zz = ld_ro(b.z + p);
+        qx = ld_ro(b.hu[phase] + p);
+        qy = ld_ro(b.hv[phase] + p);
     }
     __device__ __forceinline__ void fetch(int i, int j, double& eta, double& zz, double& qx, double& qy,
                                           double& nn) const {
