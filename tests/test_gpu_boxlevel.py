@@ -39,6 +39,8 @@ BIG_DECOMPOSITIONS = {
                  ((1024, 1024), (2047, 2047))],
     "ragged": [((0, 0), (999, 2047)), ((1000, 0), (2047, 1039)), ((1000, 1040), (1599, 2047)),
                ((1600, 1040), (2047, 2047))],
+    # boxes thinner than a tile and than its halo: a 32 x 32 tile of a 3-row box reads two boxes beyond it
+    "thin": [((0, 0), (2047, 2)), ((0, 3), (6, 2047)), ((7, 3), (2047, 2044)), ((7, 2045), (2047, 2047))],
 }
 
 
