@@ -34,7 +34,7 @@ def run_points(hxlib, method, arith, states, aux, dev):
 
 def term_scale(states):
     """Magnitude of the terms a face flux is made of (h u^2 + g h^2 / 2 + |h u|
-    on both sides): fluxes that cancel to ~0 are judged against it."""
+    on both sides): fluxes that cancel to ~0 are measured against it."""
     s = np.asarray(states, dtype=np.float64)
     thrust = 0.0
     if s.shape[1] == 10:  # classic states also carry the bed: add the thrust g h |dz|
