@@ -1,6 +1,6 @@
 """CPU oracle for the HydroEXA per-level advance (TEST INFRASTRUCTURE ONLY).
 
-This package is the checker the CUDA path is compared against.  Only tests/,
+This package is what the CUDA path is compared against.  Only tests/,
 ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg import it; the
 product package ``hydroexa_gb300`` never does.
 
