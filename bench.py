@@ -20,6 +20,7 @@ instead, on a bounded sample of the workload per step.
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -296,14 +297,18 @@ def main():
             assert rc == 0, rc
         for _ in range(2):
             e2e_step()
-        ke = max(3, min(args.steps, 20))  # enough calls that one slow host copy does not set the figure
+        # enough calls (~1 s) that one call slowed by the host does not set the figure; no collection of
+        # Python garbage between the calls (the host thread issues each call's work)
+        ke = max(3, min(2 * args.steps, 40))
         barrier()
         marks = [torch.cuda.Event(enable_timing=True) for _ in range(ke + 1)]
+        gc.disable()
         marks[0].record(stream)
         for k in range(ke):
             e2e_step()
             marks[k + 1].record(stream)
         marks[-1].synchronize()
+        gc.enable()
         ems = ranks.reduce_real_max([marks[0].elapsed_time(marks[-1])])[0]
         calls = sorted(marks[k].elapsed_time(marks[k + 1]) for k in range(ke))
         L.hx_host_cache_release()
