@@ -654,7 +654,10 @@ int hx_write_plotfile_f64(const char* prefix, int iteration, double time, int nl
  * (src/state/AmrMeshState_AMR.cpp:667-767, include/boundaries/BCFill.H:211-296)
  * and the U_ext / Terrain_ext / Eta_ext copies (HydrostaticRoe.cpp:456-500)
  * are not needed.  Each step is one launch over the tiles of all boxes with
- * one CFL chain for the level; results equal the single-box run bit for bit.
+ * one CFL chain for the level (levels from 2048 x 2048 cells: 32 x 32 tiles
+ * walked by one block per SM, each tile staged from the boxes that own its
+ * cells; below that, 32 x 8 tiles one block each); results equal the
+ * single-box run bit for bit.
  * Boxes must not overlap and must cover the domain (coarse-fine ghosts still
  * need FillPatch).  On return *final_in_alt says which state of each box
  * holds the result.  work: hx_boxlevel_work_bytes bytes of device memory.
