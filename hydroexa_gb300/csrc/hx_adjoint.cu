@@ -631,8 +631,12 @@ __global__ void __launch_bounds__(ANT) k_adj_faces(AdjArgs A) {
         const int gi = x0 + c - H3, gj = y0 + r - H3;
         double e = 0, zz = 0, qx = 0, qy = 0, nn = 0;
         const bool in_grown = gi >= -2 && gi <= nx + 1 && gj >= -2 && gj <= ny + 1;
-        if (in_grown) A.src.fetch(gi, gj, e, zz, qx, qy, nn);
-        const double hp = max0_i(e - zz);
+        // the forward's own depth: in the fast form a cell of the level takes its stored depth (a ghost the
+        // rebuild from its rule's eta and z); both have dh'/dh = 1, dh'/dz = 0 where h' > 0
+        const bool stored = FAST && gi >= 0 && gi < nx && gj >= 0 && gj < ny;
+        if (stored) A.src.fetch_in(gi, gj, e, zz, qx, qy);  // e: h
+        else if (in_grown) A.src.fetch(gi, gj, e, zz, qx, qy, nn);
+        const double hp = stored ? max0_i(e) : max0_i(e - zz);
         S.hp[r][c] = hp;
         S.eta[r][c] = hp + zz;
         if constexpr (FAST) {  // the forward's own velocity arithmetic, so the limiters take its branches
