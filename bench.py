@@ -318,6 +318,23 @@ def main():
                # the spread of the calls (each includes its host copies, whose rate varies with the host)
                "ms_per_call": {"min": calls[0], "median": calls[len(calls) // 2], "max": calls[-1]}}
 
+    # the exact arithmetic form on the same level (bit-equal to the oracle and to the reference's drivers),
+    # a few steps: its rate beside the fast form's headline
+    exact = None
+    if args.arith == "fast":
+        xs = 5
+        assert lev.run(method, 1, case.cfl, arith=capi.HX_ARITH_EXACT) == 0  # warm-up
+        barrier()
+        x0 = torch.cuda.Event(enable_timing=True)
+        x1 = torch.cuda.Event(enable_timing=True)
+        x0.record(stream)
+        lev.run(method, xs, case.cfl, arith=capi.HX_ARITH_EXACT, check_status=False)
+        x1.record(stream)
+        x1.synchronize()
+        xms = ranks.reduce_real_max([x0.elapsed_time(x1)])[0]
+        exact = {"value": ws * cells * xs / (xms * 1e-3) / 1e6, "unit": UNIT, "ms_per_step": xms / xs, "steps": xs,
+                 "what": "HX_ARITH_EXACT: the reference's operation order, no multiply-add contraction"}
+
     ens = None
     if args.precision == "f64" and args.method == "hydrostatic" and not args.no_ensemble:
         del lev
@@ -347,6 +364,7 @@ def main():
             "ensemble": ensemble_summary(ens),
             "adjoint": adjoint_summary(adj),
             "epilogue": epi,
+            "exact_form": exact,
             "details_file": args.details if (ens is not None or adj is not None) else None,
             "config": dict(config_dict(), arith=args.arith, nx=NX, ny=NY, precision=args.precision.upper(),
                            method={"hydrostatic": "HydrostaticRoe", "roe": "Roe (no NODATA)"}[args.method]),
