@@ -317,7 +317,7 @@ struct BlockSync {
     __device__ __forceinline__ int slot() const { return 0; }
 };
 
-template <int NTv, int K = 1, class Sync = BlockSync>
+template <int NTv, int K = 1, class Sync = BlockSync, bool FAST = true>
 __device__ __forceinline__ void screened_fold(const ScreenCell<double>* c, double dx, double dy, double idx,
                                               double idy, double& rate, double& mv, unsigned& flags,
                                               const Sync& sy = Sync{}) {
@@ -385,9 +385,9 @@ __device__ __forceinline__ void screened_fold(const ScreenCell<double>* c, doubl
         if (cand[k] && !same) {
             double rc, mc;
             unsigned f = 0;
-            dt_cell_contrib<double, true>(c[k].h, c[k].hu, c[k].hv, false, dx, dy, idx, idy, rc, mc, f);
+            dt_cell_contrib<double, FAST>(c[k].h, c[k].hu, c[k].hv, false, dx, dy, idx, idy, rc, mc, f);
             flags |= f;
-            rate = nnmax_i(rate, rc);
+            rate = nnmax_i(rate, rc);  // non-negative: the integer max is the max either form takes
             mv = nnmax_i(mv, mc);
         }
     }
@@ -717,8 +717,8 @@ __device__ __forceinline__ void hydro_tile_body(HydroSmem<R, TXv, TYv>& S, const
     R rate = R(0), mv = R(0);
     unsigned flags = 0, pflags = 0;
     const R cx = S.kc[0], cy = S.kc[1], idx = S.kc[2], idy = S.kc[3];
-    // the FP64 fast form folds the next CFL bound through the float screen
-    constexpr bool SCREEN = FAST && sizeof(R) == 8 && CELLS <= NTv && !LINEAR && !Div::on;  // at most a cell a thread
+    // FP64 folds the next CFL bound through the float screen (the candidates in the form's own arithmetic)
+    constexpr bool SCREEN = sizeof(R) == 8 && CELLS <= NTv && !LINEAR && !Div::on;  // at most a cell a thread
     const bool fold = dt_out != nullptr || defer != nullptr;
     ScreenCell<R> sc;
     for (int k = t; k < CELLS; k += NTv) {
@@ -742,7 +742,7 @@ __device__ __forceinline__ void hydro_tile_body(HydroSmem<R, TXv, TYv>& S, const
         if constexpr (EPI) epi_cell<R, FAST>(*epi, gi, gj, sc.h, sc.hu, sc.hv, S.z[ty + 2][tx + 2], nplane.ld(gi, gj), *eacc);
     }
     if constexpr (SCREEN) {
-        if (fold) screened_fold<NTv, 1, Sync>(&sc, dx, dy, idx, idy, rate, mv, flags, sy);
+        if (fold) screened_fold<NTv, 1, Sync, FAST>(&sc, dx, dy, idx, idy, rate, mv, flags, sy);
     }
     if (defer) {
         if constexpr (FAST) {
@@ -1583,7 +1583,7 @@ __global__ void __launch_bounds__(NT) k_dt_reduce(Cells3<R> U, Plane<R> Z, IBox 
     const int i = vb.lo0 + blockIdx.x * TX + (threadIdx.x & (TX - 1));
     R rate = R(0), mv = R(0);
     unsigned flags = 0;
-    if constexpr (FAST && sizeof(R) == 8) {  // through the float screen: FP64 for the candidates only
+    if constexpr (sizeof(R) == 8) {  // through the float screen: FP64 for the candidates only
         ScreenCell<double> c[ROWS_PER_THREAD];
 #pragma unroll
         for (int r = 0; r < ROWS_PER_THREAD; ++r) {
@@ -1595,7 +1595,7 @@ __global__ void __launch_bounds__(NT) k_dt_reduce(Cells3<R> U, Plane<R> Z, IBox 
             c[r].nod = is_nodata(Z.ld(i, j));
             c[r].live = true;
         }
-        screened_fold<NT, ROWS_PER_THREAD>(c, dx, dy, idx, idy, rate, mv, flags);
+        screened_fold<NT, ROWS_PER_THREAD, BlockSync, FAST>(c, dx, dy, idx, idy, rate, mv, flags);
     } else {
         for (int r = 0; r < ROWS_PER_THREAD; ++r) {  // a 32 x (8 ROWS) block: fewer blocks, fewer atomics
             const int j = vb.lo1 + ((int)blockIdx.y * ROWS_PER_THREAD + r) * TY + threadIdx.x / TX;
