@@ -449,6 +449,10 @@ int hx_level_run_f32(int method, hx_level_f32* L, float* h_alt, float* hu_alt, f
  * the next call of that size on that device (hx_host_cache_release frees the
  * calling thread's caches on every device).  The copies overlap the computation in row bands, and they can only
  * when the host buffers are page-locked (cudaHostAlloc or cudaHostRegister).
+ * The hydrostatic first step of the leading bands computes its flux differences
+ * as the rows land and updates once the level's dt is known; the share of rows
+ * so split follows each call's measured upload and compute times (the cache
+ * keeps it; hx_debug_host_split_frac reads it) and does not change the result.
  * The call returns once the state is back in h, hu, hv: the status bits
  * (>= 0) or a negative error.
  */
